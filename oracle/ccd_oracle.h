@@ -1,0 +1,67 @@
+/* ORACLE / TEST INFRASTRUCTURE ONLY.
+ *
+ * Plain-C restatement of the reference's continuous-time collision detection
+ * path (evouga/collisiondetection): the primitive CTCD tests (src/CTCD.cpp),
+ * the Jenkins-Traub root finder they use (src/rpoly.h), the swept k-DOP / AABB
+ * candidate search (src/KDOPBroadPhase.cpp, src/AABBBroadPhase.cpp) and the
+ * CTCD narrow phase over stencils (src/CTCDNarrowPhase.cpp) for the two-entry
+ * (start, end) history.
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
+ * this library, and only as the checker.  It is pinned against the reference's
+ * own sources (oracle/_ref, built from the reference tree by oracle/Makefile)
+ * through the fixtures in tests/golden/.
+ */
+#ifndef CCD_ORACLE_H
+#define CCD_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Primitive tests; x holds the points in the reference's argument order
+ * (include/CTCD.h:36-79): VF/EE 8 points (24 doubles), VE 6 (18), VV 4 (12).
+ * Return 1 on a hit and write *t; on a miss *t is left untouched. */
+int oracle_vf(const double *x, double eta, double *t);
+int oracle_ee(const double *x, double eta, double *t);
+int oracle_ve(const double *x, double eta, double *t);
+int oracle_vv(const double *x, double eta, double *t);
+
+/* Batched form over n primitives of one kind (0=VF 1=EE 2=VE 3=VV), using
+ * nthreads host threads (<=1: the calling thread only).  eta has n entries
+ * when eta_per_test, else one.  t[i] is written only where hit[i]==1. */
+void oracle_batch(int kind, int64_t n, const double *x, const double *eta, int eta_per_test, uint8_t *hit, double *t,
+                  int nthreads);
+
+/* Swept-primitive candidate search.  kind 0 = 13-DOP (KDOPBroadPhase),
+ * 1 = AABB (AABBBroadPhase).  faces is F x 3 (row per face), fixed is NULL or
+ * one byte per vertex.  Results are held until oracle_broadphase_get copies
+ * them out (VF rows p,q0,q1,q2; EE rows p0,p1,q0,q1), in the reference's
+ * std::set order.  Returns 0, or -1 on allocation failure. */
+int oracle_broadphase(int kind, int nverts, const double *qstart, const double *qend, int nfaces,
+                      const int32_t *faces, double eta, const uint8_t *fixed, int64_t *n_vf, int64_t *n_ee);
+void oracle_broadphase_get(int32_t *vf, int32_t *ee);
+/* Number of non-neighbouring face pairs whose swept volumes overlap in the
+ * last oracle_broadphase call. */
+int64_t oracle_broadphase_face_pairs(void);
+
+/* CTCD narrow phase over stencils (CTCDNarrowPhase::checkVFS / checkEES) on
+ * the history qstart (t=0) -> qend (t=1).  hit[i] = stencil i collides;
+ * t[i] = contact time reported by the first test in the chain that hit
+ * (untouched on a miss); which[i] = 0 primitive (VF/EE), 1 vertex-edge,
+ * 2 vertex-vertex, -1 miss.  Any of t / which may be NULL. */
+void oracle_narrowphase(int nverts, const double *qstart, const double *qend, int64_t n_vf, const int32_t *vf,
+                        const double *vf_eta, int64_t n_ee, const int32_t *ee, const double *ee_eta, uint8_t *vf_hit,
+                        uint8_t *ee_hit, double *vf_t, double *ee_t, int8_t *vf_which, int8_t *ee_which,
+                        int nthreads);
+
+/* Stencil canonical forms (src/Stencils.h): writes the canonical 4-tuple. */
+void oracle_vf_canon(int p, int q0, int q1, int q2, int32_t *out);
+void oracle_ee_canon(int p0, int p1, int q0, int q1, int32_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

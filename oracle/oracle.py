@@ -1,0 +1,167 @@
+"""ORACLE / TEST INFRASTRUCTURE ONLY.
+
+ctypes loader for the C restatement (oracle/_build/libccd_oracle.so) and, where
+it was built, the reference compiled from its own sources
+(oracle/_ref/libccd_ref.so).  Only tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg import this module, and only as the checker.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libccd_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libccd_ref.so")
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+
+
+def build(ref: bool = False) -> None:
+    """Compile the C restatement (and the reference, when asked and present)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+class _Lib:
+    def __init__(self, path: str, prefix: str):
+        self.lib = ctypes.CDLL(path)
+        self.prefix = prefix
+        L = self.lib
+        for k in ("vf", "ee", "ve", "vv"):
+            fn = getattr(L, f"{prefix}_{k}")
+            fn.argtypes = [_P, ctypes.c_double, _P]
+            fn.restype = ctypes.c_int
+
+    def prim(self, kind: str, x, eta: float):
+        """One primitive test; returns (hit, t or None)."""
+        x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+        t = ctypes.c_double(np.nan)
+        h = getattr(self.lib, f"{self.prefix}_{kind}")(_ptr(x), eta, ctypes.byref(t))
+        return int(h), (t.value if h else None)
+
+
+class Oracle(_Lib):
+    def __init__(self, path: str = ORACLE_SO):
+        if not os.path.exists(path):
+            build()
+        super().__init__(path, "oracle")
+        L = self.lib
+        L.oracle_batch.argtypes = [ctypes.c_int, _I64, _P, _P, ctypes.c_int, _P, _P, ctypes.c_int]
+        L.oracle_broadphase.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int, _P, ctypes.c_double, _P,
+                                        _P, _P]
+        L.oracle_broadphase.restype = ctypes.c_int
+        L.oracle_broadphase_get.argtypes = [_P, _P]
+        L.oracle_broadphase_face_pairs.restype = ctypes.c_int64
+        L.oracle_narrowphase.argtypes = [ctypes.c_int, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P,
+                                         ctypes.c_int]
+
+    def batch(self, kind: int, x, eta, nthreads: int = 1):
+        """kind 0..3 (VF, EE, VE, VV); eta scalar or per-row.  Returns
+        (hit uint8[n], t float64[n]) with t NaN where there is no hit."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        n = x.shape[0]
+        eta_a = np.ascontiguousarray(np.atleast_1d(np.asarray(eta, dtype=np.float64)))
+        per = 1 if eta_a.size == n and n != 1 else 0
+        hit = np.zeros(n, np.uint8)
+        t = np.full(n, np.nan)
+        self.lib.oracle_batch(kind, n, _ptr(x), _ptr(eta_a), per, _ptr(hit), _ptr(t), nthreads)
+        return hit, t
+
+    def broadphase(self, kind: int, qstart, qend, faces, eta: float, fixed=None):
+        qstart = np.ascontiguousarray(qstart, dtype=np.float64).ravel()
+        qend = np.ascontiguousarray(qend, dtype=np.float64).ravel()
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        nvf, nee = ctypes.c_int64(), ctypes.c_int64()
+        rc = self.lib.oracle_broadphase(kind, qstart.size // 3, _ptr(qstart), _ptr(qend), faces.shape[0], _ptr(faces),
+                                        eta, _ptr(fx), ctypes.byref(nvf), ctypes.byref(nee))
+        if rc != 0:
+            raise MemoryError("oracle_broadphase failed")
+        vf = np.zeros((nvf.value, 4), np.int32)
+        ee = np.zeros((nee.value, 4), np.int32)
+        self.lib.oracle_broadphase_get(_ptr(vf), _ptr(ee))
+        return vf, ee
+
+    def face_pairs(self) -> int:
+        return int(self.lib.oracle_broadphase_face_pairs())
+
+    def narrowphase(self, qstart, qend, vf, vf_eta, ee, ee_eta, nthreads: int = 1):
+        qstart = np.ascontiguousarray(qstart, dtype=np.float64).ravel()
+        qend = np.ascontiguousarray(qend, dtype=np.float64).ravel()
+        vf = np.ascontiguousarray(vf, dtype=np.int32).reshape(-1, 4)
+        ee = np.ascontiguousarray(ee, dtype=np.int32).reshape(-1, 4)
+        vfe = np.ascontiguousarray(np.broadcast_to(np.asarray(vf_eta, np.float64), (vf.shape[0],)))
+        eee = np.ascontiguousarray(np.broadcast_to(np.asarray(ee_eta, np.float64), (ee.shape[0],)))
+        out = {
+            "vf_hit": np.zeros(vf.shape[0], np.uint8), "ee_hit": np.zeros(ee.shape[0], np.uint8),
+            "vf_t": np.full(vf.shape[0], np.nan), "ee_t": np.full(ee.shape[0], np.nan),
+            "vf_which": np.zeros(vf.shape[0], np.int8), "ee_which": np.zeros(ee.shape[0], np.int8),
+        }
+        self.lib.oracle_narrowphase(qstart.size // 3, _ptr(qstart), _ptr(qend), vf.shape[0], _ptr(vf), _ptr(vfe),
+                                    ee.shape[0], _ptr(ee), _ptr(eee), _ptr(out["vf_hit"]), _ptr(out["ee_hit"]),
+                                    _ptr(out["vf_t"]), _ptr(out["ee_t"]), _ptr(out["vf_which"]),
+                                    _ptr(out["ee_which"]), nthreads)
+        return out
+
+
+class Reference(_Lib):
+    """The reference's own compiled sources (development container only)."""
+
+    def __init__(self, path: str = REF_SO):
+        super().__init__(path, "ref")
+        L = self.lib
+        L.ref_batch.argtypes = [ctypes.c_int, _I64, _P, _P, ctypes.c_int, _P, _P]
+        L.ref_broadphase.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int, _P, ctypes.c_double, _P, _P,
+                                     _P]
+        L.ref_broadphase_get.argtypes = [_P, _P]
+        L.ref_narrowphase.argtypes = [ctypes.c_int, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P]
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(REF_SO)
+
+    def batch(self, kind: int, x, eta):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        n = x.shape[0]
+        eta_a = np.ascontiguousarray(np.atleast_1d(np.asarray(eta, dtype=np.float64)))
+        per = 1 if eta_a.size == n and n != 1 else 0
+        hit = np.zeros(n, np.uint8)
+        t = np.full(n, np.nan)
+        self.lib.ref_batch(kind, n, _ptr(x), _ptr(eta_a), per, _ptr(hit), _ptr(t))
+        return hit, t
+
+    def broadphase(self, kind: int, qstart, qend, faces, eta: float, fixed=None):
+        qstart = np.ascontiguousarray(qstart, dtype=np.float64).ravel()
+        qend = np.ascontiguousarray(qend, dtype=np.float64).ravel()
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        nvf, nee = ctypes.c_int64(), ctypes.c_int64()
+        self.lib.ref_broadphase(kind, qstart.size // 3, _ptr(qstart), _ptr(qend), faces.shape[0], _ptr(faces), eta,
+                                _ptr(fx), ctypes.byref(nvf), ctypes.byref(nee))
+        vf = np.zeros((nvf.value, 4), np.int32)
+        ee = np.zeros((nee.value, 4), np.int32)
+        self.lib.ref_broadphase_get(_ptr(vf), _ptr(ee))
+        return vf, ee
+
+    def narrowphase(self, qstart, qend, vf, vf_eta, ee, ee_eta):
+        qstart = np.ascontiguousarray(qstart, dtype=np.float64).ravel()
+        qend = np.ascontiguousarray(qend, dtype=np.float64).ravel()
+        vf = np.ascontiguousarray(vf, dtype=np.int32).reshape(-1, 4)
+        ee = np.ascontiguousarray(ee, dtype=np.int32).reshape(-1, 4)
+        vfe = np.ascontiguousarray(np.broadcast_to(np.asarray(vf_eta, np.float64), (vf.shape[0],)))
+        eee = np.ascontiguousarray(np.broadcast_to(np.asarray(ee_eta, np.float64), (ee.shape[0],)))
+        vh = np.zeros(vf.shape[0], np.uint8)
+        eh = np.zeros(ee.shape[0], np.uint8)
+        self.lib.ref_narrowphase(qstart.size // 3, _ptr(qstart), _ptr(qend), vf.shape[0], _ptr(vf), _ptr(vfe),
+                                 ee.shape[0], _ptr(ee), _ptr(eee), _ptr(vh), _ptr(eh))
+        return vh, eh

@@ -1,0 +1,146 @@
+// ORACLE / TEST INFRASTRUCTURE ONLY.  Never linked into the product.
+//
+// extern "C" wrapper over the reference library's own, unmodified sources
+// (src/CTCD.cpp, src/History.cpp, src/Mesh.cpp, src/KDOPBroadPhase.cpp,
+// src/AABBBroadPhase.cpp, src/CTCDNarrowPhase.cpp), compiled by
+// oracle/Makefile against the project-written Eigen-API subset.  It exists so
+// that tests/golden/make_golden.py can pin the C restatement (ccd_oracle.c)
+// against the reference itself.  The reference tree is only present in the
+// development container, so this library is never built on the GPU host.
+#include <stdint.h>
+
+#include <set>
+#include <vector>
+
+#include "CTCD.h"
+#include "CTCDNarrowPhase.h"
+#include "History.h"
+#include "KDOPBroadPhase.h"
+#include "Mesh.h"
+
+using Eigen::Vector3d;
+
+// AABBBroadPhase.h and KDOPBroadPhase.h both define a class NodeComparator, so
+// the AABB broad phase is driven from its own translation unit.
+void ref_aabb_candidates(const History &h, const Mesh &m, double eta, std::set<VertexFaceStencil> &vfs,
+                         std::set<EdgeEdgeStencil> &ees, const std::set<int> &fixedVerts);
+
+static Vector3d v3(const double *p) { return Vector3d(p[0], p[1], p[2]); }
+
+extern "C" {
+
+// One call of each primitive test, argument order of include/CTCD.h:36-79.
+// Returns hit (0/1); *t is written only on a hit, as in the reference.
+int ref_vf(const double *x, double eta, double *t) {
+  return CTCD::vertexFaceCTCD(v3(x + 0), v3(x + 3), v3(x + 6), v3(x + 9), v3(x + 12), v3(x + 15), v3(x + 18),
+                              v3(x + 21), eta, *t);
+}
+int ref_ee(const double *x, double eta, double *t) {
+  return CTCD::edgeEdgeCTCD(v3(x + 0), v3(x + 3), v3(x + 6), v3(x + 9), v3(x + 12), v3(x + 15), v3(x + 18),
+                            v3(x + 21), eta, *t);
+}
+int ref_ve(const double *x, double eta, double *t) {
+  return CTCD::vertexEdgeCTCD(v3(x + 0), v3(x + 3), v3(x + 6), v3(x + 9), v3(x + 12), v3(x + 15), eta, *t);
+}
+int ref_vv(const double *x, double eta, double *t) {
+  return CTCD::vertexVertexCTCD(v3(x + 0), v3(x + 3), v3(x + 6), v3(x + 9), eta, *t);
+}
+
+// Batched form: kind 0=VF(24 doubles) 1=EE(24) 2=VE(18) 3=VV(12).
+// eta has n entries when eta_per_test, else one.
+void ref_batch(int kind, int64_t n, const double *x, const double *eta, int eta_per_test, uint8_t *hit,
+               double *t) {
+  static const int width[4] = {24, 24, 18, 12};
+  for (int64_t i = 0; i < n; i++) {
+    const double *xi = x + i * width[kind];
+    double e = eta_per_test ? eta[i] : eta[0];
+    int h = 0;
+    switch (kind) {
+      case 0: h = ref_vf(xi, e, &t[i]); break;
+      case 1: h = ref_ee(xi, e, &t[i]); break;
+      case 2: h = ref_ve(xi, e, &t[i]); break;
+      default: h = ref_vv(xi, e, &t[i]); break;
+    }
+    hit[i] = (uint8_t)h;
+  }
+}
+
+// ---------------------------------------------------------------- mesh path
+static std::vector<int32_t> g_vf, g_ee;
+
+static void build_mesh(int nverts, const double *q, int nfaces, const int32_t *faces, Mesh &m) {
+  m.vertices.resize(3 * nverts);
+  for (int i = 0; i < 3 * nverts; i++) m.vertices[i] = q[i];
+  m.faces.resize(3, nfaces);
+  for (int f = 0; f < nfaces; f++)
+    for (int j = 0; j < 3; j++) m.faces.coeffRef(j, f) = faces[3 * f + j];
+}
+
+static Eigen::VectorXd vecx(int nverts, const double *q) {
+  Eigen::VectorXd v(3 * nverts);
+  for (int i = 0; i < 3 * nverts; i++) v[i] = q[i];
+  return v;
+}
+
+// Runs KDOPBroadPhase (kind 0) or AABBBroadPhase (kind 1) on the 2-entry
+// history (qstart at t=0, qend at t=1).  fixed may be NULL.  Results are kept
+// until ref_broadphase_get copies them out, in std::set iteration order.
+void ref_broadphase(int kind, int nverts, const double *qstart, const double *qend, int nfaces, const int32_t *faces,
+                    double eta, const uint8_t *fixed, int64_t *n_vf, int64_t *n_ee) {
+  Mesh m;
+  build_mesh(nverts, qstart, nfaces, faces, m);
+  History h(vecx(nverts, qstart));
+  h.finishHistory(vecx(nverts, qend));
+  std::set<int> fixedVerts;
+  if (fixed)
+    for (int i = 0; i < nverts; i++)
+      if (fixed[i]) fixedVerts.insert(i);
+  std::set<VertexFaceStencil> vfs;
+  std::set<EdgeEdgeStencil> ees;
+  if (kind == 0) {
+    KDOPBroadPhase bp;
+    bp.findCollisionCandidates(h, m, eta, vfs, ees, fixedVerts);
+  } else {
+    ref_aabb_candidates(h, m, eta, vfs, ees, fixedVerts);
+  }
+  g_vf.clear();
+  g_ee.clear();
+  for (std::set<VertexFaceStencil>::const_iterator it = vfs.begin(); it != vfs.end(); ++it) {
+    g_vf.push_back(it->p); g_vf.push_back(it->q0); g_vf.push_back(it->q1); g_vf.push_back(it->q2);
+  }
+  for (std::set<EdgeEdgeStencil>::const_iterator it = ees.begin(); it != ees.end(); ++it) {
+    g_ee.push_back(it->p0); g_ee.push_back(it->p1); g_ee.push_back(it->q0); g_ee.push_back(it->q1);
+  }
+  *n_vf = (int64_t)(g_vf.size() / 4);
+  *n_ee = (int64_t)(g_ee.size() / 4);
+}
+
+void ref_broadphase_get(int32_t *vf, int32_t *ee) {
+  for (size_t i = 0; i < g_vf.size(); i++) vf[i] = g_vf[i];
+  for (size_t i = 0; i < g_ee.size(); i++) ee[i] = g_ee[i];
+}
+
+// CTCDNarrowPhase::findCollisions over canonical stencils with per-stencil eta;
+// hit[i] = whether stencil i is in the returned set.
+void ref_narrowphase(int nverts, const double *qstart, const double *qend, int64_t n_vf, const int32_t *vf,
+                     const double *vf_eta, int64_t n_ee, const int32_t *ee, const double *ee_eta, uint8_t *vf_hit,
+                     uint8_t *ee_hit) {
+  History h(vecx(nverts, qstart));
+  h.finishHistory(vecx(nverts, qend));
+  std::set<std::pair<VertexFaceStencil, double> > cvf;
+  std::set<std::pair<EdgeEdgeStencil, double> > cee;
+  for (int64_t i = 0; i < n_vf; i++)
+    cvf.insert(std::make_pair(VertexFaceStencil(vf[4 * i], vf[4 * i + 1], vf[4 * i + 2], vf[4 * i + 3]), vf_eta[i]));
+  for (int64_t i = 0; i < n_ee; i++)
+    cee.insert(std::make_pair(EdgeEdgeStencil(ee[4 * i], ee[4 * i + 1], ee[4 * i + 2], ee[4 * i + 3]), ee_eta[i]));
+  std::set<VertexFaceStencil> ovf;
+  std::set<EdgeEdgeStencil> oee;
+  CTCDNarrowPhase np;
+  np.findCollisions(h, cvf, cee, ovf, oee);
+  for (int64_t i = 0; i < n_vf; i++)
+    vf_hit[i] = (uint8_t)ovf.count(VertexFaceStencil(vf[4 * i], vf[4 * i + 1], vf[4 * i + 2], vf[4 * i + 3]));
+  for (int64_t i = 0; i < n_ee; i++)
+    ee_hit[i] = (uint8_t)oee.count(EdgeEdgeStencil(ee[4 * i], ee[4 * i + 1], ee[4 * i + 2], ee[4 * i + 3]));
+}
+
+}  // extern "C"

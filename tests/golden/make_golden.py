@@ -1,0 +1,180 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Runs the reference library's own sources, compiled unmodified by
+``make -C oracle ref`` (oracle/_ref/libccd_ref.so), on seeded inputs and on
+the reference's example meshes, and writes:
+
+* ``kat_testctcd.json`` -- the four hand-built cases of the reference's
+  example/testCTCD.cpp (it prints hit and t; the values here are the ones the
+  reference computes).
+* ``prims.npz`` -- seeded swept primitives of the four kinds (random,
+  near-degenerate and hand-built edge cases) with the reference's hit / t.
+* ``meshes.npz`` -- the two-sphere scene and the reference's start/end mesh
+  pairs meshes/test1.obj -> test2.obj and meshes/V0_prob3_402.obj ->
+  V1_prob3_402.obj, with digests of the reference's k-DOP and AABB candidate
+  sets and its CTCD narrow-phase result.
+
+Only runs where the reference tree exists:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF_TREE = os.environ.get("CCD_REFERENCE_TREE", "/root/reference")
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from collisiondetection_gb300 import workloads as W  # noqa: E402
+import oracle as O  # noqa: E402
+
+
+def digest(*arrays) -> str:
+    h = hashlib.sha256()
+    for a in arrays:
+        a = np.ascontiguousarray(a)
+        h.update(str(a.dtype).encode())
+        h.update(str(a.shape).encode())
+        h.update(a.tobytes())
+    return h.hexdigest()
+
+
+def load_obj(path):
+    """The reference's examples read 'v x y z' and 1-based 'f a b c' lines
+    (example/AlecTest.cpp:9-55)."""
+    V, F = [], []
+    with open(path) as fh:
+        for line in fh:
+            s = line.split()
+            if not s:
+                continue
+            if s[0] == "v":
+                V.append([float(a) for a in s[1:4]])
+            elif s[0] == "f":
+                F.append([int(a) - 1 for a in s[1:4]])
+    return np.array(V, np.float64), np.array(F, np.int32)
+
+
+KAT = [
+    ("ee", [[0, 0, 0], [1, 0, 0], [2, 0, 0], [2, 1, 0], [0, 0, 0], [1, 0, 0], [2, 1, 0], [-1, -1, 0]]),
+    ("vf", [[.5, .5, 1], [0, 0, 0], [1, 0, 0], [0, 1, 0], [.5, .5, 1], [0, 0, 0], [1, 0, 3], [0, 1, 0]]),
+    ("ve", [[.5, 0, 1], [0, 0, 0], [1, 0, 0], [.5, 0, -3], [0, 0, 0], [1, 0, 0]]),
+    ("vv", [[0, 0, 0], [1, 0, 0], [6, 0, 0], [1, 0, 0]]),
+]
+
+
+def edge_cases(kind: int) -> np.ndarray:
+    """Hand-built degenerate inputs for one primitive kind."""
+    k = W.NPTS[kind]
+    rng = np.random.default_rng(1000 + kind)
+    rows = []
+    base_s = rng.uniform(0, 1, size=(k, 3))
+    base_e = base_s + rng.normal(0, 0.1, size=(k, 3))
+    rows.append(np.concatenate([base_s.ravel(), base_s.ravel()]))                     # no motion
+    rows.append(np.zeros(6 * k))                                                        # all points equal
+    pts = np.tile(rng.uniform(0, 1, size=3), (k, 1))
+    rows.append(np.concatenate([pts.ravel(), (pts + rng.normal(0, .1, 3)).ravel()]))    # all coincide, move together
+    flat_s, flat_e = base_s.copy(), base_e.copy()
+    flat_s[:, 2] = 0.25
+    flat_e[:, 2] = 0.25
+    rows.append(np.concatenate([flat_s.ravel(), flat_e.ravel()]))                       # exactly coplanar (z const)
+    line_s = np.outer(np.linspace(0, 1, k), [1, 2, 3]) * 0.3
+    rows.append(np.concatenate([line_s.ravel(), (line_s + 0.1).ravel()]))               # collinear, translating
+    rows.append(np.concatenate([base_s.ravel() * 1e3, base_e.ravel() * 1e3]))           # large coordinates
+    rows.append(np.concatenate([base_s.ravel() * 1e-3, base_e.ravel() * 1e-3]))         # small coordinates
+    rows.append(np.concatenate([base_s.ravel() + 1e3, base_e.ravel() + 1e3]))           # far from origin
+    sw = base_s.copy()
+    sw[0] = base_e[0]
+    rows.append(np.concatenate([base_s.ravel(), sw.ravel()]))                           # one point jumps
+    if kind == W.KIND_VF:
+        tri = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float)
+        for z0, z1 in ((1, -1), (0, 0), (1e-7, -1e-7), (5e-7, 5e-7), (0, 1)):
+            for xy in ((0.2, 0.2), (1.0, 0.0), (0.5, 0.5), (2, 2)):
+                v0 = np.array([xy[0], xy[1], z0])
+                v1 = np.array([xy[0], xy[1], z1])
+                rows.append(np.concatenate([np.vstack([v0, tri]).ravel(), np.vstack([v1, tri]).ravel()]))
+    if kind == W.KIND_EE:
+        for dz in (1e-7, 0.0, 5e-7, 2e-6):
+            e0 = np.array([[0, 0, 0], [1, 0, 0]], float)
+            e1s = np.array([[0.5, -1, 1], [0.5, 1, 1]], float)
+            e1e = np.array([[0.5, -1, -1], [0.5, 1, -1]], float)
+            rows.append(np.concatenate([np.vstack([e0, e1s]).ravel(), np.vstack([e0, e1e]).ravel()]))
+            par_s = np.array([[0, 0, 0], [1, 0, 0], [0, 0, dz], [1, 0, dz]], float)      # parallel edges
+            rows.append(np.concatenate([par_s.ravel(), (par_s + [0, 0.1, 0]).ravel()]))
+            rows.append(np.concatenate([par_s.ravel(), par_s.ravel()]))
+    return np.array(rows, np.float64)
+
+
+def main() -> None:
+    if not os.path.isdir(REF_TREE):
+        sys.exit(f"reference tree not found at {REF_TREE}")
+    O.build(ref=True)
+    ref = O.Reference()
+
+    kat = []
+    for name, pts in KAT:
+        h, t = ref.prim(name, pts, 1e-6)
+        kat.append({"kind": name, "points": pts, "eta": 1e-6, "hit": h, "t": t, "t_hex": float(t).hex()})
+    with open(os.path.join(HERE, "kat_testctcd.json"), "w") as fh:
+        json.dump(kat, fh, indent=1)
+
+    sizes = {W.KIND_VF: 1200, W.KIND_EE: 1200, W.KIND_VE: 600, W.KIND_VV: 600}
+    out = {}
+    for kind, n in sizes.items():
+        x = np.concatenate([W.primitive_batch(kind, n, seed=20240 + kind), edge_cases(kind)])
+        rng = np.random.default_rng(77 + kind)
+        eta = np.full(x.shape[0], 1e-6)
+        pick = rng.permutation(x.shape[0])
+        eta[pick[: x.shape[0] // 10]] = 1e-3
+        eta[pick[x.shape[0] // 10: x.shape[0] // 5]] = 0.0
+        hit, t = ref.batch(kind, x, eta)
+        out[f"x{kind}"] = x
+        out[f"eta{kind}"] = eta
+        out[f"hit{kind}"] = hit
+        out[f"t{kind}"] = t
+    np.savez_compressed(os.path.join(HERE, "prims.npz"), **out)
+
+    meshes = {}
+    qs, qe, f = W.two_spheres(seed=1)
+    meshes["spheres"] = (qs, qe, f, 1e-6)
+    v0, f0 = load_obj(os.path.join(REF_TREE, "meshes", "test1.obj"))
+    v1, _ = load_obj(os.path.join(REF_TREE, "meshes", "test2.obj"))
+    meshes["test12"] = (v0.ravel(), v1.ravel(), f0, 1e-6)
+    v0, f0 = load_obj(os.path.join(REF_TREE, "meshes", "V0_prob3_402.obj"))
+    v1, _ = load_obj(os.path.join(REF_TREE, "meshes", "V1_prob3_402.obj"))
+    meshes["prob3"] = (v0.ravel(), v1.ravel(), f0, 1e-8)
+
+    arrays, meta = {}, {}
+    for name, (qs, qe, f, eta) in meshes.items():
+        arrays[f"{name}_qstart"] = qs
+        arrays[f"{name}_qend"] = qe
+        arrays[f"{name}_faces"] = f
+        fixed = np.zeros(qs.size // 3, np.uint8)
+        fixed[: qs.size // 6] = 1
+        arrays[f"{name}_fixed"] = fixed
+        entry = {"eta": eta}
+        for kind, label in ((0, "kdop"), (1, "aabb")):
+            for fx_label, fx in (("", None), ("_fixed", fixed)):
+                vf, ee = ref.broadphase(kind, qs, qe, f, eta, fx)
+                entry[f"{label}{fx_label}"] = {"n_vf": int(vf.shape[0]), "n_ee": int(ee.shape[0]),
+                                               "digest": digest(vf, ee)}
+        vf, ee = ref.broadphase(0, qs, qe, f, eta)
+        vh, eh = ref.narrowphase(qs, qe, vf, eta, ee, eta)
+        arrays[f"{name}_hit_vf"] = vf[vh.astype(bool)]
+        arrays[f"{name}_hit_ee"] = ee[eh.astype(bool)]
+        entry["narrow"] = {"n_vf_hit": int(vh.sum()), "n_ee_hit": int(eh.sum()), "digest": digest(vh, eh)}
+        meta[name] = entry
+    np.savez_compressed(os.path.join(HERE, "meshes.npz"), **arrays)
+    with open(os.path.join(HERE, "meshes.json"), "w") as fh:
+        json.dump(meta, fh, indent=1, sort_keys=True)
+    print("wrote", sorted(os.listdir(HERE)))
+
+
+if __name__ == "__main__":
+    main()

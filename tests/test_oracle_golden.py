@@ -1,0 +1,88 @@
+"""The C restatement (oracle/) against fixtures produced by the reference's
+own sources (tests/golden/make_golden.py).  CPU only."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+
+def _digest(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        a = np.ascontiguousarray(a)
+        h.update(str(a.dtype).encode())
+        h.update(str(a.shape).encode())
+        h.update(a.tobytes())
+    return h.hexdigest()
+
+
+def test_testctcd_known_answers(oracle, golden_dir):
+    kat = json.load(open(os.path.join(golden_dir, "kat_testctcd.json")))
+    assert len(kat) == 4
+    for case in kat:
+        h, t = oracle.prim(case["kind"], case["points"], case["eta"])
+        assert h == case["hit"] == 1
+        assert float(t).hex() == case["t_hex"]
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2, 3])
+def test_primitives_bit_exact(oracle, golden_dir, kind):
+    g = np.load(os.path.join(golden_dir, "prims.npz"))
+    x, eta, hit, t = g[f"x{kind}"], g[f"eta{kind}"], g[f"hit{kind}"], g[f"t{kind}"]
+    h2, t2 = oracle.batch(kind, x, eta)
+    np.testing.assert_array_equal(h2, hit)
+    same = (t2.view(np.uint64) == t.view(np.uint64)) | (np.isnan(t) & np.isnan(t2))
+    assert same.all(), np.nonzero(~same)[0][:10]
+    assert hit.sum() > 0 and (hit == 0).sum() > 0
+
+
+def test_threaded_batch_matches_serial(oracle, golden_dir):
+    g = np.load(os.path.join(golden_dir, "prims.npz"))
+    for kind in range(4):
+        h1, t1 = oracle.batch(kind, g[f"x{kind}"], g[f"eta{kind}"], nthreads=1)
+        h4, t4 = oracle.batch(kind, g[f"x{kind}"], g[f"eta{kind}"], nthreads=4)
+        np.testing.assert_array_equal(h1, h4)
+        np.testing.assert_array_equal(t1, t4)
+
+
+@pytest.mark.parametrize("mesh", ["test12", "prob3", "spheres"])
+def test_broadphase_candidate_sets(oracle, golden_dir, mesh):
+    meta = json.load(open(os.path.join(golden_dir, "meshes.json")))[mesh]
+    g = np.load(os.path.join(golden_dir, "meshes.npz"))
+    qs, qe, f, fixed = g[f"{mesh}_qstart"], g[f"{mesh}_qend"], g[f"{mesh}_faces"], g[f"{mesh}_fixed"]
+    for kind, label in ((0, "kdop"), (1, "aabb")):
+        for fx_label, fx in (("", None), ("_fixed", fixed)):
+            vf, ee = oracle.broadphase(kind, qs, qe, f, meta["eta"], fx)
+            exp = meta[f"{label}{fx_label}"]
+            assert (vf.shape[0], ee.shape[0]) == (exp["n_vf"], exp["n_ee"])
+            assert _digest(vf, ee) == exp["digest"]
+
+
+@pytest.mark.parametrize("mesh", ["test12", "prob3", "spheres"])
+def test_narrowphase_colliding_set(oracle, golden_dir, mesh):
+    meta = json.load(open(os.path.join(golden_dir, "meshes.json")))[mesh]
+    g = np.load(os.path.join(golden_dir, "meshes.npz"))
+    qs, qe, f = g[f"{mesh}_qstart"], g[f"{mesh}_qend"], g[f"{mesh}_faces"]
+    eta = meta["eta"]
+    vf, ee = oracle.broadphase(0, qs, qe, f, eta)
+    out = oracle.narrowphase(qs, qe, vf, eta, ee, eta, nthreads=2)
+    assert _digest(out["vf_hit"], out["ee_hit"]) == meta["narrow"]["digest"]
+    np.testing.assert_array_equal(vf[out["vf_hit"].astype(bool)], g[f"{mesh}_hit_vf"])
+    np.testing.assert_array_equal(ee[out["ee_hit"].astype(bool)], g[f"{mesh}_hit_ee"])
+    # every hit reports which test in the chain fired and a time
+    assert (out["vf_which"][out["vf_hit"] == 1] >= 0).all()
+    assert np.isfinite(out["ee_t"][out["ee_hit"] == 1]).all()
+
+
+def test_stencil_canonical_forms(oracle):
+    import ctypes
+
+    r = (ctypes.c_int32 * 4)()
+    oracle.lib.oracle_vf_canon(7, 9, 3, 5, r)
+    assert list(r) == [7, 3, 5, 9]
+    oracle.lib.oracle_ee_canon(9, 4, 2, 8, r)
+    assert list(r) == [2, 8, 4, 9]
+    oracle.lib.oracle_ee_canon(1, 4, 8, 2, r)
+    assert list(r) == [1, 4, 2, 8]
