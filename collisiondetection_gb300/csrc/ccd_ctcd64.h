@@ -1,0 +1,887 @@
+// FP64 continuous-time collision tests, op-for-op with the reference
+// (evouga/collisiondetection src/CTCD.cpp and src/rpoly.h).
+//
+// Every expression keeps the reference's evaluation order with one IEEE
+// rounding per operation (no contraction: see ccd_common.h).  Vector algebra
+// follows the Eigen contract: dot = (a0*b0 + a1*b1) + a2*b2, cross = component
+// formula.  The only departures are
+//  * exp/log in the root bound are correctly rounded (ccd_math.h) where the
+//    reference calls the host C library;
+//  * cos/sin of the constant 94-degree shift rotation are folded to constants;
+//  * the two root-bound loops that never end on non-finite coefficients
+//    (src/rpoly.h:151-158, 163-173) are capped; hitting the cap sets
+//    kStatusRootLimit and reports the polynomial as having no roots.
+#pragma once
+
+#include "ccd_common.h"
+#include "ccd_math.h"
+
+namespace ccd {
+
+// ------------------------------------------------------------------ 3-vectors
+struct v3d {
+  double x, y, z;
+};
+CCD_HD v3d ld3(const double *p) { return v3d{p[0], p[1], p[2]}; }
+CCD_HD v3d operator+(v3d a, v3d b) { return v3d{a.x + b.x, a.y + b.y, a.z + b.z}; }
+CCD_HD v3d operator-(v3d a, v3d b) { return v3d{a.x - b.x, a.y - b.y, a.z - b.z}; }
+CCD_HD v3d operator*(double s, v3d a) { return v3d{s * a.x, s * a.y, s * a.z}; }
+CCD_HD double dot(v3d a, v3d b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+CCD_HD v3d cross(v3d a, v3d b) {
+  return v3d{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+CCD_HD double norm(v3d a) { return sqrt(dot(a, a)); }
+
+// ------------------------------------------------------------------ time spans
+// TimeInterval (include/CTCD.h:7-26): endpoints ordered, clamped to [0,1].
+struct Span {
+  double l, u;
+};
+CCD_HD Span make_span(double a, double b) {
+  if (a > b) {
+    double t = a;
+    a = b;
+    b = t;
+  }
+  return Span{smax(a, 0.0), smin(b, 1.0)};
+}
+CCD_HD bool meet(Span a, Span b) { return !(a.l > b.u || b.l > a.u); }
+
+// At most deg+1 <= 7 segments come out of one polynomial.
+struct SpanList {
+  int n;
+  Span s[7];
+  CCD_HD void clear() { n = 0; }
+  CCD_HD void push(double a, double b) { s[n++] = make_span(a, b); }
+};
+
+// Overlap / intersection over a fixed set of spans (TimeInterval::overlap and
+// ::intersect, src/CTCD.cpp:15-36).
+template <int K>
+CCD_HD bool all_meet(const Span (&s)[K]) {
+CCD_UNROLL
+  for (int i = 0; i < K; i++)
+CCD_UNROLL
+    for (int j = i + 1; j < K; j++)
+      if (!meet(s[i], s[j])) return false;
+  return true;
+}
+template <int K>
+CCD_HD double common_lo(const Span (&s)[K]) {
+  double l = 0.0;
+CCD_UNROLL
+  for (int i = 0; i < K; i++) l = smax(s[i].l, l);
+  return l;
+}
+
+// ------------------------------------------------------------------ quadratics
+// CTCD::getQuadRoots (src/CTCD.cpp:38-56).
+CCD_HD int quad_roots(double a, double b, double c, double &t0, double &t1) {
+  int sign = (b < 0) ? -1 : 1;
+  double disc = b * b - 4 * a * c;
+  if (disc >= 0) {
+    double q = -0.5 * (b + sign * sqrt(disc));
+    t0 = q / a;
+    t1 = c / q;
+    if (t0 > t1) {
+      double t = t0;
+      t0 = t1;
+      t1 = t;
+    }
+    return 2;
+  }
+  return 0;
+}
+
+// CTCD::checkInterval (src/CTCD.cpp:59-79).
+CCD_HD void keep_if_sign(double t1, double t2, const double *op, int degree, SpanList &out, bool want_pos) {
+  t1 = smax(0.0, t1);
+  t2 = smax(0.0, t2);
+  t1 = smin(1.0, t1);
+  t2 = smin(1.0, t2);
+  double tm = (t2 + t1) / 2;
+  double f = op[0];
+  for (int i = 1; i <= degree; i++) {
+    f *= tm;
+    f += op[i];
+  }
+  if (want_pos ? (f >= 0) : (f <= 0)) out.push(t1, t2);
+}
+
+// CTCD::couldHaveRoots (src/CTCD.cpp:81-94).
+CCD_HD bool sign_possible(const double *op, int degree, bool want_pos) {
+  double acc = 0;
+  if (want_pos ? (op[0] > 0) : (op[0] < 0)) acc = op[0];
+  for (int i = 1; i < degree; i++) {
+    acc *= 1.0;
+    if (want_pos ? (op[i] > 0) : (op[i] < 0)) acc += op[i];
+  }
+  acc *= 1.0;
+  acc += op[degree];
+  return !(want_pos ? (acc < 0) : (acc > 0));
+}
+
+// std::sort on <= 16 doubles in libstdc++ is an insertion sort; the same
+// permutation is reproduced for root lists that contain NaN.
+CCD_HD void sort_roots(double *a, int n) {
+  for (int i = 1; i < n; i++) {
+    double v = a[i];
+    if (v < a[0]) {
+      for (int j = i; j > 0; j--) a[j] = a[j - 1];
+      a[0] = v;
+    } else {
+      int j = i;
+      while (v < a[j - 1]) {
+        a[j] = a[j - 1];
+        j--;
+      }
+      a[j] = v;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ Jenkins-Traub
+// Three-stage real-polynomial root finder (ACM TOMS 493) as vendored by the
+// reference in C. Bond's C translation (src/rpoly.h).  Same numerical steps,
+// constants and iteration limits; the goto structure is written as loops.
+struct RootFinder {
+  double p[7], qp[7], k[7], qk[7], svk[7];
+  double sr, u, v, a, b, c, d, a1, a3, a7, e, f, g, h;
+  double szr, szi, lzr, lzi;
+  int n;
+
+  static constexpr double kEps = 2.22e-16;  // are = mre = eta in the reference
+
+  // p / (x^2 + u x + v): quotient q, remainder (ra, rb)  (rpoly.h:680-695)
+  CCD_HD static void divide(int nn, double u, double v, const double *p, double *q, double &ra, double &rb) {
+    double bb = p[0];
+    q[0] = bb;
+    double aa = p[1] - bb * u;
+    q[1] = aa;
+    for (int i = 2; i <= nn; i++) {
+      double cc = p[i] - aa * u - bb * v;
+      q[i] = cc;
+      bb = aa;
+      aa = cc;
+    }
+    ra = aa;
+    rb = bb;
+  }
+
+  // zeros of a z^2 + b1 z + c  (rpoly.h:702-754)
+  CCD_HD static void quadratic(double a, double b1, double c, double &sr, double &si, double &lr, double &li) {
+    if (a == 0.0) {
+      sr = (b1 != 0.0) ? -c / b1 : 0.0;
+      lr = 0.0;
+      si = 0.0;
+      li = 0.0;
+      return;
+    }
+    if (c == 0.0) {
+      sr = 0.0;
+      lr = -b1 / a;
+      si = 0.0;
+      li = 0.0;
+      return;
+    }
+    double b = b1 / 2.0, d, e;
+    if (fabs(b) < fabs(c)) {
+      e = (c < 0.0) ? -a : a;
+      e = b * (b / fabs(c)) - e;
+      d = sqrt(fabs(e)) * sqrt(fabs(c));
+    } else {
+      e = 1.0 - (a / b) * (c / b);
+      d = sqrt(fabs(e)) * fabs(b);
+    }
+    if (e < 0.0) {
+      sr = -b / a;
+      lr = sr;
+      si = fabs(d / a);
+      li = -si;
+    } else {
+      if (b >= 0.0) d = -d;
+      lr = (-b + d) / a;
+      sr = 0.0;
+      if (lr != 0.0) sr = (c / lr) / a;
+      si = 0.0;
+      li = 0.0;
+    }
+  }
+
+  // rpoly.h:566-597
+  CCD_HD int scalars() {
+    divide(n - 1, u, v, k, qk, c, d);
+    if (!(fabs(c) > fabs(k[n - 1] * 100.0 * kEps)) && !(fabs(d) > fabs(k[n - 2] * 100.0 * kEps))) return 3;
+    if (fabs(d) < fabs(c)) {
+      e = a / c;
+      f = d / c;
+      g = u * e;
+      h = v * b;
+      a3 = a * e + (h / c + g) * b;
+      a1 = b - a * (d / c);
+      a7 = a + g * d + h * f;
+      return 1;
+    }
+    e = a / d;
+    f = c / d;
+    g = u * b;
+    h = v * b;
+    a3 = (a + g) * e + h * (b / d);
+    a1 = b * f - a;
+    a7 = (f + u) * a + h;
+    return 2;
+  }
+
+  // rpoly.h:601-636
+  CCD_HD void next_k(int type) {
+    if (type == 3) {
+      k[0] = 0.0;
+      k[1] = 0.0;
+      for (int i = 2; i < n; i++) k[i] = qk[i - 2];
+      return;
+    }
+    double ref = (type == 1) ? b : a;
+    if (fabs(a1) <= fabs(ref) * kEps * 10.0) {
+      k[0] = 0.0;
+      k[1] = -a7 * qp[0];
+      for (int i = 2; i < n; i++) k[i] = a3 * qk[i - 2] - a7 * qp[i - 1];
+      return;
+    }
+    a7 /= a1;
+    a3 /= a1;
+    k[0] = qp[0];
+    k[1] = qp[1] - a7 * qp[0];
+    for (int i = 2; i < n; i++) k[i] = a3 * qk[i - 2] - a7 * qp[i - 1] + qp[i];
+  }
+
+  // rpoly.h:640-675
+  CCD_HD void estimate(int type, double &uu, double &vv) const {
+    if (type == 3) {
+      uu = 0.0;
+      vv = 0.0;
+      return;
+    }
+    double a4, a5;
+    if (type == 2) {
+      a4 = (a + g) * f + h;
+      a5 = (f + u) * c + v * d;
+    } else {
+      a4 = a + u * b + h * f;
+      a5 = c + (u + v * f) * d;
+    }
+    double b1 = -k[n - 1] / p[n];
+    double b2 = -(k[n - 2] + b1 * p[n - 1]) / p[n];
+    double c1 = v * b2 * a1;
+    double c2 = b1 * a7;
+    double c3 = b1 * b1 * a3;
+    double c4 = c1 - c2 - c3;
+    double den = a5 + b1 * a4 - c4;
+    if (den == 0.0) {
+      uu = 0.0;
+      vv = 0.0;
+      return;
+    }
+    uu = u - (u * (c3 + c2) + v * (b1 * a1 + b2 * a7)) / den;
+    vv = v * (1.0 + c4 / den);
+  }
+
+  // One real zero by the variable-shift iteration (rpoly.h:473-558).
+  CCD_HD int real_iter(double &sx, bool &near_double) {
+    double pv, kv, t = 0, x = sx, mp, omp = 0, ee;
+    near_double = false;
+    for (int j = 1;; j++) {
+      pv = p[0];
+      qp[0] = pv;
+      for (int i = 1; i <= n; i++) {
+        pv = pv * x + p[i];
+        qp[i] = pv;
+      }
+      mp = fabs(pv);
+      double ms = fabs(x);
+      ee = (kEps / (kEps + kEps)) * fabs(qp[0]);
+      for (int i = 1; i <= n; i++) ee = ee * ms + fabs(qp[i]);
+      if (mp <= 20.0 * ((kEps + kEps) * ee - kEps * mp)) {
+        szr = x;
+        szi = 0.0;
+        return 1;
+      }
+      if (j > 10) return 0;
+      if (j >= 2 && !(fabs(t) > 0.001 * fabs(x - t) || mp < omp)) {
+        near_double = true;
+        sx = x;
+        return 0;
+      }
+      omp = mp;
+      kv = k[0];
+      qk[0] = kv;
+      for (int i = 1; i < n; i++) {
+        kv = kv * x + k[i];
+        qk[i] = kv;
+      }
+      if (fabs(kv) <= fabs(k[n - 1]) * 10.0 * kEps) {
+        k[0] = 0.0;
+        for (int i = 1; i < n; i++) k[i] = qk[i - 1];
+      } else {
+        t = -pv / kv;
+        k[0] = qp[0];
+        for (int i = 1; i < n; i++) k[i] = t * qk[i - 1] + qp[i];
+      }
+      kv = k[0];
+      for (int i = 1; i < n; i++) kv = kv * x + k[i];
+      t = 0.0;
+      if (fabs(kv) > fabs(k[n - 1] * 10.0 * kEps)) t = -pv / kv;
+      x += t;
+    }
+  }
+
+  // A quadratic factor by the variable-shift iteration (rpoly.h:390-467).
+  CCD_HD int quad_iter(double uu, double vv) {
+    double ui, vi, mp, omp = 0, ee, relstp = 0, t, zm;
+    int tried = 0, j = 0;
+    u = uu;
+    v = vv;
+    for (;;) {
+      quadratic(1.0, u, v, szr, szi, lzr, lzi);
+      if (fabs(fabs(szr) - fabs(lzr)) > 0.01 * fabs(lzr)) return 0;
+      divide(n, u, v, p, qp, a, b);
+      mp = fabs(a - szr * b) + fabs(szi * b);
+      zm = sqrt(fabs(v));
+      ee = 2.0 * fabs(qp[0]);
+      t = -szr * b;
+      for (int i = 1; i < n; i++) ee = ee * zm + fabs(qp[i]);
+      ee = ee * zm + fabs(a + t);
+      ee *= (5.0 * kEps + 4.0 * kEps);
+      ee = ee - (5.0 * kEps + 2.0 * kEps) * (fabs(a + t) + fabs(b) * zm) + 2.0 * kEps * fabs(t);
+      if (mp <= 20.0 * ee) return 2;
+      j++;
+      if (j > 20) return 0;
+      if (j >= 2 && !(relstp > 0.01 || mp < omp || tried)) {
+        if (relstp < kEps) relstp = kEps;
+        relstp = sqrt(relstp);
+        u = u - u * relstp;
+        v = v + v * relstp;
+        divide(n, u, v, p, qp, a, b);
+        for (int i = 0; i < 5; i++) next_k(scalars());
+        tried = 1;
+        j = 0;
+      }
+      omp = mp;
+      next_k(scalars());
+      int type = scalars();
+      estimate(type, ui, vi);
+      if (vi == 0.0) return 0;
+      relstp = fabs((vi - v) / vi);
+      u = ui;
+      v = vi;
+    }
+  }
+
+  // Fixed-shift stage, then variable-shift iterations (rpoly.h:277-383).
+  CCD_HD int fixed_shift(int l2, double oss_init) {
+    double svu = 0, svv = 0, ui, vi, xs = 0;
+    double betas = 0.25, betav = 0.25, oss = oss_init, ovv = v, ss, vv, ts, tv;
+    double ots = 0, otv = 0;
+    divide(n, u, v, p, qp, a, b);
+    int type = scalars();
+    for (int j = 0; j < l2; j++) {
+      next_k(type);
+      type = scalars();
+      estimate(type, ui, vi);
+      vv = vi;
+      ss = 0.0;
+      if (k[n - 1] != 0.0) ss = -p[n] / k[n - 1];
+      tv = 1.0;
+      ts = 1.0;
+      if (j != 0 && type != 3) {
+        if (vv != 0.0) tv = fabs((vv - ovv) / vv);
+        if (ss != 0.0) ts = fabs((ss - oss) / ss);
+        double tvv = (tv < otv) ? tv * otv : 1.0;
+        double tss = (ts < ots) ? ts * ots : 1.0;
+        bool vpass = tvv < betav, spass = tss < betas;
+        if (spass || vpass) {
+          svu = u;
+          svv = v;
+          for (int i = 0; i < n; i++) svk[i] = k[i];
+          xs = ss;
+          bool vtried = false, stried = false;
+          int step = ((spass && !vpass) || tss < tvv) ? 1 : 0;  // 0 quadratic, 1 linear, 2 restore
+          for (;;) {
+            if (step == 0) {
+              int nz = quad_iter(ui, vi);
+              if (nz > 0) return nz;
+              vtried = true;
+              betav *= 0.25;
+              if (stried || !spass) {
+                step = 2;
+                continue;
+              }
+              for (int i = 0; i < n; i++) k[i] = svk[i];
+              step = 1;
+            } else if (step == 1) {
+              bool near_double;
+              int nz = real_iter(xs, near_double);
+              if (nz > 0) return nz;
+              stried = true;
+              betas *= 0.25;
+              if (!near_double) {
+                step = 2;
+                continue;
+              }
+              ui = -(xs + xs);
+              vi = xs * xs;
+              step = 0;
+            } else {
+              u = svu;
+              v = svv;
+              for (int i = 0; i < n; i++) k[i] = svk[i];
+              if (vpass && !vtried) {
+                step = 0;
+                continue;
+              }
+              divide(n, u, v, p, qp, a, b);
+              type = scalars();
+              break;
+            }
+          }
+        }
+      }
+      ovv = vv;
+      oss = ss;
+      otv = tv;
+      ots = ts;
+    }
+    return 0;
+  }
+
+  // Driver (rpoly.h:49-261).  Returns the number of zeros found (real parts in
+  // zr), or -1.  Only the real parts are kept: the caller ignores the rest.
+  CCD_HD int solve(const double *op, int degree, double *zr, uint8_t &status) {
+    const double infin = 3.4e38, smalno = 1.2e-38;
+    const double lo = smalno / kEps;
+    const double cosr = -0x1.1db902ec147e0p-4;  // cos(94.0 * 0.017453293)
+    const double sinr = 0x1.fec0b6fc05f20p-1;   // sin(94.0 * 0.017453293)
+    double xx = 0x1.6a09e667f3bcdp-1;           // sqrt(0.5)
+    double yy = -xx;
+    double temp[7], pt[7];
+    n = degree;
+    if (op[0] == 0.0) return -1;
+    while (op[n] == 0.0) {
+      zr[degree - n] = 0.0;
+      n--;
+    }
+    if (n < 1) return -1;
+    for (int i = 0; i <= n; i++) p[i] = op[i];
+
+    while (n > 0) {
+      if (n == 1) {
+        zr[degree - 1] = -p[1] / p[0];
+        n = 0;
+        break;
+      }
+      if (n == 2) {
+        double si, li;
+        quadratic(p[0], p[1], p[2], zr[degree - 2], si, zr[degree - 1], li);
+        n = 0;
+        break;
+      }
+      double maxc = 0.0, minc = infin, x, xm, ff, df, dx;
+      for (int i = 0; i <= n; i++) {
+        x = fabs(p[i]);
+        if (x > maxc) maxc = x;
+        if (x != 0.0 && x < minc) minc = x;
+      }
+      double sc = lo / minc;
+      bool keep = (sc > 1.0 && infin / sc < maxc) || (sc <= 1.0 && maxc < 10.0);
+      if (!keep) {
+        if (sc == 0.0) sc = smalno;
+        int l = (int)(cr_log(sc) / 0x1.62e42fefa39efp-1 + 0.5);  // log(sc) / log(2.0)
+        double factor = ldexp(1.0, l);                            // pow(2.0, l), exact
+        if (factor != 1.0)
+          for (int i = 0; i <= n; i++) p[i] = factor * p[i];
+      }
+      for (int i = 0; i <= n; i++) pt[i] = fabs(p[i]);
+      pt[n] = -pt[n];
+      x = cr_exp((cr_log(-pt[n]) - cr_log(pt[0])) / (double)n);
+      if (pt[n - 1] != 0.0) {
+        xm = -pt[n] / pt[n - 1];
+        if (xm < x) x = xm;
+      }
+      for (int it = 0;; it++) {
+        if (it >= 4096) {
+          status |= kStatusRootLimit;
+          return -1;
+        }
+        xm = x * 0.1;
+        ff = pt[0];
+        for (int i = 1; i <= n; i++) ff = ff * xm + pt[i];
+        if (ff <= 0.0) break;
+        x = xm;
+      }
+      dx = x;
+      for (int it = 0; fabs(dx / x) > 0.005; it++) {
+        if (it >= 4096) {
+          status |= kStatusRootLimit;
+          return -1;
+        }
+        ff = pt[0];
+        df = ff;
+        for (int i = 1; i < n; i++) {
+          ff = ff * x + pt[i];
+          df = df * x + ff;
+        }
+        ff = ff * x + pt[n];
+        dx = ff / df;
+        x -= dx;
+      }
+      double bnd = x;
+      int nm1 = n - 1;
+      for (int i = 1; i < n; i++) k[i] = (double)(n - i) * p[i] / (double)n;
+      k[0] = p[0];
+      double aa = p[n], bb = p[n - 1];
+      bool zerok = (k[n - 1] == 0);
+      for (int jj = 0; jj < 5; jj++) {
+        double cc = k[n - 1];
+        if (!zerok) {
+          double t = -aa / cc;
+          for (int i = 0; i < nm1; i++) {
+            int j = n - i - 1;
+            k[j] = t * k[j - 1] + p[j];
+          }
+          k[0] = p[0];
+          zerok = (fabs(k[n - 1]) <= fabs(bb) * kEps * 10.0);
+        } else {
+          for (int i = 0; i < nm1; i++) {
+            int j = n - i - 1;
+            k[j] = k[j - 1];
+          }
+          k[0] = 0.0;
+          zerok = (k[n - 1] == 0.0);
+        }
+      }
+      for (int i = 0; i < n; i++) temp[i] = k[i];
+      bool found = false;
+      for (int cnt = 0; cnt < 20; cnt++) {
+        double xxx = cosr * xx - sinr * yy;
+        yy = sinr * xx + cosr * yy;
+        xx = xxx;
+        sr = bnd * xx;
+        u = -2.0 * sr;
+        v = bnd;
+        int nz = fixed_shift(20 * (cnt + 1), sr);
+        if (nz != 0) {
+          int j = degree - n;
+          zr[j] = szr;
+          n -= nz;
+          for (int i = 0; i <= n; i++) p[i] = qp[i];
+          if (nz != 1) zr[j + 1] = lzr;
+          found = true;
+          break;
+        }
+        for (int i = 0; i < n; i++) k[i] = temp[i];
+      }
+      if (!found) break;
+    }
+    return degree - n;
+  }
+};
+
+// ------------------------------------------------------------------ sign intervals
+// CTCD::findIntervals (src/CTCD.cpp:98-177): sub-intervals of [0,1] on which
+// the polynomial op (descending powers, degree n <= 6) is >= 0 (want_pos) or
+// <= 0.  op is normalised in place, as in the reference.
+CCD_HDI inline void sign_spans(double *op, int n, SpanList &out, bool want_pos, uint8_t &status) {
+  int roots = 0, deg = n;
+  double tr[6];
+  double maxval = 0;
+  for (int i = 0; i <= n; i++) maxval = smax(maxval, fabs(op[i]));
+  if (maxval != 0)
+    for (int i = 0; i <= n; i++) op[i] /= maxval;
+  for (int i = 0; i < n; i++) {
+    if (op[i] == 0)
+      deg--;
+    else
+      break;
+  }
+  if (deg < n)
+    for (int i = 0; i <= deg; i++) op[i] = op[i + n - deg];
+  if (deg > 2) {
+    if (!sign_possible(op, deg, want_pos)) return;
+    RootFinder rf;
+    roots = rf.solve(op, deg, tr, status);
+  } else if (deg == 2) {
+    roots = quad_roots(op[0], op[1], op[2], tr[0], tr[1]);
+  } else if (deg == 1) {
+    tr[0] = -op[1] / op[0];
+    roots = 1;
+  } else {
+    if (want_pos ? (op[0] >= 0) : (op[0] <= 0)) out.push(0, 1.0);
+    return;
+  }
+  if (roots > 0) {
+    sort_roots(tr, roots);
+    if (tr[0] >= 0) keep_if_sign(0, tr[0], op, deg, out, want_pos);
+    for (int i = 0; i < roots - 1; i++)
+      if (!((tr[i] < 0 && tr[i + 1] < 0) || (tr[i] > 1.0 && tr[i + 1] > 1.0)))
+        keep_if_sign(tr[i], tr[i + 1], op, deg, out, want_pos);
+    if (tr[roots - 1] <= 1.0) keep_if_sign(tr[roots - 1], 1.0, op, deg, out, want_pos);
+  } else {
+    keep_if_sign(0.0, 1.0, op, deg, out, want_pos);
+  }
+}
+
+// ------------------------------------------------------------------ polynomials
+// CTCD::barycentricPoly3D (src/CTCD.cpp:179-213), quartic, want_pos.
+CCD_HDI inline void bary_spans(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d v30, SpanList &out,
+                               uint8_t &status) {
+  double A = dot(x10, x10);
+  double B = 2 * dot(x10, v10);
+  double C = dot(v10, v10);
+  double D = dot(x20, x10);
+  double E = dot(x20, v10) + dot(v20, x10);
+  double F = dot(v20, v10);
+  double G = dot(x30, x20);
+  double H = dot(x30, v20) + dot(v30, x20);
+  double I = dot(v30, v20);
+  double J = dot(x30, x10);
+  double K = dot(x30, v10) + dot(v30, x10);
+  double L = dot(v30, v10);
+  double op[5];
+  op[0] = F * L - C * I;
+  op[1] = F * K + E * L - C * H - B * I;
+  op[2] = F * J + D * L + E * K - C * G - A * I - B * H;
+  op[3] = D * K + E * J - A * H - B * G;
+  op[4] = D * J - A * G;
+  out.clear();
+  sign_spans(op, 4, out, true, status);
+}
+
+// CTCD::planePoly3D (src/CTCD.cpp:215-229), cubic, want_pos.
+CCD_HDI inline void plane_spans(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d v30, SpanList &out,
+                                uint8_t &status) {
+  double op[4];
+  v3d vv = cross(v20, v30);
+  op[0] = dot(v10, vv);
+  op[1] = dot(x10, vv) + dot(v10, cross(x20, v30)) + dot(v10, cross(v20, x30));
+  op[2] = dot(x10, cross(x20, v30)) + dot(x10, cross(v20, x30)) + dot(v10, cross(x20, x30));
+  op[3] = dot(x10, cross(x20, x30));
+  out.clear();
+  sign_spans(op, 3, out, true, status);
+}
+
+// CTCD::distancePoly3D (src/CTCD.cpp:231-257), sextic, want_neg.
+CCD_HDI inline void dist_spans(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d v30, double minD, SpanList &out,
+                               uint8_t &status) {
+  v3d G = cross(v20, v30);
+  v3d xv = cross(x20, v30), vx = cross(v20, x30);
+  v3d E = cross(x20, x30);
+  double A = dot(v10, G);
+  double B = dot(x10, G) + dot(v10, xv) + dot(v10, vx);
+  double C = dot(x10, xv) + dot(x10, vx) + dot(v10, E);
+  double D = dot(x10, E);
+  v3d F = xv + vx;
+  double op[7];
+  op[0] = A * A;
+  op[1] = 2 * A * B;
+  op[2] = B * B + 2 * A * C - dot(G, G) * minD;
+  op[3] = 2 * A * D + 2 * B * C - 2 * dot(G, F) * minD;
+  op[4] = 2 * B * D + C * C - (2 * dot(G, E) + dot(F, F)) * minD;
+  op[5] = 2 * C * D - 2 * dot(F, E) * minD;
+  op[6] = D * D - dot(E, E) * minD;
+  out.clear();
+  sign_spans(op, 6, out, false, status);
+}
+
+// ------------------------------------------------------------------ primitive tests
+// CTCD::edgeEdgeCTCD (src/CTCD.cpp:259-411).  x: q0s p0s q1s p1s q0e p0e q1e p1e.
+CCD_HDI inline bool ee_ctcd(const double *x, double eta, double &tout, uint8_t &status) {
+  v3d q0s = ld3(x), p0s = ld3(x + 3), q1s = ld3(x + 6), p1s = ld3(x + 9);
+  v3d q0e = ld3(x + 12), p0e = ld3(x + 15), q1e = ld3(x + 18), p1e = ld3(x + 21);
+  double minD = eta * eta;
+  v3d vp0 = p0e - p0s, vp1 = p1e - p1s, vq0 = q0e - q0s, vq1 = q1e - q1s;
+  SpanList raw, cop, par, a0, a1, b0, b1;
+  dist_spans(p0s - p1s, p0s - q0s, p1s - q1s, vp0 - vp1, vp0 - vq0, vp1 - vq1, minD, raw, status);
+  cop.clear();
+  par.clear();
+  for (int i = 0; i < raw.n; i++) {
+    double midt = (raw.s[i].u + raw.s[i].l) / 2;
+    v3d e0 = (q0s - p0s) + midt * (vq0 - vp0);
+    v3d e1 = (q1s - p1s) + midt * (vq1 - vp1);
+    if (norm(cross(e0, e1)) < 1e-8)
+      par.s[par.n++] = raw.s[i];
+    else
+      cop.s[cop.n++] = raw.s[i];
+  }
+  if (cop.n == 0) return false;
+  v3d x10 = p1s - q1s, v10 = vp1 - vq1;
+  bary_spans(x10, p0s - q0s, q0s - q1s, v10, vp0 - vq0, vq0 - vq1, a0, status);
+  if (a0.n == 0) return false;
+  bary_spans(x10, q0s - p0s, p0s - q1s, v10, vq0 - vp0, vp0 - vq1, a1, status);
+  if (a1.n == 0) return false;
+  x10 = p0s - q0s;
+  v10 = vp0 - vq0;
+  bary_spans(x10, p1s - q1s, q1s - q0s, v10, vp1 - vq1, vq1 - vq0, b0, status);
+  if (b0.n == 0) return false;
+  bary_spans(x10, q1s - p1s, p1s - q0s, v10, vq1 - vp1, vp1 - vq0, b1, status);
+  if (b1.n == 0) return false;
+  bool hit = false;
+  double mint = 1.0;
+  for (int i = 0; i < cop.n; i++)
+    for (int j = 0; j < a0.n; j++)
+      for (int k = 0; k < a1.n; k++)
+        for (int l = 0; l < b0.n; l++)
+          for (int m = 0; m < b1.n; m++) {
+            Span set[5] = {cop.s[i], a0.s[j], a1.s[k], b0.s[l], b1.s[m]};
+            if (!all_meet(set)) continue;
+            Span isect{common_lo(set), 1.0};
+            double u = 1.0;
+            for (int q = 0; q < 5; q++) u = smin(set[q].u, u);
+            isect.u = u;
+            bool skip = false;
+            for (int q = 0; q < par.n; q++)
+              if (meet(isect, par.s[q])) {
+                skip = true;
+                break;
+              }
+            if (!skip) {
+              mint = smin(mint, isect.l);
+              hit = true;
+            }
+          }
+  if (hit) tout = mint;
+  return hit;
+}
+
+// CTCD::vertexFaceCTCD (src/CTCD.cpp:413-508).  x: q0s..q3s q0e..q3e.
+CCD_HDI inline bool vf_ctcd(const double *x, double eta, double &tout, uint8_t &status) {
+  v3d q0s = ld3(x), q1s = ld3(x + 3), q2s = ld3(x + 6), q3s = ld3(x + 9);
+  double minD = eta * eta;
+  v3d v0 = ld3(x + 12) - q0s, v1 = ld3(x + 15) - q1s, v2 = ld3(x + 18) - q2s, v3 = ld3(x + 21) - q3s;
+  SpanList cop, e1, e2, e3;
+  plane_spans(q0s - q1s, cross(q3s - q1s, q2s - q1s), q3s - q1s, v0 - v1, cross(v3 - v1, v2 - v1), v3 - v1, e1,
+              status);
+  if (e1.n == 0) return false;
+  plane_spans(q0s - q2s, cross(q1s - q2s, q3s - q2s), q1s - q2s, v0 - v2, cross(v1 - v2, v3 - v2), v1 - v2, e2,
+              status);
+  if (e2.n == 0) return false;
+  plane_spans(q0s - q3s, cross(q2s - q3s, q1s - q3s), q2s - q3s, v0 - v3, cross(v2 - v3, v1 - v3), v2 - v3, e3,
+              status);
+  if (e3.n == 0) return false;
+  dist_spans(q0s - q1s, q2s - q1s, q3s - q1s, v0 - v1, v2 - v1, v3 - v1, minD, cop, status);
+  if (cop.n == 0) return false;
+  bool hit = false;
+  double mint = 1.0;
+  for (int i = 0; i < cop.n; i++)
+    for (int j = 0; j < e1.n; j++)
+      for (int k = 0; k < e2.n; k++)
+        for (int l = 0; l < e3.n; l++) {
+          Span set[4] = {cop.s[i], e1.s[j], e2.s[k], e3.s[l]};
+          if (all_meet(set)) {
+            mint = smin(common_lo(set), mint);
+            hit = true;
+          }
+        }
+  if (hit) tout = mint;
+  return hit;
+}
+
+// CTCD::vertexEdgeCTCD (src/CTCD.cpp:511-602).  x: q0s q1s q2s q0e q1e q2e.
+CCD_HDI inline bool ve_ctcd(const double *x, double eta, double &tout, uint8_t &status) {
+  v3d q0s = ld3(x), q1s = ld3(x + 3), q2s = ld3(x + 6);
+  double minD = eta * eta;
+  v3d v0 = ld3(x + 9) - q0s, v1 = ld3(x + 12) - q1s, v2 = ld3(x + 15) - q2s;
+  v3d ab = q2s - q1s, ac = q0s - q1s, cb = q2s - q0s;
+  v3d vab = v2 - v1, vac = v0 - v1, vcb = v2 - v0;
+  SpanList colin, e1, e2;
+  double op[5];
+  op[0] = dot(vab, vac);
+  op[1] = dot(ac, vab) + dot(ab, vac);
+  op[2] = dot(ab, ac);
+  e1.clear();
+  sign_spans(op, 2, e1, true, status);
+  if (e1.n == 0) return false;
+  op[0] = dot(vab, vcb);
+  op[1] = dot(cb, vab) + dot(ab, vcb);
+  op[2] = dot(ab, cb);
+  e2.clear();
+  sign_spans(op, 2, e2, true, status);
+  if (e2.n == 0) return false;
+  double A = dot(ab, ab);
+  double B = 2 * dot(ab, vab);
+  double C = dot(vab, vab);
+  double D = dot(ac, ac);
+  double E = 2 * dot(ac, vac);
+  double F = dot(vac, vac);
+  double G = dot(ac, ab);
+  double H = dot(vab, ac) + dot(vac, ab);
+  double I = dot(vab, vac);
+  op[4] = A * D - G * G - minD * A;
+  op[3] = B * D + A * E - 2 * G * H - minD * B;
+  op[2] = B * E + A * F + C * D - H * H - 2 * G * I - minD * C;
+  op[1] = B * F + C * E - 2 * H * I;
+  op[0] = C * F - I * I;
+  colin.clear();
+  sign_spans(op, 4, colin, false, status);
+  if (colin.n == 0) return false;
+  bool hit = false;
+  double mint = 1.0;
+  for (int i = 0; i < colin.n; i++)
+    for (int j = 0; j < e1.n; j++)
+      for (int k = 0; k < e2.n; k++) {
+        Span set[3] = {colin.s[i], e1.s[j], e2.s[k]};
+        if (all_meet(set)) {
+          mint = smin(common_lo(set), mint);
+          hit = true;
+        }
+      }
+  if (hit) tout = mint;
+  return hit;
+}
+
+// CTCD::vertexVertexCTCD (src/CTCD.cpp:604-692).  x: q1s q2s q1e q2e.  The
+// reported time is the raw root and may lie outside [0,1].
+CCD_HDI inline bool vv_ctcd(const double *x, double eta, double &tout) {
+  v3d q1s = ld3(x), q2s = ld3(x + 3);
+  v3d v1 = ld3(x + 6) - q1s, v2 = ld3(x + 9) - q2s;
+  double min_d = eta * eta;
+  double t1 = 0, t2 = 0;
+  int roots;
+  double a = dot(v1, v1) + dot(v2, v2) - 2 * dot(v1, v2);
+  double b = 2 * (dot(v1, q1s) - dot(v2, q1s) - dot(v1, q2s) + dot(v2, q2s));
+  double c = dot(q1s, q1s) + dot(q2s, q2s) - 2 * dot(q1s, q2s) - min_d;
+  if (a != 0) {
+    roots = quad_roots(a, b, c, t1, t2);
+  } else if (b != 0) {
+    t1 = -c / b;
+    roots = 1;
+  } else {
+    if (c <= 0) {
+      tout = 0;
+      return true;
+    }
+    return false;
+  }
+  double op[3] = {a, b, c};
+  SpanList iv;
+  iv.clear();
+  if (roots == 2) {
+    keep_if_sign(0, t1, op, 2, iv, false);
+    if (iv.n) { tout = 0; return true; }
+    keep_if_sign(t1, t2, op, 2, iv, false);
+    if (iv.n) { tout = t1; return true; }
+    keep_if_sign(t2, 1.0, op, 2, iv, false);
+    if (iv.n) { tout = t2; return true; }
+    return false;
+  }
+  if (roots == 1) {
+    keep_if_sign(0, t1, op, 2, iv, false);
+    if (iv.n) { tout = 0; return true; }
+    keep_if_sign(t1, 1.0, op, 2, iv, false);
+    if (iv.n) { tout = t1; return true; }
+    return false;
+  }
+  keep_if_sign(0, 1.0, op, 2, iv, false);
+  if (iv.n) { tout = 0; return true; }
+  return false;
+}
+
+}  // namespace ccd

@@ -1,0 +1,145 @@
+"""Primitive CTCD kernels on the GPU through the C ABI, against the golden
+fixtures (produced by the reference itself) and the oracle.
+
+Parity bar: identical hit flags; contact times within 1e-12 relative (the
+reference's host exp/log are not correctly rounded on ~0.1% of inputs, the
+device ones are, so a contact time may differ in the last bits)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import collisiondetection_gb300 as C
+
+pytestmark = pytest.mark.gpu
+
+KINDS = [C.VERTEX_FACE, C.EDGE_EDGE, C.VERTEX_EDGE, C.VERTEX_VERTEX]
+PATHS = [C.PATH_FP64, C.PATH_CULL_REFINE]
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from collisiondetection_gb300 import build as B
+
+    B.build_library()
+    c = C.Context(0)
+    yield c
+    c.close()
+
+
+def _assert_same(h, t, h_ref, t_ref, what):
+    bad = np.nonzero(h != h_ref)[0]
+    assert bad.size == 0, f"{what}: hit differs at rows {bad[:10]}"
+    m = h_ref == 1
+    rel = np.abs(t[m] - t_ref[m]) / np.maximum(np.abs(t_ref[m]), 1e-300)
+    assert not m.any() or rel.max() <= TOL, f"{what}: contact time off by {rel.max():.3g}"
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("path", PATHS)
+def test_golden_fixtures(ctx, golden_dir, kind, path):
+    g = np.load(os.path.join(golden_dir, "prims.npz"))
+    h, t = ctx.prim_batch(kind, g[f"x{kind}"], g[f"eta{kind}"], path=path)
+    _assert_same(h, t, g[f"hit{kind}"], g[f"t{kind}"], f"kind {kind} path {path}")
+    st = ctx.stats()
+    assert st["hits"] == int(g[f"hit{kind}"].sum()) and st["status_flags"] == 0
+
+
+def test_testctcd_known_answers_single_calls(ctx, golden_dir):
+    kat = json.load(open(os.path.join(golden_dir, "kat_testctcd.json")))
+    kinds = {"vf": C.VERTEX_FACE, "ee": C.EDGE_EDGE, "ve": C.VERTEX_EDGE, "vv": C.VERTEX_VERTEX}
+    for case in kat:
+        h, t = ctx.single(kinds[case["kind"]], case["points"], case["eta"])
+        assert h == case["hit"] == 1
+        assert abs(t - case["t"]) <= TOL * abs(case["t"])
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_random_batches_match_oracle(ctx, oracle, kind):
+    rows = C.workloads.primitive_batch(kind, 100000, seed=2024)
+    h_ref, t_ref = oracle.batch(kind, rows, 1e-6, nthreads=os.cpu_count() or 4)
+    for path in PATHS:
+        h, t = ctx.prim_batch(kind, rows, 1e-6, path=path)
+        _assert_same(h, t, h_ref, t_ref, f"kind {kind} path {path}")
+
+
+@pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE])
+def test_cull_refine_equals_fp64_at_scale(ctx, kind):
+    # Size-independent property at a size the oracle does not finish quickly:
+    # the FP32 stage never changes a result, and rejects most rows.
+    rows = C.workloads.primitive_batch(kind, 2_000_000, seed=99)
+    h64, t64 = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_FP64)
+    assert ctx.stats()["survivors"] == rows.shape[0]
+    h32, t32 = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_CULL_REFINE)
+    st = ctx.stats()
+    np.testing.assert_array_equal(h32, h64)
+    np.testing.assert_array_equal(t32[h64 == 1], t64[h64 == 1])
+    assert st["survivors"] < 0.4 * rows.shape[0]
+    assert st["hits"] == int(h64.sum())
+
+
+def test_t_untouched_on_miss_and_eta_per_row(ctx):
+    rows = C.workloads.primitive_batch(C.VERTEX_FACE, 5000, seed=5)
+    sentinel = np.full(rows.shape[0], -7.25)
+    h, t = ctx.prim_batch(C.VERTEX_FACE, rows, 1e-6, t=sentinel)
+    assert np.all(t[h == 0] == -7.25)
+    assert np.all(t[h == 1] >= 0.0)
+    eta = np.full(rows.shape[0], 1e-6)
+    h2, t2 = ctx.prim_batch(C.VERTEX_FACE, rows, eta, t=sentinel)
+    np.testing.assert_array_equal(h, h2)
+    np.testing.assert_array_equal(t, t2)
+
+
+def test_device_entry_point_matches_host(ctx):
+    torch = pytest.importorskip("torch")
+    rows = C.workloads.primitive_batch(C.EDGE_EDGE, 50000, seed=8)
+    h_ref, t_ref = ctx.prim_batch(C.EDGE_EDGE, rows, 1e-6)
+    d_rows = torch.from_numpy(rows).cuda()
+    d_eta = torch.full((1,), 1e-6, dtype=torch.float64, device="cuda")
+    d_hit = torch.zeros(rows.shape[0], dtype=torch.uint8, device="cuda")
+    d_t = torch.full((rows.shape[0],), float("nan"), dtype=torch.float64, device="cuda")
+    d_st = torch.zeros(rows.shape[0], dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    ctx.prim_batch_device(C.EDGE_EDGE, rows.shape[0], d_rows.data_ptr(), d_eta.data_ptr(), 1, d_hit.data_ptr(),
+                          d_t.data_ptr(), d_st.data_ptr())
+    ctx.synchronize()
+    np.testing.assert_array_equal(d_hit.cpu().numpy(), h_ref)
+    np.testing.assert_array_equal(d_t.cpu().numpy()[h_ref == 1], t_ref[h_ref == 1])
+    assert int(d_st.sum()) == 0
+    assert ctx.stats()["hits"] == int(h_ref.sum())
+
+
+def test_profiling_timings(ctx):
+    rows = C.workloads.primitive_batch(C.VERTEX_FACE, 200000, seed=6)
+    ctx.set_profiling(True)
+    ctx.prim_batch(C.VERTEX_FACE, rows, 1e-6, path=C.PATH_CULL_REFINE)
+    tm = ctx.timings()
+    ctx.set_profiling(False)
+    assert tm["launches"] == 2 and tm["cull_ms"] > 0 and tm["refine_ms"] > 0
+
+
+def test_empty_and_invalid_batches(ctx):
+    h, t = ctx.prim_batch(C.VERTEX_FACE, np.zeros((0, 24)), 1e-6)
+    assert h.size == 0
+    rows = C.workloads.primitive_batch(C.VERTEX_FACE, 10, seed=1)
+    with pytest.raises(C.CcdError):
+        ctx.prim_batch(C.VERTEX_FACE, rows, np.full(3, 1e-6))  # eta_count neither 1 nor n
+    with pytest.raises(C.CcdError):
+        ctx.prim_batch(7, rows, 1e-6)
+
+
+def test_nonfinite_rows_terminate(ctx):
+    # The reference loops forever on NaN coefficients (src/rpoly.h:151-158);
+    # the device code caps that loop and reports it through the status bits.
+    rows = C.workloads.primitive_batch(C.VERTEX_FACE, 64, seed=3)
+    rows[::2, 5] = np.nan
+    rows[1::4, 20] = np.inf
+    for path in PATHS:
+        h, _ = ctx.prim_batch(C.VERTEX_FACE, rows, 1e-6, path=path)
+        st = ctx.stats()
+        assert st["rows"] == 64
+    good = C.workloads.primitive_batch(C.VERTEX_FACE, 64, seed=3)
+    h2, _ = ctx.prim_batch(C.VERTEX_FACE, good, 1e-6)
+    assert ctx.stats()["status_flags"] == 0
