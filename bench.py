@@ -207,7 +207,10 @@ def run_ours(args, rank, world, local, pg):
     rows_per_step = n_vf + n_ee
 
     ctx = C.Context(local)
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: the context launches on it and the events below are
+    # recorded on it (handle 0, the legacy stream, selects the context's own).
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     d = {}
     for name, arr in (("vf", vf), ("ee", ee)):

@@ -9,6 +9,7 @@
 
 #include "../../include/ccd_gb300.h"
 #include "narrow.cuh"
+#include "stages.cuh"
 
 #define CCD_VERSION_NUMBER 100  // 0.1.0
 
@@ -16,6 +17,16 @@ namespace {
 
 // Rows per chunk of the host-memory batch pipeline (two chunks in flight).
 constexpr int64_t kChunkRows = 1 << 20;
+// Survivor rows per tile of the staged refinement (bounds its scratch to
+// about 0.9 GB per execution slot).
+constexpr int64_t kStageTileRows = 1 << 20;
+
+// Scratch of the staged refinement, grown on demand.
+struct StageBuf {
+  void *mem = nullptr;
+  int64_t cap = 0;
+  ccd::StageScratch view{};
+};
 
 struct Slot {
   double *rows = nullptr;
@@ -28,6 +39,7 @@ struct Slot {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
   int64_t cap = 0;
+  StageBuf stage;
 };
 
 // Events bracketing the kernels of one batch (profiling only).
@@ -35,6 +47,7 @@ struct PhaseEvents {
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   bool used = false;
   bool culled = false;
+  int stage_launches = 0;
 };
 
 }  // namespace
@@ -46,6 +59,7 @@ struct ccd_context {
   cudaStream_t stream = nullptr;
   Slot slot[2];
   // scratch for the device-memory entry points
+  StageBuf stage;
   int32_t *d_surv = nullptr;
   int64_t surv_cap = 0;
   ccd::BatchCounters *d_counters = nullptr;
@@ -79,6 +93,18 @@ int cuda_fail(ccd_context *ctx, cudaError_t e, const char *what) {
     if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
   } while (0)
 
+int ensure_stage(ccd_context *ctx, StageBuf &sb, int64_t rows, cudaStream_t s) {
+  int64_t cap = std::min<int64_t>(std::max<int64_t>(rows, 1), kStageTileRows);
+  if (sb.cap >= cap) return CCD_OK;
+  CCD_CUDA(cudaStreamSynchronize(s));
+  cudaFree(sb.mem);
+  sb = StageBuf{};
+  CCD_CUDA(cudaMalloc(&sb.mem, ccd::stage_scratch_bytes(cap)));
+  sb.cap = cap;
+  sb.view = ccd::stage_scratch_view(sb.mem, cap);
+  return CCD_OK;
+}
+
 int free_slot(ccd_context *ctx, Slot &s) {
   cudaFree(s.rows);
   cudaFree(s.eta);
@@ -87,6 +113,7 @@ int free_slot(ccd_context *ctx, Slot &s) {
   cudaFree(s.surv);
   cudaFree(s.counters);
   cudaFreeHost(s.h_counters);
+  cudaFree(s.stage.mem);
   cudaStream_t stream = s.stream;
   cudaEvent_t done = s.done;
   s = Slot{};
@@ -140,7 +167,7 @@ int collect_phase(ccd_context *ctx, PhaseEvents &pe) {
     CCD_CUDA(cudaEventElapsedTime(&b, pe.ev[1], pe.ev[2]));
     ctx->timings.cull_ms += a;
     ctx->timings.refine_ms += b;
-    ctx->timings.launches += 2;
+    ctx->timings.launches += 1 + pe.stage_launches;
   } else {
     ctx->timings.refine_ms += a;
     ctx->timings.launches += 1;
@@ -150,8 +177,8 @@ int collect_phase(ccd_context *ctx, PhaseEvents &pe) {
 }
 
 // Enqueues the kernels of one batch whose buffers are all on the device.
-int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *surv, cudaStream_t s,
-                  PhaseEvents *pe) {
+int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *surv, StageBuf &stage,
+                  cudaStream_t s, PhaseEvents *pe) {
   CCD_CUDA(cudaMemsetAsync(b.counters, 0, sizeof(ccd::BatchCounters), s));
   if (pe) {
     int rc = ensure_phase_events(ctx, *pe);
@@ -165,10 +192,14 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     CCD_CUDA(ccd::launch_prims_fp64(b, ctx->num_sms, s));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[1], s));
   } else {
+    int rc = ensure_stage(ctx, stage, b.n, s);
+    if (rc) return rc;
     CCD_CUDA(ccd::launch_prims_cull(b, surv, ctx->num_sms, s));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[1], s));
-    CCD_CUDA(ccd::launch_prims_refine(b, surv, ctx->num_sms, s));
+    int launches = 0;
+    CCD_CUDA(ccd::launch_stages(b, surv, stage.view, ctx->num_sms, s, &launches));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[2], s));
+    if (pe) pe->stage_launches = launches;
   }
   if (pe) {
     pe->used = true;
@@ -262,6 +293,7 @@ int ccd_context_destroy(ccd_context *ctx) {
   for (auto &pe : ctx->dev_ring)
     for (auto &e : pe.ev)
       if (e) cudaEventDestroy(e);
+  cudaFree(ctx->stage.mem);
   cudaFree(ctx->d_surv);
   cudaFree(ctx->d_counters);
   cudaFreeHost(ctx->h_counters);
@@ -343,7 +375,7 @@ int ccd_prim_batch_device(ccd_context *ctx, int kind, int path, int64_t n, const
     }
   }
   ccd::PrimBatch b{kind, n, rows, eta, eta_count == n && n != 1, hit, t, status, ctx->d_counters};
-  rc = enqueue_batch(ctx, b, path, ctx->d_surv, ctx->stream, pe);
+  rc = enqueue_batch(ctx, b, path, ctx->d_surv, ctx->stage, ctx->stream, pe);
   if (rc) return rc;
   CCD_CUDA(cudaMemcpyAsync(ctx->h_counters, ctx->d_counters, sizeof(ccd::BatchCounters), cudaMemcpyDeviceToHost,
                            ctx->stream));
@@ -386,7 +418,7 @@ int ccd_prim_batch(ccd_context *ctx, int kind, int path, int64_t n, const double
     // t is written only where hit: start from the caller's values.
     CCD_CUDA(cudaMemcpyAsync(s.t, t + off, (size_t)m * sizeof(double), cudaMemcpyHostToDevice, s.stream));
     ccd::PrimBatch b{kind, m, s.rows, s.eta, per_row, s.hit, s.t, nullptr, s.counters};
-    rc = enqueue_batch(ctx, b, path, s.surv, s.stream, ctx->profiling ? &ctx->phase[c & 1] : nullptr);
+    rc = enqueue_batch(ctx, b, path, s.surv, s.stage, s.stream, ctx->profiling ? &ctx->phase[c & 1] : nullptr);
     if (rc) return rc;
     CCD_CUDA(cudaMemcpyAsync(hit + off, s.hit, (size_t)m, cudaMemcpyDeviceToHost, s.stream));
     CCD_CUDA(cudaMemcpyAsync(t + off, s.t, (size_t)m * sizeof(double), cudaMemcpyDeviceToHost, s.stream));

@@ -14,11 +14,15 @@
 #define CCD_HD __host__ __device__ __forceinline__
 #define CCD_HDI __host__ __device__
 #define CCD_UNROLL _Pragma("unroll")
+// One out-of-line copy of large routines keeps the kernels' instruction
+// footprint small (the root finder and exp/log are called from many sites).
+#define CCD_NOINLINE __host__ __device__ __noinline__ inline
 #else
 #include <cmath>
 #define CCD_HD inline
 #define CCD_HDI
 #define CCD_UNROLL
+#define CCD_NOINLINE __attribute__((noinline)) inline
 #endif
 
 namespace ccd {

@@ -455,7 +455,7 @@ struct RootFinder {
 
   // Driver (rpoly.h:49-261).  Returns the number of zeros found (real parts in
   // zr), or -1.  Only the real parts are kept: the caller ignores the rest.
-  CCD_HD int solve(const double *op, int degree, double *zr, uint8_t &status) {
+  CCD_NOINLINE int solve(const double *op, int degree, double *zr, uint8_t &status) {
     const double infin = 3.4e38, smalno = 1.2e-38;
     const double lo = smalno / kEps;
     const double cosr = -0x1.1db902ec147e0p-4;  // cos(94.0 * 0.017453293)
@@ -586,12 +586,14 @@ struct RootFinder {
 };
 
 // ------------------------------------------------------------------ sign intervals
-// CTCD::findIntervals (src/CTCD.cpp:98-177): sub-intervals of [0,1] on which
-// the polynomial op (descending powers, degree n <= 6) is >= 0 (want_pos) or
-// <= 0.  op is normalised in place, as in the reference.
-CCD_HDI inline void sign_spans(double *op, int n, SpanList &out, bool want_pos, uint8_t &status) {
-  int roots = 0, deg = n;
-  double tr[6];
+// CTCD::findIntervals (src/CTCD.cpp:98-177), in three pieces so that the
+// staged kernels can run the root finder as a separate job:
+//   reduce_poly   normalise by max|c| and drop exactly-zero leading terms;
+//   low_degree_spans / root_spans   the two ways the spans are produced.
+
+// Normalises op (degree n) in place and returns the reduced degree.
+CCD_HD int reduce_poly(double *op, int n) {
+  int deg = n;
   double maxval = 0;
   for (int i = 0; i <= n; i++) maxval = smax(maxval, fabs(op[i]));
   if (maxval != 0)
@@ -604,19 +606,11 @@ CCD_HDI inline void sign_spans(double *op, int n, SpanList &out, bool want_pos, 
   }
   if (deg < n)
     for (int i = 0; i <= deg; i++) op[i] = op[i + n - deg];
-  if (deg > 2) {
-    if (!sign_possible(op, deg, want_pos)) return;
-    RootFinder rf;
-    roots = rf.solve(op, deg, tr, status);
-  } else if (deg == 2) {
-    roots = quad_roots(op[0], op[1], op[2], tr[0], tr[1]);
-  } else if (deg == 1) {
-    tr[0] = -op[1] / op[0];
-    roots = 1;
-  } else {
-    if (want_pos ? (op[0] >= 0) : (op[0] <= 0)) out.push(0, 1.0);
-    return;
-  }
+  return deg;
+}
+
+// Spans from `roots` real root parts tr (unsorted; roots <= 0: none found).
+CCD_HD void root_spans(const double *op, int deg, double *tr, int roots, SpanList &out, bool want_pos) {
   if (roots > 0) {
     sort_roots(tr, roots);
     if (tr[0] >= 0) keep_if_sign(0, tr[0], op, deg, out, want_pos);
@@ -629,10 +623,41 @@ CCD_HDI inline void sign_spans(double *op, int n, SpanList &out, bool want_pos, 
   }
 }
 
+// Spans of a reduced polynomial of degree <= 2.
+CCD_HD void low_degree_spans(const double *op, int deg, SpanList &out, bool want_pos) {
+  double tr[2];
+  int roots;
+  if (deg == 2) {
+    roots = quad_roots(op[0], op[1], op[2], tr[0], tr[1]);
+  } else if (deg == 1) {
+    tr[0] = -op[1] / op[0];
+    roots = 1;
+  } else {
+    if (want_pos ? (op[0] >= 0) : (op[0] <= 0)) out.push(0, 1.0);
+    return;
+  }
+  root_spans(op, deg, tr, roots, out, want_pos);
+}
+
+// Full findIntervals on op (degree n <= 6), normalised in place.
+CCD_NOINLINE void sign_spans(double *op, int n, SpanList &out, bool want_pos, uint8_t &status) {
+  int deg = reduce_poly(op, n);
+  if (deg > 2) {
+    if (!sign_possible(op, deg, want_pos)) return;
+    double tr[6];
+    RootFinder rf;
+    int roots = rf.solve(op, deg, tr, status);
+    root_spans(op, deg, tr, roots, out, want_pos);
+  } else {
+    low_degree_spans(op, deg, out, want_pos);
+  }
+}
+
 // ------------------------------------------------------------------ polynomials
+// Coefficients (descending powers) exactly as the reference forms them.
+
 // CTCD::barycentricPoly3D (src/CTCD.cpp:179-213), quartic, want_pos.
-CCD_HDI inline void bary_spans(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d v30, SpanList &out,
-                               uint8_t &status) {
+CCD_HD void bary_coeffs(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d v30, double *op) {
   double A = dot(x10, x10);
   double B = 2 * dot(x10, v10);
   double C = dot(v10, v10);
@@ -645,32 +670,24 @@ CCD_HDI inline void bary_spans(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d 
   double J = dot(x30, x10);
   double K = dot(x30, v10) + dot(v30, x10);
   double L = dot(v30, v10);
-  double op[5];
   op[0] = F * L - C * I;
   op[1] = F * K + E * L - C * H - B * I;
   op[2] = F * J + D * L + E * K - C * G - A * I - B * H;
   op[3] = D * K + E * J - A * H - B * G;
   op[4] = D * J - A * G;
-  out.clear();
-  sign_spans(op, 4, out, true, status);
 }
 
 // CTCD::planePoly3D (src/CTCD.cpp:215-229), cubic, want_pos.
-CCD_HDI inline void plane_spans(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d v30, SpanList &out,
-                                uint8_t &status) {
-  double op[4];
+CCD_HD void plane_coeffs(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d v30, double *op) {
   v3d vv = cross(v20, v30);
   op[0] = dot(v10, vv);
   op[1] = dot(x10, vv) + dot(v10, cross(x20, v30)) + dot(v10, cross(v20, x30));
   op[2] = dot(x10, cross(x20, v30)) + dot(x10, cross(v20, x30)) + dot(v10, cross(x20, x30));
   op[3] = dot(x10, cross(x20, x30));
-  out.clear();
-  sign_spans(op, 3, out, true, status);
 }
 
 // CTCD::distancePoly3D (src/CTCD.cpp:231-257), sextic, want_neg.
-CCD_HDI inline void dist_spans(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d v30, double minD, SpanList &out,
-                               uint8_t &status) {
+CCD_HD void dist_coeffs(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d v30, double minD, double *op) {
   v3d G = cross(v20, v30);
   v3d xv = cross(x20, v30), vx = cross(v20, x30);
   v3d E = cross(x20, x30);
@@ -679,7 +696,6 @@ CCD_HDI inline void dist_spans(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d 
   double C = dot(x10, xv) + dot(x10, vx) + dot(v10, E);
   double D = dot(x10, E);
   v3d F = xv + vx;
-  double op[7];
   op[0] = A * A;
   op[1] = 2 * A * B;
   op[2] = B * B + 2 * A * C - dot(G, G) * minD;
@@ -687,19 +703,78 @@ CCD_HDI inline void dist_spans(v3d x10, v3d x20, v3d x30, v3d v10, v3d v20, v3d 
   op[4] = 2 * B * D + C * C - (2 * dot(G, E) + dot(F, F)) * minD;
   op[5] = 2 * C * D - 2 * dot(F, E) * minD;
   op[6] = D * D - dot(E, E) * minD;
-  out.clear();
-  sign_spans(op, 6, out, false, status);
 }
 
-// ------------------------------------------------------------------ primitive tests
-// CTCD::edgeEdgeCTCD (src/CTCD.cpp:259-411).  x: q0s p0s q1s p1s q0e p0e q1e p1e.
-CCD_HDI inline bool ee_ctcd(const double *x, double eta, double &tout, uint8_t &status) {
+// The polynomials of one vertex-face row (src/CTCD.cpp:423-472): slots 0-2 are
+// the three edge-side cubics (want >= 0), slot 3 the distance sextic (want <= 0).
+// x: q0s..q3s q0e..q3e.
+struct VFPolys {
+  static constexpr int kSlots = 4;
+  static CCD_HD int degree(int slot) { return slot < 3 ? 3 : 6; }
+  static CCD_HD bool want_pos(int slot) { return slot < 3; }
+  static CCD_HD void coeffs(const double *x, double eta, int slot, double *op) {
+    v3d q0s = ld3(x), q1s = ld3(x + 3), q2s = ld3(x + 6), q3s = ld3(x + 9);
+    v3d v0 = ld3(x + 12) - q0s, v1 = ld3(x + 15) - q1s, v2 = ld3(x + 18) - q2s, v3 = ld3(x + 21) - q3s;
+    if (slot == 0)
+      plane_coeffs(q0s - q1s, cross(q3s - q1s, q2s - q1s), q3s - q1s, v0 - v1, cross(v3 - v1, v2 - v1), v3 - v1, op);
+    else if (slot == 1)
+      plane_coeffs(q0s - q2s, cross(q1s - q2s, q3s - q2s), q1s - q2s, v0 - v2, cross(v1 - v2, v3 - v2), v1 - v2, op);
+    else if (slot == 2)
+      plane_coeffs(q0s - q3s, cross(q2s - q3s, q1s - q3s), q2s - q3s, v0 - v3, cross(v2 - v3, v1 - v3), v2 - v3, op);
+    else
+      dist_coeffs(q0s - q1s, q2s - q1s, q3s - q1s, v0 - v1, v2 - v1, v3 - v1, eta * eta, op);
+  }
+};
+
+// The polynomials of one edge-edge row (src/CTCD.cpp:270-350): slot 0 the
+// distance sextic (want <= 0), slots 1-4 the barycentric quartics a0 a1 b0 b1.
+// x: q0s p0s q1s p1s q0e p0e q1e p1e.
+struct EEPolys {
+  static constexpr int kSlots = 5;
+  static CCD_HD int degree(int slot) { return slot == 0 ? 6 : 4; }
+  static CCD_HD bool want_pos(int slot) { return slot != 0; }
+  static CCD_HD void coeffs(const double *x, double eta, int slot, double *op) {
+    v3d q0s = ld3(x), p0s = ld3(x + 3), q1s = ld3(x + 6), p1s = ld3(x + 9);
+    v3d vp0 = ld3(x + 15) - p0s, vp1 = ld3(x + 21) - p1s, vq0 = ld3(x + 12) - q0s, vq1 = ld3(x + 18) - q1s;
+    if (slot == 0)
+      dist_coeffs(p0s - p1s, p0s - q0s, p1s - q1s, vp0 - vp1, vp0 - vq0, vp1 - vq1, eta * eta, op);
+    else if (slot == 1)
+      bary_coeffs(p1s - q1s, p0s - q0s, q0s - q1s, vp1 - vq1, vp0 - vq0, vq0 - vq1, op);
+    else if (slot == 2)
+      bary_coeffs(p1s - q1s, q0s - p0s, p0s - q1s, vp1 - vq1, vq0 - vp0, vp0 - vq1, op);
+    else if (slot == 3)
+      bary_coeffs(p0s - q0s, p1s - q1s, q1s - q0s, vp0 - vq0, vp1 - vq1, vq1 - vq0, op);
+    else
+      bary_coeffs(p0s - q0s, q1s - p1s, p1s - q0s, vp0 - vq0, vq1 - vp1, vp1 - vq0, op);
+  }
+};
+
+// ------------------------------------------------------------------ interval logic
+// Final decision of vertexFaceCTCD from its four lists (src/CTCD.cpp:477-507).
+CCD_HD bool vf_combine(const SpanList &e1, const SpanList &e2, const SpanList &e3, const SpanList &cop,
+                       double &tout) {
+  if (e1.n == 0 || e2.n == 0 || e3.n == 0 || cop.n == 0) return false;
+  bool hit = false;
+  double mint = 1.0;
+  for (int i = 0; i < cop.n; i++)
+    for (int j = 0; j < e1.n; j++)
+      for (int k = 0; k < e2.n; k++)
+        for (int l = 0; l < e3.n; l++) {
+          Span set[4] = {cop.s[i], e1.s[j], e2.s[k], e3.s[l]};
+          if (all_meet(set)) {
+            mint = smin(common_lo(set), mint);
+            hit = true;
+          }
+        }
+  if (hit) tout = mint;
+  return hit;
+}
+
+// Splits the distance spans of an edge-edge row into non-parallel (cop) and
+// parallel ones (src/CTCD.cpp:291-308).
+CCD_HD void ee_split_parallel(const double *x, const SpanList &raw, SpanList &cop, SpanList &par) {
   v3d q0s = ld3(x), p0s = ld3(x + 3), q1s = ld3(x + 6), p1s = ld3(x + 9);
-  v3d q0e = ld3(x + 12), p0e = ld3(x + 15), q1e = ld3(x + 18), p1e = ld3(x + 21);
-  double minD = eta * eta;
-  v3d vp0 = p0e - p0s, vp1 = p1e - p1s, vq0 = q0e - q0s, vq1 = q1e - q1s;
-  SpanList raw, cop, par, a0, a1, b0, b1;
-  dist_spans(p0s - p1s, p0s - q0s, p1s - q1s, vp0 - vp1, vp0 - vq0, vp1 - vq1, minD, raw, status);
+  v3d vp0 = ld3(x + 15) - p0s, vp1 = ld3(x + 21) - p1s, vq0 = ld3(x + 12) - q0s, vq1 = ld3(x + 18) - q1s;
   cop.clear();
   par.clear();
   for (int i = 0; i < raw.n; i++) {
@@ -711,18 +786,12 @@ CCD_HDI inline bool ee_ctcd(const double *x, double eta, double &tout, uint8_t &
     else
       cop.s[cop.n++] = raw.s[i];
   }
-  if (cop.n == 0) return false;
-  v3d x10 = p1s - q1s, v10 = vp1 - vq1;
-  bary_spans(x10, p0s - q0s, q0s - q1s, v10, vp0 - vq0, vq0 - vq1, a0, status);
-  if (a0.n == 0) return false;
-  bary_spans(x10, q0s - p0s, p0s - q1s, v10, vq0 - vp0, vp0 - vq1, a1, status);
-  if (a1.n == 0) return false;
-  x10 = p0s - q0s;
-  v10 = vp0 - vq0;
-  bary_spans(x10, p1s - q1s, q1s - q0s, v10, vp1 - vq1, vq1 - vq0, b0, status);
-  if (b0.n == 0) return false;
-  bary_spans(x10, q1s - p1s, p1s - q0s, v10, vq1 - vp1, vp1 - vq0, b1, status);
-  if (b1.n == 0) return false;
+}
+
+// Final decision of edgeEdgeCTCD (src/CTCD.cpp:310-410).
+CCD_HD bool ee_combine(const SpanList &cop, const SpanList &par, const SpanList &a0, const SpanList &a1,
+                       const SpanList &b0, const SpanList &b1, double &tout) {
+  if (cop.n == 0 || a0.n == 0 || a1.n == 0 || b0.n == 0 || b1.n == 0) return false;
   bool hit = false;
   double mint = 1.0;
   for (int i = 0; i < cop.n; i++)
@@ -751,37 +820,38 @@ CCD_HDI inline bool ee_ctcd(const double *x, double eta, double &tout, uint8_t &
   return hit;
 }
 
+// ------------------------------------------------------------------ primitive tests
+// One thread per row, with the reference's early exits.
+
+// CTCD::edgeEdgeCTCD (src/CTCD.cpp:259-411).  x: q0s p0s q1s p1s q0e p0e q1e p1e.
+CCD_HDI inline bool ee_ctcd(const double *x, double eta, double &tout, uint8_t &status) {
+  SpanList raw, cop, par, l[4];
+  double op[7];
+  EEPolys::coeffs(x, eta, 0, op);
+  raw.clear();
+  sign_spans(op, 6, raw, false, status);
+  ee_split_parallel(x, raw, cop, par);
+  if (cop.n == 0) return false;
+  for (int s = 0; s < 4; s++) {
+    EEPolys::coeffs(x, eta, s + 1, op);
+    l[s].clear();
+    sign_spans(op, 4, l[s], true, status);
+    if (l[s].n == 0) return false;
+  }
+  return ee_combine(cop, par, l[0], l[1], l[2], l[3], tout);
+}
+
 // CTCD::vertexFaceCTCD (src/CTCD.cpp:413-508).  x: q0s..q3s q0e..q3e.
 CCD_HDI inline bool vf_ctcd(const double *x, double eta, double &tout, uint8_t &status) {
-  v3d q0s = ld3(x), q1s = ld3(x + 3), q2s = ld3(x + 6), q3s = ld3(x + 9);
-  double minD = eta * eta;
-  v3d v0 = ld3(x + 12) - q0s, v1 = ld3(x + 15) - q1s, v2 = ld3(x + 18) - q2s, v3 = ld3(x + 21) - q3s;
-  SpanList cop, e1, e2, e3;
-  plane_spans(q0s - q1s, cross(q3s - q1s, q2s - q1s), q3s - q1s, v0 - v1, cross(v3 - v1, v2 - v1), v3 - v1, e1,
-              status);
-  if (e1.n == 0) return false;
-  plane_spans(q0s - q2s, cross(q1s - q2s, q3s - q2s), q1s - q2s, v0 - v2, cross(v1 - v2, v3 - v2), v1 - v2, e2,
-              status);
-  if (e2.n == 0) return false;
-  plane_spans(q0s - q3s, cross(q2s - q3s, q1s - q3s), q2s - q3s, v0 - v3, cross(v2 - v3, v1 - v3), v2 - v3, e3,
-              status);
-  if (e3.n == 0) return false;
-  dist_spans(q0s - q1s, q2s - q1s, q3s - q1s, v0 - v1, v2 - v1, v3 - v1, minD, cop, status);
-  if (cop.n == 0) return false;
-  bool hit = false;
-  double mint = 1.0;
-  for (int i = 0; i < cop.n; i++)
-    for (int j = 0; j < e1.n; j++)
-      for (int k = 0; k < e2.n; k++)
-        for (int l = 0; l < e3.n; l++) {
-          Span set[4] = {cop.s[i], e1.s[j], e2.s[k], e3.s[l]};
-          if (all_meet(set)) {
-            mint = smin(common_lo(set), mint);
-            hit = true;
-          }
-        }
-  if (hit) tout = mint;
-  return hit;
+  SpanList l[4];
+  double op[7];
+  for (int s = 0; s < 4; s++) {
+    VFPolys::coeffs(x, eta, s, op);
+    l[s].clear();
+    sign_spans(op, VFPolys::degree(s), l[s], VFPolys::want_pos(s), status);
+    if (l[s].n == 0) return false;
+  }
+  return vf_combine(l[0], l[1], l[2], l[3], tout);
 }
 
 // CTCD::vertexEdgeCTCD (src/CTCD.cpp:511-602).  x: q0s q1s q2s q0e q1e q2e.

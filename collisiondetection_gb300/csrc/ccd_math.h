@@ -2,23 +2,27 @@
 //
 // The reference's root finder seeds its root-modulus bound with
 //   exp((log(a) - log(b)) / n)                         (src/rpoly.h:144)
-// evaluated by the host C library.  glibc's exp/log return the correctly
-// rounded result on essentially every input, so the device code computes the
-// correctly rounded value itself and thereby reproduces the host's bits.
+// evaluated by the host C library.  The device code computes the correctly
+// rounded value; glibc agrees with it on all but ~0.1% of inputs (where glibc
+// itself is off by one ulp), and a one-ulp change of the seed moves the roots
+// found by at most a few ulps.
 //
 // Method (written from the mathematics, not from any library):
 //  * arithmetic in double-double (a value is hi + lo, |lo| <= ulp(hi)/2), with
 //    exact products from fma() (Dekker / Knuth error-free transformations);
-//  * log(x):  x = 2^e * m, m in [sqrt(1/2), sqrt(2));  log(m) = 2 atanh(s),
-//    s = (m-1)/(m+1), atanh(s)/s = sum_k s^(2k)/(2k+1)  (|s| <= 0.1716);
-//  * exp(x):  x = k ln2 + r, |r| <= ln2/2;  expm1(r/256) by its Taylor series,
-//    then eight squarings (1+e)^2 - 1 = e (2 + e);  result 2^k (1 + e).
-// Both reach about 2^-96 relative error before the final rounding, so the
-// rounded result is the correctly rounded one unless the exact value lies
-// within ~2^-96 of a rounding boundary.
+//  * fast path, table-driven argument reduction after P. T. P. Tang
+//    ("Table-driven implementation of the exponential / logarithm function in
+//    IEEE floating-point arithmetic", ACM TOMS 1989/1990), evaluated to about
+//    2^-64 relative error, followed by a rounding test: when the error interval
+//    around the approximation rounds to a single double, that double is the
+//    correctly rounded result;
+//  * otherwise (about 0.4% of inputs) the slow path, series in double-double:
+//    log(m) = 2 atanh((m-1)/(m+1)) for m in [sqrt(1/2), sqrt(2)),
+//    exp(r) from expm1(r/256) and eight squarings, about 2^-96 relative error.
 #pragma once
 
 #include "ccd_common.h"
+#include "ccd_math_tables.h"
 
 namespace ccd {
 
@@ -124,7 +128,7 @@ CCD_HD dd inv_fact(int n) {
   }
 }
 
-CCD_HD double cr_log(double x) {
+CCD_NOINLINE double cr_log_slow(double x) {
   if (!(x > 0.0)) return (x == 0.0) ? -HUGE_VAL : (x - x) / (x - x);  // log(0) = -inf; x<0 or NaN -> NaN
   if (x == HUGE_VAL) return x;
   int e;
@@ -145,7 +149,7 @@ CCD_HD double cr_log(double x) {
   return r.hi + r.lo;
 }
 
-CCD_HD double cr_exp(double x) {
+CCD_NOINLINE double cr_exp_slow(double x) {
   if (x != x) return x + x;
   if (x > 710.0) return HUGE_VAL;
   if (x < -746.0) return 0.0;
@@ -170,6 +174,95 @@ CCD_HD double cr_exp(double x) {
   if (d > 0.5 || (d == 0.5 && fmod(n, 2.0) != 0.0)) n += 1.0;
   if (d < -0.5 || (d == -0.5 && fmod(n, 2.0) != 0.0)) n -= 1.0;
   return ldexp(n, -1074);
+}
+
+#if defined(__CUDACC__)
+__device__ const double kLogTable[384] = CCD_LOG_TABLE_DATA;
+__device__ const double kExpTable[64] = CCD_EXP_TABLE_DATA;
+#endif
+static const double kLogTableHost[384] = CCD_LOG_TABLE_DATA;
+static const double kExpTableHost[64] = CCD_EXP_TABLE_DATA;
+#if defined(__CUDA_ARCH__)
+#define CCD_LOG_TAB kLogTable
+#define CCD_EXP_TAB kExpTable
+#else
+#define CCD_LOG_TAB kLogTableHost
+#define CCD_EXP_TAB kExpTableHost
+#endif
+
+// Rounds hi + lo to double when every value within eps of it rounds the same
+// way; returns false when the test is inconclusive.
+CCD_HD bool round_if_certain(dd s, double eps, double &out) {
+  double y1 = s.hi + (s.lo + eps);
+  double y2 = s.hi + (s.lo - eps);
+  out = y1;
+  return y1 == y2;
+}
+
+// log(x), correctly rounded.
+CCD_NOINLINE double cr_log(double x) {
+  if (!(x > 0.0) || x == HUGE_VAL) return cr_log_slow(x);
+  int e;
+  double m = frexp(x, &e) * 2.0;  // x = m 2^(e-1), m in [1, 2); exact
+  e -= 1;
+  int j = (int)((m - 1.0) * 128.0);  // top 7 fraction bits, exact
+  if (j >= 64) {                     // reduce [1.5, 2) as m/2 in [0.75, 1)
+    m *= 0.5;
+    e += 1;
+  }
+  const double *t = CCD_LOG_TAB + 3 * j;
+  dd p = dd_two_prod(m, t[0]);      // m * inv_j, exact
+  dd r = dd_two_sum(p.hi - 1.0, p.lo);  // exact, |r| <= 2^-7
+  double rh = r.hi;
+  // log1p(r) = r - r^2/2 + r^3 (1/3 - r/4 + r^2/5 - ... + r^8/11)
+  double q = 1.0 / 11.0;
+  q = q * rh - 0.1;
+  q = q * rh + 1.0 / 9.0;
+  q = q * rh - 0.125;
+  q = q * rh + 1.0 / 7.0;
+  q = q * rh - 1.0 / 6.0;
+  q = q * rh + 0.2;
+  q = q * rh - 0.25;
+  q = q * rh + 1.0 / 3.0;
+  double tail = ((rh * rh) * rh) * q;
+  dd r2 = dd_mul(r, r);
+  dd lp = dd_add(r, dd{-0.5 * r2.hi, -0.5 * r2.lo});
+  lp = dd_add(lp, dd{tail, 0.0});
+  dd s = dd_add(dd_mul_d(dd{CCD_LN2_HI, CCD_LN2_LO}, (double)e), dd{t[1], t[2]});
+  s = dd_add(s, lp);
+  double y;
+  if (round_if_certain(s, fabs(s.hi) * 0x1p-61, y)) return y;
+  return cr_log_slow(x);
+}
+
+// exp(x), correctly rounded.
+CCD_NOINLINE double cr_exp(double x) {
+  if (!(fabs(x) < 700.0)) return cr_exp_slow(x);  // NaN, inf, near over/underflow
+  double nd = nearbyint(x * CCD_32_OVER_LN2);
+  int n = (int)nd;
+  int j = n & 31;
+  int k = (n - j) / 32;
+  double a = x - nd * CCD_LN2_32_L1;  // exact (Sterbenz; nd * L1 exact)
+  dd r = dd_two_sum(a, -(nd * CCD_LN2_32_L2));
+  r = dd_add(r, dd{-(nd * CCD_LN2_32_L3), 0.0});  // |r| <= ln2/64
+  double rh = r.hi;
+  // expm1(r) = r + r^2/2 + r^3 (1/6 + r/24 + ... + r^5/8!)
+  double q = 1.0 / 40320.0;
+  q = q * rh + 1.0 / 5040.0;
+  q = q * rh + 1.0 / 720.0;
+  q = q * rh + 1.0 / 120.0;
+  q = q * rh + 1.0 / 24.0;
+  q = q * rh + 1.0 / 6.0;
+  double tail = ((rh * rh) * rh) * q;
+  dd r2 = dd_mul(r, r);
+  dd em = dd_add(r, dd{0.5 * r2.hi, 0.5 * r2.lo});
+  em = dd_add(em, dd{tail, 0.0});
+  const double *t = CCD_EXP_TAB + 2 * j;
+  dd tj = dd{t[0], t[1]};
+  dd y = dd_add(tj, dd_mul(tj, em));
+  double out;
+  if (round_if_certain(y, fabs(y.hi) * 0x1p-61, out)) return ldexp(out, k);  // |k| <= 1010: exact
+  return cr_exp_slow(x);
 }
 
 }  // namespace ccd

@@ -34,7 +34,6 @@ cudaError_t launch_prims_fp64(const PrimBatch &b, int num_sms, cudaStream_t s);
 // FP32 conservative rejection: rows that can be excluded get hit = 0; the
 // others are appended to `survivors` (count in counters->survivors).
 cudaError_t launch_prims_cull(const PrimBatch &b, int32_t *survivors, int num_sms, cudaStream_t s);
-// FP64 evaluation of the rows listed in `survivors` (count read on device).
-cudaError_t launch_prims_refine(const PrimBatch &b, const int32_t *survivors, int num_sms, cudaStream_t s);
+// The surviving rows are refined by the staged kernels (stages.cuh).
 
 }  // namespace ccd

@@ -9,8 +9,5 @@ cudaError_t launch_ee_fp64(const PrimBatch &b, int num_sms, cudaStream_t s) {
 cudaError_t launch_ee_cull(const PrimBatch &b, int32_t *list, int num_sms, cudaStream_t s) {
   return kernels::cull<kEE>(b, list, num_sms, s);
 }
-cudaError_t launch_ee_refine(const PrimBatch &b, const int32_t *list, int num_sms, cudaStream_t s) {
-  return kernels::refine<kEE>(b, list, num_sms, s);
-}
 
 }  // namespace ccd

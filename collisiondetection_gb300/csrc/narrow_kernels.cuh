@@ -73,31 +73,6 @@ __global__ void __launch_bounds__(kThreads) prims_fp64_kernel(PrimBatch b) {
   flush_counters(b.counters, hits, flags, surv);
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(kThreads) prims_refine_kernel(PrimBatch b, const int32_t *__restrict__ list) {
-  unsigned hits = 0, flags = 0;
-  const int64_t count = (int64_t)b.counters->survivors;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  const int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t warp_base = base - (threadIdx.x & 31);
-  for (int64_t w = warp_base; w < count; w += stride) {
-    int64_t k = w + (threadIdx.x & 31);
-    if (k < count) {
-      int64_t i = list[k];
-      double eta = b.eta_per_row ? __ldg(b.eta + i) : __ldg(b.eta);
-      double t = 0.0;
-      uint8_t st = 0;
-      bool h = eval_row<KIND>(b.rows, i, eta, t, st);
-      b.hit[i] = h;
-      if (h) b.t[i] = t;
-      if (b.status) b.status[i] = st;
-      hits += h;
-      flags += (st != 0);
-    }
-  }
-  flush_counters(b.counters, hits, flags, 0);
-}
-
 // FP32 rejection pass.  Rows that cannot hit get hit = 0; the others are
 // compacted into `list` with one atomic per warp (ballot + popc prefix).
 template <int KIND>
@@ -145,11 +120,6 @@ inline int grid_for(int64_t n, int num_sms, int blocks_per_sm) {
 template <int KIND>
 cudaError_t fp64(const PrimBatch &b, int num_sms, cudaStream_t s) {
   prims_fp64_kernel<KIND><<<grid_for(b.n, num_sms, 8), kThreads, 0, s>>>(b);
-  return cudaGetLastError();
-}
-template <int KIND>
-cudaError_t refine(const PrimBatch &b, const int32_t *list, int num_sms, cudaStream_t s) {
-  prims_refine_kernel<KIND><<<grid_for(b.n, num_sms, 8), kThreads, 0, s>>>(b, list);
   return cudaGetLastError();
 }
 template <int KIND>

@@ -10,11 +10,5 @@ cudaError_t launch_ve_fp64(const PrimBatch &b, int num_sms, cudaStream_t s) {
 cudaError_t launch_vv_fp64(const PrimBatch &b, int num_sms, cudaStream_t s) {
   return kernels::fp64<kVV>(b, num_sms, s);
 }
-cudaError_t launch_ve_refine(const PrimBatch &b, const int32_t *list, int num_sms, cudaStream_t s) {
-  return kernels::refine<kVE>(b, list, num_sms, s);
-}
-cudaError_t launch_vv_refine(const PrimBatch &b, const int32_t *list, int num_sms, cudaStream_t s) {
-  return kernels::refine<kVV>(b, list, num_sms, s);
-}
 
 }  // namespace ccd

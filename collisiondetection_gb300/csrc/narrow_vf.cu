@@ -9,8 +9,5 @@ cudaError_t launch_vf_fp64(const PrimBatch &b, int num_sms, cudaStream_t s) {
 cudaError_t launch_vf_cull(const PrimBatch &b, int32_t *list, int num_sms, cudaStream_t s) {
   return kernels::cull<kVF>(b, list, num_sms, s);
 }
-cudaError_t launch_vf_refine(const PrimBatch &b, const int32_t *list, int num_sms, cudaStream_t s) {
-  return kernels::refine<kVF>(b, list, num_sms, s);
-}
 
 }  // namespace ccd

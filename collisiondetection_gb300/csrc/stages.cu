@@ -1,0 +1,49 @@
+// Staged FP64 refinement (stages.cuh): scratch layout and the launchers for
+// vertex-face and edge-edge rows.
+#include "stages.cuh"
+
+namespace ccd {
+
+namespace {
+constexpr size_t kAlign = 256;
+size_t up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+}  // namespace
+
+size_t stage_scratch_bytes(int64_t cap) {
+  const size_t c = (size_t)cap;
+  return up(kMaxSlots * 7 * c * sizeof(double)) * 3 + up(kMaxSlots * c * sizeof(int32_t)) +
+         up(kMaxSlots * c) * 2 + up(kMaxSlots * sizeof(unsigned)) + up(c * sizeof(uint32_t));
+}
+
+StageScratch stage_scratch_view(void *base, int64_t cap) {
+  const size_t c = (size_t)cap;
+  char *p = (char *)base;
+  StageScratch sc;
+  sc.cap = cap;
+  sc.coef = (double *)p;
+  p += up(kMaxSlots * 7 * c * sizeof(double));
+  sc.span_l = (double *)p;
+  p += up(kMaxSlots * 7 * c * sizeof(double));
+  sc.span_u = (double *)p;
+  p += up(kMaxSlots * 7 * c * sizeof(double));
+  sc.job_row = (int32_t *)p;
+  p += up(kMaxSlots * c * sizeof(int32_t));
+  sc.job_deg = (uint8_t *)p;
+  p += up(kMaxSlots * c);
+  sc.span_n = (uint8_t *)p;
+  p += up(kMaxSlots * c);
+  sc.queue = (unsigned *)p;
+  p += up(kMaxSlots * sizeof(unsigned));
+  sc.row_status = (uint32_t *)p;
+  return sc;
+}
+
+cudaError_t launch_stages(const PrimBatch &b, const int32_t *list, const StageScratch &sc, int num_sms,
+                          cudaStream_t s, int *launches) {
+  if (b.n <= 0) return cudaSuccess;
+  if (b.kind == kVF) return stages::run<VFPolys>(b, list, sc, num_sms, s, launches);
+  if (b.kind == kEE) return stages::run<EEPolys>(b, list, sc, num_sms, s, launches);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace ccd

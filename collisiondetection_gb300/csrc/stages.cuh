@@ -1,0 +1,219 @@
+// Staged FP64 refinement of the rows that survive the FP32 stage.
+//
+// One thread per row keeps a warp busy only as long as its most expensive row
+// (the reference's early exits and the root finder's data-dependent iteration
+// counts differ from row to row), and FP64 issue slots are scarce on this GPU
+// (1/64 of the FP32 rate), so masked lanes are expensive.  The refinement is
+// therefore split into three kernels over a tile of survivor rows:
+//
+//   stage_build    thread per row: every polynomial of the row in FP64
+//                  (reference expressions), normalised and degree-reduced;
+//                  lists of degree <= 2 are finished here, the others are
+//                  queued per polynomial slot (one queue per slot, so every
+//                  queue holds polynomials of one nominal degree);
+//   stage_roots    thread per queued polynomial: Jenkins-Traub + sign spans;
+//   stage_combine  thread per row: the interval-overlap decision.
+//
+// The result equals the reference's: every list the reference computes is
+// computed the same way, and the extra lists computed for rows the reference
+// would have abandoned early do not change the decision (it is "no hit" as
+// soon as any list is empty).
+#pragma once
+
+#include "ccd_ctcd64.h"
+#include "narrow.cuh"
+
+namespace ccd {
+
+constexpr int kMaxSlots = 5;
+constexpr int kStageThreads = 128;
+
+// Device scratch for one tile of `cap` survivor rows (layouts are slot-major,
+// then coefficient / span index, then row, so warps access consecutive rows).
+struct StageScratch {
+  int64_t cap;
+  double *coef;         // [slot][k < 7][cap]   queued polynomial coefficients
+  int32_t *job_row;     // [slot][cap]          tile row of each queued polynomial
+  uint8_t *job_deg;     // [slot][cap]
+  double *span_l;       // [slot][k < 7][cap]
+  double *span_u;       // [slot][k < 7][cap]
+  uint8_t *span_n;      // [slot][cap]
+  unsigned *queue;      // [slot]               queued polynomials per slot
+  uint32_t *row_status; // [cap]
+};
+
+size_t stage_scratch_bytes(int64_t cap);
+// Carves the scratch arrays out of one allocation of stage_scratch_bytes(cap).
+StageScratch stage_scratch_view(void *base, int64_t cap);
+
+// Enqueues build/roots/combine over every tile of the survivor list.
+// Returns the number of kernels launched through *launches.
+cudaError_t launch_stages(const PrimBatch &b, const int32_t *list, const StageScratch &sc, int num_sms,
+                          cudaStream_t s, int *launches);
+
+namespace stages {
+
+__device__ __forceinline__ void store_spans(const StageScratch &sc, int slot, int64_t r, const SpanList &sl) {
+  sc.span_n[slot * sc.cap + r] = (uint8_t)sl.n;
+  for (int k = 0; k < sl.n; k++) {
+    sc.span_l[(slot * 7 + k) * sc.cap + r] = sl.s[k].l;
+    sc.span_u[(slot * 7 + k) * sc.cap + r] = sl.s[k].u;
+  }
+}
+
+__device__ __forceinline__ void load_spans(const StageScratch &sc, int slot, int64_t r, SpanList &sl) {
+  sl.n = sc.span_n[slot * sc.cap + r];
+  for (int k = 0; k < sl.n; k++) {
+    sl.s[k].l = sc.span_l[(slot * 7 + k) * sc.cap + r];
+    sl.s[k].u = sc.span_u[(slot * 7 + k) * sc.cap + r];
+  }
+}
+
+template <class Polys>
+__global__ void __launch_bounds__(kStageThreads) stage_build(PrimBatch b, const int32_t *__restrict__ list,
+                                                             int64_t tile_begin, StageScratch sc) {
+  const unsigned lane = threadIdx.x & 31;
+  const int64_t count = (int64_t)b.counters->survivors;
+  const int64_t end = count < tile_begin + sc.cap ? count : tile_begin + sc.cap;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t warp_base = tile_begin + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x - lane);
+  for (int64_t w = warp_base; w < end; w += stride) {
+    const int64_t r = w + lane;
+    const bool active = r < end;
+    const int64_t tr = r - tile_begin;
+    double x[24];
+    double eta = 0.0;
+    if (active) {
+      const int64_t i = list[r];
+      const double *src = b.rows + i * 24;
+#pragma unroll
+      for (int j = 0; j < 24; j++) x[j] = __ldg(src + j);
+      eta = b.eta_per_row ? __ldg(b.eta + i) : __ldg(b.eta);
+      sc.row_status[tr] = 0;
+    }
+    for (int slot = 0; slot < Polys::kSlots; slot++) {
+      double op[7];
+      bool queue = false;
+      int deg = 0;
+      if (active) {
+        const bool pos = Polys::want_pos(slot);
+        Polys::coeffs(x, eta, slot, op);
+        deg = reduce_poly(op, Polys::degree(slot));
+        SpanList sl;
+        sl.clear();
+        if (deg > 2) {
+          queue = sign_possible(op, deg, pos);  // otherwise the list stays empty
+        } else {
+          low_degree_spans(op, deg, sl, pos);
+        }
+        if (!queue) store_spans(sc, slot, tr, sl);
+      }
+      const unsigned mask = __ballot_sync(0xffffffffu, queue);
+      if (mask) {
+        unsigned base = 0;
+        const int leader = __ffs(mask) - 1;
+        if ((int)lane == leader) base = atomicAdd(&sc.queue[slot], (unsigned)__popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (queue) {
+          const int64_t j = base + __popc(mask & ((1u << lane) - 1u));
+          for (int k = 0; k <= deg; k++) sc.coef[(slot * 7 + k) * sc.cap + j] = op[k];
+          sc.job_row[slot * sc.cap + j] = (int32_t)tr;
+          sc.job_deg[slot * sc.cap + j] = (uint8_t)deg;
+        }
+      }
+    }
+  }
+}
+
+template <class Polys>
+__global__ void __launch_bounds__(kStageThreads) stage_roots(StageScratch sc) {
+  const int slot = blockIdx.y;
+  const int64_t count = sc.queue[slot];
+  const bool pos = Polys::want_pos(slot);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
+    const int deg = sc.job_deg[slot * sc.cap + j];
+    double op[7];
+    for (int k = 0; k <= deg; k++) op[k] = sc.coef[(slot * 7 + k) * sc.cap + j];
+    double tr[6];
+    uint8_t st = 0;
+    RootFinder rf;
+    const int roots = rf.solve(op, deg, tr, st);
+    SpanList sl;
+    sl.clear();
+    root_spans(op, deg, tr, roots, sl, pos);
+    const int64_t row = sc.job_row[slot * sc.cap + j];
+    store_spans(sc, slot, row, sl);
+    if (st) atomicOr(&sc.row_status[row], (uint32_t)st);
+  }
+}
+
+template <class Polys>
+__global__ void __launch_bounds__(kStageThreads) stage_combine(PrimBatch b, const int32_t *__restrict__ list,
+                                                               int64_t tile_begin, StageScratch sc) {
+  const unsigned lane = threadIdx.x & 31;
+  const int64_t count = (int64_t)b.counters->survivors;
+  const int64_t end = count < tile_begin + sc.cap ? count : tile_begin + sc.cap;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t warp_base = tile_begin + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x - lane);
+  unsigned hits = 0, flags = 0;
+  for (int64_t w = warp_base; w < end; w += stride) {
+    const int64_t r = w + lane;
+    if (r < end) {
+      const int64_t tr = r - tile_begin;
+      const int64_t i = list[r];
+      SpanList l[Polys::kSlots];
+      for (int slot = 0; slot < Polys::kSlots; slot++) load_spans(sc, slot, tr, l[slot]);
+      double t = 0.0;
+      bool h;
+      if constexpr (Polys::kSlots == 4) {
+        h = vf_combine(l[0], l[1], l[2], l[3], t);
+      } else {
+        double x[24];
+        const double *src = b.rows + i * 24;
+#pragma unroll
+        for (int j = 0; j < 24; j++) x[j] = __ldg(src + j);
+        SpanList cop, par;
+        ee_split_parallel(x, l[0], cop, par);
+        h = ee_combine(cop, par, l[1], l[2], l[3], l[4], t);
+      }
+      const uint8_t st = (uint8_t)sc.row_status[tr];
+      b.hit[i] = h;
+      if (h) b.t[i] = t;
+      if (b.status) b.status[i] = st;
+      hits += h;
+      flags += (st != 0);
+    }
+  }
+  const unsigned hsum = __reduce_add_sync(0xffffffffu, hits);
+  const unsigned fsum = __reduce_add_sync(0xffffffffu, flags);
+  if (lane == 0) {
+    if (hsum) atomicAdd(&b.counters->hits, (unsigned long long)hsum);
+    if (fsum) atomicAdd(&b.counters->status_flags, (unsigned long long)fsum);
+  }
+}
+
+inline int stage_grid(int64_t work, int num_sms) {
+  int64_t need = (work + kStageThreads - 1) / kStageThreads;
+  int64_t cap = (int64_t)num_sms * 16;
+  return (int)(need < 1 ? 1 : (need < cap ? need : cap));
+}
+
+template <class Polys>
+cudaError_t run(const PrimBatch &b, const int32_t *list, const StageScratch &sc, int num_sms, cudaStream_t s,
+                int *launches) {
+  const int64_t tiles = (b.n + sc.cap - 1) / sc.cap;
+  const int grid = stage_grid(sc.cap, num_sms);
+  for (int64_t tile = 0; tile < tiles; tile++) {
+    cudaError_t e = cudaMemsetAsync(sc.queue, 0, kMaxSlots * sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    stage_build<Polys><<<grid, kStageThreads, 0, s>>>(b, list, tile * sc.cap, sc);
+    stage_roots<Polys><<<dim3(grid, Polys::kSlots), kStageThreads, 0, s>>>(sc);
+    stage_combine<Polys><<<grid, kStageThreads, 0, s>>>(b, list, tile * sc.cap, sc);
+    *launches += 3;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace stages
+}  // namespace ccd

@@ -117,3 +117,17 @@ def test_fp32_cull_never_rejects_nonfinite():
         rej = _cull(kind, x[:3], 1e-6)
         assert rej.sum() == 0
         assert _cull(kind, x[3:4], np.nan).sum() == 0
+
+
+def test_fast_exp_log_equal_slow_exact_paths():
+    # The table-driven fast paths either prove their rounding or fall back;
+    # both must give the correctly rounded double of the series versions.
+    lib = math_lib()
+    rng = np.random.default_rng(12)
+    xl = np.concatenate([rng.uniform(0.5, 2, 200000), np.exp(rng.uniform(-744, 709, 200000)),
+                         1 + rng.normal(0, 1e-9, 20000), 1 - np.abs(rng.normal(0, 1e-12, 20000)),
+                         [1.0, 0.75, 1.5, 5e-324, 1.7e308, np.nextafter(1.0, 0.0), np.nextafter(1.0, 2.0)]])
+    np.testing.assert_array_equal(_run(lib, "hc_log", xl).view(np.uint64), _run(lib, "hc_log_slow", xl).view(np.uint64))
+    xe = np.concatenate([rng.uniform(-745, 709.7, 200000), rng.normal(0, 1e-8, 20000),
+                         [0.0, -0.0, 699.99, -699.99, 700.1, -700.1, 709.78, -745.1]])
+    np.testing.assert_array_equal(_run(lib, "hc_exp", xe).view(np.uint64), _run(lib, "hc_exp_slow", xe).view(np.uint64))
