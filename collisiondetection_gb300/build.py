@@ -18,7 +18,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libccd_gb300.so")
 
 CU_SOURCES = ["narrow_vf.cu", "narrow_ee.cu", "narrow_vevv.cu", "narrow.cu", "stages.cu", "capi.cu"]
-HEADERS = ["ccd_common.h", "ccd_math.h", "ccd_math_tables.h", "ccd_ctcd64.h", "ccd_cull32.h", "narrow.cuh", "narrow_kernels.cuh", "stages.cuh"]
+HEADERS = ["ccd_common.h", "ccd_math.h", "ccd_math_tables.h", "ccd_jt.h", "ccd_ctcd64.h", "ccd_cull32.h", "narrow.cuh", "narrow_kernels.cuh", "stages.cuh"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

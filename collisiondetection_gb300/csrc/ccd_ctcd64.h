@@ -10,11 +10,13 @@
 //  * cos/sin of the constant 94-degree shift rotation are folded to constants;
 //  * the two root-bound loops that never end on non-finite coefficients
 //    (src/rpoly.h:151-158, 163-173) are capped; hitting the cap sets
-//    kStatusRootLimit and reports the polynomial as having no roots.
+//    kStatusRootLimit and reports the polynomial as having no roots
+//    (ccd_jt.h).
 #pragma once
 
 #include "ccd_common.h"
 #include "ccd_math.h"
+#include "ccd_jt.h"
 
 namespace ccd {
 
@@ -141,449 +143,8 @@ CCD_HD void sort_roots(double *a, int n) {
 }
 
 // ------------------------------------------------------------------ Jenkins-Traub
-// Three-stage real-polynomial root finder (ACM TOMS 493) as vendored by the
-// reference in C. Bond's C translation (src/rpoly.h).  Same numerical steps,
-// constants and iteration limits; the goto structure is written as loops.
-struct RootFinder {
-  double p[7], qp[7], k[7], qk[7], svk[7];
-  double sr, u, v, a, b, c, d, a1, a3, a7, e, f, g, h;
-  double szr, szi, lzr, lzi;
-  int n;
-
-  static constexpr double kEps = 2.22e-16;  // are = mre = eta in the reference
-
-  // p / (x^2 + u x + v): quotient q, remainder (ra, rb)  (rpoly.h:680-695)
-  CCD_HD static void divide(int nn, double u, double v, const double *p, double *q, double &ra, double &rb) {
-    double bb = p[0];
-    q[0] = bb;
-    double aa = p[1] - bb * u;
-    q[1] = aa;
-    for (int i = 2; i <= nn; i++) {
-      double cc = p[i] - aa * u - bb * v;
-      q[i] = cc;
-      bb = aa;
-      aa = cc;
-    }
-    ra = aa;
-    rb = bb;
-  }
-
-  // zeros of a z^2 + b1 z + c  (rpoly.h:702-754)
-  CCD_HD static void quadratic(double a, double b1, double c, double &sr, double &si, double &lr, double &li) {
-    if (a == 0.0) {
-      sr = (b1 != 0.0) ? -c / b1 : 0.0;
-      lr = 0.0;
-      si = 0.0;
-      li = 0.0;
-      return;
-    }
-    if (c == 0.0) {
-      sr = 0.0;
-      lr = -b1 / a;
-      si = 0.0;
-      li = 0.0;
-      return;
-    }
-    double b = b1 / 2.0, d, e;
-    if (fabs(b) < fabs(c)) {
-      e = (c < 0.0) ? -a : a;
-      e = b * (b / fabs(c)) - e;
-      d = sqrt(fabs(e)) * sqrt(fabs(c));
-    } else {
-      e = 1.0 - (a / b) * (c / b);
-      d = sqrt(fabs(e)) * fabs(b);
-    }
-    if (e < 0.0) {
-      sr = -b / a;
-      lr = sr;
-      si = fabs(d / a);
-      li = -si;
-    } else {
-      if (b >= 0.0) d = -d;
-      lr = (-b + d) / a;
-      sr = 0.0;
-      if (lr != 0.0) sr = (c / lr) / a;
-      si = 0.0;
-      li = 0.0;
-    }
-  }
-
-  // rpoly.h:566-597
-  CCD_HD int scalars() {
-    divide(n - 1, u, v, k, qk, c, d);
-    if (!(fabs(c) > fabs(k[n - 1] * 100.0 * kEps)) && !(fabs(d) > fabs(k[n - 2] * 100.0 * kEps))) return 3;
-    if (fabs(d) < fabs(c)) {
-      e = a / c;
-      f = d / c;
-      g = u * e;
-      h = v * b;
-      a3 = a * e + (h / c + g) * b;
-      a1 = b - a * (d / c);
-      a7 = a + g * d + h * f;
-      return 1;
-    }
-    e = a / d;
-    f = c / d;
-    g = u * b;
-    h = v * b;
-    a3 = (a + g) * e + h * (b / d);
-    a1 = b * f - a;
-    a7 = (f + u) * a + h;
-    return 2;
-  }
-
-  // rpoly.h:601-636
-  CCD_HD void next_k(int type) {
-    if (type == 3) {
-      k[0] = 0.0;
-      k[1] = 0.0;
-      for (int i = 2; i < n; i++) k[i] = qk[i - 2];
-      return;
-    }
-    double ref = (type == 1) ? b : a;
-    if (fabs(a1) <= fabs(ref) * kEps * 10.0) {
-      k[0] = 0.0;
-      k[1] = -a7 * qp[0];
-      for (int i = 2; i < n; i++) k[i] = a3 * qk[i - 2] - a7 * qp[i - 1];
-      return;
-    }
-    a7 /= a1;
-    a3 /= a1;
-    k[0] = qp[0];
-    k[1] = qp[1] - a7 * qp[0];
-    for (int i = 2; i < n; i++) k[i] = a3 * qk[i - 2] - a7 * qp[i - 1] + qp[i];
-  }
-
-  // rpoly.h:640-675
-  CCD_HD void estimate(int type, double &uu, double &vv) const {
-    if (type == 3) {
-      uu = 0.0;
-      vv = 0.0;
-      return;
-    }
-    double a4, a5;
-    if (type == 2) {
-      a4 = (a + g) * f + h;
-      a5 = (f + u) * c + v * d;
-    } else {
-      a4 = a + u * b + h * f;
-      a5 = c + (u + v * f) * d;
-    }
-    double b1 = -k[n - 1] / p[n];
-    double b2 = -(k[n - 2] + b1 * p[n - 1]) / p[n];
-    double c1 = v * b2 * a1;
-    double c2 = b1 * a7;
-    double c3 = b1 * b1 * a3;
-    double c4 = c1 - c2 - c3;
-    double den = a5 + b1 * a4 - c4;
-    if (den == 0.0) {
-      uu = 0.0;
-      vv = 0.0;
-      return;
-    }
-    uu = u - (u * (c3 + c2) + v * (b1 * a1 + b2 * a7)) / den;
-    vv = v * (1.0 + c4 / den);
-  }
-
-  // One real zero by the variable-shift iteration (rpoly.h:473-558).
-  CCD_HD int real_iter(double &sx, bool &near_double) {
-    double pv, kv, t = 0, x = sx, mp, omp = 0, ee;
-    near_double = false;
-    for (int j = 1;; j++) {
-      pv = p[0];
-      qp[0] = pv;
-      for (int i = 1; i <= n; i++) {
-        pv = pv * x + p[i];
-        qp[i] = pv;
-      }
-      mp = fabs(pv);
-      double ms = fabs(x);
-      ee = (kEps / (kEps + kEps)) * fabs(qp[0]);
-      for (int i = 1; i <= n; i++) ee = ee * ms + fabs(qp[i]);
-      if (mp <= 20.0 * ((kEps + kEps) * ee - kEps * mp)) {
-        szr = x;
-        szi = 0.0;
-        return 1;
-      }
-      if (j > 10) return 0;
-      if (j >= 2 && !(fabs(t) > 0.001 * fabs(x - t) || mp < omp)) {
-        near_double = true;
-        sx = x;
-        return 0;
-      }
-      omp = mp;
-      kv = k[0];
-      qk[0] = kv;
-      for (int i = 1; i < n; i++) {
-        kv = kv * x + k[i];
-        qk[i] = kv;
-      }
-      if (fabs(kv) <= fabs(k[n - 1]) * 10.0 * kEps) {
-        k[0] = 0.0;
-        for (int i = 1; i < n; i++) k[i] = qk[i - 1];
-      } else {
-        t = -pv / kv;
-        k[0] = qp[0];
-        for (int i = 1; i < n; i++) k[i] = t * qk[i - 1] + qp[i];
-      }
-      kv = k[0];
-      for (int i = 1; i < n; i++) kv = kv * x + k[i];
-      t = 0.0;
-      if (fabs(kv) > fabs(k[n - 1] * 10.0 * kEps)) t = -pv / kv;
-      x += t;
-    }
-  }
-
-  // A quadratic factor by the variable-shift iteration (rpoly.h:390-467).
-  CCD_HD int quad_iter(double uu, double vv) {
-    double ui, vi, mp, omp = 0, ee, relstp = 0, t, zm;
-    int tried = 0, j = 0;
-    u = uu;
-    v = vv;
-    for (;;) {
-      quadratic(1.0, u, v, szr, szi, lzr, lzi);
-      if (fabs(fabs(szr) - fabs(lzr)) > 0.01 * fabs(lzr)) return 0;
-      divide(n, u, v, p, qp, a, b);
-      mp = fabs(a - szr * b) + fabs(szi * b);
-      zm = sqrt(fabs(v));
-      ee = 2.0 * fabs(qp[0]);
-      t = -szr * b;
-      for (int i = 1; i < n; i++) ee = ee * zm + fabs(qp[i]);
-      ee = ee * zm + fabs(a + t);
-      ee *= (5.0 * kEps + 4.0 * kEps);
-      ee = ee - (5.0 * kEps + 2.0 * kEps) * (fabs(a + t) + fabs(b) * zm) + 2.0 * kEps * fabs(t);
-      if (mp <= 20.0 * ee) return 2;
-      j++;
-      if (j > 20) return 0;
-      if (j >= 2 && !(relstp > 0.01 || mp < omp || tried)) {
-        if (relstp < kEps) relstp = kEps;
-        relstp = sqrt(relstp);
-        u = u - u * relstp;
-        v = v + v * relstp;
-        divide(n, u, v, p, qp, a, b);
-        for (int i = 0; i < 5; i++) next_k(scalars());
-        tried = 1;
-        j = 0;
-      }
-      omp = mp;
-      next_k(scalars());
-      int type = scalars();
-      estimate(type, ui, vi);
-      if (vi == 0.0) return 0;
-      relstp = fabs((vi - v) / vi);
-      u = ui;
-      v = vi;
-    }
-  }
-
-  // Fixed-shift stage, then variable-shift iterations (rpoly.h:277-383).
-  CCD_HD int fixed_shift(int l2, double oss_init) {
-    double svu = 0, svv = 0, ui, vi, xs = 0;
-    double betas = 0.25, betav = 0.25, oss = oss_init, ovv = v, ss, vv, ts, tv;
-    double ots = 0, otv = 0;
-    divide(n, u, v, p, qp, a, b);
-    int type = scalars();
-    for (int j = 0; j < l2; j++) {
-      next_k(type);
-      type = scalars();
-      estimate(type, ui, vi);
-      vv = vi;
-      ss = 0.0;
-      if (k[n - 1] != 0.0) ss = -p[n] / k[n - 1];
-      tv = 1.0;
-      ts = 1.0;
-      if (j != 0 && type != 3) {
-        if (vv != 0.0) tv = fabs((vv - ovv) / vv);
-        if (ss != 0.0) ts = fabs((ss - oss) / ss);
-        double tvv = (tv < otv) ? tv * otv : 1.0;
-        double tss = (ts < ots) ? ts * ots : 1.0;
-        bool vpass = tvv < betav, spass = tss < betas;
-        if (spass || vpass) {
-          svu = u;
-          svv = v;
-          for (int i = 0; i < n; i++) svk[i] = k[i];
-          xs = ss;
-          bool vtried = false, stried = false;
-          int step = ((spass && !vpass) || tss < tvv) ? 1 : 0;  // 0 quadratic, 1 linear, 2 restore
-          for (;;) {
-            if (step == 0) {
-              int nz = quad_iter(ui, vi);
-              if (nz > 0) return nz;
-              vtried = true;
-              betav *= 0.25;
-              if (stried || !spass) {
-                step = 2;
-                continue;
-              }
-              for (int i = 0; i < n; i++) k[i] = svk[i];
-              step = 1;
-            } else if (step == 1) {
-              bool near_double;
-              int nz = real_iter(xs, near_double);
-              if (nz > 0) return nz;
-              stried = true;
-              betas *= 0.25;
-              if (!near_double) {
-                step = 2;
-                continue;
-              }
-              ui = -(xs + xs);
-              vi = xs * xs;
-              step = 0;
-            } else {
-              u = svu;
-              v = svv;
-              for (int i = 0; i < n; i++) k[i] = svk[i];
-              if (vpass && !vtried) {
-                step = 0;
-                continue;
-              }
-              divide(n, u, v, p, qp, a, b);
-              type = scalars();
-              break;
-            }
-          }
-        }
-      }
-      ovv = vv;
-      oss = ss;
-      otv = tv;
-      ots = ts;
-    }
-    return 0;
-  }
-
-  // Driver (rpoly.h:49-261).  Returns the number of zeros found (real parts in
-  // zr), or -1.  Only the real parts are kept: the caller ignores the rest.
-  CCD_NOINLINE int solve(const double *op, int degree, double *zr, uint8_t &status) {
-    const double infin = 3.4e38, smalno = 1.2e-38;
-    const double lo = smalno / kEps;
-    const double cosr = -0x1.1db902ec147e0p-4;  // cos(94.0 * 0.017453293)
-    const double sinr = 0x1.fec0b6fc05f20p-1;   // sin(94.0 * 0.017453293)
-    double xx = 0x1.6a09e667f3bcdp-1;           // sqrt(0.5)
-    double yy = -xx;
-    double temp[7], pt[7];
-    n = degree;
-    if (op[0] == 0.0) return -1;
-    while (op[n] == 0.0) {
-      zr[degree - n] = 0.0;
-      n--;
-    }
-    if (n < 1) return -1;
-    for (int i = 0; i <= n; i++) p[i] = op[i];
-
-    while (n > 0) {
-      if (n == 1) {
-        zr[degree - 1] = -p[1] / p[0];
-        n = 0;
-        break;
-      }
-      if (n == 2) {
-        double si, li;
-        quadratic(p[0], p[1], p[2], zr[degree - 2], si, zr[degree - 1], li);
-        n = 0;
-        break;
-      }
-      double maxc = 0.0, minc = infin, x, xm, ff, df, dx;
-      for (int i = 0; i <= n; i++) {
-        x = fabs(p[i]);
-        if (x > maxc) maxc = x;
-        if (x != 0.0 && x < minc) minc = x;
-      }
-      double sc = lo / minc;
-      bool keep = (sc > 1.0 && infin / sc < maxc) || (sc <= 1.0 && maxc < 10.0);
-      if (!keep) {
-        if (sc == 0.0) sc = smalno;
-        int l = (int)(cr_log(sc) / 0x1.62e42fefa39efp-1 + 0.5);  // log(sc) / log(2.0)
-        double factor = ldexp(1.0, l);                            // pow(2.0, l), exact
-        if (factor != 1.0)
-          for (int i = 0; i <= n; i++) p[i] = factor * p[i];
-      }
-      for (int i = 0; i <= n; i++) pt[i] = fabs(p[i]);
-      pt[n] = -pt[n];
-      x = cr_exp((cr_log(-pt[n]) - cr_log(pt[0])) / (double)n);
-      if (pt[n - 1] != 0.0) {
-        xm = -pt[n] / pt[n - 1];
-        if (xm < x) x = xm;
-      }
-      for (int it = 0;; it++) {
-        if (it >= 4096) {
-          status |= kStatusRootLimit;
-          return -1;
-        }
-        xm = x * 0.1;
-        ff = pt[0];
-        for (int i = 1; i <= n; i++) ff = ff * xm + pt[i];
-        if (ff <= 0.0) break;
-        x = xm;
-      }
-      dx = x;
-      for (int it = 0; fabs(dx / x) > 0.005; it++) {
-        if (it >= 4096) {
-          status |= kStatusRootLimit;
-          return -1;
-        }
-        ff = pt[0];
-        df = ff;
-        for (int i = 1; i < n; i++) {
-          ff = ff * x + pt[i];
-          df = df * x + ff;
-        }
-        ff = ff * x + pt[n];
-        dx = ff / df;
-        x -= dx;
-      }
-      double bnd = x;
-      int nm1 = n - 1;
-      for (int i = 1; i < n; i++) k[i] = (double)(n - i) * p[i] / (double)n;
-      k[0] = p[0];
-      double aa = p[n], bb = p[n - 1];
-      bool zerok = (k[n - 1] == 0);
-      for (int jj = 0; jj < 5; jj++) {
-        double cc = k[n - 1];
-        if (!zerok) {
-          double t = -aa / cc;
-          for (int i = 0; i < nm1; i++) {
-            int j = n - i - 1;
-            k[j] = t * k[j - 1] + p[j];
-          }
-          k[0] = p[0];
-          zerok = (fabs(k[n - 1]) <= fabs(bb) * kEps * 10.0);
-        } else {
-          for (int i = 0; i < nm1; i++) {
-            int j = n - i - 1;
-            k[j] = k[j - 1];
-          }
-          k[0] = 0.0;
-          zerok = (k[n - 1] == 0.0);
-        }
-      }
-      for (int i = 0; i < n; i++) temp[i] = k[i];
-      bool found = false;
-      for (int cnt = 0; cnt < 20; cnt++) {
-        double xxx = cosr * xx - sinr * yy;
-        yy = sinr * xx + cosr * yy;
-        xx = xxx;
-        sr = bnd * xx;
-        u = -2.0 * sr;
-        v = bnd;
-        int nz = fixed_shift(20 * (cnt + 1), sr);
-        if (nz != 0) {
-          int j = degree - n;
-          zr[j] = szr;
-          n -= nz;
-          for (int i = 0; i <= n; i++) p[i] = qp[i];
-          if (nz != 1) zr[j + 1] = lzr;
-          found = true;
-          break;
-        }
-        for (int i = 0; i < n; i++) k[i] = temp[i];
-      }
-      if (!found) break;
-    }
-    return degree - n;
-  }
-};
+// The root finder (src/rpoly.h) lives in ccd_jt.h as a resumable state
+// machine; jt_solve runs it to completion in one thread.
 
 // ------------------------------------------------------------------ sign intervals
 // CTCD::findIntervals (src/CTCD.cpp:98-177), in three pieces so that the
@@ -645,8 +206,7 @@ CCD_NOINLINE void sign_spans(double *op, int n, SpanList &out, bool want_pos, ui
   if (deg > 2) {
     if (!sign_possible(op, deg, want_pos)) return;
     double tr[6];
-    RootFinder rf;
-    int roots = rf.solve(op, deg, tr, status);
+    int roots = jt_solve(op, deg, tr, status);
     root_spans(op, deg, tr, roots, out, want_pos);
   } else {
     low_degree_spans(op, deg, out, want_pos);

@@ -11,8 +11,9 @@ size_t up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 size_t stage_scratch_bytes(int64_t cap) {
   const size_t c = (size_t)cap;
-  return up(kMaxSlots * 7 * c * sizeof(double)) * 3 + up(kMaxSlots * c * sizeof(int32_t)) +
-         up(kMaxSlots * c) * 2 + up(kMaxSlots * sizeof(unsigned)) + up(c * sizeof(uint32_t));
+  return up(kMaxSlots * 7 * c * sizeof(double)) * 3 + up(kMaxSlots * 6 * c * sizeof(double)) +
+         up(kMaxSlots * c * sizeof(int32_t)) +
+         up(kMaxSlots * c) * 2 + up((kMaxSlots + 1) * sizeof(unsigned)) + up(c * sizeof(uint32_t));
 }
 
 StageScratch stage_scratch_view(void *base, int64_t cap) {
@@ -26,6 +27,8 @@ StageScratch stage_scratch_view(void *base, int64_t cap) {
   p += up(kMaxSlots * 7 * c * sizeof(double));
   sc.span_u = (double *)p;
   p += up(kMaxSlots * 7 * c * sizeof(double));
+  sc.roots = (double *)p;
+  p += up(kMaxSlots * 6 * c * sizeof(double));
   sc.job_row = (int32_t *)p;
   p += up(kMaxSlots * c * sizeof(int32_t));
   sc.job_deg = (uint8_t *)p;
@@ -33,7 +36,7 @@ StageScratch stage_scratch_view(void *base, int64_t cap) {
   sc.span_n = (uint8_t *)p;
   p += up(kMaxSlots * c);
   sc.queue = (unsigned *)p;
-  p += up(kMaxSlots * sizeof(unsigned));
+  p += up((kMaxSlots + 1) * sizeof(unsigned));
   sc.row_status = (uint32_t *)p;
   return sc;
 }

@@ -11,7 +11,12 @@
 //                  lists of degree <= 2 are finished here, the others are
 //                  queued per polynomial slot (one queue per slot, so every
 //                  queue holds polynomials of one nominal degree);
-//   stage_roots    thread per queued polynomial: Jenkins-Traub + sign spans;
+//   stage_roots    the queued polynomials through the Jenkins-Traub state
+//                  machine (ccd_jt.h): every warp keeps a pool of 64 solver
+//                  states in shared memory and, each iteration, advances up to
+//                  32 of them that are in the same phase (the most populated
+//                  one), refilling finished slots from the queues -- so lanes
+//                  stay busy on equal work without any block-wide barrier;
 //   stage_combine  thread per row: the interval-overlap decision.
 //
 // The result equals the reference's: every list the reference computes is
@@ -38,8 +43,9 @@ struct StageScratch {
   double *span_l;       // [slot][k < 7][cap]
   double *span_u;       // [slot][k < 7][cap]
   uint8_t *span_n;      // [slot][cap]
-  unsigned *queue;      // [slot]               queued polynomials per slot
+  unsigned *queue;      // [slot] queued polynomials per slot; [kMaxSlots] next job to start
   uint32_t *row_status; // [cap]
+  double *roots;        // [slot][k < 6][cap]   roots found by the solver
 };
 
 size_t stage_scratch_bytes(int64_t cap);
@@ -125,26 +131,132 @@ __global__ void __launch_bounds__(kStageThreads) stage_build(PrimBatch b, const 
   }
 }
 
+// Solver slots per warp (one warp per block), and the block's shared memory.
+constexpr int kWarpPool = 64;
+constexpr size_t kPoolSmem = (size_t)kWarpPool * (jt::kDoubles * sizeof(double) + jt::kInts * sizeof(int));
+
+// Spans of a finished solve, written to the polynomial's row slot.
 template <class Polys>
-__global__ void __launch_bounds__(kStageThreads) stage_roots(StageScratch sc) {
-  const int slot = blockIdx.y;
-  const int64_t count = sc.queue[slot];
-  const bool pos = Polys::want_pos(slot);
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
-    const int deg = sc.job_deg[slot * sc.cap + j];
-    double op[7];
-    for (int k = 0; k <= deg; k++) op[k] = sc.coef[(slot * 7 + k) * sc.cap + j];
-    double tr[6];
-    uint8_t st = 0;
-    RootFinder rf;
-    const int roots = rf.solve(op, deg, tr, st);
-    SpanList sl;
-    sl.clear();
-    root_spans(op, deg, tr, roots, sl, pos);
-    const int64_t row = sc.job_row[slot * sc.cap + j];
-    store_spans(sc, slot, row, sl);
-    if (st) atomicOr(&sc.row_status[row], (uint32_t)st);
+__device__ __forceinline__ void finish_job(const StageScratch &sc, const jt::PoolState<kWarpPool> &st, int slot,
+                                           int64_t j) {
+  const int deg = sc.job_deg[slot * sc.cap + j];
+  double op[7], tr[6];
+  for (int k = 0; k <= deg; k++) op[k] = sc.coef[(slot * 7 + k) * sc.cap + j];
+  for (int k = 0; k < deg; k++) tr[k] = st.Z(k);
+  SpanList sl;
+  sl.clear();
+  root_spans(op, deg, tr, st.I(jt::ROOTS), sl, Polys::want_pos(slot));
+  const int64_t row = sc.job_row[slot * sc.cap + j];
+  store_spans(sc, slot, row, sl);
+  const int status = st.I(jt::STATUS);
+  if (status) atomicOr(&sc.row_status[row], (uint32_t)status);
+}
+
+__device__ __forceinline__ int job_queue(const int *qbase, int nslots, int64_t g) {
+  int q = 0;
+  while (q + 1 < nslots && g >= qbase[q + 1]) q++;
+  return q;
+}
+
+template <class Polys>
+__global__ void __launch_bounds__(32) stage_roots(StageScratch sc) {
+  extern __shared__ double pool_d[];
+  int *pool_i = (int *)(pool_d + (size_t)kWarpPool * jt::kDoubles);
+  __shared__ int64_t job_of[kWarpPool];
+  __shared__ int sel[32];
+  __shared__ int qbase[kMaxSlots + 1];
+  const int lane = threadIdx.x;
+  const unsigned lt = (1u << lane) - 1u;
+  if (lane == 0) {
+    int acc = 0;
+    for (int q = 0; q < Polys::kSlots; q++) {
+      qbase[q] = acc;
+      acc += (int)sc.queue[q];
+    }
+    qbase[Polys::kSlots] = acc;
+  }
+  for (int k = lane; k < kWarpPool; k += 32) pool_i[jt::MODE * kWarpPool + k] = jt::kEmpty;
+  __syncwarp();
+  const int njobs = qbase[Polys::kSlots];
+  auto state = [&](int k) {
+    const int64_t g = job_of[k];
+    const int q = job_queue(qbase, Polys::kSlots, g);
+    const int64_t j = g - qbase[q];
+    return jt::PoolState<kWarpPool>{pool_d, pool_i, k, sc.roots + (int64_t)q * 6 * sc.cap + j, sc.cap};
+  };
+  int *mode = pool_i + jt::MODE * kWarpPool;
+  bool exhausted = njobs == 0;
+  for (;;) {
+    // Write out finished solves.
+    for (int k = lane; k < kWarpPool; k += 32) {
+      if (mode[k] == jt::kDone) {
+        const jt::PoolState<kWarpPool> st = state(k);
+        const int64_t g = job_of[k];
+        const int q = job_queue(qbase, Polys::kSlots, g);
+        finish_job<Polys>(sc, st, q, g - qbase[q]);
+        mode[k] = jt::kEmpty;
+      }
+    }
+    __syncwarp();
+    // Refill empty slots: one atomic per warp reserves consecutive jobs.
+    if (!exhausted) {
+      const unsigned e0 = __ballot_sync(0xffffffffu, mode[lane] == jt::kEmpty);
+      const unsigned e1 = __ballot_sync(0xffffffffu, mode[lane + 32] == jt::kEmpty);
+      const int nempty = __popc(e0) + __popc(e1);
+      if (nempty) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(&sc.queue[kMaxSlots], (unsigned)nempty);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if ((int64_t)base + nempty >= njobs) exhausted = true;
+        for (int h = 0; h < 2; h++) {
+          const unsigned e = h ? e1 : e0;
+          if (!((e >> lane) & 1u)) continue;
+          const int k = lane + 32 * h;
+          const int64_t g = (int64_t)base + (h ? __popc(e0) : 0) + __popc(e & lt);
+          if (g >= njobs) continue;
+          job_of[k] = g;
+          const int q = job_queue(qbase, Polys::kSlots, g);
+          const int64_t j = g - qbase[q];
+          const int deg = sc.job_deg[q * sc.cap + j];
+          double op[7];
+          for (int c = 0; c <= deg; c++) op[c] = sc.coef[(q * 7 + c) * sc.cap + j];
+          const jt::PoolState<kWarpPool> st{pool_d, pool_i, k, sc.roots + (int64_t)q * 6 * sc.cap + j, sc.cap};
+          jt::start(st, op, deg);
+        }
+      }
+    }
+    __syncwarp();
+    // The most populated working phase.
+    int best = 0, bestc = 0;
+    bool pending = false;
+    for (int m = jt::kInit; m <= jt::kDone; m++) {
+      const int c = __popc(__ballot_sync(0xffffffffu, mode[lane] == m)) +
+                    __popc(__ballot_sync(0xffffffffu, mode[lane + 32] == m));
+      if (m == jt::kDone) {
+        pending = c > 0;
+      } else if (c > bestc) {
+        best = m;
+        bestc = c;
+      }
+    }
+    if (bestc == 0) {
+      if (exhausted && !pending) break;
+      continue;
+    }
+    // Up to 32 slots of that phase, one per lane.
+    const unsigned b0 = __ballot_sync(0xffffffffu, mode[lane] == best);
+    const unsigned b1 = __ballot_sync(0xffffffffu, mode[lane + 32] == best);
+    if ((b0 >> lane) & 1u) {
+      const int r = __popc(b0 & lt);
+      sel[r] = lane;
+    }
+    if ((b1 >> lane) & 1u) {
+      const int r = __popc(b0) + __popc(b1 & lt);
+      if (r < 32) sel[r] = lane + 32;
+    }
+    __syncwarp();
+    if (lane < bestc) jt::step(state(sel[lane]));
+    __syncwarp();
   }
 }
 
@@ -202,13 +314,21 @@ inline int stage_grid(int64_t work, int num_sms) {
 template <class Polys>
 cudaError_t run(const PrimBatch &b, const int32_t *list, const StageScratch &sc, int num_sms, cudaStream_t s,
                 int *launches) {
+  static bool smem_set = false;
+  if (!smem_set) {
+    cudaError_t e = cudaFuncSetAttribute(stage_roots<Polys>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kPoolSmem);
+    if (e != cudaSuccess) return e;
+    smem_set = true;
+  }
   const int64_t tiles = (b.n + sc.cap - 1) / sc.cap;
   const int grid = stage_grid(sc.cap, num_sms);
+  const int pool_grid = num_sms * 5;  // five 40 KB warp pools fit one SM's shared memory
   for (int64_t tile = 0; tile < tiles; tile++) {
-    cudaError_t e = cudaMemsetAsync(sc.queue, 0, kMaxSlots * sizeof(unsigned), s);
+    cudaError_t e = cudaMemsetAsync(sc.queue, 0, (kMaxSlots + 1) * sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     stage_build<Polys><<<grid, kStageThreads, 0, s>>>(b, list, tile * sc.cap, sc);
-    stage_roots<Polys><<<dim3(grid, Polys::kSlots), kStageThreads, 0, s>>>(sc);
+    stage_roots<Polys><<<pool_grid, 32, kPoolSmem, s>>>(sc);
     stage_combine<Polys><<<grid, kStageThreads, 0, s>>>(b, list, tile * sc.cap, sc);
     *launches += 3;
   }

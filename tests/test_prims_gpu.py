@@ -117,7 +117,7 @@ def test_profiling_timings(ctx):
     ctx.prim_batch(C.VERTEX_FACE, rows, 1e-6, path=C.PATH_CULL_REFINE)
     tm = ctx.timings()
     ctx.set_profiling(False)
-    assert tm["launches"] == 2 and tm["cull_ms"] > 0 and tm["refine_ms"] > 0
+    assert tm["launches"] == 4 and tm["cull_ms"] > 0 and tm["refine_ms"] > 0  # cull + build, roots, combine
 
 
 def test_empty_and_invalid_batches(ctx):
