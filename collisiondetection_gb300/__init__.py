@@ -7,7 +7,8 @@ include/ccd_gb300.h.  This package holds the build helper, the ctypes binding
 and the synthetic workload generators.
 """
 from . import workloads  # noqa: F401
-from ._native import (EDGE_EDGE, PATH_CULL_REFINE, PATH_FP64, ROW_WIDTH, VERTEX_EDGE, VERTEX_FACE,  # noqa: F401
-                      VERTEX_VERTEX, CcdError, Context, header_functions, load)
+from ._native import (BROADPHASE_AABB, BROADPHASE_KDOP13, EDGE_EDGE, PATH_CULL_REFINE, PATH_FP64,  # noqa: F401
+                      ROW_WIDTH, VERTEX_EDGE, VERTEX_FACE, VERTEX_VERTEX, CcdError, Context, Mesh,
+                      header_functions, load)
 
 __version__ = "0.1.0"

@@ -18,6 +18,7 @@ HEADER = os.path.join(ROOT, "include", "ccd_gb300.h")
 CCD_OK = 0
 VERTEX_FACE, EDGE_EDGE, VERTEX_EDGE, VERTEX_VERTEX = 0, 1, 2, 3
 PATH_FP64, PATH_CULL_REFINE = 0, 1
+BROADPHASE_KDOP13, BROADPHASE_AABB = 0, 1
 ROW_WIDTH = {VERTEX_FACE: 24, EDGE_EDGE: 24, VERTEX_EDGE: 18, VERTEX_VERTEX: 12}
 
 _P = ctypes.c_void_p
@@ -31,6 +32,11 @@ class CcdError(RuntimeError):
 class BatchStats(ctypes.Structure):
     _fields_ = [("rows", ctypes.c_int64), ("survivors", ctypes.c_int64), ("hits", ctypes.c_int64),
                 ("status_flags", ctypes.c_int64)]
+
+
+class MeshStats(ctypes.Structure):
+    _fields_ = [("face_pairs", ctypes.c_int64), ("n_vf", ctypes.c_int64), ("n_ee", ctypes.c_int64),
+                ("vf_hits", ctypes.c_int64), ("ee_hits", ctypes.c_int64)]
 
 
 class BatchTimings(ctypes.Structure):
@@ -72,6 +78,18 @@ def load(path: str = LIB):
         fn.argtypes = [_P, _P, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     L.ccd_prim_batch.argtypes = [_P, ctypes.c_int, ctypes.c_int, _I64, _P, _P, _I64, _P, _P]
     L.ccd_prim_batch_device.argtypes = [_P, ctypes.c_int, ctypes.c_int, _I64, _P, _P, _I64, _P, _P, _P]
+    L.ccd_mesh_create.argtypes = [_P, ctypes.c_int32, ctypes.c_int32, _P, ctypes.POINTER(_P)]
+    L.ccd_mesh_destroy.argtypes = [_P]
+    L.ccd_mesh_set_positions.argtypes = [_P, _P, _P]
+    L.ccd_mesh_set_positions_device.argtypes = [_P, _P, _P]
+    L.ccd_mesh_set_fixed.argtypes = [_P, _P]
+    L.ccd_broadphase.argtypes = [_P, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]
+    L.ccd_broadphase_get.argtypes = [_P, _P, _P]
+    L.ccd_narrowphase.argtypes = [_P, ctypes.c_int, _I64, _P, _P, _I64, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P]
+    L.ccd_mesh_detect.argtypes = [_P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                  ctypes.POINTER(_I64), ctypes.POINTER(_I64)]
+    L.ccd_mesh_get_collisions.argtypes = [_P, _P, _P, _P, _P]
+    L.ccd_mesh_last_stats.argtypes = [_P, ctypes.POINTER(MeshStats)]
     _lib = L
     return L
 
@@ -162,3 +180,120 @@ class Context:
         addresses (e.g. torch tensor data_ptr()).  Asynchronous."""
         self._check(self.lib.ccd_prim_batch_device(self.handle, kind, path, n, rows_ptr, eta_ptr, eta_count,
                                                    hit_ptr, t_ptr, status_ptr), "ccd_prim_batch_device")
+
+
+def _stencils(a) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a.reshape(-1, 4)
+
+
+class Mesh:
+    """A mesh resident on a context's device (ccd_mesh_*): the reference's
+    Mesh faces plus a two-entry History (start, end) of vertex positions.
+
+    broadphase() mirrors BroadPhase::findCollisionCandidates
+    (src/RetrospectiveDetection.h:13) and narrowphase() mirrors
+    CTCDNarrowPhase::findCollisions (src/CTCDNarrowPhase.cpp:9-24)."""
+
+    def __init__(self, ctx: Context, faces, qstart=None, qend=None, fixed=None, nverts: int | None = None):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        f = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+        if nverts is None:
+            if qstart is None:
+                raise ValueError("nverts or qstart is required")
+            nverts = np.asarray(qstart).size // 3
+        self.nverts, self.nfaces = int(nverts), int(f.shape[0])
+        h = _P()
+        ctx._check(self.lib.ccd_mesh_create(ctx.handle, self.nverts, self.nfaces, _ptr(f), ctypes.byref(h)),
+                   "ccd_mesh_create")
+        self.handle = h
+        if qstart is not None:
+            self.set_positions(qstart, qend)
+        if fixed is not None:
+            self.set_fixed(fixed)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.ccd_mesh_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_positions(self, qstart, qend):
+        qs = np.ascontiguousarray(qstart, dtype=np.float64).ravel()
+        qe = np.ascontiguousarray(qend, dtype=np.float64).ravel()
+        if qs.size != 3 * self.nverts or qe.size != 3 * self.nverts:
+            raise ValueError("positions must hold 3 * nverts doubles")
+        self.ctx._check(self.lib.ccd_mesh_set_positions(self.handle, _ptr(qs), _ptr(qe)), "ccd_mesh_set_positions")
+
+    def set_positions_device(self, qstart_ptr: int, qend_ptr: int):
+        self.ctx._check(self.lib.ccd_mesh_set_positions_device(self.handle, qstart_ptr, qend_ptr),
+                        "ccd_mesh_set_positions_device")
+
+    def set_fixed(self, fixed):
+        fx = None
+        if fixed is not None:
+            fx = np.ascontiguousarray(fixed, dtype=np.uint8).ravel()
+            if fx.size != self.nverts:
+                raise ValueError("fixed must hold nverts flags")
+        self.ctx._check(self.lib.ccd_mesh_set_fixed(self.handle, _ptr(fx)), "ccd_mesh_set_fixed")
+
+    def broadphase(self, kind: int = BROADPHASE_KDOP13, outer_eta: float = 1e-6):
+        """Candidate stencils (vf [n][4], ee [n][4]) in the reference's set order."""
+        nvf, nee = _I64(), _I64()
+        self.ctx._check(self.lib.ccd_broadphase(self.handle, kind, outer_eta, ctypes.byref(nvf), ctypes.byref(nee)),
+                        "ccd_broadphase")
+        vf = np.zeros((nvf.value, 4), np.int32)
+        ee = np.zeros((nee.value, 4), np.int32)
+        self.ctx._check(self.lib.ccd_broadphase_get(self.handle, _ptr(vf), _ptr(ee)), "ccd_broadphase_get")
+        return vf, ee
+
+    def narrowphase(self, vf, vf_eta, ee, ee_eta, path: int = PATH_CULL_REFINE):
+        """Per-stencil results: dict of vf_hit / ee_hit (uint8), vf_t / ee_t
+        (NaN where no hit) and vf_which / ee_which (0 primitive, 1 vertex-edge,
+        2 vertex-vertex, -1 miss)."""
+        vf, ee = _stencils(vf), _stencils(ee)
+        vfe = np.ascontiguousarray(np.atleast_1d(np.asarray(vf_eta, np.float64)))
+        eee = np.ascontiguousarray(np.atleast_1d(np.asarray(ee_eta, np.float64)))
+        nv, ne = vf.shape[0], ee.shape[0]
+        out = {"vf_hit": np.zeros(nv, np.uint8), "ee_hit": np.zeros(ne, np.uint8),
+               "vf_t": np.full(nv, np.nan), "ee_t": np.full(ne, np.nan),
+               "vf_which": np.zeros(nv, np.int8), "ee_which": np.zeros(ne, np.int8)}
+        self.ctx._check(self.lib.ccd_narrowphase(self.handle, path, nv, _ptr(vf), _ptr(vfe), vfe.size, ne, _ptr(ee),
+                                                 _ptr(eee), eee.size, _ptr(out["vf_hit"]), _ptr(out["ee_hit"]),
+                                                 _ptr(out["vf_t"]), _ptr(out["ee_t"]), _ptr(out["vf_which"]),
+                                                 _ptr(out["ee_which"])), "ccd_narrowphase")
+        return out
+
+    def detect(self, kind: int = BROADPHASE_KDOP13, outer_eta: float = 1e-6, eta: float = 1e-6,
+               path: int = PATH_CULL_REFINE, fetch: bool = True):
+        """Broad phase + narrow phase on the device.  Returns the colliding
+        (vf, vf_t, ee, ee_t) in set order, or the two counts if fetch is False."""
+        nvf, nee = _I64(), _I64()
+        self.ctx._check(self.lib.ccd_mesh_detect(self.handle, kind, outer_eta, eta, path, ctypes.byref(nvf),
+                                                 ctypes.byref(nee)), "ccd_mesh_detect")
+        if not fetch:
+            return nvf.value, nee.value
+        vf = np.zeros((nvf.value, 4), np.int32)
+        ee = np.zeros((nee.value, 4), np.int32)
+        vft = np.zeros(nvf.value)
+        eet = np.zeros(nee.value)
+        self.ctx._check(self.lib.ccd_mesh_get_collisions(self.handle, _ptr(vf), _ptr(vft), _ptr(ee), _ptr(eet)),
+                        "ccd_mesh_get_collisions")
+        return vf, vft, ee, eet
+
+    def stats(self) -> dict:
+        st = MeshStats()
+        self.ctx._check(self.lib.ccd_mesh_last_stats(self.handle, ctypes.byref(st)), "ccd_mesh_last_stats")
+        return {f: getattr(st, f) for f, _ in MeshStats._fields_}

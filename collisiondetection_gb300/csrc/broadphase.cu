@@ -1,0 +1,526 @@
+// Swept-volume candidate search (broadphase.cuh).
+#include <math.h>
+
+#include <algorithm>
+
+#include "broadphase.cuh"
+#include "ccd_common.h"
+#include "radix_sort.cuh"
+
+namespace ccd {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kStack = 128;
+constexpr uint64_t kNoKey = ~0ull;
+// Face pairs per call: 9 edge-edge keys per pair stay below the sort's 2^31.
+constexpr int64_t kMaxPairs = (int64_t)1 << 27;
+
+struct Axes {
+  double a[13][3];
+};
+
+inline unsigned grid_of(int64_t n) { return (unsigned)std::max<int64_t>(1, (n + kThreads - 1) / kThreads); }
+
+// ------------------------------------------------------------------ leaves
+template <int K>
+__global__ void __launch_bounds__(kThreads) leaf_slabs(MeshTopology topo, BroadphaseParams p, Axes ax, double *lo64,
+                                                       double *hi64, float *flo, float *fhi, float *bounds) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  float cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+  if (f < topo.nf) {
+    double lo[K], hi[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      lo[k] = INFINITY;
+      hi[k] = -INFINITY;
+    }
+    for (int j = 0; j < 3; j++) {
+      const int v = topo.faces[3 * f + j];
+      for (int e = 0; e < 2; e++) {
+        const double *pos = (e ? p.qe : p.qs) + 3 * (int64_t)v;
+        const double px = pos[0], py = pos[1], pz = pos[2];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+          // KDOPBroadPhase.cpp:66-67 (pos . axis) / AABBBroadPhase.cpp:38-39 (pos[k])
+          const double val = (K == 13) ? (px * ax.a[k][0] + py * ax.a[k][1]) + pz * ax.a[k][2]
+                                       : (k == 0 ? px : (k == 1 ? py : pz));
+          lo[k] = smin(val - p.eta, lo[k]);
+          hi[k] = smax(val + p.eta, hi[k]);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      lo64[(int64_t)k * topo.nf + f] = lo[k];
+      hi64[(int64_t)k * topo.nf + f] = hi[k];
+      flo[(int64_t)k * topo.nf + f] = __double2float_rd(lo[k]);
+      fhi[(int64_t)k * topo.nf + f] = __double2float_ru(hi[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const float c = 0.5f * (__double2float_rd(lo[k]) + __double2float_ru(hi[k]));
+      cmin[k] = c;
+      cmax[k] = c;
+    }
+  }
+  // Bounds of the slab centres (for the Morton grid): warp reduce, then
+  // atomics on the order-preserving integer image of the floats.
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      cmin[k] = fminf(cmin[k], __shfl_xor_sync(0xffffffffu, cmin[k], o));
+      cmax[k] = fmaxf(cmax[k], __shfl_xor_sync(0xffffffffu, cmax[k], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+    for (int k = 0; k < 3; k++) {
+      if (cmin[k] <= cmax[k]) {
+        atomicMin((int *)&bounds[k], __float_as_int(cmin[k]) >= 0 ? __float_as_int(cmin[k])
+                                                                   : (int)(0x80000000u - (unsigned)__float_as_int(cmin[k])));
+        atomicMax((int *)&bounds[3 + k], __float_as_int(cmax[k]) >= 0 ? __float_as_int(cmax[k])
+                                                                       : (int)(0x80000000u - (unsigned)__float_as_int(cmax[k])));
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ float ordered_to_float(int v) {
+  return v >= 0 ? __int_as_float(v) : __int_as_float((int)(0x80000000u - (unsigned)v));
+}
+
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+  x &= 1023u;
+  x = (x | (x << 16)) & 0x030000FFu;
+  x = (x | (x << 8)) & 0x0300F00Fu;
+  x = (x | (x << 4)) & 0x030C30C3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+
+__global__ void __launch_bounds__(kThreads) morton_keys(int nf, const float *flo, const float *fhi, const float *bounds,
+                                                        uint64_t *keys) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  uint32_t m = 0;
+  for (int k = 0; k < 3; k++) {
+    const float lo = ordered_to_float(((const int *)bounds)[k]);
+    const float hi = ordered_to_float(((const int *)bounds)[3 + k]);
+    const float c = 0.5f * (flo[(int64_t)k * nf + f] + fhi[(int64_t)k * nf + f]);
+    float u = (hi > lo) ? (c - lo) / (hi - lo) : 0.5f;
+    u = fminf(fmaxf(u, 0.0f), 1.0f);
+    uint32_t q = (uint32_t)(u * 1023.0f);
+    m |= spread10(q) << (2 - k);
+  }
+  keys[f] = ((uint64_t)m << 32) | (uint32_t)f;
+}
+
+// Leaf FP32 slabs in Morton order.
+template <int K>
+__global__ void __launch_bounds__(kThreads) gather_leaves(int nf, const uint64_t *keys, const float *flo,
+                                                          const float *fhi, float *llo, float *lhi) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nf) return;
+  const int f = (int)(uint32_t)keys[s];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    llo[(int64_t)k * nf + s] = flo[(int64_t)k * nf + f];
+    lhi[(int64_t)k * nf + s] = fhi[(int64_t)k * nf + f];
+  }
+}
+
+// ------------------------------------------------------------------ LBVH (Karras 2012)
+__device__ __forceinline__ int key_delta(const uint64_t *keys, int n, int i, int64_t j) {
+  if (j < 0 || j >= n) return -1;
+  return __clzll(keys[i] ^ keys[j]);  // keys are unique
+}
+
+__global__ void __launch_bounds__(kThreads) build_lbvh(int n, const uint64_t *keys, int32_t *child, int32_t *range,
+                                                       int32_t *parent) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = (key_delta(keys, n, i, i + 1) - key_delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = key_delta(keys, n, i, i - d);
+  int64_t lmax = 2;
+  while (key_delta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+  int64_t l = 0;
+  for (int64_t t = lmax / 2; t >= 1; t /= 2)
+    if (key_delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = (int)(i + l * d);
+  const int dnode = key_delta(keys, n, i, j);
+  int64_t sp = 0;
+  for (int64_t div = 2;; div *= 2) {
+    const int64_t t = (l + div - 1) / div;
+    if (key_delta(keys, n, i, i + (sp + t) * d) > dnode) sp += t;
+    if (t <= 1) break;
+  }
+  const int gamma = (int)(i + sp * d) + (d < 0 ? -1 : 0);
+  const int first = i < j ? i : j, last = i < j ? j : i;
+  const int left = (first == gamma) ? ~gamma : gamma;
+  const int right = (last == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+  child[2 * i] = left;
+  child[2 * i + 1] = right;
+  range[2 * i] = first;
+  range[2 * i + 1] = last;
+  parent[left >= 0 ? left : (n - 1) + ~left] = i;
+  parent[right >= 0 ? right : (n - 1) + ~right] = i;
+  if (i == 0) parent[0] = -1;
+}
+
+// Bottom-up FP32 slab unions; the second child to arrive at a node builds it.
+template <int K>
+__global__ void __launch_bounds__(kThreads) refit(int n, const int32_t *child, const int32_t *parent, uint32_t *arrive,
+                                                  const float *llo, const float *lhi, float *nlo, float *nhi,
+                                                  unsigned long long *counters) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int node = parent[(n - 1) + s];
+  // Unique 64-bit keys bound the depth by 65; a longer walk means a broken
+  // tree and is reported instead of followed.
+  for (int level = 0; node >= 0; level++) {
+    if (level > 70) {
+      atomicOr(&counters[3], 2ull);
+      return;
+    }
+    __threadfence();
+    if (atomicAdd(&arrive[node], 1u) == 0) return;
+    __threadfence();
+    const int c0 = child[2 * node], c1 = child[2 * node + 1];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const float lo0 = c0 >= 0 ? __ldcg(&nlo[(int64_t)k * (n - 1) + c0]) : llo[(int64_t)k * n + ~c0];
+      const float hi0 = c0 >= 0 ? __ldcg(&nhi[(int64_t)k * (n - 1) + c0]) : lhi[(int64_t)k * n + ~c0];
+      const float lo1 = c1 >= 0 ? __ldcg(&nlo[(int64_t)k * (n - 1) + c1]) : llo[(int64_t)k * n + ~c1];
+      const float hi1 = c1 >= 0 ? __ldcg(&nhi[(int64_t)k * (n - 1) + c1]) : lhi[(int64_t)k * n + ~c1];
+      __stcg(&nlo[(int64_t)k * (n - 1) + node], fminf(lo0, lo1));
+      __stcg(&nhi[(int64_t)k * (n - 1) + node], fmaxf(hi0, hi1));
+    }
+    node = parent[node];
+  }
+}
+
+// ------------------------------------------------------------------ traversal
+template <int K>
+__global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n, const uint64_t *keys,
+                                                       const int32_t *child, const int32_t *range, const float *llo,
+                                                       const float *lhi, const float *nlo, const float *nhi,
+                                                       const double *lo64, const double *hi64, uint32_t *pairs,
+                                                       uint64_t cap, unsigned long long *counters) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n || n < 2) return;
+  float qlo[K], qhi[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    qlo[k] = llo[(int64_t)k * n + s];
+    qhi[k] = lhi[(int64_t)k * n + s];
+  }
+  const int fa = (int)(uint32_t)keys[s];
+  const int a0 = topo.faces[3 * fa], a1 = topo.faces[3 * fa + 1], a2 = topo.faces[3 * fa + 2];
+  int stack[kStack];
+  int sp = 0;
+  stack[sp++] = 0;
+  // A valid tree is visited at most once per node (n - 1 internal nodes).
+  for (int visits = 0; sp > 0; visits++) {
+    if (visits >= n) {
+      atomicOr(&counters[3], 2ull);
+      return;
+    }
+    const int node = stack[--sp];
+    for (int c = 0; c < 2; c++) {
+      const int ch = child[2 * node + c];
+      if (ch < 0) {
+        const int j = ~ch;
+        if (j <= s) continue;
+        bool sep = false;
+#pragma unroll
+        for (int k = 0; k < K; k++) sep |= (qhi[k] < llo[(int64_t)k * n + j]) || (lhi[(int64_t)k * n + j] < qlo[k]);
+        if (sep) continue;
+        // The reference's exact FP64 test (KDOPBroadPhase.cpp:132-137).
+        const int fb = (int)(uint32_t)keys[j];
+        for (int k = 0; k < K && !sep; k++)
+          sep = (hi64[(int64_t)k * topo.nf + fa] < lo64[(int64_t)k * topo.nf + fb]) ||
+                (hi64[(int64_t)k * topo.nf + fb] < lo64[(int64_t)k * topo.nf + fa]);
+        if (sep) continue;
+        // Mesh::neighboringFaces (src/Mesh.cpp:13-20).
+        const int b0 = topo.faces[3 * fb], b1 = topo.faces[3 * fb + 1], b2 = topo.faces[3 * fb + 2];
+        if (a0 == b0 || a0 == b1 || a0 == b2 || a1 == b0 || a1 == b1 || a1 == b2 || a2 == b0 || a2 == b1 ||
+            a2 == b2)
+          continue;
+        const unsigned long long idx = atomicAdd(&counters[0], 1ull);
+        if (idx < cap) {
+          pairs[2 * (int64_t)idx] = (uint32_t)fa;
+          pairs[2 * (int64_t)idx + 1] = (uint32_t)fb;
+        }
+      } else {
+        if (range[2 * ch + 1] <= s) continue;
+        bool sep = false;
+#pragma unroll
+        for (int k = 0; k < K; k++)
+          sep |= (qhi[k] < nlo[(int64_t)k * (n - 1) + ch]) || (nhi[(int64_t)k * (n - 1) + ch] < qlo[k]);
+        if (sep) continue;
+        if (sp < kStack)
+          stack[sp++] = ch;
+        else
+          atomicOr(&counters[3], 1ull);  // stack overflow: reported as an error
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ stencils
+// KDOPBroadPhase.cpp:150-183: 6 vertex-face and 9 edge-edge stencils per
+// pair, skipping those whose four vertices are all fixed.
+__global__ void __launch_bounds__(kThreads) stencil_keys(MeshTopology topo, const uint8_t *fixed,
+                                                         const uint32_t *pairs, int64_t npairs, uint64_t *vf_keys,
+                                                         uint64_t *ee_keys) {
+  const int64_t pi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pi >= npairs) return;
+  const int fa = (int)pairs[2 * pi], fb = (int)pairs[2 * pi + 1];
+  int A[3], B[3];
+  bool FA[3], FB[3];
+  for (int i = 0; i < 3; i++) {
+    A[i] = topo.faces[3 * fa + i];
+    B[i] = topo.faces[3 * fb + i];
+    FA[i] = fixed && fixed[A[i]];
+    FB[i] = fixed && fixed[B[i]];
+  }
+  const bool allA = FA[0] && FA[1] && FA[2], allB = FB[0] && FB[1] && FB[2];
+  const uint64_t ra = (uint32_t)topo.face_rank[fa], rb = (uint32_t)topo.face_rank[fb];
+  for (int i = 0; i < 3; i++) {
+    vf_keys[6 * pi + 2 * i] = (FA[i] && allB) ? kNoKey : ((uint64_t)(uint32_t)A[i] << 32) | rb;
+    vf_keys[6 * pi + 2 * i + 1] = (FB[i] && allA) ? kNoKey : ((uint64_t)(uint32_t)B[i] << 32) | ra;
+    for (int j = 0; j < 3; j++) {
+      const bool all = FA[i] && FA[(i + 1) % 3] && FB[j] && FB[(j + 1) % 3];
+      const uint32_t e1 = (uint32_t)topo.face_edges[3 * fa + i], e2 = (uint32_t)topo.face_edges[3 * fb + j];
+      ee_keys[9 * pi + 3 * i + j] =
+          all ? kNoKey : (((uint64_t)(e1 < e2 ? e1 : e2) << 32) | (uint64_t)(e1 < e2 ? e2 : e1));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) first_of_run(const uint64_t *keys, int64_t n, uint32_t *flags) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t k = keys[i];
+  flags[i] = (k != kNoKey && (i == 0 || keys[i - 1] != k)) ? 1u : 0u;
+}
+
+// Unique keys -> stencils (reference order: keys are sorted).
+__global__ void __launch_bounds__(kThreads) decode_vf(MeshTopology topo, const uint64_t *keys, const uint32_t *flags,
+                                                      const uint32_t *pos, int64_t n, int32_t *out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !flags[i]) return;
+  const uint64_t k = keys[i];
+  const int64_t o = pos[i];
+  const int r = (int)(uint32_t)k;
+  out[4 * o] = (int32_t)(k >> 32);
+  out[4 * o + 1] = topo.rank_triple[3 * r];
+  out[4 * o + 2] = topo.rank_triple[3 * r + 1];
+  out[4 * o + 3] = topo.rank_triple[3 * r + 2];
+}
+
+__global__ void __launch_bounds__(kThreads) decode_ee(MeshTopology topo, const uint64_t *keys, const uint32_t *flags,
+                                                      const uint32_t *pos, int64_t n, int32_t *out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !flags[i]) return;
+  const uint64_t k = keys[i];
+  const int64_t o = pos[i];
+  const int r1 = (int)(k >> 32), r2 = (int)(uint32_t)k;
+  out[4 * o] = topo.rank_edge[2 * r1];
+  out[4 * o + 1] = topo.rank_edge[2 * r1 + 1];
+  out[4 * o + 2] = topo.rank_edge[2 * r2];
+  out[4 * o + 3] = topo.rank_edge[2 * r2 + 1];
+}
+
+template <class T>
+cudaError_t grow(T **p, int64_t *cap, int64_t need) {
+  if (*cap >= need && *p) return cudaSuccess;
+  cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  int64_t c = std::max<int64_t>(need, 1);
+  cudaError_t e = cudaMalloc(p, (size_t)c * sizeof(T));
+  if (e == cudaSuccess) *cap = c;
+  return e;
+}
+
+Axes make_axes() {
+  // The 13 k-DOP directions of KDOPBroadPhase.cpp:12-31, normalised as the
+  // reference does (component / norm, norm = sqrt((x*x + y*y) + z*z)).
+  static const double dirs[13][3] = {{1, 0, 0},  {0, 1, 0},  {0, 0, 1},  {1, 1, 0},  {1, -1, 0},
+                                     {0, 1, 1},  {0, 1, -1}, {1, 0, 1},  {1, 0, -1}, {1, 1, 1},
+                                     {1, 1, -1}, {1, -1, 1}, {1, -1, -1}};
+  Axes ax;
+  for (int k = 0; k < 13; k++) {
+    volatile double x = dirs[k][0], y = dirs[k][1], z = dirs[k][2];
+    volatile double xx = x * x, yy = y * y, zz = z * z;
+    volatile double s = xx + yy;
+    s = s + zz;
+    const double nrm = sqrt((double)s);
+    ax.a[k][0] = x / nrm;
+    ax.a[k][1] = y / nrm;
+    ax.a[k][2] = z / nrm;
+  }
+  return ax;
+}
+
+}  // namespace
+
+void broadphase_free(BroadphaseBuffers &b) {
+  void *ptrs[] = {b.lo64, b.hi64, b.leaf_lo, b.leaf_hi, b.node_lo, b.node_hi, b.node_child, b.node_range, b.parent,
+                  b.arrive, b.keys, b.keys_alt, b.vals, b.vals_alt, b.bounds, b.counters, b.pairs, b.vf_keys,
+                  b.ee_keys, b.flags, b.scan, b.temp};
+  for (void *p : ptrs) cudaFree(p);
+  b = BroadphaseBuffers{};
+}
+
+#define BP_CUDA(call)        \
+  do {                       \
+    cudaError_t e_ = (call); \
+    if (e_ != cudaSuccess) { \
+      *err = e_;             \
+      return 2;              \
+    }                        \
+  } while (0)
+
+// Returns 0 on success, 2 on a CUDA error (*err), 3 on a malformed tree
+// (traversal stack overflow or a walk longer than the tree allows), 4 when the
+// candidate face pairs exceed 2^27.
+int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, BroadphaseBuffers &b, int32_t **vf_out,
+                   int64_t *vf_cap, int32_t **ee_out, int64_t *ee_cap, int64_t *n_vf, int64_t *n_ee,
+                   int64_t *n_pairs, int num_sms, cudaStream_t s, cudaError_t *err) {
+  (void)num_sms;
+  *n_vf = *n_ee = *n_pairs = 0;
+  const int nf = topo.nf;
+  if (nf < 2) return 0;
+  const bool kdop = p.kind == kBvhKdop13;
+  // Buffers sized by the face count.
+  if (b.cap_faces < nf) {
+    broadphase_free(b);
+    const size_t F = (size_t)nf;
+    BP_CUDA(cudaMalloc(&b.lo64, 13 * F * sizeof(double)));
+    BP_CUDA(cudaMalloc(&b.hi64, 13 * F * sizeof(double)));
+    BP_CUDA(cudaMalloc(&b.leaf_lo, 2 * 13 * F * sizeof(float)));  // [sorted | face-indexed]
+    BP_CUDA(cudaMalloc(&b.leaf_hi, 2 * 13 * F * sizeof(float)));
+    BP_CUDA(cudaMalloc(&b.node_lo, 13 * F * sizeof(float)));
+    BP_CUDA(cudaMalloc(&b.node_hi, 13 * F * sizeof(float)));
+    BP_CUDA(cudaMalloc(&b.node_child, 2 * F * sizeof(int32_t)));
+    BP_CUDA(cudaMalloc(&b.node_range, 2 * F * sizeof(int32_t)));
+    BP_CUDA(cudaMalloc(&b.parent, 2 * F * sizeof(int32_t)));
+    BP_CUDA(cudaMalloc(&b.arrive, F * sizeof(uint32_t)));
+    BP_CUDA(cudaMalloc(&b.keys, F * sizeof(uint64_t)));
+    BP_CUDA(cudaMalloc(&b.vals, F * sizeof(uint64_t)));  // second Morton key buffer
+    BP_CUDA(cudaMalloc(&b.bounds, 8 * sizeof(float)));
+    BP_CUDA(cudaMalloc(&b.counters, 4 * sizeof(unsigned long long)));
+    b.cap_faces = nf;
+  }
+  // Pair-sized buffers; grown when a traversal reports more pairs.
+  auto ensure_pairs = [&](int64_t cap) -> int {
+    if (b.cap_pairs >= cap && b.pairs) return 0;
+    void *ptrs[] = {b.pairs, b.vf_keys, b.ee_keys, b.keys_alt, b.flags, b.scan, b.temp};
+    for (void *q : ptrs) cudaFree(q);
+    b.pairs = nullptr;
+    b.vf_keys = b.ee_keys = b.keys_alt = nullptr;
+    b.flags = b.scan = nullptr;
+    b.temp = nullptr;
+    b.cap_pairs = 0;
+    const int64_t nkeys = std::max<int64_t>(9 * cap, nf);
+    BP_CUDA(cudaMalloc(&b.pairs, (size_t)cap * 2 * sizeof(uint32_t)));
+    BP_CUDA(cudaMalloc(&b.vf_keys, (size_t)6 * cap * sizeof(uint64_t)));
+    BP_CUDA(cudaMalloc(&b.ee_keys, (size_t)9 * cap * sizeof(uint64_t)));
+    BP_CUDA(cudaMalloc(&b.keys_alt, (size_t)nkeys * sizeof(uint64_t)));
+    BP_CUDA(cudaMalloc(&b.flags, (size_t)nkeys * sizeof(uint32_t)));
+    BP_CUDA(cudaMalloc(&b.scan, (size_t)nkeys * sizeof(uint32_t)));
+    b.temp_bytes = std::max(radix_sort_temp_bytes(nkeys), scan_temp_bytes(nkeys));
+    BP_CUDA(cudaMalloc(&b.temp, b.temp_bytes));
+    b.cap_pairs = cap;
+    return 0;
+  };
+  int rc = ensure_pairs(std::max<int64_t>(b.cap_pairs, std::min<int64_t>(std::max<int64_t>(8 * (int64_t)nf, 4096), kMaxPairs)));
+  if (rc) return rc;
+
+  float *flo = b.leaf_lo + 13 * (size_t)nf, *fhi = b.leaf_hi + 13 * (size_t)nf;
+  const Axes ax = make_axes();
+  {
+    // centre bounds as order-preserving ints: +inf for minima, -inf for maxima
+    const int pinf = 0x7f800000, ninf = (int)(0x80000000u - 0xff800000u);
+    int hb[6] = {pinf, pinf, pinf, ninf, ninf, ninf};
+    BP_CUDA(cudaMemcpyAsync(b.bounds, hb, sizeof(hb), cudaMemcpyHostToDevice, s));
+  }
+  if (kdop)
+    leaf_slabs<13><<<grid_of(nf), kThreads, 0, s>>>(topo, p, ax, b.lo64, b.hi64, flo, fhi, b.bounds);
+  else
+    leaf_slabs<3><<<grid_of(nf), kThreads, 0, s>>>(topo, p, ax, b.lo64, b.hi64, flo, fhi, b.bounds);
+  BP_CUDA(cudaGetLastError());
+  morton_keys<<<grid_of(nf), kThreads, 0, s>>>(nf, flo, fhi, b.bounds, b.keys);
+  BP_CUDA(cudaGetLastError());
+  BP_CUDA(radix_sort_u64(b.keys, (uint64_t *)b.vals, nullptr, nullptr, nf, 0, 64, b.temp, b.temp_bytes, s));
+  if (kdop)
+    gather_leaves<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, flo, fhi, b.leaf_lo, b.leaf_hi);
+  else
+    gather_leaves<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, flo, fhi, b.leaf_lo, b.leaf_hi);
+  build_lbvh<<<grid_of(nf - 1), kThreads, 0, s>>>(nf, b.keys, b.node_child, b.node_range, b.parent);
+  BP_CUDA(cudaMemsetAsync(b.arrive, 0, (size_t)nf * sizeof(uint32_t), s));
+  BP_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(unsigned long long), s));
+  if (kdop)
+    refit<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.node_child, b.parent, b.arrive, b.leaf_lo, b.leaf_hi, b.node_lo,
+                                               b.node_hi, b.counters);
+  else
+    refit<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.node_child, b.parent, b.arrive, b.leaf_lo, b.leaf_hi, b.node_lo,
+                                              b.node_hi, b.counters);
+  BP_CUDA(cudaGetLastError());
+
+  for (;;) {
+    BP_CUDA(cudaMemsetAsync(b.counters, 0, 3 * sizeof(unsigned long long), s));  // keeps the error word
+    if (kdop)
+      find_pairs<13><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, b.node_child, b.node_range, b.leaf_lo,
+                                                      b.leaf_hi, b.node_lo, b.node_hi, b.lo64, b.hi64, b.pairs,
+                                                      (uint64_t)b.cap_pairs, b.counters);
+    else
+      find_pairs<3><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, b.node_child, b.node_range, b.leaf_lo,
+                                                     b.leaf_hi, b.node_lo, b.node_hi, b.lo64, b.hi64, b.pairs,
+                                                     (uint64_t)b.cap_pairs, b.counters);
+    BP_CUDA(cudaGetLastError());
+    unsigned long long hc[4];
+    BP_CUDA(cudaMemcpyAsync(hc, b.counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
+    BP_CUDA(cudaStreamSynchronize(s));
+    if (hc[3]) return 3;
+    *n_pairs = hc[0];
+    if ((int64_t)hc[0] <= b.cap_pairs) break;
+    if ((int64_t)hc[0] > kMaxPairs) return 4;
+    rc = ensure_pairs(std::min<int64_t>(2 * (int64_t)hc[0], kMaxPairs));  // the tree stays valid; only the pair buffers grow
+    if (rc) return rc;
+  }
+  const int64_t np = *n_pairs;
+  if (np == 0) return 0;
+  stencil_keys<<<grid_of(np), kThreads, 0, s>>>(topo, p.fixed, b.pairs, np, b.vf_keys, b.ee_keys);
+  BP_CUDA(cudaGetLastError());
+  // Sort, mark the first of each run of equal keys, scan, decode.
+  for (int which = 0; which < 2; which++) {
+    uint64_t *keys = which == 0 ? b.vf_keys : b.ee_keys;
+    const int64_t n = (which == 0 ? 6 : 9) * np;
+    BP_CUDA(radix_sort_u64(keys, b.keys_alt, nullptr, nullptr, n, 0, 64, b.temp, b.temp_bytes, s));
+    first_of_run<<<grid_of(n), kThreads, 0, s>>>(keys, n, b.flags);
+    BP_CUDA(cudaGetLastError());
+    uint32_t *total = (uint32_t *)(b.counters + 1 + which);
+    BP_CUDA(exclusive_scan_u32(b.flags, b.scan, n, total, b.temp, b.temp_bytes, s));
+    uint32_t count = 0;
+    BP_CUDA(cudaMemcpyAsync(&count, total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    BP_CUDA(cudaStreamSynchronize(s));
+    if (which == 0) {
+      BP_CUDA(grow(vf_out, vf_cap, 4 * (int64_t)count));
+      decode_vf<<<grid_of(n), kThreads, 0, s>>>(topo, keys, b.flags, b.scan, n, *vf_out);
+      *n_vf = count;
+    } else {
+      BP_CUDA(grow(ee_out, ee_cap, 4 * (int64_t)count));
+      decode_ee<<<grid_of(n), kThreads, 0, s>>>(topo, keys, b.flags, b.scan, n, *ee_out);
+      *n_ee = count;
+    }
+    BP_CUDA(cudaGetLastError());
+  }
+  BP_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+}  // namespace ccd

@@ -1,0 +1,78 @@
+// Swept-volume candidate search on the GPU: the candidate set of the
+// reference's KDOPBroadPhase / AABBBroadPhase::findCollisionCandidates
+// (src/KDOPBroadPhase.cpp:34-185, src/AABBBroadPhase.cpp:9-152) on a
+// two-entry history (start, end).
+//
+// The reference builds a median-split tree over per-face swept slabs and
+// self-intersects it; a face pair is reached exactly when its two leaf slabs
+// overlap on every axis (a parent's slab contains its children's), so the
+// candidate set is a function of the leaf slabs alone.  Here:
+//   1. leaf slabs in FP64 with the reference's arithmetic (pos . axis -+ eta,
+//      min/max over 3 vertices x 2 history entries), plus outward-rounded FP32
+//      copies (lower bounds rounded down, upper bounds up);
+//   2. Morton codes of the FP32 slab centres, radix sort, Karras LBVH,
+//      bottom-up refit of FP32 slabs (atomic arrival counters);
+//   3. stack traversal per leaf over leaves later in Morton order with the
+//      conservative FP32 test, then the reference's exact FP64 test
+//      (strict '<' rejection) and neighbour exclusion (any shared vertex);
+//   4. 6 vertex-face + 9 edge-edge stencils per pair (fixed-vertex filter),
+//      as 64-bit keys (vertex, face rank) and (edge rank, edge rank) whose
+//      order is the reference's std::set order; radix sort + unique.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ccd {
+
+enum BvhKind : int { kBvhKdop13 = 0, kBvhAabb = 1 };
+
+// Static topology of a mesh, ranks computed on the host once per mesh.
+struct MeshTopology {
+  int32_t nv, nf;
+  const int32_t *faces;        // [nf][3]
+  const int32_t *face_rank;    // [nf] rank of the face's sorted vertex triple
+  const int32_t *rank_triple;  // [nranks][3] sorted triple of each face rank
+  const int32_t *face_edges;   // [nf][3] rank of edge (v_i, v_{i+1 mod 3})
+  const int32_t *rank_edge;    // [nedges][2] (a <= b) of each edge rank
+};
+
+// Device buffers of one broad-phase call; grown by the caller.
+struct BroadphaseBuffers {
+  int64_t cap_faces = 0, cap_pairs = 0;
+  // per face / node
+  double *lo64 = nullptr, *hi64 = nullptr;        // [13][nf]
+  float *leaf_lo = nullptr, *leaf_hi = nullptr;   // [13][nf]   by sorted position
+  float *node_lo = nullptr, *node_hi = nullptr;   // [13][nf-1] internal nodes
+  int32_t *node_child = nullptr;                  // [nf-1][2]  >= 0 internal, < 0 leaf ~s
+  int32_t *node_range = nullptr;                  // [nf-1][2]  first, last sorted leaf
+  int32_t *parent = nullptr;                      // [2 nf]     internal then leaves
+  uint32_t *arrive = nullptr;                     // [nf]
+  uint64_t *keys = nullptr, *keys_alt = nullptr;  // [max(nf, 9 pairs)]
+  uint32_t *vals = nullptr, *vals_alt = nullptr;  // [2 nf]: second Morton key buffer
+  float *bounds = nullptr;                        // [6]
+  unsigned long long *counters = nullptr;         // [4] pairs, vf, ee, overflow
+  uint32_t *pairs = nullptr;                      // [cap_pairs][2]
+  uint64_t *vf_keys = nullptr, *ee_keys = nullptr;
+  uint32_t *flags = nullptr, *scan = nullptr;
+  void *temp = nullptr;
+  size_t temp_bytes = 0;
+};
+
+struct BroadphaseParams {
+  int kind;
+  double eta;
+  const double *qs, *qe;  // [nv][3]
+  const uint8_t *fixed;   // [nv] or null
+};
+
+// Runs the candidate search; on return (stream synchronised) n_vf / n_ee
+// hold the counts and vf_out / ee_out (device, [n][4] int32) the stencils in
+// the reference's order.  The output arrays are grown as needed.
+int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, BroadphaseBuffers &buf, int32_t **vf_out,
+                   int64_t *vf_cap, int32_t **ee_out, int64_t *ee_cap, int64_t *n_vf, int64_t *n_ee,
+                   int64_t *n_pairs, int num_sms, cudaStream_t s, cudaError_t *err);
+
+void broadphase_free(BroadphaseBuffers &buf);
+
+}  // namespace ccd

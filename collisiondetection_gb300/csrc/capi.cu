@@ -7,75 +7,11 @@
 #include <new>
 #include <string>
 
-#include "../../include/ccd_gb300.h"
-#include "narrow.cuh"
-#include "stages.cuh"
+#include "context.cuh"
 
 #define CCD_VERSION_NUMBER 100  // 0.1.0
 
-namespace {
-
-// Rows per chunk of the host-memory batch pipeline (two chunks in flight).
-constexpr int64_t kChunkRows = 1 << 20;
-// Survivor rows per tile of the staged refinement (bounds its scratch to
-// about 0.9 GB per execution slot).
-constexpr int64_t kStageTileRows = 1 << 20;
-
-// Scratch of the staged refinement, grown on demand.
-struct StageBuf {
-  void *mem = nullptr;
-  int64_t cap = 0;
-  ccd::StageScratch view{};
-};
-
-struct Slot {
-  double *rows = nullptr;
-  double *eta = nullptr;
-  uint8_t *hit = nullptr;
-  double *t = nullptr;
-  int32_t *surv = nullptr;
-  ccd::BatchCounters *counters = nullptr;    // device
-  ccd::BatchCounters *h_counters = nullptr;  // pinned host
-  cudaStream_t stream = nullptr;
-  cudaEvent_t done = nullptr;
-  int64_t cap = 0;
-  StageBuf stage;
-};
-
-// Events bracketing the kernels of one batch (profiling only).
-struct PhaseEvents {
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-  bool used = false;
-  bool culled = false;
-  int stage_launches = 0;
-};
-
-}  // namespace
-
-struct ccd_context {
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t own_stream = nullptr;
-  cudaStream_t stream = nullptr;
-  Slot slot[2];
-  // scratch for the device-memory entry points
-  StageBuf stage;
-  int32_t *d_surv = nullptr;
-  int64_t surv_cap = 0;
-  ccd::BatchCounters *d_counters = nullptr;
-  ccd::BatchCounters *h_counters = nullptr;
-  bool pending_stats = false;
-  ccd_batch_stats last{};
-  // per-kernel timing
-  bool profiling = false;
-  PhaseEvents phase[2];      // host-pipeline slots
-  PhaseEvents dev_ring[32];  // device entry points, collected lazily
-  int dev_next = 0;
-  ccd_batch_timings timings{};
-  std::string err;
-};
-
-namespace {
+namespace ccd_capi {
 
 int fail(ccd_context *ctx, int code, const std::string &msg) {
   if (ctx) ctx->err = msg;
@@ -87,11 +23,6 @@ int cuda_fail(ccd_context *ctx, cudaError_t e, const char *what) {
   return fail(ctx, code, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define CCD_CUDA(call)                                   \
-  do {                                                   \
-    cudaError_t e_ = (call);                             \
-    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
-  } while (0)
 
 int ensure_stage(ccd_context *ctx, StageBuf &sb, int64_t rows, cudaStream_t s) {
   int64_t cap = std::min<int64_t>(std::max<int64_t>(rows, 1), kStageTileRows);
@@ -214,7 +145,9 @@ void add_stats(ccd_batch_stats &st, const ccd::BatchCounters &c) {
   st.status_flags += (int64_t)c.status_flags;
 }
 
-}  // namespace
+}  // namespace ccd_capi
+
+using namespace ccd_capi;
 
 extern "C" {
 

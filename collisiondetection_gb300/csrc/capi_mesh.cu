@@ -1,0 +1,451 @@
+// C ABI (include/ccd_gb300.h): meshes, broad phase, narrow phase over stencils.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "broadphase.cuh"
+#include "context.cuh"
+#include "mesh.cuh"
+#include "radix_sort.cuh"
+
+using namespace ccd_capi;
+
+namespace {
+
+// Stencils per chunk of the narrow phase (bounds its row scratch to about
+// 1.2 GB).
+constexpr int64_t kNarrowChunk = 1 << 20;
+
+// Per-chunk rows and results of the narrow-phase chain.
+struct NarrowScratch {
+  int64_t cap = 0;  // stencils
+  double *prim = nullptr, *ve = nullptr, *vv = nullptr;
+  double *eta_prim = nullptr, *eta_ve = nullptr, *eta_vv = nullptr;
+  uint8_t *h_prim = nullptr, *h_ve = nullptr, *h_vv = nullptr;
+  double *t_prim = nullptr, *t_ve = nullptr, *t_vv = nullptr;
+  int32_t *surv = nullptr;
+  ccd::BatchCounters *counters = nullptr;
+  StageBuf stage;
+};
+
+template <class T>
+int grow(ccd_context *ctx, T **p, int64_t *cap, int64_t need) {
+  if (*cap >= need && *p) return CCD_OK;
+  cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  const int64_t c = std::max<int64_t>(need, 1);
+  CCD_CUDA(cudaMalloc(p, (size_t)c * sizeof(T)));
+  *cap = c;
+  return CCD_OK;
+}
+
+}  // namespace
+
+struct ccd_mesh {
+  ccd_context *ctx = nullptr;
+  int32_t nv = 0, nf = 0;
+  int32_t *faces = nullptr, *face_rank = nullptr, *rank_triple = nullptr, *face_edges = nullptr,
+          *rank_edge = nullptr;
+  double *qs = nullptr, *qe = nullptr;
+  uint8_t *fixed = nullptr;
+  bool has_fixed = false;
+  ccd::BroadphaseBuffers bp;
+  // candidates of the last broad phase: [0] vertex-face, [1] edge-edge
+  int32_t *cand[2] = {nullptr, nullptr};
+  int64_t cand_cap[2] = {0, 0};
+  int64_t n_cand[2] = {0, 0};
+  bool have_cand = false;
+  NarrowScratch ns;
+  // narrow-phase inputs/outputs of the host entry point and of detect
+  int32_t *in_st = nullptr;
+  int64_t in_st_cap = 0;
+  double *in_eta = nullptr;
+  int64_t in_eta_cap = 0;
+  uint8_t *hit = nullptr;
+  int64_t hit_cap = 0;
+  double *t = nullptr;
+  int64_t t_cap = 0;
+  int8_t *which = nullptr;
+  int64_t which_cap = 0;
+  double *d_eta = nullptr;
+  // collisions of the last detect
+  int32_t *col[2] = {nullptr, nullptr};
+  int64_t col_cap[2] = {0, 0};
+  double *col_t[2] = {nullptr, nullptr};
+  int64_t col_t_cap[2] = {0, 0};
+  int64_t n_col[2] = {0, 0};
+  bool have_col = false;
+  uint32_t *flags = nullptr, *pos = nullptr;
+  int64_t flags_cap = 0, pos_cap = 0;
+  char *scan_temp = nullptr;
+  int64_t scan_temp_cap = 0;
+  uint32_t *d_count = nullptr;
+  ccd_mesh_stats stats{};
+};
+
+namespace {
+
+int mesh_fail(ccd_mesh *m, int code, const std::string &msg) { return fail(m ? m->ctx : nullptr, code, msg); }
+
+int ensure_narrow(ccd_mesh *m, int64_t chunk) {
+  ccd_context *ctx = m->ctx;
+  NarrowScratch &n = m->ns;
+  if (n.cap >= chunk) return CCD_OK;
+  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+  void *ptrs[] = {n.prim, n.ve, n.vv, n.eta_prim, n.eta_ve, n.eta_vv, n.h_prim, n.h_ve, n.h_vv,
+                  n.t_prim, n.t_ve, n.t_vv, n.surv, n.counters, n.stage.mem};
+  for (void *p : ptrs) cudaFree(p);
+  n = NarrowScratch{};
+  const size_t c = (size_t)chunk, c4 = 4 * (size_t)chunk;
+  CCD_CUDA(cudaMalloc(&n.prim, c * 24 * sizeof(double)));
+  CCD_CUDA(cudaMalloc(&n.ve, c4 * 18 * sizeof(double)));
+  CCD_CUDA(cudaMalloc(&n.vv, c4 * 12 * sizeof(double)));
+  CCD_CUDA(cudaMalloc(&n.eta_prim, c * sizeof(double)));
+  CCD_CUDA(cudaMalloc(&n.eta_ve, c4 * sizeof(double)));
+  CCD_CUDA(cudaMalloc(&n.eta_vv, c4 * sizeof(double)));
+  CCD_CUDA(cudaMalloc(&n.h_prim, c));
+  CCD_CUDA(cudaMalloc(&n.h_ve, c4));
+  CCD_CUDA(cudaMalloc(&n.h_vv, c4));
+  CCD_CUDA(cudaMalloc(&n.t_prim, c * sizeof(double)));
+  CCD_CUDA(cudaMalloc(&n.t_ve, c4 * sizeof(double)));
+  CCD_CUDA(cudaMalloc(&n.t_vv, c4 * sizeof(double)));
+  CCD_CUDA(cudaMalloc(&n.surv, c4 * sizeof(int32_t)));
+  CCD_CUDA(cudaMalloc(&n.counters, sizeof(ccd::BatchCounters)));
+  n.cap = chunk;
+  return CCD_OK;
+}
+
+// The narrow-phase chain over n device stencils of one kind; results into
+// device arrays hit[n], t[n] (optional), which[n] (optional).
+int narrow_device(ccd_mesh *m, int kind, int path, int64_t n, const int32_t *st, const double *eta, bool eta_per_row,
+                  uint8_t *hit, double *t, int8_t *which) {
+  ccd_context *ctx = m->ctx;
+  if (n == 0) return CCD_OK;
+  const int64_t chunk = std::min<int64_t>(n, kNarrowChunk);
+  int rc = ensure_narrow(m, chunk);
+  if (rc) return rc;
+  NarrowScratch &ns = m->ns;
+  const int nsub = kind == CCD_VERTEX_FACE ? 3 : 4;
+  cudaStream_t s = ctx->stream;
+  for (int64_t off = 0; off < n; off += chunk) {
+    const int64_t c = std::min<int64_t>(chunk, n - off);
+    CCD_CUDA(ccd::gather_stencil_rows(kind, st + 4 * off, c, m->qs, m->qe, eta_per_row ? eta + off : eta,
+                                      eta_per_row ? 1 : 0, ns.prim, ns.ve, ns.vv, ns.eta_prim, ns.eta_ve, ns.eta_vv,
+                                      s));
+    const ccd::PrimBatch bp{kind, c, ns.prim, ns.eta_prim, true, ns.h_prim, ns.t_prim, nullptr, ns.counters};
+    rc = enqueue_batch(ctx, bp, path, ns.surv, ns.stage, s, nullptr);
+    if (rc) return rc;
+    const ccd::PrimBatch bve{CCD_VERTEX_EDGE, nsub * c, ns.ve, ns.eta_ve, true, ns.h_ve, ns.t_ve, nullptr,
+                             ns.counters};
+    rc = enqueue_batch(ctx, bve, CCD_PATH_FP64, ns.surv, ns.stage, s, nullptr);
+    if (rc) return rc;
+    const ccd::PrimBatch bvv{CCD_VERTEX_VERTEX, nsub * c, ns.vv, ns.eta_vv, true, ns.h_vv, ns.t_vv, nullptr,
+                             ns.counters};
+    rc = enqueue_batch(ctx, bvv, CCD_PATH_FP64, ns.surv, ns.stage, s, nullptr);
+    if (rc) return rc;
+    CCD_CUDA(ccd::combine_chain(kind, c, ns.h_prim, ns.t_prim, ns.h_ve, ns.t_ve, ns.h_vv, ns.t_vv, hit + off,
+                                t ? t + off : nullptr, which ? which + off : nullptr, s));
+  }
+  return CCD_OK;
+}
+
+int run_broadphase(ccd_mesh *m, int kind, double outer_eta) {
+  ccd_context *ctx = m->ctx;
+  m->have_cand = false;
+  m->have_col = false;
+  m->stats = ccd_mesh_stats{};
+  const ccd::MeshTopology topo{m->nv, m->nf, m->faces, m->face_rank, m->rank_triple, m->face_edges, m->rank_edge};
+  const ccd::BroadphaseParams p{kind, outer_eta, m->qs, m->qe, m->has_fixed ? m->fixed : nullptr};
+  cudaError_t err = cudaSuccess;
+  int64_t npairs = 0;
+  const int rc = ccd::broadphase_run(topo, p, m->bp, &m->cand[0], &m->cand_cap[0], &m->cand[1], &m->cand_cap[1],
+                                     &m->n_cand[0], &m->n_cand[1], &npairs, ctx->num_sms, ctx->stream, &err);
+  if (rc == 2) return cuda_fail(ctx, err, "broadphase");
+  if (rc == 3) return mesh_fail(m, CCD_ERR_CUDA, "broadphase: traversal stack overflow");
+  if (rc == 4) return mesh_fail(m, CCD_ERR_OUT_OF_MEMORY, "broadphase: more than 2^27 overlapping face pairs");
+  m->stats.face_pairs = npairs;
+  m->stats.n_vf = m->n_cand[0];
+  m->stats.n_ee = m->n_cand[1];
+  m->have_cand = true;
+  return CCD_OK;
+}
+
+int check_eta(ccd_mesh *m, int64_t n, const double *eta, int64_t eta_count) {
+  if (n == 0) return CCD_OK;
+  if (!eta || (eta_count != 1 && eta_count != n))
+    return mesh_fail(m, CCD_ERR_INVALID_ARGUMENT, "eta must hold 1 or n values");
+  return CCD_OK;
+}
+
+void free_mesh_buffers(ccd_mesh *m) {
+  void *ptrs[] = {m->faces, m->face_rank, m->rank_triple, m->face_edges, m->rank_edge, m->qs, m->qe, m->fixed,
+                  m->cand[0], m->cand[1], m->in_st, m->in_eta, m->hit, m->t, m->which, m->d_eta,
+                  m->col[0], m->col[1], m->col_t[0], m->col_t[1], m->flags, m->pos, m->scan_temp, m->d_count,
+                  m->ns.prim, m->ns.ve, m->ns.vv, m->ns.eta_prim, m->ns.eta_ve, m->ns.eta_vv, m->ns.h_prim,
+                  m->ns.h_ve, m->ns.h_vv, m->ns.t_prim, m->ns.t_ve, m->ns.t_vv, m->ns.surv, m->ns.counters,
+                  m->ns.stage.mem};
+  for (void *p : ptrs) cudaFree(p);
+  ccd::broadphase_free(m->bp);
+}
+
+}  // namespace
+
+extern "C" {
+
+int ccd_mesh_create(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int32_t *faces, ccd_mesh **out) {
+  if (!ctx || !out) return CCD_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (nverts <= 0 || nfaces < 0 || (nfaces > 0 && !faces))
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "mesh needs nverts > 0, nfaces >= 0 and a face array");
+  if ((int64_t)nverts > ((int64_t)1 << 30) || (int64_t)nfaces > ((int64_t)1 << 30))
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "mesh larger than 2^30 vertices or faces");
+  ccd::HostTopology topo;
+  if (!ccd::build_topology(nverts, nfaces, faces, topo))
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "face vertex index out of range");
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  ccd_mesh *m = new (std::nothrow) ccd_mesh();
+  if (!m) return fail(ctx, CCD_ERR_OUT_OF_MEMORY, "host allocation");
+  m->ctx = ctx;
+  m->nv = nverts;
+  m->nf = nfaces;
+  auto upload = [&](int32_t **dst, const int32_t *src, size_t count) -> int {
+    CCD_CUDA(cudaMalloc(dst, std::max<size_t>(count, 1) * sizeof(int32_t)));
+    if (count) CCD_CUDA(cudaMemcpy(*dst, src, count * sizeof(int32_t), cudaMemcpyHostToDevice));
+    return CCD_OK;
+  };
+  int rc = upload(&m->faces, faces, 3 * (size_t)nfaces);
+  if (!rc) rc = upload(&m->face_rank, topo.face_rank.data(), topo.face_rank.size());
+  if (!rc) rc = upload(&m->rank_triple, topo.rank_triple.data(), topo.rank_triple.size());
+  if (!rc) rc = upload(&m->face_edges, topo.face_edges.data(), topo.face_edges.size());
+  if (!rc) rc = upload(&m->rank_edge, topo.rank_edge.data(), topo.rank_edge.size());
+  auto alloc = [&]() -> int {
+    CCD_CUDA(cudaMalloc(&m->qs, 3 * (size_t)nverts * sizeof(double)));
+    CCD_CUDA(cudaMalloc(&m->qe, 3 * (size_t)nverts * sizeof(double)));
+    CCD_CUDA(cudaMemset(m->qs, 0, 3 * (size_t)nverts * sizeof(double)));
+    CCD_CUDA(cudaMemset(m->qe, 0, 3 * (size_t)nverts * sizeof(double)));
+    CCD_CUDA(cudaMalloc(&m->fixed, (size_t)nverts));
+    CCD_CUDA(cudaMalloc(&m->d_eta, sizeof(double)));
+    CCD_CUDA(cudaMalloc(&m->d_count, sizeof(uint32_t)));
+    return CCD_OK;
+  };
+  if (!rc) rc = alloc();
+  if (rc) {
+    free_mesh_buffers(m);
+    delete m;
+    return rc;
+  }
+  *out = m;
+  return CCD_OK;
+}
+
+int ccd_mesh_destroy(ccd_mesh *m) {
+  if (!m) return CCD_OK;
+  cudaSetDevice(m->ctx->device);
+  cudaStreamSynchronize(m->ctx->stream);
+  free_mesh_buffers(m);
+  delete m;
+  return CCD_OK;
+}
+
+int ccd_mesh_set_positions(ccd_mesh *m, const double *qstart, const double *qend) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  if (!qstart || !qend) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null positions");
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  const size_t bytes = 3 * (size_t)m->nv * sizeof(double);
+  CCD_CUDA(cudaMemcpyAsync(m->qs, qstart, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  CCD_CUDA(cudaMemcpyAsync(m->qe, qend, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+  m->have_cand = m->have_col = false;
+  return CCD_OK;
+}
+
+int ccd_mesh_set_positions_device(ccd_mesh *m, const double *qstart, const double *qend) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  if (!qstart || !qend) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null positions");
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  const size_t bytes = 3 * (size_t)m->nv * sizeof(double);
+  CCD_CUDA(cudaMemcpyAsync(m->qs, qstart, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  CCD_CUDA(cudaMemcpyAsync(m->qe, qend, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  m->have_cand = m->have_col = false;
+  return CCD_OK;
+}
+
+int ccd_mesh_set_fixed(ccd_mesh *m, const uint8_t *fixed) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  if (fixed) {
+    // Normalise to 0/1 on the host.
+    std::vector<uint8_t> f(fixed, fixed + m->nv);
+    for (auto &x : f) x = x ? 1 : 0;
+    CCD_CUDA(cudaMemcpy(m->fixed, f.data(), (size_t)m->nv, cudaMemcpyHostToDevice));
+  }
+  m->has_fixed = fixed != nullptr;
+  m->have_cand = m->have_col = false;
+  return CCD_OK;
+}
+
+int ccd_broadphase(ccd_mesh *m, int kind, double outer_eta, int64_t *n_vf, int64_t *n_ee) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  if (kind != CCD_BROADPHASE_KDOP13 && kind != CCD_BROADPHASE_AABB)
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown broadphase kind");
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  int rc = run_broadphase(m, kind, outer_eta);
+  if (rc) return rc;
+  if (n_vf) *n_vf = m->n_cand[0];
+  if (n_ee) *n_ee = m->n_cand[1];
+  return CCD_OK;
+}
+
+int ccd_broadphase_get(ccd_mesh *m, int32_t *vf, int32_t *ee) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  if (!m->have_cand) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "no broad phase result on this mesh");
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  if (vf && m->n_cand[0])
+    CCD_CUDA(cudaMemcpy(vf, m->cand[0], (size_t)m->n_cand[0] * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (ee && m->n_cand[1])
+    CCD_CUDA(cudaMemcpy(ee, m->cand[1], (size_t)m->n_cand[1] * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return CCD_OK;
+}
+
+int ccd_narrowphase(ccd_mesh *m, int path, int64_t n_vf, const int32_t *vf, const double *vf_eta,
+                    int64_t vf_eta_count, int64_t n_ee, const int32_t *ee, const double *ee_eta, int64_t ee_eta_count,
+                    uint8_t *vf_hit, uint8_t *ee_hit, double *vf_t, double *ee_t, int8_t *vf_which,
+                    int8_t *ee_which) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  if (path != CCD_PATH_FP64 && path != CCD_PATH_CULL_REFINE)
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown path");
+  if (n_vf < 0 || n_ee < 0 || n_vf > INT32_MAX / 4 || n_ee > INT32_MAX / 4)
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "stencil counts must be in [0, 2^29)");
+  if ((n_vf && (!vf || !vf_hit)) || (n_ee && (!ee || !ee_hit)))
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null stencil or hit array");
+  int rc = check_eta(m, n_vf, vf_eta, vf_eta_count);
+  if (!rc) rc = check_eta(m, n_ee, ee_eta, ee_eta_count);
+  if (rc) return rc;
+  // Reject out-of-range vertex indices before anything touches the device.
+  for (int k = 0; k < 2; k++) {
+    const int32_t *st = k ? ee : vf;
+    const int64_t n = k ? n_ee : n_vf;
+    for (int64_t i = 0; i < 4 * n; i++)
+      if (st[i] < 0 || st[i] >= m->nv) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "stencil vertex out of range");
+  }
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  m->stats.n_vf = n_vf;
+  m->stats.n_ee = n_ee;
+  m->stats.vf_hits = m->stats.ee_hits = 0;
+  m->stats.face_pairs = 0;
+  std::vector<double> tbuf;
+  for (int k = 0; k < 2; k++) {
+    const int64_t n = k ? n_ee : n_vf;
+    if (n == 0) continue;
+    const int32_t *st = k ? ee : vf;
+    const double *eta = k ? ee_eta : vf_eta;
+    const int64_t eta_count = k ? ee_eta_count : vf_eta_count;
+    uint8_t *hit = k ? ee_hit : vf_hit;
+    double *t = k ? ee_t : vf_t;
+    int8_t *which = k ? ee_which : vf_which;
+    rc = grow(ctx, &m->in_st, &m->in_st_cap, 4 * n);
+    if (!rc) rc = grow(ctx, &m->in_eta, &m->in_eta_cap, eta_count);
+    if (!rc) rc = grow(ctx, &m->hit, &m->hit_cap, n);
+    if (!rc) rc = grow(ctx, &m->t, &m->t_cap, n);
+    if (!rc) rc = grow(ctx, &m->which, &m->which_cap, n);
+    if (rc) return rc;
+    CCD_CUDA(cudaMemcpyAsync(m->in_st, st, (size_t)n * 4 * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    CCD_CUDA(cudaMemcpyAsync(m->in_eta, eta, (size_t)eta_count * sizeof(double), cudaMemcpyHostToDevice,
+                             ctx->stream));
+    rc = narrow_device(m, k ? CCD_EDGE_EDGE : CCD_VERTEX_FACE, path, n, m->in_st, m->in_eta, eta_count == n && n != 1,
+                       m->hit, m->t, m->which);
+    if (rc) return rc;
+    CCD_CUDA(cudaMemcpyAsync(hit, m->hit, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (which) CCD_CUDA(cudaMemcpyAsync(which, m->which, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (t) {
+      tbuf.resize((size_t)n);
+      CCD_CUDA(cudaMemcpyAsync(tbuf.data(), m->t, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+    int64_t hits = 0;
+    for (int64_t i = 0; i < n; i++) {
+      hits += hit[i] != 0;
+      if (t && hit[i]) t[i] = tbuf[(size_t)i];
+    }
+    (k ? m->stats.ee_hits : m->stats.vf_hits) = hits;
+  }
+  return CCD_OK;
+}
+
+int ccd_mesh_detect(ccd_mesh *m, int broadphase_kind, double outer_eta, double eta, int path, int64_t *vf_hits,
+                    int64_t *ee_hits) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  if (broadphase_kind != CCD_BROADPHASE_KDOP13 && broadphase_kind != CCD_BROADPHASE_AABB)
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown broadphase kind");
+  if (path != CCD_PATH_FP64 && path != CCD_PATH_CULL_REFINE)
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown path");
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  int rc = run_broadphase(m, broadphase_kind, outer_eta);
+  if (rc) return rc;
+  CCD_CUDA(cudaMemcpyAsync(m->d_eta, &eta, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  const int64_t nmax = std::max(m->n_cand[0], m->n_cand[1]);
+  rc = grow(ctx, &m->hit, &m->hit_cap, nmax);
+  if (!rc) rc = grow(ctx, &m->t, &m->t_cap, nmax);
+  if (!rc) rc = grow(ctx, &m->flags, &m->flags_cap, nmax);
+  if (!rc) rc = grow(ctx, &m->pos, &m->pos_cap, nmax);
+  if (!rc) rc = grow(ctx, &m->scan_temp, &m->scan_temp_cap, (int64_t)ccd::scan_temp_bytes(nmax));
+  if (rc) return rc;
+  for (int k = 0; k < 2; k++) {
+    const int64_t n = m->n_cand[k];
+    rc = grow(ctx, &m->col[k], &m->col_cap[k], 4 * n);
+    if (!rc) rc = grow(ctx, &m->col_t[k], &m->col_t_cap[k], n);
+    if (rc) return rc;
+    rc = narrow_device(m, k ? CCD_EDGE_EDGE : CCD_VERTEX_FACE, path, n, m->cand[k], m->d_eta, false, m->hit, m->t,
+                       nullptr);
+    if (rc) return rc;
+    CCD_CUDA(ccd::compact_hits(m->cand[k], m->hit, m->t, n, m->flags, m->pos, m->d_count, m->scan_temp,
+                               (size_t)m->scan_temp_cap, m->col[k], m->col_t[k], ctx->stream));
+    uint32_t count = 0;
+    CCD_CUDA(cudaMemcpyAsync(&count, m->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+    m->n_col[k] = count;
+  }
+  m->stats.vf_hits = m->n_col[0];
+  m->stats.ee_hits = m->n_col[1];
+  m->have_col = true;
+  if (vf_hits) *vf_hits = m->n_col[0];
+  if (ee_hits) *ee_hits = m->n_col[1];
+  return CCD_OK;
+}
+
+int ccd_mesh_get_collisions(ccd_mesh *m, int32_t *vf, double *vf_t, int32_t *ee, double *ee_t) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  if (!m->have_col) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "no detection result on this mesh");
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  int32_t *st[2] = {vf, ee};
+  double *tt[2] = {vf_t, ee_t};
+  for (int k = 0; k < 2; k++) {
+    const int64_t n = m->n_col[k];
+    if (!n) continue;
+    if (st[k]) CCD_CUDA(cudaMemcpy(st[k], m->col[k], (size_t)n * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (tt[k]) CCD_CUDA(cudaMemcpy(tt[k], m->col_t[k], (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  return CCD_OK;
+}
+
+int ccd_mesh_last_stats(const ccd_mesh *m, ccd_mesh_stats *out) {
+  if (!m || !out) return CCD_ERR_INVALID_ARGUMENT;
+  *out = m->stats;
+  return CCD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,97 @@
+// Internal state behind the C ABI, shared by the primitive-batch and mesh
+// translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/ccd_gb300.h"
+#include "narrow.cuh"
+#include "stages.cuh"
+
+namespace ccd_capi {
+
+// Rows per chunk of the host-memory batch pipeline (two chunks in flight).
+constexpr int64_t kChunkRows = 1 << 20;
+// Survivor rows per tile of the staged refinement (bounds its scratch to
+// about 0.9 GB per execution slot).
+constexpr int64_t kStageTileRows = 1 << 20;
+
+// Scratch of the staged refinement, grown on demand.
+struct StageBuf {
+  void *mem = nullptr;
+  int64_t cap = 0;
+  ccd::StageScratch view{};
+};
+
+struct Slot {
+  double *rows = nullptr;
+  double *eta = nullptr;
+  uint8_t *hit = nullptr;
+  double *t = nullptr;
+  int32_t *surv = nullptr;
+  ccd::BatchCounters *counters = nullptr;    // device
+  ccd::BatchCounters *h_counters = nullptr;  // pinned host
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  int64_t cap = 0;
+  StageBuf stage;
+};
+
+// Events bracketing the kernels of one batch (profiling only).
+struct PhaseEvents {
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  bool used = false;
+  bool culled = false;
+  int stage_launches = 0;
+};
+
+}  // namespace ccd_capi
+
+using ccd_capi::PhaseEvents;
+using ccd_capi::Slot;
+using ccd_capi::StageBuf;
+
+struct ccd_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  Slot slot[2];
+  // scratch for the device-memory entry points
+  StageBuf stage;
+  int32_t *d_surv = nullptr;
+  int64_t surv_cap = 0;
+  ccd::BatchCounters *d_counters = nullptr;
+  ccd::BatchCounters *h_counters = nullptr;
+  bool pending_stats = false;
+  ccd_batch_stats last{};
+  // per-kernel timing
+  bool profiling = false;
+  PhaseEvents phase[2];      // host-pipeline slots
+  PhaseEvents dev_ring[32];  // device entry points, collected lazily
+  int dev_next = 0;
+  ccd_batch_timings timings{};
+  std::string err;
+};
+
+
+namespace ccd_capi {
+
+int fail(ccd_context *ctx, int code, const std::string &msg);
+int cuda_fail(ccd_context *ctx, cudaError_t e, const char *what);
+// Grows a staged-refinement scratch to cover min(rows, tile) survivor rows.
+int ensure_stage(ccd_context *ctx, StageBuf &sb, int64_t rows, cudaStream_t s);
+// Enqueues the kernels of one batch whose buffers are all on the device.
+int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *surv, StageBuf &stage,
+                  cudaStream_t s, PhaseEvents *pe);
+
+}  // namespace ccd_capi
+
+#define CCD_CUDA(call)                                       \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return ccd_capi::cuda_fail(ctx, e_, #call); \
+  } while (0)

@@ -118,6 +118,83 @@ int ccd_prim_batch(ccd_context *ctx, int kind, int path, int64_t n, const double
 int ccd_prim_batch_device(ccd_context *ctx, int kind, int path, int64_t n, const double *rows, const double *eta,
                           int64_t eta_count, uint8_t *hit, double *t, uint8_t *status);
 
+/* ------------------------------------------------------------------ meshes
+ * A triangle mesh resident on its context's device: the faces of the
+ * reference's Mesh (src/Mesh.h: Matrix3Xi faces, 3 x F, column-major, which
+ * is [F][3] int32 in memory) and one step of its History with two entries,
+ * start (time 0) and end (time 1) (src/History.h; VectorXd positions,
+ * [V][3] doubles, xyz per vertex).  Stencils are int32 [n][4]:
+ *   vertex-face  p q0 q1 q2   (VertexFaceStencil, src/Stencils.h:7-81)
+ *   edge-edge    p0 p1 q0 q1  (EdgeEdgeStencil,   src/Stencils.h:83-137)
+ * Candidate lists come out canonical (q0 <= q1 <= q2; p0 <= p1, q0 <= q1,
+ * p0 <= q0) and in the reference's std::set order.  A mesh uses its
+ * context's stream and is not thread-safe; it must be destroyed before its
+ * context. */
+typedef struct ccd_mesh ccd_mesh;
+
+typedef enum {
+  CCD_BROADPHASE_KDOP13 = 0, /* KDOPBroadPhase (src/KDOPBroadPhase.cpp) */
+  CCD_BROADPHASE_AABB = 1    /* AABBBroadPhase (src/AABBBroadPhase.cpp) */
+} ccd_broadphase_kind;
+
+/* Counters of the most recent broad/narrow phase call on a mesh. */
+typedef struct {
+  int64_t face_pairs; /* face pairs whose swept volumes overlap, neighbours excluded */
+  int64_t n_vf;       /* vertex-face stencils tested (candidates) */
+  int64_t n_ee;       /* edge-edge stencils tested (candidates) */
+  int64_t vf_hits;    /* colliding vertex-face stencils */
+  int64_t ee_hits;    /* colliding edge-edge stencils */
+} ccd_mesh_stats;
+
+/* faces: nfaces x 3 vertex indices in [0, nverts).  Topology is fixed for the
+ * mesh's lifetime; positions change per step. */
+int ccd_mesh_create(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int32_t *faces, ccd_mesh **out);
+int ccd_mesh_destroy(ccd_mesh *mesh);
+/* Start and end positions of the step (History entries at t = 0 and 1), host
+ * memory; blocks until copied. */
+int ccd_mesh_set_positions(ccd_mesh *mesh, const double *qstart, const double *qend);
+/* The same from device memory; enqueued on the context's stream. */
+int ccd_mesh_set_positions_device(ccd_mesh *mesh, const double *qstart, const double *qend);
+/* fixedVerts as nverts bytes (non-zero = fixed), or NULL for none. */
+int ccd_mesh_set_fixed(ccd_mesh *mesh, const uint8_t *fixed);
+
+/* BroadPhase::findCollisionCandidates (src/RetrospectiveDetection.h:13;
+ * KDOPBroadPhase.cpp:34-40, AABBBroadPhase.cpp:9-15): every vertex-face and
+ * edge-edge stencil of the non-neighbouring face pairs whose swept volumes,
+ * padded by outer_eta, overlap, minus stencils whose four vertices are all
+ * fixed.  Writes the counts; the stencils stay on the device. */
+int ccd_broadphase(ccd_mesh *mesh, int kind, double outer_eta, int64_t *n_vf, int64_t *n_ee);
+/* Copies the last broad phase's stencils to host arrays of [n_vf][4] and
+ * [n_ee][4] int32 (either may be NULL). */
+int ccd_broadphase_get(ccd_mesh *mesh, int32_t *vf, int32_t *ee);
+
+/* NarrowPhase::findCollisions with CTCDNarrowPhase (src/CTCDNarrowPhase.cpp:
+ * 9-135) over caller stencils in host memory: hit[i] = 1 if stencil i
+ * collides during the step with its eta (eta arrays hold 1 shared value or one
+ * per stencil), tested as vertex-face (or edge-edge), then its 3 (4)
+ * vertex-edge, then its 3 (4) vertex-vertex sub-tests.  The reference returns
+ * the set of colliding stencils; here the caller gets one flag per input.
+ * Optional outputs (NULL to skip): t of the first sub-test that hits (written
+ * only where hit = 1; a vertex-vertex t can be negative, as in the reference),
+ * and which sub-test hit (0 primitive, 1 vertex-edge, 2 vertex-vertex, -1
+ * miss).  path: ccd_path of the primitive tests. */
+int ccd_narrowphase(ccd_mesh *mesh, int path, int64_t n_vf, const int32_t *vf, const double *vf_eta,
+                    int64_t vf_eta_count, int64_t n_ee, const int32_t *ee, const double *ee_eta, int64_t ee_eta_count,
+                    uint8_t *vf_hit, uint8_t *ee_hit, double *vf_t, double *ee_t, int8_t *vf_which,
+                    int8_t *ee_which);
+
+/* One detection step on the device, as the reference's callers chain it
+ * (example/AlecTest.cpp:97-111): broad phase with outer_eta, then the narrow
+ * phase over every candidate with eta.  Writes the numbers of colliding
+ * stencils (optional); the collisions stay on the device for
+ * ccd_mesh_get_collisions, the candidates for ccd_broadphase_get. */
+int ccd_mesh_detect(ccd_mesh *mesh, int broadphase_kind, double outer_eta, double eta, int path, int64_t *vf_hits,
+                    int64_t *ee_hits);
+/* Colliding stencils of the last ccd_mesh_detect in the reference's set
+ * order with the t of their first hitting sub-test; any pointer may be NULL. */
+int ccd_mesh_get_collisions(ccd_mesh *mesh, int32_t *vf, double *vf_t, int32_t *ee, double *ee_t);
+int ccd_mesh_last_stats(const ccd_mesh *mesh, ccd_mesh_stats *out);
+
 #ifdef __cplusplus
 }
 #endif
