@@ -1,0 +1,247 @@
+// Drop-in adapters between the reference's C++ types (evouga/collisiondetection)
+// and the C ABI of libccd_gb300.so (ccd_gb300.h).  Header-only; compiled
+// inside the reference's own build, with its headers (CTCD.h, History.h,
+// Mesh.h, Stencils.h, RetrospectiveDetection.h) and Eigen on the include path.
+//
+//   ccd_gb300::vertexFaceCTCD ... vertexVertexCTCD
+//       same signatures and results as the CTCD statics (include/CTCD.h:36-79);
+//       the body of each CTCD static can forward to them
+//   ccd_gb300::GpuKDOPBroadPhase, ccd_gb300::GpuAABBBroadPhase : BroadPhase
+//       findCollisionCandidates (src/RetrospectiveDetection.h:13)
+//   ccd_gb300::GpuCTCDNarrowPhase : NarrowPhase
+//       findCollisions (src/RetrospectiveDetection.h:20), CTCDNarrowPhase's results
+//
+// The GPU path covers histories of two entries per vertex (start at time 0,
+// end at time 1: History(qstart) + finishHistory(qend)); a longer history
+// raises std::runtime_error.  Errors of the C ABI raise std::runtime_error
+// with the library's message.
+#ifndef CCD_GB300_REFERENCE_HPP
+#define CCD_GB300_REFERENCE_HPP
+
+#include <stdint.h>
+
+#include <algorithm>
+#include <memory>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "CTCD.h"
+#include "History.h"
+#include "Mesh.h"
+#include "RetrospectiveDetection.h"
+#include "Stencils.h"
+#include "ccd_gb300.h"
+
+namespace ccd_gb300 {
+
+inline void check(ccd_context *ctx, int rc, const char *what) {
+  if (rc != CCD_OK)
+    throw std::runtime_error(std::string(what) + ": " + ccd_status_string(rc) + ": " + ccd_last_error(ctx));
+}
+
+// One process-wide context on device 0, created on first use.
+inline ccd_context *default_context() {
+  static ccd_context *ctx = [] {
+    ccd_context *c = nullptr;
+    const int rc = ccd_context_create(0, &c);
+    if (rc != CCD_OK) throw std::runtime_error(std::string("ccd_context_create: ") + ccd_status_string(rc));
+    return c;
+  }();
+  return ctx;
+}
+
+inline void put(double *dst, const Eigen::Vector3d &v) {
+  dst[0] = v[0];
+  dst[1] = v[1];
+  dst[2] = v[2];
+}
+
+// ------------------------------------------------------------------ CTCD statics
+inline bool edgeEdgeCTCD(const Eigen::Vector3d &q0start, const Eigen::Vector3d &p0start,
+                         const Eigen::Vector3d &q1start, const Eigen::Vector3d &p1start,
+                         const Eigen::Vector3d &q0end, const Eigen::Vector3d &p0end, const Eigen::Vector3d &q1end,
+                         const Eigen::Vector3d &p1end, double eta, double &t) {
+  double x[24];
+  const Eigen::Vector3d *pts[8] = {&q0start, &p0start, &q1start, &p1start, &q0end, &p0end, &q1end, &p1end};
+  for (int i = 0; i < 8; i++) put(x + 3 * i, *pts[i]);
+  int hit = 0;
+  check(default_context(), ccd_edge_edge_ctcd(default_context(), x, eta, &hit, &t), "ccd_edge_edge_ctcd");
+  return hit != 0;
+}
+
+inline bool vertexFaceCTCD(const Eigen::Vector3d &q0start, const Eigen::Vector3d &q1start,
+                           const Eigen::Vector3d &q2start, const Eigen::Vector3d &q3start,
+                           const Eigen::Vector3d &q0end, const Eigen::Vector3d &q1end, const Eigen::Vector3d &q2end,
+                           const Eigen::Vector3d &q3end, double eta, double &t) {
+  double x[24];
+  const Eigen::Vector3d *pts[8] = {&q0start, &q1start, &q2start, &q3start, &q0end, &q1end, &q2end, &q3end};
+  for (int i = 0; i < 8; i++) put(x + 3 * i, *pts[i]);
+  int hit = 0;
+  check(default_context(), ccd_vertex_face_ctcd(default_context(), x, eta, &hit, &t), "ccd_vertex_face_ctcd");
+  return hit != 0;
+}
+
+inline bool vertexEdgeCTCD(const Eigen::Vector3d &q0start, const Eigen::Vector3d &q1start,
+                           const Eigen::Vector3d &q2start, const Eigen::Vector3d &q0end, const Eigen::Vector3d &q1end,
+                           const Eigen::Vector3d &q2end, double eta, double &t) {
+  double x[18];
+  const Eigen::Vector3d *pts[6] = {&q0start, &q1start, &q2start, &q0end, &q1end, &q2end};
+  for (int i = 0; i < 6; i++) put(x + 3 * i, *pts[i]);
+  int hit = 0;
+  check(default_context(), ccd_vertex_edge_ctcd(default_context(), x, eta, &hit, &t), "ccd_vertex_edge_ctcd");
+  return hit != 0;
+}
+
+inline bool vertexVertexCTCD(const Eigen::Vector3d &q1start, const Eigen::Vector3d &q2start,
+                             const Eigen::Vector3d &q1end, const Eigen::Vector3d &q2end, double eta, double &t) {
+  double x[12];
+  const Eigen::Vector3d *pts[4] = {&q1start, &q2start, &q1end, &q2end};
+  for (int i = 0; i < 4; i++) put(x + 3 * i, *pts[i]);
+  int hit = 0;
+  check(default_context(), ccd_vertex_vertex_ctcd(default_context(), x, eta, &hit, &t), "ccd_vertex_vertex_ctcd");
+  return hit != 0;
+}
+
+// ------------------------------------------------------------------ meshes
+// A device mesh that follows the faces of the reference Mesh it is given:
+// re-created when the topology changes, positions uploaded on every call.
+class DeviceMesh {
+ public:
+  explicit DeviceMesh(ccd_context *ctx = default_context()) : ctx_(ctx) {}
+  ~DeviceMesh() { ccd_mesh_destroy(mesh_); }
+  DeviceMesh(const DeviceMesh &) = delete;
+  DeviceMesh &operator=(const DeviceMesh &) = delete;
+
+  // Uploads faces (if changed), the two history entries and the fixed set.
+  ccd_mesh *sync(const History &h, const Mesh &m, const std::set<int> *fixedVerts) {
+    const int nf = (int)m.faces.cols();
+    std::vector<int32_t> faces(3 * (size_t)nf);
+    for (int f = 0; f < nf; f++)
+      for (int j = 0; j < 3; j++) faces[3 * (size_t)f + j] = m.faces.coeff(j, f);
+    const int nv = (int)(m.vertices.size() / 3);
+    if (!mesh_ || faces != faces_ || nv != nv_) {
+      ccd_mesh_destroy(mesh_);
+      mesh_ = nullptr;
+      check(ctx_, ccd_mesh_create(ctx_, nv, nf, faces.data(), &mesh_), "ccd_mesh_create");
+      faces_.swap(faces);
+      nv_ = nv;
+    }
+    qs_.resize(3 * (size_t)nv);
+    qe_.resize(3 * (size_t)nv);
+    for (int v = 0; v < nv; v++) {
+      const std::vector<HistoryEntry> &e = h.getVertexHistory(v);
+      if (e.size() != 2) throw std::runtime_error("ccd_gb300: only two-entry histories (start, end) are supported");
+      put(&qs_[3 * (size_t)v], e.front().pos);
+      put(&qe_[3 * (size_t)v], e.back().pos);
+    }
+    check(ctx_, ccd_mesh_set_positions(mesh_, qs_.data(), qe_.data()), "ccd_mesh_set_positions");
+    if (fixedVerts) {
+      std::vector<uint8_t> fx((size_t)nv, 0);
+      bool any = false;
+      for (int v : *fixedVerts)
+        if (v >= 0 && v < nv) fx[(size_t)v] = 1, any = true;
+      check(ctx_, ccd_mesh_set_fixed(mesh_, any ? fx.data() : nullptr), "ccd_mesh_set_fixed");
+    }
+    return mesh_;
+  }
+  ccd_context *context() const { return ctx_; }
+
+ private:
+  ccd_context *ctx_;
+  ccd_mesh *mesh_ = nullptr;
+  std::vector<int32_t> faces_;
+  int nv_ = -1;
+  std::vector<double> qs_, qe_;
+};
+
+// ------------------------------------------------------------------ broad phases
+template <int Kind>
+class GpuBroadPhase : public BroadPhase {
+ public:
+  explicit GpuBroadPhase(ccd_context *ctx = default_context()) : mesh_(ctx) {}
+
+  // Clears and fills the sets, as KDOPBroadPhase.cpp:34-40 does.
+  virtual void findCollisionCandidates(const History &h, const Mesh &m, double outerEta,
+                                       std::set<VertexFaceStencil> &vfs, std::set<EdgeEdgeStencil> &ees,
+                                       const std::set<int> &fixedVerts) {
+    vfs.clear();
+    ees.clear();
+    ccd_mesh *dm = mesh_.sync(h, m, &fixedVerts);
+    int64_t nvf = 0, nee = 0;
+    check(mesh_.context(), ccd_broadphase(dm, Kind, outerEta, &nvf, &nee), "ccd_broadphase");
+    std::vector<int32_t> vf(4 * (size_t)nvf), ee(4 * (size_t)nee);
+    check(mesh_.context(), ccd_broadphase_get(dm, vf.data(), ee.data()), "ccd_broadphase_get");
+    // The lists are in set order: append at the end.
+    for (int64_t i = 0; i < nvf; i++)
+      vfs.insert(vfs.end(), VertexFaceStencil(vf[4 * i], vf[4 * i + 1], vf[4 * i + 2], vf[4 * i + 3]));
+    for (int64_t i = 0; i < nee; i++)
+      ees.insert(ees.end(), EdgeEdgeStencil(ee[4 * i], ee[4 * i + 1], ee[4 * i + 2], ee[4 * i + 3]));
+  }
+
+ private:
+  DeviceMesh mesh_;
+};
+
+typedef GpuBroadPhase<CCD_BROADPHASE_KDOP13> GpuKDOPBroadPhase;
+typedef GpuBroadPhase<CCD_BROADPHASE_AABB> GpuAABBBroadPhase;
+
+// ------------------------------------------------------------------ narrow phase
+class GpuCTCDNarrowPhase : public NarrowPhase {
+ public:
+  explicit GpuCTCDNarrowPhase(ccd_context *ctx = default_context(), int path = CCD_PATH_CULL_REFINE)
+      : ctx_(ctx), path_(path) {}
+
+  // Appends the colliding stencils to vfs / ees (which are not cleared), as
+  // CTCDNarrowPhase::findCollisions does (src/CTCDNarrowPhase.cpp:9-24).  The
+  // mesh positions come from the history; the narrow phase needs no faces.
+  virtual void findCollisions(const History &h, const std::set<std::pair<VertexFaceStencil, double> > &candidateVFS,
+                              const std::set<std::pair<EdgeEdgeStencil, double> > &candidateEES,
+                              std::set<VertexFaceStencil> &vfs, std::set<EdgeEdgeStencil> &ees) {
+    int nv = 0;
+    for (const auto &c : candidateVFS) nv = std::max(nv, std::max(c.first.p, c.first.q2) + 1);
+    for (const auto &c : candidateEES) nv = std::max(nv, std::max(c.first.p1, c.first.q1) + 1);
+    if (nv == 0) return;
+    Mesh points;
+    points.vertices.resize(3 * nv);
+    points.faces.resize(3, 0);
+    ccd_mesh *dm = mesh_for(h, points);
+    std::vector<int32_t> vf, ee;
+    std::vector<double> vfe, eee;
+    for (const auto &c : candidateVFS) {
+      vf.insert(vf.end(), {c.first.p, c.first.q0, c.first.q1, c.first.q2});
+      vfe.push_back(c.second);
+    }
+    for (const auto &c : candidateEES) {
+      ee.insert(ee.end(), {c.first.p0, c.first.p1, c.first.q0, c.first.q1});
+      eee.push_back(c.second);
+    }
+    std::vector<uint8_t> vh(vfe.size()), eh(eee.size());
+    check(ctx_,
+          ccd_narrowphase(dm, path_, (int64_t)vfe.size(), vf.data(), vfe.data(), (int64_t)vfe.size(),
+                          (int64_t)eee.size(), ee.data(), eee.data(), (int64_t)eee.size(), vh.data(), eh.data(),
+                          nullptr, nullptr, nullptr, nullptr),
+          "ccd_narrowphase");
+    size_t i = 0;
+    for (const auto &c : candidateVFS)
+      if (vh[i++]) vfs.insert(c.first);
+    i = 0;
+    for (const auto &c : candidateEES)
+      if (eh[i++]) ees.insert(c.first);
+  }
+
+ private:
+  ccd_mesh *mesh_for(const History &h, const Mesh &points) {
+    if (!dev_) dev_.reset(new DeviceMesh(ctx_));
+    return dev_->sync(h, points, nullptr);
+  }
+  ccd_context *ctx_;
+  int path_;
+  std::unique_ptr<DeviceMesh> dev_;
+};
+
+}  // namespace ccd_gb300
+
+#endif  // CCD_GB300_REFERENCE_HPP
