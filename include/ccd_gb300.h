@@ -118,6 +118,27 @@ int ccd_prim_batch(ccd_context *ctx, int kind, int path, int64_t n, const double
 int ccd_prim_batch_device(ccd_context *ctx, int kind, int path, int64_t n, const double *rows, const double *eta,
                           int64_t eta_count, uint8_t *hit, double *t, uint8_t *status);
 
+/* ---------------------------------------------------------- allocation-free batch
+ * No counterpart in the reference.  The same computation and results as
+ * ccd_prim_batch_device with CCD_PATH_CULL_REFINE (no per-row status), for
+ * callers that must not allocate device memory while they run: every byte of
+ * scratch comes from one fixed region of about 9.4 MB per device, set aside
+ * when the library's device code is loaded.  Needs no context; all pointers
+ * are device memory; enqueued on `stream` (a cudaStream_t, NULL for the
+ * legacy default stream) of the current device; returns without waiting.
+ *   - n > CCD_NOALLOC_MAX_ROWS is rejected with CCD_ERR_INVALID_ARGUMENT
+ *     before any work is enqueued (split larger batches into calls);
+ *   - the first call on a device does its setup (scratch address, SM count)
+ *     with that device current; make it before any stream capture that should
+ *     contain later calls;
+ *   - the region is shared by all calls on a device: calls whose device work
+ *     can overlap in time (different streams, several host threads) race and
+ *     corrupt each other's results, so keep them on one stream or serialise
+ *     them. */
+#define CCD_NOALLOC_MAX_ROWS 65536
+int ccd_prim_batch_device_noalloc(int kind, int64_t n, const double *rows, const double *eta, int64_t eta_count,
+                                  uint8_t *hit, double *t, void *stream);
+
 /* ------------------------------------------------------------------ meshes
  * A triangle mesh resident on its context's device: the faces of the
  * reference's Mesh (src/Mesh.h: Matrix3Xi faces, 3 x F, column-major, which
