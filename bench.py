@@ -43,6 +43,10 @@ def parse():
     ap.add_argument("--n-ee", type=int, default=10_000_000)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-sample", type=int, default=2_000_000, help="rows per kind per reference step")
+    ap.add_argument("--mesh", type=int, default=1, help="also time the mesh configurations (1) or not (0)")
+    ap.add_argument("--cloth-grid", type=int, default=256)
+    ap.add_argument("--cloth-level", type=int, default=6)
+    ap.add_argument("--cloth-steps", type=int, default=50)
     return ap.parse_args()
 
 
@@ -159,6 +163,89 @@ def cpu_baseline(vf, ee, max_rows=None):
             "sample": f"{vf.shape[0]} VF + {ee.shape[0]} EE rows of the same workload, {dt:.2f} s wall"}
 
 
+def mesh_section(ctx, stream, rank, args):
+    """Mesh configurations through the mesh entry points, one detection step
+    = set positions (host -> device) + broad phase + narrow phase over every
+    candidate + read back the colliding stencils.  Unit: candidate stencil
+    tests per second (the reference's exact candidate set; broad phase in
+    the wall time).  The oracle times the same steps on the host cores."""
+    import collisiondetection_gb300 as C
+    from collisiondetection_gb300 import workloads as W
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    orc = O.Oracle()
+    threads = os.cpu_count() or 1
+    out = {}
+
+    def run_steps(m, frames, kind, eta, reps):
+        ctx.synchronize()
+        tests, hits, dts = 0, 0, []
+        for _ in range(reps):
+            for k in range(len(frames) - 1):
+                torch_sync()
+                t0 = time.perf_counter()
+                m.set_positions(frames[k], frames[k + 1])
+                vf, vft, ee, eet = m.detect(kind, eta, eta, path=C.PATH_CULL_REFINE)
+                dts.append(time.perf_counter() - t0)
+                st = m.stats()
+                tests += st["n_vf"] + st["n_ee"]
+                hits += vf.shape[0] + ee.shape[0]
+        return tests, hits, dts
+
+    def torch_sync():
+        import torch
+
+        torch.cuda.synchronize()
+
+    def oracle_steps(frames, faces, eta, idx):
+        t_bp = t_np = 0.0
+        for k in idx:
+            t0 = time.perf_counter()
+            vf, ee = orc.broadphase(0, frames[k], frames[k + 1], faces, eta)
+            t1 = time.perf_counter()
+            orc.narrowphase(frames[k], frames[k + 1], vf, eta, ee, eta, nthreads=threads)
+            t2 = time.perf_counter()
+            t_bp += t1 - t0
+            t_np += t2 - t1
+        return 1e3 * t_bp / len(idx), 1e3 * t_np / len(idx)
+
+    # Two level-3 icospheres (2 x 642 v / 1,280 f), 0.8 approach + N(0, 0.01) jitter.
+    qs, qe, f = W.two_spheres(seed=1)
+    frames = np.stack([qs, qe])
+    with C.Mesh(ctx, f, qs, qe) as m:
+        for label, kind in (("kdop", C.BROADPHASE_KDOP13), ("aabb", C.BROADPHASE_AABB)):
+            run_steps(m, frames, kind, 1e-6, 3)  # warm-up
+            tests, hits, dts = run_steps(m, frames, kind, 1e-6, 20)
+            ms = 1e3 * statistics.median(dts)
+            out[f"two_spheres_{label}"] = {
+                "ms_per_step": ms, "stencil_tests_per_step": tests // 20, "collisions_per_step": hits // 20,
+                "value": (tests // 20) / (ms / 1e3), "unit": "stencil tests/s"}
+    if rank == 0:
+        bp, nph = oracle_steps(frames, f, 1e-6, [0])
+        out["two_spheres_kdop"]["cpu_oracle"] = {"broadphase_ms": bp, "narrowphase_ms": nph,
+                                                 "cores": {"broadphase": 1, "narrowphase": threads}}
+    # Cloth on sphere: sheet + level-6 icosphere, one step per frame pair.
+    faces, frames = W.cloth_frames(grid=args.cloth_grid, level=args.cloth_level, seed=0, steps=args.cloth_steps)
+    with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3) as m:
+        run_steps(m, frames[:4], C.BROADPHASE_KDOP13, 1e-6, 1)  # warm-up
+        tests, hits, dts = run_steps(m, frames, C.BROADPHASE_KDOP13, 1e-6, 1)
+        total = sum(dts)
+        out["cloth_on_sphere_kdop"] = {
+            "faces": int(faces.shape[0]), "vertices": int(frames.shape[1] // 3), "steps": len(dts),
+            "ms_per_step": 1e3 * total / len(dts), "ms_per_step_p50": 1e3 * statistics.median(dts),
+            "ms_per_step_max": 1e3 * max(dts), "stencil_tests": tests, "collisions": hits,
+            "value": tests / total, "unit": "stencil tests/s"}
+    if rank == 0:
+        idx = [len(frames) - 2, len(frames) // 2]
+        bp, nph = oracle_steps(frames, faces, 1e-6, idx)
+        out["cloth_on_sphere_kdop"]["cpu_oracle"] = {"broadphase_ms": bp, "narrowphase_ms": nph, "sample_steps": idx,
+                                                    "cores": {"broadphase": 1, "narrowphase": threads}}
+    return out
+
+
 def run_reference(args, rank, world, pg):
     if rank != 0:
         return
@@ -269,10 +356,20 @@ def run_ours(args, rank, world, local, pg):
         ctx.synchronize()
         counts[name] = ctx.stats()
 
-    # end to end through the host-memory entry point (copies inside the timed region)
-    host = {"vf": (vf, np.zeros(n_vf, np.uint8), np.full(n_vf, np.nan)),
-            "ee": (ee, np.zeros(n_ee, np.uint8), np.full(n_ee, np.nan))}
-    eta_h = np.array([ETA])
+    # end to end through the host-memory entry point (copies inside the timed
+    # region), from pinned host buffers
+    keep = []
+
+    def pinned(arr):
+        t = torch.empty(arr.shape, dtype=getattr(torch, str(arr.dtype)), pin_memory=True)
+        keep.append(t)
+        out = t.numpy()
+        out[...] = arr
+        return out
+
+    host = {"vf": (pinned(vf), pinned(np.zeros(n_vf, np.uint8)), pinned(np.full(n_vf, np.nan))),
+            "ee": (pinned(ee), pinned(np.zeros(n_ee, np.uint8)), pinned(np.full(n_ee, np.nan)))}
+    eta_h = pinned(np.array([ETA]))
 
     def e2e_step():
         for kind, name in ((C.VERTEX_FACE, "vf"), (C.EDGE_EDGE, "ee")):
@@ -306,7 +403,8 @@ def run_ours(args, rank, world, local, pg):
     if tm["cull_ms"] >= tm["refine_ms"]:
         kname, bytes_launch, ms_launch = "prims_cull_kernel", cull_bytes / 2, cull_ms_launch
     else:
-        kname, bytes_launch, ms_launch = "prims_refine_kernel", refine_bytes / 2, refine_ms_launch
+        kname, bytes_launch, ms_launch = ("staged FP64 refine (stage_build + stage_roots + stage_combine)",
+                                          refine_bytes / 2, refine_ms_launch)
     achieved = bytes_launch / (ms_launch / 1e3) / 1e9
     roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_src} hbm_gbs", "traffic": None,
@@ -314,6 +412,7 @@ def run_ours(args, rank, world, local, pg):
                 "share": {"cull": tm["cull_ms"] / (tm["cull_ms"] + tm["refine_ms"]),
                           "refine": tm["refine_ms"] / (tm["cull_ms"] + tm["refine_ms"])}}
     cpu = cpu_baseline(vf, ee) if rank == 0 else None
+    mesh = mesh_section(ctx, stream, rank, args) if args.mesh else None
 
     if rank == 0:
         line = {
@@ -329,11 +428,12 @@ def run_ours(args, rank, world, local, pg):
             "hits": {"vf": counts["vf"]["hits"], "ee": counts["ee"]["hits"]},
             "status_flags": counts["vf"]["status_flags"] + counts["ee"]["status_flags"],
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "entry_point": "ccd_prim_batch (pageable host buffers)", "matches_device_path": same},
+                    "entry_point": "ccd_prim_batch (pinned host buffers)", "matches_device_path": same},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": int(tm["launches"]),
+            "mesh": mesh,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -14,6 +14,32 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kStack = 128;
 constexpr uint64_t kNoKey = ~0ull;
+
+// Bit widths of the packed keys: Morton code << fbits | face (Morton keys),
+// vertex << rbits | face rank (vertex-face), edge rank << ebits | edge rank
+// (edge-edge).  An emitted key stays below 2^(width of the key), so kNoKey
+// sorts after every emitted key when the sort covers one more bit.
+struct KeyBits {
+  int fbits, rbits, ebits;
+  uint64_t fmask, rmask, emask;
+};
+
+inline int bits_for(int64_t x) {
+  int b = 1;
+  while (b < 62 && ((int64_t)1 << b) <= x) b++;
+  return b;
+}
+
+inline KeyBits key_bits(const MeshTopology &t) {
+  KeyBits k;
+  k.fbits = bits_for(t.nf - 1);
+  k.rbits = bits_for(std::max(t.nranks - 1, 1));
+  k.ebits = bits_for(std::max(t.nedges - 1, 1));
+  k.fmask = ((uint64_t)1 << k.fbits) - 1;
+  k.rmask = ((uint64_t)1 << k.rbits) - 1;
+  k.emask = ((uint64_t)1 << k.ebits) - 1;
+  return k;
+}
 // Face pairs per call: 9 edge-edge keys per pair stay below the sort's 2^31.
 constexpr int64_t kMaxPairs = (int64_t)1 << 27;
 
@@ -100,7 +126,7 @@ __device__ __forceinline__ uint32_t spread10(uint32_t x) {
 }
 
 __global__ void __launch_bounds__(kThreads) morton_keys(int nf, const float *flo, const float *fhi, const float *bounds,
-                                                        uint64_t *keys) {
+                                                        KeyBits kb, uint64_t *keys) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   uint32_t m = 0;
@@ -113,16 +139,16 @@ __global__ void __launch_bounds__(kThreads) morton_keys(int nf, const float *flo
     uint32_t q = (uint32_t)(u * 1023.0f);
     m |= spread10(q) << (2 - k);
   }
-  keys[f] = ((uint64_t)m << 32) | (uint32_t)f;
+  keys[f] = ((uint64_t)m << kb.fbits) | (uint32_t)f;
 }
 
 // Leaf FP32 slabs in Morton order.
 template <int K>
-__global__ void __launch_bounds__(kThreads) gather_leaves(int nf, const uint64_t *keys, const float *flo,
-                                                          const float *fhi, float *llo, float *lhi) {
+__global__ void __launch_bounds__(kThreads) gather_leaves(int nf, const uint64_t *keys, uint64_t fmask,
+                                                          const float *flo, const float *fhi, float *llo, float *lhi) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nf) return;
-  const int f = (int)(uint32_t)keys[s];
+  const int f = (int)(keys[s] & fmask);
 #pragma unroll
   for (int k = 0; k < K; k++) {
     llo[(int64_t)k * nf + s] = flo[(int64_t)k * nf + f];
@@ -202,7 +228,7 @@ __global__ void __launch_bounds__(kThreads) refit(int n, const int32_t *child, c
 
 // ------------------------------------------------------------------ traversal
 template <int K>
-__global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n, const uint64_t *keys,
+__global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n, const uint64_t *keys, uint64_t fmask,
                                                        const int32_t *child, const int32_t *range, const float *llo,
                                                        const float *lhi, const float *nlo, const float *nhi,
                                                        const double *lo64, const double *hi64, uint32_t *pairs,
@@ -215,7 +241,7 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
     qlo[k] = llo[(int64_t)k * n + s];
     qhi[k] = lhi[(int64_t)k * n + s];
   }
-  const int fa = (int)(uint32_t)keys[s];
+  const int fa = (int)(keys[s] & fmask);
   const int a0 = topo.faces[3 * fa], a1 = topo.faces[3 * fa + 1], a2 = topo.faces[3 * fa + 2];
   int stack[kStack];
   int sp = 0;
@@ -237,7 +263,7 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
         for (int k = 0; k < K; k++) sep |= (qhi[k] < llo[(int64_t)k * n + j]) || (lhi[(int64_t)k * n + j] < qlo[k]);
         if (sep) continue;
         // The reference's exact FP64 test (KDOPBroadPhase.cpp:132-137).
-        const int fb = (int)(uint32_t)keys[j];
+        const int fb = (int)(keys[j] & fmask);
         for (int k = 0; k < K && !sep; k++)
           sep = (hi64[(int64_t)k * topo.nf + fa] < lo64[(int64_t)k * topo.nf + fb]) ||
                 (hi64[(int64_t)k * topo.nf + fb] < lo64[(int64_t)k * topo.nf + fa]);
@@ -271,7 +297,7 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
 // ------------------------------------------------------------------ stencils
 // KDOPBroadPhase.cpp:150-183: 6 vertex-face and 9 edge-edge stencils per
 // pair, skipping those whose four vertices are all fixed.
-__global__ void __launch_bounds__(kThreads) stencil_keys(MeshTopology topo, const uint8_t *fixed,
+__global__ void __launch_bounds__(kThreads) stencil_keys(MeshTopology topo, KeyBits kb, const uint8_t *fixed,
                                                          const uint32_t *pairs, int64_t npairs, uint64_t *vf_keys,
                                                          uint64_t *ee_keys) {
   const int64_t pi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -288,13 +314,13 @@ __global__ void __launch_bounds__(kThreads) stencil_keys(MeshTopology topo, cons
   const bool allA = FA[0] && FA[1] && FA[2], allB = FB[0] && FB[1] && FB[2];
   const uint64_t ra = (uint32_t)topo.face_rank[fa], rb = (uint32_t)topo.face_rank[fb];
   for (int i = 0; i < 3; i++) {
-    vf_keys[6 * pi + 2 * i] = (FA[i] && allB) ? kNoKey : ((uint64_t)(uint32_t)A[i] << 32) | rb;
-    vf_keys[6 * pi + 2 * i + 1] = (FB[i] && allA) ? kNoKey : ((uint64_t)(uint32_t)B[i] << 32) | ra;
+    vf_keys[6 * pi + 2 * i] = (FA[i] && allB) ? kNoKey : ((uint64_t)(uint32_t)A[i] << kb.rbits) | rb;
+    vf_keys[6 * pi + 2 * i + 1] = (FB[i] && allA) ? kNoKey : ((uint64_t)(uint32_t)B[i] << kb.rbits) | ra;
     for (int j = 0; j < 3; j++) {
       const bool all = FA[i] && FA[(i + 1) % 3] && FB[j] && FB[(j + 1) % 3];
       const uint32_t e1 = (uint32_t)topo.face_edges[3 * fa + i], e2 = (uint32_t)topo.face_edges[3 * fb + j];
       ee_keys[9 * pi + 3 * i + j] =
-          all ? kNoKey : (((uint64_t)(e1 < e2 ? e1 : e2) << 32) | (uint64_t)(e1 < e2 ? e2 : e1));
+          all ? kNoKey : (((uint64_t)(e1 < e2 ? e1 : e2) << kb.ebits) | (uint64_t)(e1 < e2 ? e2 : e1));
     }
   }
 }
@@ -307,26 +333,28 @@ __global__ void __launch_bounds__(kThreads) first_of_run(const uint64_t *keys, i
 }
 
 // Unique keys -> stencils (reference order: keys are sorted).
-__global__ void __launch_bounds__(kThreads) decode_vf(MeshTopology topo, const uint64_t *keys, const uint32_t *flags,
+__global__ void __launch_bounds__(kThreads) decode_vf(MeshTopology topo, KeyBits kb, const uint64_t *keys,
+                                                      const uint32_t *flags,
                                                       const uint32_t *pos, int64_t n, int32_t *out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || !flags[i]) return;
   const uint64_t k = keys[i];
   const int64_t o = pos[i];
-  const int r = (int)(uint32_t)k;
-  out[4 * o] = (int32_t)(k >> 32);
+  const int r = (int)(k & kb.rmask);
+  out[4 * o] = (int32_t)(k >> kb.rbits);
   out[4 * o + 1] = topo.rank_triple[3 * r];
   out[4 * o + 2] = topo.rank_triple[3 * r + 1];
   out[4 * o + 3] = topo.rank_triple[3 * r + 2];
 }
 
-__global__ void __launch_bounds__(kThreads) decode_ee(MeshTopology topo, const uint64_t *keys, const uint32_t *flags,
+__global__ void __launch_bounds__(kThreads) decode_ee(MeshTopology topo, KeyBits kb, const uint64_t *keys,
+                                                      const uint32_t *flags,
                                                       const uint32_t *pos, int64_t n, int32_t *out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || !flags[i]) return;
   const uint64_t k = keys[i];
   const int64_t o = pos[i];
-  const int r1 = (int)(k >> 32), r2 = (int)(uint32_t)k;
+  const int r1 = (int)(k >> kb.ebits), r2 = (int)(k & kb.emask);
   out[4 * o] = topo.rank_edge[2 * r1];
   out[4 * o + 1] = topo.rank_edge[2 * r1 + 1];
   out[4 * o + 2] = topo.rank_edge[2 * r2];
@@ -453,13 +481,15 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   else
     leaf_slabs<3><<<grid_of(nf), kThreads, 0, s>>>(topo, p, ax, b.lo64, b.hi64, flo, fhi, b.bounds);
   BP_CUDA(cudaGetLastError());
-  morton_keys<<<grid_of(nf), kThreads, 0, s>>>(nf, flo, fhi, b.bounds, b.keys);
+  const KeyBits kb = key_bits(topo);
+  morton_keys<<<grid_of(nf), kThreads, 0, s>>>(nf, flo, fhi, b.bounds, kb, b.keys);
   BP_CUDA(cudaGetLastError());
-  BP_CUDA(radix_sort_u64(b.keys, (uint64_t *)b.vals, nullptr, nullptr, nf, 0, 64, b.temp, b.temp_bytes, s));
+  BP_CUDA(radix_sort_u64(b.keys, (uint64_t *)b.vals, nullptr, nullptr, nf, 0, 30 + kb.fbits, b.temp, b.temp_bytes,
+                         s));
   if (kdop)
-    gather_leaves<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, flo, fhi, b.leaf_lo, b.leaf_hi);
+    gather_leaves<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, flo, fhi, b.leaf_lo, b.leaf_hi);
   else
-    gather_leaves<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, flo, fhi, b.leaf_lo, b.leaf_hi);
+    gather_leaves<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, flo, fhi, b.leaf_lo, b.leaf_hi);
   build_lbvh<<<grid_of(nf - 1), kThreads, 0, s>>>(nf, b.keys, b.node_child, b.node_range, b.parent);
   BP_CUDA(cudaMemsetAsync(b.arrive, 0, (size_t)nf * sizeof(uint32_t), s));
   BP_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(unsigned long long), s));
@@ -474,11 +504,11 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   for (;;) {
     BP_CUDA(cudaMemsetAsync(b.counters, 0, 3 * sizeof(unsigned long long), s));  // keeps the error word
     if (kdop)
-      find_pairs<13><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, b.node_child, b.node_range, b.leaf_lo,
+      find_pairs<13><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, kb.fmask, b.node_child, b.node_range, b.leaf_lo,
                                                       b.leaf_hi, b.node_lo, b.node_hi, b.lo64, b.hi64, b.pairs,
                                                       (uint64_t)b.cap_pairs, b.counters);
     else
-      find_pairs<3><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, b.node_child, b.node_range, b.leaf_lo,
+      find_pairs<3><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, kb.fmask, b.node_child, b.node_range, b.leaf_lo,
                                                      b.leaf_hi, b.node_lo, b.node_hi, b.lo64, b.hi64, b.pairs,
                                                      (uint64_t)b.cap_pairs, b.counters);
     BP_CUDA(cudaGetLastError());
@@ -494,13 +524,15 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   }
   const int64_t np = *n_pairs;
   if (np == 0) return 0;
-  stencil_keys<<<grid_of(np), kThreads, 0, s>>>(topo, p.fixed, b.pairs, np, b.vf_keys, b.ee_keys);
+  stencil_keys<<<grid_of(np), kThreads, 0, s>>>(topo, kb, p.fixed, b.pairs, np, b.vf_keys, b.ee_keys);
   BP_CUDA(cudaGetLastError());
   // Sort, mark the first of each run of equal keys, scan, decode.
   for (int which = 0; which < 2; which++) {
     uint64_t *keys = which == 0 ? b.vf_keys : b.ee_keys;
     const int64_t n = (which == 0 ? 6 : 9) * np;
-    BP_CUDA(radix_sort_u64(keys, b.keys_alt, nullptr, nullptr, n, 0, 64, b.temp, b.temp_bytes, s));
+    // One bit above the packed key so that kNoKey (all ones) sorts last.
+    const int key_bits_used = which == 0 ? bits_for(std::max(topo.nv - 1, 1)) + kb.rbits : 2 * kb.ebits;
+    BP_CUDA(radix_sort_u64(keys, b.keys_alt, nullptr, nullptr, n, 0, key_bits_used + 1, b.temp, b.temp_bytes, s));
     first_of_run<<<grid_of(n), kThreads, 0, s>>>(keys, n, b.flags);
     BP_CUDA(cudaGetLastError());
     uint32_t *total = (uint32_t *)(b.counters + 1 + which);
@@ -510,11 +542,11 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
     BP_CUDA(cudaStreamSynchronize(s));
     if (which == 0) {
       BP_CUDA(grow(vf_out, vf_cap, 4 * (int64_t)count));
-      decode_vf<<<grid_of(n), kThreads, 0, s>>>(topo, keys, b.flags, b.scan, n, *vf_out);
+      decode_vf<<<grid_of(n), kThreads, 0, s>>>(topo, kb, keys, b.flags, b.scan, n, *vf_out);
       *n_vf = count;
     } else {
       BP_CUDA(grow(ee_out, ee_cap, 4 * (int64_t)count));
-      decode_ee<<<grid_of(n), kThreads, 0, s>>>(topo, keys, b.flags, b.scan, n, *ee_out);
+      decode_ee<<<grid_of(n), kThreads, 0, s>>>(topo, kb, keys, b.flags, b.scan, n, *ee_out);
       *n_ee = count;
     }
     BP_CUDA(cudaGetLastError());

@@ -16,8 +16,9 @@
 //      conservative FP32 test, then the reference's exact FP64 test
 //      (strict '<' rejection) and neighbour exclusion (any shared vertex);
 //   4. 6 vertex-face + 9 edge-edge stencils per pair (fixed-vertex filter),
-//      as 64-bit keys (vertex, face rank) and (edge rank, edge rank) whose
-//      order is the reference's std::set order; radix sort + unique.
+//      as integer keys (vertex, face rank) and (edge rank, edge rank), packed
+//      into as few bits as the mesh needs, whose order is the reference's
+//      std::set order; radix sort over those bits + unique.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -30,6 +31,7 @@ enum BvhKind : int { kBvhKdop13 = 0, kBvhAabb = 1 };
 // Static topology of a mesh, ranks computed on the host once per mesh.
 struct MeshTopology {
   int32_t nv, nf;
+  int32_t nranks, nedges;      // distinct sorted face triples, distinct edges
   const int32_t *faces;        // [nf][3]
   const int32_t *face_rank;    // [nf] rank of the face's sorted vertex triple
   const int32_t *rank_triple;  // [nranks][3] sorted triple of each face rank

@@ -30,9 +30,11 @@ int ensure_stage(ccd_context *ctx, StageBuf &sb, int64_t rows, cudaStream_t s) {
   CCD_CUDA(cudaStreamSynchronize(s));
   cudaFree(sb.mem);
   sb = StageBuf{};
-  CCD_CUDA(cudaMalloc(&sb.mem, ccd::stage_scratch_bytes(cap)));
+  const size_t stage_bytes = ccd::stage_scratch_bytes(cap);
+  CCD_CUDA(cudaMalloc(&sb.mem, stage_bytes + ccd::wave_scratch_bytes(cap)));
   sb.cap = cap;
   sb.view = ccd::stage_scratch_view(sb.mem, cap);
+  ccd::attach_wave(sb.view, (char *)sb.mem + stage_bytes);
   return CCD_OK;
 }
 
@@ -116,12 +118,18 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     if (rc) return rc;
     CCD_CUDA(cudaEventRecord(pe->ev[0], s));
   }
-  // The FP32 stage covers vertex-face and edge-edge rows; the two degenerate
-  // kinds are cheap in FP64 and always take the FP64 kernel.
-  bool culled = !(path == CCD_PATH_FP64 || b.kind >= CCD_VERTEX_EDGE);
+  // The FP32 stage covers vertex-face, edge-edge and vertex-edge rows;
+  // vertex-vertex rows (one quadratic) always take the FP64 kernel.
+  bool culled = !(path == CCD_PATH_FP64 || b.kind == CCD_VERTEX_VERTEX);
   if (!culled) {
     CCD_CUDA(ccd::launch_prims_fp64(b, ctx->num_sms, s));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[1], s));
+  } else if (b.kind == CCD_VERTEX_EDGE) {
+    CCD_CUDA(ccd::launch_prims_cull(b, surv, ctx->num_sms, s));
+    if (pe) CCD_CUDA(cudaEventRecord(pe->ev[1], s));
+    CCD_CUDA(ccd::launch_prims_fp64_list(b, surv, ctx->num_sms, s));
+    if (pe) CCD_CUDA(cudaEventRecord(pe->ev[2], s));
+    if (pe) pe->stage_launches = 1;
   } else {
     int rc = ensure_stage(ctx, stage, b.n, s);
     if (rc) return rc;

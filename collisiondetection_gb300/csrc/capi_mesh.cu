@@ -50,6 +50,7 @@ int grow(ccd_context *ctx, T **p, int64_t *cap, int64_t need) {
 struct ccd_mesh {
   ccd_context *ctx = nullptr;
   int32_t nv = 0, nf = 0;
+  int32_t nranks = 0, nedges = 0;
   int32_t *faces = nullptr, *face_rank = nullptr, *rank_triple = nullptr, *face_edges = nullptr,
           *rank_edge = nullptr;
   double *qs = nullptr, *qe = nullptr;
@@ -143,7 +144,7 @@ int narrow_device(ccd_mesh *m, int kind, int path, int64_t n, const int32_t *st,
     if (rc) return rc;
     const ccd::PrimBatch bve{CCD_VERTEX_EDGE, nsub * c, ns.ve, ns.eta_ve, true, ns.h_ve, ns.t_ve, nullptr,
                              ns.counters};
-    rc = enqueue_batch(ctx, bve, CCD_PATH_FP64, ns.surv, ns.stage, s, nullptr);
+    rc = enqueue_batch(ctx, bve, path, ns.surv, ns.stage, s, nullptr);
     if (rc) return rc;
     const ccd::PrimBatch bvv{CCD_VERTEX_VERTEX, nsub * c, ns.vv, ns.eta_vv, true, ns.h_vv, ns.t_vv, nullptr,
                              ns.counters};
@@ -160,14 +161,15 @@ int run_broadphase(ccd_mesh *m, int kind, double outer_eta) {
   m->have_cand = false;
   m->have_col = false;
   m->stats = ccd_mesh_stats{};
-  const ccd::MeshTopology topo{m->nv, m->nf, m->faces, m->face_rank, m->rank_triple, m->face_edges, m->rank_edge};
+  const ccd::MeshTopology topo{m->nv,        m->nf,        m->nranks,    m->nedges,   m->faces,
+                               m->face_rank, m->rank_triple, m->face_edges, m->rank_edge};
   const ccd::BroadphaseParams p{kind, outer_eta, m->qs, m->qe, m->has_fixed ? m->fixed : nullptr};
   cudaError_t err = cudaSuccess;
   int64_t npairs = 0;
   const int rc = ccd::broadphase_run(topo, p, m->bp, &m->cand[0], &m->cand_cap[0], &m->cand[1], &m->cand_cap[1],
                                      &m->n_cand[0], &m->n_cand[1], &npairs, ctx->num_sms, ctx->stream, &err);
   if (rc == 2) return cuda_fail(ctx, err, "broadphase");
-  if (rc == 3) return mesh_fail(m, CCD_ERR_CUDA, "broadphase: traversal stack overflow");
+  if (rc == 3) return mesh_fail(m, CCD_ERR_CUDA, "broadphase: malformed tree (traversal beyond its size)");
   if (rc == 4) return mesh_fail(m, CCD_ERR_OUT_OF_MEMORY, "broadphase: more than 2^27 overlapping face pairs");
   m->stats.face_pairs = npairs;
   m->stats.n_vf = m->n_cand[0];
@@ -214,6 +216,8 @@ int ccd_mesh_create(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int3
   m->ctx = ctx;
   m->nv = nverts;
   m->nf = nfaces;
+  m->nranks = (int32_t)(topo.rank_triple.size() / 3);
+  m->nedges = (int32_t)(topo.rank_edge.size() / 2);
   auto upload = [&](int32_t **dst, const int32_t *src, size_t count) -> int {
     CCD_CUDA(cudaMalloc(dst, std::max<size_t>(count, 1) * sizeof(int32_t)));
     if (count) CCD_CUDA(cudaMemcpy(*dst, src, count * sizeof(int32_t), cudaMemcpyHostToDevice));

@@ -1,4 +1,5 @@
-// Conservative FP32 rejection for the vertex-face and edge-edge tests.
+// Conservative FP32 rejection for the vertex-face, edge-edge and vertex-edge
+// tests.
 //
 // The reference returns "no collision" as soon as one of its interval lists
 // is empty (src/CTCD.cpp:441-475 for vertex-face, 310-350 for edge-edge).  A
@@ -74,7 +75,11 @@ CCD_UNROLL
     s += op[N - i].m;
   }
   float b[N + 1];
-  if (N == 3) {
+  if (N == 2) {
+    b[0] = a[0];
+    b[1] = a[0] + a[1] * 0.5f;
+    b[N] = a[0] + a[1] + a[N];
+  } else if (N == 3) {
     b[0] = a[0];
     b[1] = a[0] + a[1] * (1.0f / 3.0f);
     b[2] = a[0] + a[1] * (2.0f / 3.0f) + a[2] * (1.0f / 3.0f);
@@ -211,6 +216,84 @@ CCD_HD bool ee_rejects(const double *x, double eta) {
   if (surely_negative<4>(op)) return true;
   bary_terms(x10, q1s - p1s, p1s - q0s, v10, vq1 - vp1, vp1 - vq0, op);
   return surely_negative<4>(op);
+}
+
+// Lower bound of |X(t)|^2 over t in [a, a + h] for the vector quadratic
+// X(t) = X0 + X1 t + X2 t^2, or -1 when none is found.  For n = X(mid),
+// |X(t)| >= |n.X(t)| / |n|; n.X(t) is a scalar quadratic, re-expanded in
+// s = (t - a) / h in FP32 with running error bounds and bounded by its
+// Bernstein coefficients.  a and h are exact binary fractions.
+CCD_HD float cross_lower_sq(v3f X0, v3f X1, v3f X2, float a, float h) {
+  const float mid = a + 0.5f * h;
+  const float nx = X0.x.v + mid * (X1.x.v + mid * X2.x.v);
+  const float ny = X0.y.v + mid * (X1.y.v + mid * X2.y.v);
+  const float nz = X0.z.v + mid * (X1.z.v + mid * X2.z.v);
+  const v3f n{fb{nx, fabsf(nx)}, fb{ny, fabsf(ny)}, fb{nz, fabsf(nz)}};
+  const fb c0 = dotf(n, X0), c1 = dotf(n, X1), c2 = dotf(n, X2);
+  const fb A{a, a}, H{h, h}, H2{h * h, h * h};
+  const fb d0 = c0 + (c1 + c2 * A) * A;       // q(a)
+  const fb d1 = (c1 + scale(2.0f, c2 * A)) * H;  // h q'(a)
+  const fb d2 = c2 * H2;                       // h^2 q''/2
+  const float b0 = d0.v, b1 = d0.v + 0.5f * d1.v, b2 = (d0.v + d1.v) + d2.v;
+  const float lo = fminf(b0, fminf(b1, b2)), hi = fmaxf(b0, fmaxf(b1, b2));
+  // At most 20 roundings on any path (gamma_20 < 1.2e-6) plus the Bernstein
+  // combination's own (< 3 * 2^-24 of the magnitudes), with headroom.
+  const float slack = 3e-6f * ((d0.m + d1.m) + d2.m) + kAbsSlack;
+  float L;
+  if (lo - slack > 0.0f)
+    L = lo - slack;
+  else if (hi + slack < 0.0f)
+    L = -(hi + slack);
+  else
+    return -1.0f;
+  const float nn = ((nx * nx + ny * ny) + nz * nz) * 1.00001f;  // >= |n|^2
+  if (!(nn > 0.0f) || !(nn < kFinite) || !(slack < kFinite) || !(L < kFinite)) return -1.0f;
+  return ((L * L) / nn) * 0.99999f;
+}
+
+// True when vertexEdgeCTCD(x, eta) is provably false (src/CTCD.cpp:511-602).
+// x: q0s q1s q2s q0e q1e q2e (q0 = vertex, edge q1-q2).
+//
+// The two "between the endpoints" quadratics are tested like the other
+// sign lists.  The quartic is the reference's expansion of
+// A(t) D(t) - G(t)^2 - eta^2 A(t) with A = |ab|^2, D = |ac|^2, G = ab.ac, which
+// equals |X(t)|^2 - eta^2 |ab(t)|^2 with X(t) = ab(t) x ac(t) (Lagrange's
+// identity).  |X(t)|^2 is bounded from below on each quarter of [0,1]
+// (cross_lower_sq); the row is rejected when every bound exceeds
+// eta^2 max|ab(t)|^2 plus the reference's own FP64 error bound on the quartic
+// (its "<= 0" list is then empty).
+CCD_HD bool ve_rejects(const double *x, double eta) {
+  if (!(fabs(eta) < 1e300)) return false;
+  v3f q0s = ld3f(x), q1s = ld3f(x + 3), q2s = ld3f(x + 6);
+  v3f v0 = ld3f(x + 9) - q0s, v1 = ld3f(x + 12) - q1s, v2 = ld3f(x + 15) - q2s;
+  v3f ab = q2s - q1s, ac = q0s - q1s, cb = q2s - q0s;
+  v3f vab = v2 - v1, vac = v0 - v1, vcb = v2 - v0;
+  fb op[3];
+  op[0] = dotf(vab, vac);  // e1: src/CTCD.cpp:536-543
+  op[1] = dotf(ac, vab) + dotf(ab, vac);
+  op[2] = dotf(ab, ac);
+  if (surely_negative<2>(op)) return true;
+  op[0] = dotf(vab, vcb);  // e2: src/CTCD.cpp:547-555
+  op[1] = dotf(cb, vab) + dotf(ab, vcb);
+  op[2] = dotf(ab, cb);
+  if (surely_negative<2>(op)) return true;
+  // Distance from the vertex to the edge's line (src/CTCD.cpp:557-573).
+  const v3f X0 = crossf(ab, ac), X1 = crossf(ab, vac) + crossf(vab, ac), X2 = crossf(vab, vac);
+  // Upper bounds of |ab| + |vab| and |ac| + |vac| (1-norms of the values
+  // plus their FP32 error bounds).
+  auto norm1 = [](v3f a) { return (fabsf(a.x.v) + fabsf(a.y.v)) + fabsf(a.z.v); };
+  auto err1 = [](v3f a) { return (a.x.m + a.y.m) + a.z.m; };
+  const float pa = (norm1(ab) + norm1(vab) + 1e-6f * (err1(ab) + err1(vab))) * 1.00001f;
+  const float pc = (norm1(ac) + norm1(vac) + 1e-6f * (err1(ac) + err1(vac))) * 1.00001f;
+  const float P = pa * pa, Q = pc * pc;
+  const float md = (float)(eta * eta > 1e-30 ? eta * eta : 1e-30) * 1.00001f;
+  const float rhs = (md * P) * 1.00001f + 1e-14f * (2.0f * P * Q + md * P) + 1e-37f;
+  if (!(fabsf(rhs) < kFinite)) return false;
+  for (int k = 0; k < 4; k++) {
+    const float lower = cross_lower_sq(X0, X1, X2, 0.25f * (float)k, 0.25f);
+    if (!(lower > rhs)) return false;
+  }
+  return true;
 }
 
 }  // namespace ccd

@@ -87,6 +87,20 @@ struct PoolState {
   CCD_HD int &I(int f) const { return i[f * POOL + slot]; }
 };
 
+// State of job `g` in a field-major global array of `stride` jobs: field f of
+// all jobs is contiguous, so a warp advancing neighbouring jobs touches
+// neighbouring words.  The roots go to zr (stride zstride).
+struct FieldState {
+  double *d;
+  int *i;
+  int64_t g, stride;
+  double *zr;
+  int64_t zstride;
+  CCD_HD double &D(int f) const { return d[f * stride + g]; }
+  CCD_HD double &Z(int k) const { return zr[k * zstride]; }
+  CCD_HD int &I(int f) const { return i[f * stride + g]; }
+};
+
 // ---------------------------------------------------------------- primitives
 // Quotient and remainder of p by x^2 + u x + v  (rpoly.h:680-695).
 template <class S>

@@ -31,9 +31,12 @@ inline int row_width(int kind) { return kind <= 1 ? 24 : (kind == 2 ? 18 : 12); 
 // FP64 evaluation of every row.
 cudaError_t launch_prims_fp64(const PrimBatch &b, int num_sms, cudaStream_t s);
 
-// FP32 conservative rejection: rows that can be excluded get hit = 0; the
-// others are appended to `survivors` (count in counters->survivors).
+// FP32 conservative rejection (vertex-face, edge-edge, vertex-edge): rows that
+// can be excluded get hit = 0; the others are appended to `survivors` (count
+// in counters->survivors).
 cudaError_t launch_prims_cull(const PrimBatch &b, int32_t *survivors, int num_sms, cudaStream_t s);
-// The surviving rows are refined by the staged kernels (stages.cuh).
+// Vertex-face and edge-edge survivors are refined by the staged kernels
+// (stages.cuh); vertex-edge survivors by one FP64 pass over the list:
+cudaError_t launch_prims_fp64_list(const PrimBatch &b, const int32_t *survivors, int num_sms, cudaStream_t s);
 
 }  // namespace ccd

@@ -30,10 +30,14 @@ __device__ __forceinline__ bool eval_row(const double *__restrict__ rows, int64_
   const double *src = rows + i * W;
 #pragma unroll
   for (int j = 0; j < W; j++) x[j] = __ldg(src + j);
-  if (KIND == kVF) return vf_ctcd(x, eta, t, st);
-  if (KIND == kEE) return ee_ctcd(x, eta, t, st);
-  if (KIND == kVE) return ve_ctcd(x, eta, t, st);
-  return vv_ctcd(x, eta, t);
+  if constexpr (KIND == kVF)
+    return vf_ctcd(x, eta, t, st);
+  else if constexpr (KIND == kEE)
+    return ee_ctcd(x, eta, t, st);
+  else if constexpr (KIND == kVE)
+    return ve_ctcd(x, eta, t, st);
+  else
+    return vv_ctcd(x, eta, t);
 }
 
 __device__ __forceinline__ void flush_counters(BatchCounters *c, unsigned hits, unsigned flags, unsigned surv) {
@@ -73,6 +77,33 @@ __global__ void __launch_bounds__(kThreads) prims_fp64_kernel(PrimBatch b) {
   flush_counters(b.counters, hits, flags, surv);
 }
 
+// FP64 evaluation of the rows in a survivor list (count in
+// counters->survivors, written by the cull pass on the same stream).
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) prims_fp64_list_kernel(PrimBatch b, const int32_t *__restrict__ list) {
+  unsigned hits = 0, flags = 0;
+  const int64_t count = (int64_t)b.counters->survivors;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t warp_base = base - (threadIdx.x & 31);
+  for (int64_t w = warp_base; w < count; w += stride) {
+    const int64_t r = w + (threadIdx.x & 31);
+    if (r < count) {
+      const int64_t i = list[r];
+      double eta = b.eta_per_row ? __ldg(b.eta + i) : __ldg(b.eta);
+      double t = 0.0;
+      uint8_t st = 0;
+      bool h = eval_row<KIND>(b.rows, i, eta, t, st);
+      b.hit[i] = h;
+      if (h) b.t[i] = t;
+      if (b.status) b.status[i] = st;
+      hits += h;
+      flags += (st != 0);
+    }
+  }
+  flush_counters(b.counters, hits, flags, 0);
+}
+
 // FP32 rejection pass.  Rows that cannot hit get hit = 0; the others are
 // compacted into `list` with one atomic per warp (ballot + popc prefix).
 template <int KIND>
@@ -85,12 +116,19 @@ __global__ void __launch_bounds__(kThreads) prims_cull_kernel(PrimBatch b, int32
     int64_t i = w + lane;
     bool keep = false;
     if (i < b.n) {
-      double x[24];
-      const double *src = b.rows + i * 24;
+      constexpr int W = RowWidth<KIND>::value;
+      double x[W];
+      const double *src = b.rows + i * W;
 #pragma unroll
-      for (int j = 0; j < 24; j++) x[j] = __ldg(src + j);
+      for (int j = 0; j < W; j++) x[j] = __ldg(src + j);
       double eta = b.eta_per_row ? __ldg(b.eta + i) : __ldg(b.eta);
-      bool rej = (KIND == kVF) ? vf_rejects(x, eta) : ee_rejects(x, eta);
+      bool rej;
+      if constexpr (KIND == kVF)
+        rej = vf_rejects(x, eta);
+      else if constexpr (KIND == kEE)
+        rej = ee_rejects(x, eta);
+      else
+        rej = ve_rejects(x, eta);
       if (rej) {
         b.hit[i] = 0;
         if (b.status) b.status[i] = 0;
@@ -120,6 +158,11 @@ inline int grid_for(int64_t n, int num_sms, int blocks_per_sm) {
 template <int KIND>
 cudaError_t fp64(const PrimBatch &b, int num_sms, cudaStream_t s) {
   prims_fp64_kernel<KIND><<<grid_for(b.n, num_sms, 8), kThreads, 0, s>>>(b);
+  return cudaGetLastError();
+}
+template <int KIND>
+cudaError_t fp64_list(const PrimBatch &b, const int32_t *list, int num_sms, cudaStream_t s) {
+  prims_fp64_list_kernel<KIND><<<grid_for(b.n, num_sms, 8), kThreads, 0, s>>>(b, list);
   return cudaGetLastError();
 }
 template <int KIND>

@@ -38,7 +38,34 @@ StageScratch stage_scratch_view(void *base, int64_t cap) {
   sc.queue = (unsigned *)p;
   p += up((kMaxSlots + 1) * sizeof(unsigned));
   sc.row_status = (uint32_t *)p;
+  sc.jcap = 0;
+  sc.wd = nullptr;
+  sc.wi = nullptr;
+  sc.wlist = nullptr;
+  sc.wcount = nullptr;
+  sc.tail = nullptr;
   return sc;
+}
+
+size_t wave_scratch_bytes(int64_t cap) {
+  const size_t j = (size_t)kMaxSlots * (size_t)cap;
+  return up(jt::kDoubles * j * sizeof(double)) + up(jt::kInts * j * sizeof(int)) + up(8 * j * sizeof(uint32_t)) +
+         up(13 * sizeof(unsigned)) + up(j * sizeof(uint32_t));
+}
+
+void attach_wave(StageScratch &sc, void *base) {
+  const size_t j = (size_t)kMaxSlots * (size_t)sc.cap;
+  char *p = (char *)base;
+  sc.jcap = (int64_t)j;
+  sc.wd = (double *)p;
+  p += up(jt::kDoubles * j * sizeof(double));
+  sc.wi = (int *)p;
+  p += up(jt::kInts * j * sizeof(int));
+  sc.wlist = (uint32_t *)p;
+  p += up(8 * j * sizeof(uint32_t));
+  sc.wcount = (unsigned *)p;
+  p += up(13 * sizeof(unsigned));
+  sc.tail = (uint32_t *)p;
 }
 
 cudaError_t launch_stages(const PrimBatch &b, const int32_t *list, const StageScratch &sc, int num_sms,

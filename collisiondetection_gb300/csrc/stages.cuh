@@ -32,6 +32,12 @@ namespace ccd {
 
 constexpr int kMaxSlots = 5;
 constexpr int kStageThreads = 128;
+// Wavefront steps before the remaining jobs go to the pool kernel (about 99%
+// of the queued polynomials finish within 40 solver steps).
+constexpr int kWaveSteps = 48;
+// Batches below this many rows take the pool kernel alone: the wavefront
+// pays a global-memory round trip per step, which only a large batch hides.
+constexpr int64_t kWaveMinRows = (int64_t)1 << 18;
 
 // Device scratch for one tile of `cap` survivor rows (layouts are slot-major,
 // then coefficient / span index, then row, so warps access consecutive rows).
@@ -46,11 +52,24 @@ struct StageScratch {
   unsigned *queue;      // [slot] queued polynomials per slot; [kMaxSlots] next job to start
   uint32_t *row_status; // [cap]
   double *roots;        // [slot][k < 6][cap]   roots found by the solver
+  // Wavefront solver (null when not attached: the pool kernel then solves
+  // every queued polynomial).  Jobs are numbered slot by slot (queue order).
+  int64_t jcap;         // kMaxSlots * cap
+  double *wd;           // [field < jt::kDoubles][jcap]  solver states
+  int *wi;              // [field < jt::kInts][jcap]
+  uint32_t *wlist;      // [2][phase < 4][jcap]          jobs per working phase
+  unsigned *wcount;     // [3][4]                        list lengths (rotating)
+  uint32_t *tail;       // [jcap]                        jobs left for the pool kernel
 };
 
 size_t stage_scratch_bytes(int64_t cap);
-// Carves the scratch arrays out of one allocation of stage_scratch_bytes(cap).
+// Carves the scratch arrays out of one allocation of stage_scratch_bytes(cap)
+// (no wavefront solver attached).
 StageScratch stage_scratch_view(void *base, int64_t cap);
+// Bytes of the wavefront solver's scratch for a tile of `cap` rows, and its
+// attachment to a view.
+size_t wave_scratch_bytes(int64_t cap);
+void attach_wave(StageScratch &sc, void *base);
 
 // Enqueues build/roots/combine over every tile of the survivor list.
 // Returns the number of kernels launched through *launches.
@@ -136,9 +155,8 @@ constexpr int kWarpPool = 64;
 constexpr size_t kPoolSmem = (size_t)kWarpPool * (jt::kDoubles * sizeof(double) + jt::kInts * sizeof(int));
 
 // Spans of a finished solve, written to the polynomial's row slot.
-template <class Polys>
-__device__ __forceinline__ void finish_job(const StageScratch &sc, const jt::PoolState<kWarpPool> &st, int slot,
-                                           int64_t j) {
+template <class Polys, class S>
+__device__ __forceinline__ void finish_job(const StageScratch &sc, const S &st, int slot, int64_t j) {
   const int deg = sc.job_deg[slot * sc.cap + j];
   double op[7], tr[6];
   for (int k = 0; k <= deg; k++) op[k] = sc.coef[(slot * 7 + k) * sc.cap + j];
@@ -158,8 +176,10 @@ __device__ __forceinline__ int job_queue(const int *qbase, int nslots, int64_t g
   return q;
 }
 
+// `tail` (optional): solve only the jobs tail[0 .. *tail_count), from the
+// start (the jobs the wavefront solver left unfinished).
 template <class Polys>
-__global__ void __launch_bounds__(32) stage_roots(StageScratch sc) {
+__global__ void __launch_bounds__(32) stage_roots(StageScratch sc, const uint32_t *tail, const unsigned *tail_count) {
   extern __shared__ double pool_d[];
   int *pool_i = (int *)(pool_d + (size_t)kWarpPool * jt::kDoubles);
   __shared__ int64_t job_of[kWarpPool];
@@ -177,7 +197,7 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc) {
   }
   for (int k = lane; k < kWarpPool; k += 32) pool_i[jt::MODE * kWarpPool + k] = jt::kEmpty;
   __syncwarp();
-  const int njobs = qbase[Polys::kSlots];
+  const int njobs = tail ? (int)*tail_count : qbase[Polys::kSlots];
   auto state = [&](int k) {
     const int64_t g = job_of[k];
     const int q = job_queue(qbase, Polys::kSlots, g);
@@ -212,8 +232,9 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc) {
           const unsigned e = h ? e1 : e0;
           if (!((e >> lane) & 1u)) continue;
           const int k = lane + 32 * h;
-          const int64_t g = (int64_t)base + (h ? __popc(e0) : 0) + __popc(e & lt);
-          if (g >= njobs) continue;
+          const int64_t g0 = (int64_t)base + (h ? __popc(e0) : 0) + __popc(e & lt);
+          if (g0 >= njobs) continue;
+          const int64_t g = tail ? (int64_t)tail[g0] : g0;
           job_of[k] = g;
           const int q = job_queue(qbase, Polys::kSlots, g);
           const int64_t j = g - qbase[q];
@@ -257,6 +278,138 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc) {
     __syncwarp();
     if (lane < bestc) jt::step(state(sel[lane]));
     __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- wavefront solver
+// Every queued polynomial's solver state lives in global memory (FieldState).
+// wave_start starts all of them; each wave_step advances every unfinished
+// one by one step and re-bins it by its next phase, so a warp steps jobs of
+// one phase through the same code.  After a fixed number of steps the few
+// jobs still running are gathered for the pool kernel, which solves them
+// again from the start.
+constexpr int kWaveThreads = 128;
+
+__device__ __forceinline__ void queue_bases(const StageScratch &sc, int nslots, int *qbase) {
+  int acc = 0;
+  for (int q = 0; q < nslots; q++) {
+    qbase[q] = acc;
+    acc += (int)sc.queue[q];
+  }
+  qbase[nslots] = acc;
+}
+
+// Warp-aggregated append of job g to the list of phase `mode` (1..4).
+__device__ __forceinline__ void wave_append(uint32_t *lists, unsigned *counts, int64_t jcap, bool active, int mode,
+                                            int64_t g) {
+  const unsigned lane = threadIdx.x & 31;
+  for (int m = jt::kInit; m <= jt::kReal; m++) {
+    const bool mine = active && mode == m;
+    const unsigned mask = __ballot_sync(0xffffffffu, mine);
+    if (!mask) continue;
+    const int leader = __ffs(mask) - 1;
+    unsigned base = 0;
+    if ((int)lane == leader) base = atomicAdd(&counts[m - 1], (unsigned)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (mine) lists[(int64_t)(m - 1) * jcap + base + __popc(mask & ((1u << lane) - 1u))] = (uint32_t)g;
+  }
+}
+
+template <class Polys>
+__device__ __forceinline__ jt::FieldState wave_state(const StageScratch &sc, const int *qbase, int64_t g, int &q,
+                                                     int64_t &j) {
+  q = job_queue(qbase, Polys::kSlots, g);
+  j = g - qbase[q];
+  return jt::FieldState{sc.wd, sc.wi, g, sc.jcap, sc.roots + (int64_t)q * 6 * sc.cap + j, sc.cap};
+}
+
+template <class Polys>
+__global__ void __launch_bounds__(kWaveThreads) wave_start(StageScratch sc) {
+  __shared__ int qbase[kMaxSlots + 1];
+  if (threadIdx.x == 0) queue_bases(sc, Polys::kSlots, qbase);
+  __syncthreads();
+  const int64_t njobs = qbase[Polys::kSlots];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t warp_base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+  for (int64_t w = warp_base; w < njobs; w += stride) {
+    const int64_t g = w + (threadIdx.x & 31);
+    const bool active = g < njobs;
+    int mode = jt::kDone;
+    if (active) {
+      int q;
+      int64_t j;
+      const jt::FieldState s = wave_state<Polys>(sc, qbase, g, q, j);
+      const int deg = sc.job_deg[q * sc.cap + j];
+      double op[7];
+      for (int c = 0; c <= deg; c++) op[c] = sc.coef[(q * 7 + c) * sc.cap + j];
+      jt::start(s, op, deg);
+      mode = s.I(jt::MODE);
+      if (mode == jt::kDone) finish_job<Polys>(sc, s, q, j);
+    }
+    wave_append(sc.wlist, sc.wcount, sc.jcap, active, mode, g);
+  }
+}
+
+// One step of every job in lists `in` (counts cin), re-binned into lists
+// `out` (counts cout, zeroed by the caller); also zeroes czero, the counts
+// the step after next will fill.
+template <class Polys>
+__global__ void __launch_bounds__(kWaveThreads) wave_step(StageScratch sc, const uint32_t *in, const unsigned *cin,
+                                                          uint32_t *out, unsigned *cout, unsigned *czero) {
+  __shared__ int qbase[kMaxSlots + 1];
+  __shared__ int64_t off[5];
+  if (threadIdx.x == 0) {
+    queue_bases(sc, Polys::kSlots, qbase);
+    int64_t acc = 0;
+    for (int m = 0; m < 4; m++) {
+      off[m] = acc;
+      acc += cin[m];
+    }
+    off[4] = acc;
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 4) czero[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t total = off[4];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t warp_base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+  for (int64_t w = warp_base; w < total; w += stride) {
+    const int64_t r = w + (threadIdx.x & 31);
+    const bool active = r < total;
+    int mode = jt::kDone;
+    int64_t g = 0;
+    if (active) {
+      int m = 0;
+      while (m < 3 && r >= off[m + 1]) m++;
+      g = in[(int64_t)m * sc.jcap + (r - off[m])];
+      int q;
+      int64_t j;
+      const jt::FieldState s = wave_state<Polys>(sc, qbase, g, q, j);
+      jt::step(s);
+      mode = s.I(jt::MODE);
+      if (mode == jt::kDone) finish_job<Polys>(sc, s, q, j);
+    }
+    wave_append(out, cout, sc.jcap, active, mode, g);
+  }
+}
+
+// Concatenates the unfinished jobs' lists into sc.tail; the count goes to
+// tcount.
+template <class Polys>
+__global__ void __launch_bounds__(kWaveThreads) wave_gather_tail(StageScratch sc, const uint32_t *in,
+                                                                 const unsigned *cin, unsigned *tcount) {
+  int64_t off[5];
+  int64_t acc = 0;
+  for (int m = 0; m < 4; m++) {
+    off[m] = acc;
+    acc += cin[m];
+  }
+  off[4] = acc;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *tcount = (unsigned)acc;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < acc; r += stride) {
+    int m = 0;
+    while (m < 3 && r >= off[m + 1]) m++;
+    sc.tail[r] = in[(int64_t)m * sc.jcap + (r - off[m])];
   }
 }
 
@@ -324,13 +477,33 @@ cudaError_t run(const PrimBatch &b, const int32_t *list, const StageScratch &sc,
   const int64_t tiles = (b.n + sc.cap - 1) / sc.cap;
   const int grid = stage_grid(sc.cap, num_sms);
   const int pool_grid = num_sms * 5;  // five 40 KB warp pools fit one SM's shared memory
+  const int wave_grid = num_sms * 8;
   for (int64_t tile = 0; tile < tiles; tile++) {
     cudaError_t e = cudaMemsetAsync(sc.queue, 0, (kMaxSlots + 1) * sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     stage_build<Polys><<<grid, kStageThreads, 0, s>>>(b, list, tile * sc.cap, sc);
-    stage_roots<Polys><<<pool_grid, 32, kPoolSmem, s>>>(sc);
+    if (sc.wd && b.n >= kWaveMinRows) {
+      // counts: 3 rotating sets of 4, then the tail count
+      e = cudaMemsetAsync(sc.wcount, 0, 13 * sizeof(unsigned), s);
+      if (e != cudaSuccess) return e;
+      wave_start<Polys><<<wave_grid, kWaveThreads, 0, s>>>(sc);
+      for (int it = 0; it < kWaveSteps; it++) {
+        const uint32_t *in = sc.wlist + (int64_t)(it & 1) * 4 * sc.jcap;
+        uint32_t *out = sc.wlist + (int64_t)((it + 1) & 1) * 4 * sc.jcap;
+        wave_step<Polys><<<wave_grid, kWaveThreads, 0, s>>>(sc, in, sc.wcount + 4 * (it % 3), out,
+                                                            sc.wcount + 4 * ((it + 1) % 3),
+                                                            sc.wcount + 4 * ((it + 2) % 3));
+      }
+      const uint32_t *last = sc.wlist + (int64_t)(kWaveSteps & 1) * 4 * sc.jcap;
+      wave_gather_tail<Polys><<<num_sms, kWaveThreads, 0, s>>>(sc, last, sc.wcount + 4 * (kWaveSteps % 3), sc.wcount + 12);
+      stage_roots<Polys><<<pool_grid, 32, kPoolSmem, s>>>(sc, sc.tail, sc.wcount + 12);
+      *launches += kWaveSteps + 3;
+    } else {
+      stage_roots<Polys><<<pool_grid, 32, kPoolSmem, s>>>(sc, nullptr, nullptr);
+      *launches += 1;
+    }
     stage_combine<Polys><<<grid, kStageThreads, 0, s>>>(b, list, tile * sc.cap, sc);
-    *launches += 3;
+    *launches += 2;
   }
   return cudaGetLastError();
 }

@@ -249,34 +249,36 @@ def grid_sheet(nx: int, ny: int, size: float = 1.0):
     return v, f
 
 
-def sheet_on_sphere(grid: int = 256, level: int = 6, seed: int = 0, step: int = 0, gap: float = 0.05,
-                    drop: float = 0.002, wrinkle: float = 0.003, radius: float = 0.4):
-    """Cloth-on-sphere scene: a grid x grid vertex sheet on [0,1]^2 starting
+def cloth_frames(grid: int = 256, level: int = 6, seed: int = 0, steps: int = 50, gap: float = 0.05,
+                 drop: float = 0.002, wrinkle: float = 0.003, radius: float = 0.4):
+    """Cloth-on-sphere sequence: a grid x grid vertex sheet on [0,1]^2 starting
     `gap` above the top of an icosphere (subdivision `level`, centre
     (0.5, 0.5, 0), radius `radius`), in one mesh (sheet vertices first).  Each
     step moves every sheet vertex by dz = -drop + wrinkle * sin(2 pi (kx x +
     ky y) + phase), with (kx, ky, phase) drawn per step from the seed; the
-    sphere is static.  Returns (qstart (3V,), qend (3V,), faces (F, 3) int32)
-    of step `step` (positions before and after it)."""
+    sphere is static.  Returns (faces (F, 3) int32, frames (steps + 1, 3V)):
+    step k goes from frames[k] to frames[k + 1]."""
     sv, sf = grid_sheet(grid, grid)
     cv, cf = icosphere(level, radius)
     cv = cv + np.array([0.5, 0.5, 0.0])
     sv = sv + np.array([0.0, 0.0, radius + gap])
     rng = np.random.default_rng(seed)
-    z = sv[:, 2].copy()
     x, y = sv[:, 0], sv[:, 1]
-
-    def delta():
-        kx, ky = rng.uniform(1.0, 4.0, 2)
-        phase = rng.uniform(0.0, 2 * np.pi)
-        return -drop + wrinkle * np.sin(2 * np.pi * (kx * x + ky * y) + phase)
-
-    for _ in range(step):
-        z = z + delta()
-    z1 = z + delta()
-    start_sheet = np.stack([x, y, z], 1)
-    end_sheet = np.stack([x, y, z1], 1)
+    nv = sv.shape[0] + cv.shape[0]
+    frames = np.empty((steps + 1, 3 * nv))
+    z = sv[:, 2].copy()
+    for k in range(steps + 1):
+        frames[k] = np.concatenate([np.stack([x, y, z], 1), cv]).ravel()
+        if k < steps:
+            kx, ky = rng.uniform(1.0, 4.0, 2)
+            phase = rng.uniform(0.0, 2 * np.pi)
+            z = z - drop + wrinkle * np.sin(2 * np.pi * (kx * x + ky * y) + phase)
     faces = np.concatenate([sf, cf + sv.shape[0]]).astype(np.int32)
-    qs = np.concatenate([start_sheet, cv]).ravel().copy()
-    qe = np.concatenate([end_sheet, cv]).ravel().copy()
-    return qs, qe, faces
+    return faces, frames
+
+
+def sheet_on_sphere(grid: int = 256, level: int = 6, seed: int = 0, step: int = 0, gap: float = 0.05,
+                    drop: float = 0.002, wrinkle: float = 0.003, radius: float = 0.4):
+    """Step `step` of cloth_frames(...): (qstart (3V,), qend (3V,), faces)."""
+    faces, frames = cloth_frames(grid, level, seed, step + 1, gap, drop, wrinkle, radius)
+    return frames[step].copy(), frames[step + 1].copy(), faces

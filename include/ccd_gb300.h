@@ -47,7 +47,8 @@ typedef enum {
   CCD_PATH_FP64 = 0,
   /* Outward-bounded FP32 rejection of rows whose result is provably "no
    * hit", then the FP64 evaluation of the surviving rows only.  Same results
-   * as CCD_PATH_FP64 (the FP32 stage never rejects a row that hits). */
+   * as CCD_PATH_FP64 (the FP32 stage never rejects a row that hits).
+   * Vertex-vertex rows (one quadratic) are always evaluated in FP64. */
   CCD_PATH_CULL_REFINE = 1
 } ccd_path;
 
@@ -119,7 +120,7 @@ int ccd_prim_batch_device(ccd_context *ctx, int kind, int path, int64_t n, const
                           int64_t eta_count, uint8_t *hit, double *t, uint8_t *status);
 
 /* ---------------------------------------------------------- allocation-free batch
- * No counterpart in the reference.  The same computation and results as
+ * No counterpart in the reference.  The same results as
  * ccd_prim_batch_device with CCD_PATH_CULL_REFINE (no per-row status), for
  * callers that must not allocate device memory while they run: every byte of
  * scratch comes from one fixed region of about 9.4 MB per device, set aside

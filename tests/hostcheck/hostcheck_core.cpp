@@ -26,11 +26,12 @@ extern "C" void hc_batch(int kind, int64_t n, const double *x, const double *eta
 
 #include "../../collisiondetection_gb300/csrc/ccd_cull32.h"
 
-// 1 where the FP32 stage rejects the row (kinds 0 and 1 only).
+// 1 where the FP32 stage rejects the row (kinds 0, 1 and 2).
 extern "C" void hc_cull(int kind, int64_t n, const double *x, const double *eta, int eta_per_test, uint8_t *rej) {
+  const int w = kind == 2 ? 18 : 24;
   for (int64_t i = 0; i < n; i++) {
-    const double *xi = x + i * 24;
+    const double *xi = x + i * w;
     double e = eta_per_test ? eta[i] : eta[0];
-    rej[i] = kind == 0 ? ccd::vf_rejects(xi, e) : ccd::ee_rejects(xi, e);
+    rej[i] = kind == 0 ? ccd::vf_rejects(xi, e) : (kind == 1 ? ccd::ee_rejects(xi, e) : ccd::ve_rejects(xi, e));
   }
 }

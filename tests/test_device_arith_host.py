@@ -96,24 +96,49 @@ def test_fp64_core_matches_oracle_random(oracle, kind):
     assert np.all(np.abs(t[m] - t_ref[m]) <= 1e-12 * np.maximum(np.abs(t_ref[m]), 1e-300))
 
 
-@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("kind", [0, 1, 2])
 def test_fp32_cull_has_no_false_negatives(oracle, golden_dir, kind):
     from collisiondetection_gb300 import workloads as W
 
     g = np.load(f"{golden_dir}/prims.npz")
-    for x, eta in ((g[f"x{kind}"], g[f"eta{kind}"]), (W.primitive_batch(kind, 50000, seed=77), 1e-6)):
+    cases = [(g[f"x{kind}"], g[f"eta{kind}"]), (W.primitive_batch(kind, 50000, seed=77), 1e-6)]
+    if kind == 2:
+        # Larger eta: many distance hits; small motion: near-static rows.
+        cases.append((W.primitive_batch(kind, 50000, seed=78), 3e-2))
+        cases.append((W.primitive_batch(kind, 50000, seed=79, sigma=1e-3), 1e-3))
+    for x, eta in cases:
         h, _ = oracle.batch(kind, x, eta, nthreads=4)
         rej = _cull(kind, x, eta)
         assert not np.any((rej == 1) & (h == 1))
         assert rej.mean() > 0.5  # the stage does reject most random rows
 
 
+def test_vertex_edge_cull_on_mesh_stencils(oracle):
+    """Vertex-edge rows of the narrow-phase chain on a real candidate set
+    (two icospheres closing in): no false negatives, most rows rejected."""
+    from collisiondetection_gb300 import workloads as W
+
+    qs, qe, f = W.two_spheres(seed=1)
+    vf, _ = oracle.broadphase(0, qs, qe, f, 1e-6)
+    P0, P1 = qs.reshape(-1, 3), qe.reshape(-1, 3)
+    rows = []
+    for e in range(3):
+        ids = np.stack([vf[:, 0], vf[:, 1 + e], vf[:, 1 + (e + 1) % 3]], 1)
+        rows.append(np.concatenate([P0[ids].reshape(-1, 9), P1[ids].reshape(-1, 9)], 1))
+    x = np.ascontiguousarray(np.concatenate(rows))
+    for eta in (1e-6, 1e-2):
+        h, _ = oracle.batch(2, x, eta, nthreads=4)
+        rej = _cull(2, x, eta)
+        assert not np.any((rej == 1) & (h == 1))
+        assert rej.mean() > 0.85
+
+
 def test_fp32_cull_never_rejects_nonfinite():
-    x = np.random.default_rng(0).uniform(0, 1, (8, 24))
-    x[0, 3] = np.nan
-    x[1, 20] = np.inf
-    x[2, :] = 1e30  # overflows FP32
-    for kind in (0, 1):
+    for kind, w in ((0, 24), (1, 24), (2, 18)):
+        x = np.random.default_rng(0).uniform(0, 1, (8, w))
+        x[0, 3] = np.nan
+        x[1, w - 4] = np.inf
+        x[2, :] = 1e30  # overflows FP32
         rej = _cull(kind, x[:3], 1e-6)
         assert rej.sum() == 0
         assert _cull(kind, x[3:4], np.nan).sum() == 0
