@@ -73,6 +73,7 @@ def load(path: str = LIB):
     L.ccd_last_batch_stats.argtypes = [_P, ctypes.POINTER(BatchStats)]
     L.ccd_context_set_profiling.argtypes = [_P, ctypes.c_int]
     L.ccd_last_batch_timings.argtypes = [_P, ctypes.POINTER(BatchTimings)]
+    L.ccd_context_set_option.argtypes = [_P, ctypes.c_char_p, ctypes.c_int64]
     for name in ("ccd_vertex_face_ctcd", "ccd_edge_edge_ctcd", "ccd_vertex_edge_ctcd", "ccd_vertex_vertex_ctcd"):
         fn = getattr(L, name)
         fn.argtypes = [_P, _P, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
@@ -141,6 +142,10 @@ class Context:
         st = BatchStats()
         self._check(self.lib.ccd_last_batch_stats(self.handle, ctypes.byref(st)), "ccd_last_batch_stats")
         return {f: getattr(st, f) for f, _ in BatchStats._fields_}
+
+    def set_option(self, name: str, value: int):
+        """Tuning option (ccd_context_set_option): "wave_steps", "wave_min_rows"."""
+        self._check(self.lib.ccd_context_set_option(self.handle, name.encode(), int(value)), "ccd_context_set_option")
 
     def set_profiling(self, on: bool):
         self._check(self.lib.ccd_context_set_profiling(self.handle, int(bool(on))), "ccd_context_set_profiling")

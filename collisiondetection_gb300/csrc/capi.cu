@@ -136,7 +136,10 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     CCD_CUDA(ccd::launch_prims_cull(b, surv, ctx->num_sms, s));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[1], s));
     int launches = 0;
-    CCD_CUDA(ccd::launch_stages(b, surv, stage.view, ctx->num_sms, s, &launches));
+    ccd::StageScratch view = stage.view;
+    view.wave_steps = view.wd ? ctx->opt_wave_steps : 0;
+    view.wave_min_rows = ctx->opt_wave_min_rows;
+    CCD_CUDA(ccd::launch_stages(b, surv, view, ctx->num_sms, s, &launches));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[2], s));
     if (pe) pe->stage_launches = launches;
   }
@@ -272,6 +275,22 @@ int ccd_context_set_profiling(ccd_context *ctx, int on) {
   if (rc) return rc;
   ctx->profiling = on != 0;
   ctx->timings = ccd_batch_timings{};
+  return CCD_OK;
+}
+
+int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
+  if (!ctx) return CCD_ERR_INVALID_ARGUMENT;
+  if (!name) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null option name");
+  const std::string key(name);
+  if (key == "wave_steps") {
+    if (value < 0 || value > 4096) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "wave_steps must be in [0, 4096]");
+    ctx->opt_wave_steps = (int)value;
+  } else if (key == "wave_min_rows") {
+    if (value < 0) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "wave_min_rows must be >= 0");
+    ctx->opt_wave_min_rows = value;
+  } else {
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown option " + key);
+  }
   return CCD_OK;
 }
 

@@ -15,9 +15,11 @@ namespace ccd_capi {
 
 // Rows per chunk of the host-memory batch pipeline (two chunks in flight).
 constexpr int64_t kChunkRows = 1 << 20;
-// Survivor rows per tile of the staged refinement (bounds its scratch to
-// about 0.9 GB per execution slot).
-constexpr int64_t kStageTileRows = 1 << 20;
+// Survivor rows per tile of the staged refinement.  Each tile ends in a
+// latency-bound tail (the slowest root solves), so tiles are large: the
+// scratch is about 5 KB per survivor row (about 20 GB at this size; a batch
+// of n < 2^22 rows allocates for n).
+constexpr int64_t kStageTileRows = 1 << 22;
 
 // Scratch of the staged refinement, grown on demand.
 struct StageBuf {
@@ -74,6 +76,9 @@ struct ccd_context {
   PhaseEvents dev_ring[32];  // device entry points, collected lazily
   int dev_next = 0;
   ccd_batch_timings timings{};
+  // tuning options (ccd_context_set_option)
+  int opt_wave_steps = ccd::kWaveSteps;
+  int64_t opt_wave_min_rows = ccd::kWaveMinRows;
   std::string err;
 };
 

@@ -32,12 +32,15 @@ namespace ccd {
 
 constexpr int kMaxSlots = 5;
 constexpr int kStageThreads = 128;
-// Wavefront steps before the remaining jobs go to the pool kernel (about 99%
-// of the queued polynomials finish within 40 solver steps).
-constexpr int kWaveSteps = 48;
-// Batches below this many rows take the pool kernel alone: the wavefront
-// pays a global-memory round trip per step, which only a large batch hides.
+// Wavefront defaults (per-context options override them): steps before the
+// remaining jobs are finished one per warp (about 99% of the queued
+// polynomials finish within 40 solver steps, 99.9% within 120), and the batch
+// size below which the pool kernel alone solves (the wavefront pays a
+// global-memory round trip per step, which only a large batch hides).
+constexpr int kWaveSteps = 64;
 constexpr int64_t kWaveMinRows = (int64_t)1 << 18;
+// Job lists: one per (working phase, current degree 3..6).
+constexpr int kWaveBins = 16;
 
 // Device scratch for one tile of `cap` survivor rows (layouts are slot-major,
 // then coefficient / span index, then row, so warps access consecutive rows).
@@ -57,9 +60,11 @@ struct StageScratch {
   int64_t jcap;         // kMaxSlots * cap
   double *wd;           // [field < jt::kDoubles][jcap]  solver states
   int *wi;              // [field < jt::kInts][jcap]
-  uint32_t *wlist;      // [2][phase < 4][jcap]          jobs per working phase
-  unsigned *wcount;     // [3][4]                        list lengths (rotating)
-  uint32_t *tail;       // [jcap]                        jobs left for the pool kernel
+  uint32_t *wlist;      // [2][bin < 16][jcap]           jobs per (phase, degree)
+  unsigned *wcount;     // [3][16] list lengths (rotating), then the tail length
+  uint32_t *tail;       // [jcap]                        jobs left after the wavefront steps
+  int wave_steps;       // wavefront steps (0: pool kernel only)
+  int64_t wave_min_rows;
 };
 
 size_t stage_scratch_bytes(int64_t cap);
@@ -299,20 +304,24 @@ __device__ __forceinline__ void queue_bases(const StageScratch &sc, int nslots, 
   qbase[nslots] = acc;
 }
 
-// Warp-aggregated append of job g to the list of phase `mode` (1..4).
-__device__ __forceinline__ void wave_append(uint32_t *lists, unsigned *counts, int64_t jcap, bool active, int mode,
+// List of a working job: (phase, current degree).
+__device__ __forceinline__ int wave_bin(int mode, int n) {
+  n = n < 3 ? 3 : (n > 6 ? 6 : n);
+  return (mode - 1) * 4 + (n - 3);
+}
+
+// Warp-aggregated append of job g to list `bin` (lanes with equal bins share
+// one atomic).
+__device__ __forceinline__ void wave_append(uint32_t *lists, unsigned *counts, int64_t jcap, bool active, int bin,
                                             int64_t g) {
   const unsigned lane = threadIdx.x & 31;
-  for (int m = jt::kInit; m <= jt::kReal; m++) {
-    const bool mine = active && mode == m;
-    const unsigned mask = __ballot_sync(0xffffffffu, mine);
-    if (!mask) continue;
-    const int leader = __ffs(mask) - 1;
-    unsigned base = 0;
-    if ((int)lane == leader) base = atomicAdd(&counts[m - 1], (unsigned)__popc(mask));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (mine) lists[(int64_t)(m - 1) * jcap + base + __popc(mask & ((1u << lane) - 1u))] = (uint32_t)g;
-  }
+  const unsigned key = active ? (unsigned)bin : 0xffffffffu;
+  const unsigned peers = __match_any_sync(0xffffffffu, key);
+  const int leader = __ffs(peers) - 1;
+  unsigned base = 0;
+  if (active && (int)lane == leader) base = atomicAdd(&counts[bin], (unsigned)__popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (active) lists[(int64_t)bin * jcap + base + __popc(peers & ((1u << lane) - 1u))] = (uint32_t)g;
 }
 
 template <class Polys>
@@ -321,6 +330,29 @@ __device__ __forceinline__ jt::FieldState wave_state(const StageScratch &sc, con
   q = job_queue(qbase, Polys::kSlots, g);
   j = g - qbase[q];
   return jt::FieldState{sc.wd, sc.wi, g, sc.jcap, sc.roots + (int64_t)q * 6 * sc.cap + j, sc.cap};
+}
+
+// Offsets of the concatenated lists (off[kWaveBins] = total).
+__device__ __forceinline__ void list_offsets(const unsigned *cin, int64_t *off) {
+  int64_t acc = 0;
+  for (int m = 0; m < kWaveBins; m++) {
+    off[m] = acc;
+    acc += cin[m];
+  }
+  off[kWaveBins] = acc;
+}
+
+__device__ __forceinline__ int64_t list_entry(const uint32_t *in, const int64_t *off, int64_t jcap, int64_t r) {
+  int m = 0;
+  while (m + 1 < kWaveBins && r >= off[m + 1]) m++;
+  return in[(int64_t)m * jcap + (r - off[m])];
+}
+
+// Whole solver state from global (field-major) to thread-private storage.
+__device__ __forceinline__ void load_state(const jt::FieldState &fs, jt::LocalStorage &st) {
+  for (int f = 0; f < jt::kDoubles; f++) st.d[f] = fs.D(f);
+  for (int f = 0; f < jt::kInts; f++) st.i[f] = fs.I(f);
+  for (int k = 0; k < 6; k++) st.zr[k] = fs.Z(k);
 }
 
 template <class Polys>
@@ -333,9 +365,9 @@ __global__ void __launch_bounds__(kWaveThreads) wave_start(StageScratch sc) {
   const int64_t warp_base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
   for (int64_t w = warp_base; w < njobs; w += stride) {
     const int64_t g = w + (threadIdx.x & 31);
-    const bool active = g < njobs;
-    int mode = jt::kDone;
-    if (active) {
+    bool work = false;
+    int bin = 0;
+    if (g < njobs) {
       int q;
       int64_t j;
       const jt::FieldState s = wave_state<Polys>(sc, qbase, g, q, j);
@@ -343,52 +375,55 @@ __global__ void __launch_bounds__(kWaveThreads) wave_start(StageScratch sc) {
       double op[7];
       for (int c = 0; c <= deg; c++) op[c] = sc.coef[(q * 7 + c) * sc.cap + j];
       jt::start(s, op, deg);
-      mode = s.I(jt::MODE);
-      if (mode == jt::kDone) finish_job<Polys>(sc, s, q, j);
+      const int mode = s.I(jt::MODE);
+      if (mode == jt::kDone) {
+        finish_job<Polys>(sc, s, q, j);
+      } else {
+        work = true;
+        bin = wave_bin(mode, s.I(jt::N));
+      }
     }
-    wave_append(sc.wlist, sc.wcount, sc.jcap, active, mode, g);
+    wave_append(sc.wlist, sc.wcount, sc.jcap, work, bin, g);
   }
 }
 
 // One step of every job in lists `in` (counts cin), re-binned into lists
-// `out` (counts cout, zeroed by the caller); also zeroes czero, the counts
-// the step after next will fill.
+// `out` (counts cout, zeroed before); also zeroes czero, the counts the step
+// after next will fill.
 template <class Polys>
 __global__ void __launch_bounds__(kWaveThreads) wave_step(StageScratch sc, const uint32_t *in, const unsigned *cin,
                                                           uint32_t *out, unsigned *cout, unsigned *czero) {
   __shared__ int qbase[kMaxSlots + 1];
-  __shared__ int64_t off[5];
+  __shared__ int64_t off[kWaveBins + 1];
   if (threadIdx.x == 0) {
     queue_bases(sc, Polys::kSlots, qbase);
-    int64_t acc = 0;
-    for (int m = 0; m < 4; m++) {
-      off[m] = acc;
-      acc += cin[m];
-    }
-    off[4] = acc;
+    list_offsets(cin, off);
   }
-  if (blockIdx.x == 0 && threadIdx.x < 4) czero[threadIdx.x] = 0;
+  if (blockIdx.x == 0 && threadIdx.x < kWaveBins) czero[threadIdx.x] = 0;
   __syncthreads();
-  const int64_t total = off[4];
+  const int64_t total = off[kWaveBins];
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t warp_base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
   for (int64_t w = warp_base; w < total; w += stride) {
     const int64_t r = w + (threadIdx.x & 31);
-    const bool active = r < total;
-    int mode = jt::kDone;
+    bool work = false;
+    int bin = 0;
     int64_t g = 0;
-    if (active) {
-      int m = 0;
-      while (m < 3 && r >= off[m + 1]) m++;
-      g = in[(int64_t)m * sc.jcap + (r - off[m])];
+    if (r < total) {
+      g = list_entry(in, off, sc.jcap, r);
       int q;
       int64_t j;
       const jt::FieldState s = wave_state<Polys>(sc, qbase, g, q, j);
       jt::step(s);
-      mode = s.I(jt::MODE);
-      if (mode == jt::kDone) finish_job<Polys>(sc, s, q, j);
+      const int mode = s.I(jt::MODE);
+      if (mode == jt::kDone) {
+        finish_job<Polys>(sc, s, q, j);
+      } else {
+        work = true;
+        bin = wave_bin(mode, s.I(jt::N));
+      }
     }
-    wave_append(out, cout, sc.jcap, active, mode, g);
+    wave_append(out, cout, sc.jcap, work, bin, g);
   }
 }
 
@@ -397,19 +432,36 @@ __global__ void __launch_bounds__(kWaveThreads) wave_step(StageScratch sc, const
 template <class Polys>
 __global__ void __launch_bounds__(kWaveThreads) wave_gather_tail(StageScratch sc, const uint32_t *in,
                                                                  const unsigned *cin, unsigned *tcount) {
-  int64_t off[5];
-  int64_t acc = 0;
-  for (int m = 0; m < 4; m++) {
-    off[m] = acc;
-    acc += cin[m];
-  }
-  off[4] = acc;
-  if (blockIdx.x == 0 && threadIdx.x == 0) *tcount = (unsigned)acc;
+  int64_t off[kWaveBins + 1];
+  list_offsets(cin, off);
+  const int64_t total = off[kWaveBins];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *tcount = (unsigned)total;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < acc; r += stride) {
-    int m = 0;
-    while (m < 3 && r >= off[m + 1]) m++;
-    sc.tail[r] = in[(int64_t)m * sc.jcap + (r - off[m])];
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < total; r += stride)
+    sc.tail[r] = (uint32_t)list_entry(in, off, sc.jcap, r);
+}
+
+// The jobs the wavefront steps left unfinished, one per warp: lane 0 copies
+// the job's state into thread-private storage and runs it to the end (the
+// solver's own iteration limits bound the loop).  Few jobs remain by then and
+// each is a long sequential chain, so latency, not lane use, matters here.
+template <class Polys>
+__global__ void __launch_bounds__(32) wave_finish(StageScratch sc, const uint32_t *tail, const unsigned *tcount) {
+  __shared__ int qbase[kMaxSlots + 1];
+  if (threadIdx.x == 0) queue_bases(sc, Polys::kSlots, qbase);
+  __syncwarp();
+  if (threadIdx.x != 0) return;
+  const int64_t count = *tcount;
+  for (int64_t r = blockIdx.x; r < count; r += gridDim.x) {
+    const int64_t g = tail[r];
+    int q;
+    int64_t j;
+    const jt::FieldState fs = wave_state<Polys>(sc, qbase, g, q, j);
+    jt::LocalStorage st;
+    load_state(fs, st);
+    const jt::LocalState s{&st};
+    while (s.I(jt::MODE) != jt::kDone) jt::step(s);
+    finish_job<Polys>(sc, s, q, j);
   }
 }
 
@@ -482,22 +534,24 @@ cudaError_t run(const PrimBatch &b, const int32_t *list, const StageScratch &sc,
     cudaError_t e = cudaMemsetAsync(sc.queue, 0, (kMaxSlots + 1) * sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     stage_build<Polys><<<grid, kStageThreads, 0, s>>>(b, list, tile * sc.cap, sc);
-    if (sc.wd && b.n >= kWaveMinRows) {
-      // counts: 3 rotating sets of 4, then the tail count
-      e = cudaMemsetAsync(sc.wcount, 0, 13 * sizeof(unsigned), s);
+    if (sc.wd && sc.wave_steps > 0 && b.n >= sc.wave_min_rows) {
+      const int steps = sc.wave_steps;
+      const int64_t lstride = (int64_t)kWaveBins * sc.jcap;
+      // counts: 3 rotating sets, then the tail length
+      e = cudaMemsetAsync(sc.wcount, 0, (3 * kWaveBins + 1) * sizeof(unsigned), s);
       if (e != cudaSuccess) return e;
       wave_start<Polys><<<wave_grid, kWaveThreads, 0, s>>>(sc);
-      for (int it = 0; it < kWaveSteps; it++) {
-        const uint32_t *in = sc.wlist + (int64_t)(it & 1) * 4 * sc.jcap;
-        uint32_t *out = sc.wlist + (int64_t)((it + 1) & 1) * 4 * sc.jcap;
-        wave_step<Polys><<<wave_grid, kWaveThreads, 0, s>>>(sc, in, sc.wcount + 4 * (it % 3), out,
-                                                            sc.wcount + 4 * ((it + 1) % 3),
-                                                            sc.wcount + 4 * ((it + 2) % 3));
+      for (int it = 0; it < steps; it++) {
+        wave_step<Polys><<<wave_grid, kWaveThreads, 0, s>>>(
+            sc, sc.wlist + (it & 1) * lstride, sc.wcount + kWaveBins * (it % 3), sc.wlist + ((it + 1) & 1) * lstride,
+            sc.wcount + kWaveBins * ((it + 1) % 3), sc.wcount + kWaveBins * ((it + 2) % 3));
       }
-      const uint32_t *last = sc.wlist + (int64_t)(kWaveSteps & 1) * 4 * sc.jcap;
-      wave_gather_tail<Polys><<<num_sms, kWaveThreads, 0, s>>>(sc, last, sc.wcount + 4 * (kWaveSteps % 3), sc.wcount + 12);
-      stage_roots<Polys><<<pool_grid, 32, kPoolSmem, s>>>(sc, sc.tail, sc.wcount + 12);
-      *launches += kWaveSteps + 3;
+      unsigned *tcount = sc.wcount + 3 * kWaveBins;
+      wave_gather_tail<Polys><<<num_sms, kWaveThreads, 0, s>>>(sc, sc.wlist + (steps & 1) * lstride,
+                                                               sc.wcount + kWaveBins * (steps % 3), tcount);
+      // One warp per unfinished job, as many as can be resident at once.
+      wave_finish<Polys><<<num_sms * 32, 32, 0, s>>>(sc, sc.tail, tcount);
+      *launches += steps + 3;
     } else {
       stage_roots<Polys><<<pool_grid, 32, kPoolSmem, s>>>(sc, nullptr, nullptr);
       *launches += 1;
