@@ -139,6 +139,7 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     ccd::StageScratch view = stage.view;
     view.wave_steps = view.wd ? ctx->opt_wave_steps : 0;
     view.wave_min_rows = ctx->opt_wave_min_rows;
+    view.pool_budget = ctx->opt_pool_budget;
     CCD_CUDA(ccd::launch_stages(b, surv, view, ctx->num_sms, s, &launches));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[2], s));
     if (pe) pe->stage_launches = launches;
@@ -285,6 +286,9 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
   if (key == "wave_steps") {
     if (value < 0 || value > 4096) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "wave_steps must be in [0, 4096]");
     ctx->opt_wave_steps = (int)value;
+  } else if (key == "pool_budget") {
+    if (value < 0 || value > (1 << 20)) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "pool_budget must be in [0, 2^20]");
+    ctx->opt_pool_budget = (int)value;
   } else if (key == "wave_min_rows") {
     if (value < 0) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "wave_min_rows must be >= 0");
     ctx->opt_wave_min_rows = value;

@@ -79,6 +79,7 @@ struct ccd_context {
   // tuning options (ccd_context_set_option)
   int opt_wave_steps = ccd::kWaveSteps;
   int64_t opt_wave_min_rows = ccd::kWaveMinRows;
+  int opt_pool_budget = ccd::kPoolBudget;
   std::string err;
 };
 

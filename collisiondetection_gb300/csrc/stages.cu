@@ -46,13 +46,14 @@ StageScratch stage_scratch_view(void *base, int64_t cap) {
   sc.tail = nullptr;
   sc.wave_steps = 0;
   sc.wave_min_rows = 0;
+  sc.pool_budget = 0;
   return sc;
 }
 
 size_t wave_scratch_bytes(int64_t cap) {
   const size_t j = (size_t)kMaxSlots * (size_t)cap;
   return up(jt::kDoubles * j * sizeof(double)) + up(jt::kInts * j * sizeof(int)) +
-         up(2 * kWaveBins * j * sizeof(uint32_t)) + up((3 * kWaveBins + 1) * sizeof(unsigned)) +
+         up(2 * kWaveBins * j * sizeof(uint32_t)) + up((3 * kWaveBins + 2) * sizeof(unsigned)) +
          up(j * sizeof(uint32_t));
 }
 
@@ -67,10 +68,11 @@ void attach_wave(StageScratch &sc, void *base) {
   sc.wlist = (uint32_t *)p;
   p += up(2 * kWaveBins * j * sizeof(uint32_t));
   sc.wcount = (unsigned *)p;
-  p += up((3 * kWaveBins + 1) * sizeof(unsigned));
+  p += up((3 * kWaveBins + 2) * sizeof(unsigned));
   sc.tail = (uint32_t *)p;
   sc.wave_steps = kWaveSteps;
   sc.wave_min_rows = kWaveMinRows;
+  sc.pool_budget = kPoolBudget;
 }
 
 cudaError_t launch_stages(const PrimBatch &b, const int32_t *list, const StageScratch &sc, int num_sms,

@@ -4,19 +4,27 @@
 // (the reference's early exits and the root finder's data-dependent iteration
 // counts differ from row to row), and FP64 issue slots are scarce on this GPU
 // (1/64 of the FP32 rate), so masked lanes are expensive.  The refinement is
-// therefore split into three kernels over a tile of survivor rows:
+// therefore split into kernels over a tile of survivor rows:
 //
 //   stage_build    thread per row: every polynomial of the row in FP64
 //                  (reference expressions), normalised and degree-reduced;
 //                  lists of degree <= 2 are finished here, the others are
 //                  queued per polynomial slot (one queue per slot, so every
 //                  queue holds polynomials of one nominal degree);
-//   stage_roots    the queued polynomials through the Jenkins-Traub state
-//                  machine (ccd_jt.h): every warp keeps a pool of 64 solver
-//                  states in shared memory and, each iteration, advances up to
-//                  32 of them that are in the same phase (the most populated
-//                  one), refilling finished slots from the queues -- so lanes
-//                  stay busy on equal work without any block-wide barrier;
+//   root solving   the queued polynomials through the Jenkins-Traub state
+//                  machine (ccd_jt.h), in one of two ways:
+//     wavefront    (large batches) wave_start / wave_step: every solver state
+//                  lives in global memory; each launch advances every
+//                  unfinished job by one step and re-bins it by (phase,
+//                  degree), so a warp steps 32 jobs through the same code;
+//                  after a fixed number of steps the few unfinished jobs
+//                  continue in the pool kernel, and the last ones finish one
+//                  per warp (wave_finish);
+//     pool         stage_roots: every warp keeps 64 solver states in shared
+//                  memory and, each iteration, advances up to 32 of them that
+//                  are in the same phase, refilling finished slots from the
+//                  queues -- lanes stay busy on equal work without any
+//                  block-wide barrier;
 //   stage_combine  thread per row: the interval-overlap decision.
 //
 // The result equals the reference's: every list the reference computes is
@@ -32,12 +40,14 @@ namespace ccd {
 
 constexpr int kMaxSlots = 5;
 constexpr int kStageThreads = 128;
-// Wavefront defaults (per-context options override them): steps before the
-// remaining jobs are finished one per warp (about 99% of the queued
-// polynomials finish within 40 solver steps, 99.9% within 120), and the batch
-// size below which the pool kernel alone solves (the wavefront pays a
-// global-memory round trip per step, which only a large batch hides).
-constexpr int kWaveSteps = 64;
+// Wavefront defaults (per-context options override them): lock-step steps
+// before the unfinished jobs move to the pool kernel (about 99% of the queued
+// polynomials finish within 40 solver steps, 99.9% within 120), the steps the
+// pool kernel then gives each before the last ones finish one per warp, and
+// the batch size below which the pool kernel alone solves (the wavefront pays
+// a global-memory round trip per step, which only a large batch hides).
+constexpr int kWaveSteps = 48;
+constexpr int kPoolBudget = 128;
 constexpr int64_t kWaveMinRows = (int64_t)1 << 18;
 // Job lists: one per (working phase, current degree 3..6).
 constexpr int kWaveBins = 16;
@@ -61,10 +71,11 @@ struct StageScratch {
   double *wd;           // [field < jt::kDoubles][jcap]  solver states
   int *wi;              // [field < jt::kInts][jcap]
   uint32_t *wlist;      // [2][bin < 16][jcap]           jobs per (phase, degree)
-  unsigned *wcount;     // [3][16] list lengths (rotating), then the tail length
+  unsigned *wcount;     // [3][16] list lengths (rotating), then the tail and spill lengths
   uint32_t *tail;       // [jcap]                        jobs left after the wavefront steps
   int wave_steps;       // wavefront steps (0: pool kernel only)
   int64_t wave_min_rows;
+  int pool_budget;      // steps the pool kernel gives a resumed job before handing it on
 };
 
 size_t stage_scratch_bytes(int64_t cap);
@@ -181,15 +192,26 @@ __device__ __forceinline__ int job_queue(const int *qbase, int nslots, int64_t g
   return q;
 }
 
-// `tail` (optional): solve only the jobs tail[0 .. *tail_count), from the
-// start (the jobs the wavefront solver left unfinished).
+// Which jobs the pool kernel solves.  Default (list null): every queued job,
+// from the start.  After the wavefront steps: the jobs in list, resumed from
+// their field-major states; a job that takes `budget` more steps is handed on
+// (state written back, index appended to spill) to the one-per-warp finish.
+struct PoolJobs {
+  const uint32_t *list;
+  const unsigned *count;
+  int budget;
+  uint32_t *spill;
+  unsigned *spill_count;
+};
+
 template <class Polys>
-__global__ void __launch_bounds__(32) stage_roots(StageScratch sc, const uint32_t *tail, const unsigned *tail_count) {
+__global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) {
   extern __shared__ double pool_d[];
   int *pool_i = (int *)(pool_d + (size_t)kWarpPool * jt::kDoubles);
   __shared__ int64_t job_of[kWarpPool];
   __shared__ int sel[32];
   __shared__ int qbase[kMaxSlots + 1];
+  __shared__ int steps[kWarpPool];
   const int lane = threadIdx.x;
   const unsigned lt = (1u << lane) - 1u;
   if (lane == 0) {
@@ -202,7 +224,8 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, const uint32_
   }
   for (int k = lane; k < kWarpPool; k += 32) pool_i[jt::MODE * kWarpPool + k] = jt::kEmpty;
   __syncwarp();
-  const int njobs = tail ? (int)*tail_count : qbase[Polys::kSlots];
+  const uint32_t *tail = pj.list;
+  const int njobs = tail ? (int)*pj.count : qbase[Polys::kSlots];
   auto state = [&](int k) {
     const int64_t g = job_of[k];
     const int q = job_queue(qbase, Polys::kSlots, g);
@@ -241,13 +264,20 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, const uint32_
           if (g0 >= njobs) continue;
           const int64_t g = tail ? (int64_t)tail[g0] : g0;
           job_of[k] = g;
+          steps[k] = 0;
           const int q = job_queue(qbase, Polys::kSlots, g);
           const int64_t j = g - qbase[q];
-          const int deg = sc.job_deg[q * sc.cap + j];
-          double op[7];
-          for (int c = 0; c <= deg; c++) op[c] = sc.coef[(q * 7 + c) * sc.cap + j];
           const jt::PoolState<kWarpPool> st{pool_d, pool_i, k, sc.roots + (int64_t)q * 6 * sc.cap + j, sc.cap};
-          jt::start(st, op, deg);
+          if (tail) {
+            const jt::FieldState fs{sc.wd, sc.wi, g, sc.jcap, st.zr, sc.cap};
+            for (int f = 0; f < jt::kDoubles; f++) st.D(f) = fs.D(f);
+            for (int f = 0; f < jt::kInts; f++) st.I(f) = fs.I(f);
+          } else {
+            const int deg = sc.job_deg[q * sc.cap + j];
+            double op[7];
+            for (int c = 0; c <= deg; c++) op[c] = sc.coef[(q * 7 + c) * sc.cap + j];
+            jt::start(st, op, deg);
+          }
         }
       }
     }
@@ -281,7 +311,19 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, const uint32_
       if (r < 32) sel[r] = lane + 32;
     }
     __syncwarp();
-    if (lane < bestc) jt::step(state(sel[lane]));
+    if (lane < bestc) {
+      const int k = sel[lane];
+      const jt::PoolState<kWarpPool> st = state(k);
+      jt::step(st);
+      if (pj.budget > 0 && mode[k] != jt::kDone && ++steps[k] >= pj.budget) {
+        // Hand the job on: its state back home, its index to the spill list.
+        const jt::FieldState fs{sc.wd, sc.wi, job_of[k], sc.jcap, st.zr, sc.cap};
+        for (int f = 0; f < jt::kDoubles; f++) fs.D(f) = st.D(f);
+        for (int f = 0; f < jt::kInts; f++) fs.I(f) = st.I(f);
+        pj.spill[atomicAdd(pj.spill_count, 1u)] = (uint32_t)job_of[k];
+        mode[k] = jt::kEmpty;
+      }
+    }
     __syncwarp();
   }
 }
@@ -537,8 +579,8 @@ cudaError_t run(const PrimBatch &b, const int32_t *list, const StageScratch &sc,
     if (sc.wd && sc.wave_steps > 0 && b.n >= sc.wave_min_rows) {
       const int steps = sc.wave_steps;
       const int64_t lstride = (int64_t)kWaveBins * sc.jcap;
-      // counts: 3 rotating sets, then the tail length
-      e = cudaMemsetAsync(sc.wcount, 0, (3 * kWaveBins + 1) * sizeof(unsigned), s);
+      // counts: 3 rotating sets, then the tail and spill lengths
+      e = cudaMemsetAsync(sc.wcount, 0, (3 * kWaveBins + 2) * sizeof(unsigned), s);
       if (e != cudaSuccess) return e;
       wave_start<Polys><<<wave_grid, kWaveThreads, 0, s>>>(sc);
       for (int it = 0; it < steps; it++) {
@@ -546,14 +588,18 @@ cudaError_t run(const PrimBatch &b, const int32_t *list, const StageScratch &sc,
             sc, sc.wlist + (it & 1) * lstride, sc.wcount + kWaveBins * (it % 3), sc.wlist + ((it + 1) & 1) * lstride,
             sc.wcount + kWaveBins * ((it + 1) % 3), sc.wcount + kWaveBins * ((it + 2) % 3));
       }
-      unsigned *tcount = sc.wcount + 3 * kWaveBins;
+      unsigned *tcount = sc.wcount + 3 * kWaveBins, *scount = tcount + 1;
       wave_gather_tail<Polys><<<num_sms, kWaveThreads, 0, s>>>(sc, sc.wlist + (steps & 1) * lstride,
                                                                sc.wcount + kWaveBins * (steps % 3), tcount);
-      // One warp per unfinished job, as many as can be resident at once.
-      wave_finish<Polys><<<num_sms * 32, 32, 0, s>>>(sc, sc.tail, tcount);
-      *launches += steps + 3;
+      // The unfinished jobs continue in the pool kernel (many per warp); the
+      // few that exceed its step budget finish one per warp, as many warps as
+      // can be resident at once.  The wavefront lists are free again and hold
+      // the spilled jobs.
+      stage_roots<Polys><<<pool_grid, 32, kPoolSmem, s>>>(sc, PoolJobs{sc.tail, tcount, sc.pool_budget, sc.wlist, scount});
+      wave_finish<Polys><<<num_sms * 32, 32, 0, s>>>(sc, sc.wlist, scount);
+      *launches += steps + 4;
     } else {
-      stage_roots<Polys><<<pool_grid, 32, kPoolSmem, s>>>(sc, nullptr, nullptr);
+      stage_roots<Polys><<<pool_grid, 32, kPoolSmem, s>>>(sc, PoolJobs{nullptr, nullptr, 0, nullptr, nullptr});
       *launches += 1;
     }
     stage_combine<Polys><<<grid, kStageThreads, 0, s>>>(b, list, tile * sc.cap, sc);

@@ -89,11 +89,14 @@ int ccd_context_set_profiling(ccd_context *ctx, int on);
 int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
 /* Tuning options of a context, for the autotuner (results never change):
  *   "wave_steps"     root-solver steps taken in lock-step over all queued
- *                    polynomials of a large batch before the few unfinished
- *                    ones are finished one per warp (0: the per-warp pool
- *                    solver only); default 64, at most 4096
+ *                    polynomials of a large batch before the unfinished ones
+ *                    continue in the per-warp pool solver (0: the pool
+ *                    solver only); default 48, at most 4096
  *   "wave_min_rows"  smallest batch (rows) that uses those lock-step steps;
  *                    default 262144
+ *   "pool_budget"    further steps the unfinished polynomials get, many per
+ *                    warp, before the last ones are finished one per warp
+ *                    (0: no limit); default 128
  * Unknown names and out-of-range values return CCD_ERR_INVALID_ARGUMENT. */
 int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value);
 /* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
