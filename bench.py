@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-sample", type=int, default=2_000_000, help="rows per kind per reference step")
     ap.add_argument("--mesh", type=int, default=1, help="also time the mesh configurations (1) or not (0)")
+    ap.add_argument("--serve", type=int, default=1, help="also run the serving loop (1) or not (0)")
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0])
+    ap.add_argument("--serve-fp64-requests", type=int, default=6)
     ap.add_argument("--only", default="all", choices=["all", "device"],
                     help="device: only the resident cull + refine steps (a short run for profilers)")
     ap.add_argument("--cloth-grid", type=int, default=256)
@@ -248,6 +252,61 @@ def mesh_section(ctx, stream, rank, args):
     return out
 
 
+def serving_section(args):
+    """Serving loop: Poisson arrivals of collision queries (mesh + 10 steps of
+    seeded rigid + jitter motion, triangle counts log-uniform in [1e3, 5e5])
+    through the serving engine (ccd_server_*, 4 slots, 60 GB admission
+    budget).  Reports throughput and per-step latency percentiles at each
+    arrival rate, beside the same queries one at a time on the plain FP64
+    path (a subset)."""
+    import collisiondetection_gb300 as C
+    from collisiondetection_gb300 import workloads as W
+
+    rng = np.random.default_rng(7)
+    n_req = args.serve_requests
+    sizes = np.exp(rng.uniform(np.log(1e3), np.log(5e5), n_req)).astype(int)
+    reqs = [W.motion_request(int(t), 1000 + i, steps=10) for i, t in enumerate(sizes)]
+    out = {"requests": n_req, "steps_per_request": 10, "faces_mean": float(np.mean([f.shape[0] for f, _ in reqs])),
+           "slots": 4, "memory_budget_gb": 60, "rates": []}
+
+    def pct(x, q):
+        return float(np.percentile(np.asarray(x), q)) if len(x) else None
+
+    with C.Server(0, slots=4, memory_budget=60 << 30) as srv:
+        # warm-up: one small query per slot
+        for t in [srv.submit(*reqs[int(np.argmin(sizes))]) for _ in range(4)]:
+            srv.wait(t)
+        for rate in args.serve_rates:
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+            t0 = time.perf_counter()
+            tickets = []
+            for (f, fr), at in zip(reqs, arrivals):
+                delay = at - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                tickets.append(srv.submit(f, fr))
+            results = [srv.wait(t) for t in tickets]
+            wall = time.perf_counter() - t0
+            step_ms = np.concatenate([r["step_ms"] for r in results])
+            req_ms = [r["total_ms"] for r in results]
+            out["rates"].append({
+                "arrival_rate": rate, "throughput_req_s": n_req / wall,
+                "step_ms_p50": pct(step_ms, 50), "step_ms_p95": pct(step_ms, 95), "step_ms_p99": pct(step_ms, 99),
+                "request_ms_p50": pct(req_ms, 50), "request_ms_p95": pct(req_ms, 95),
+                "request_ms_p99": pct(req_ms, 99), "collisions": int(sum(len(st[0]) + len(st[2])
+                                                                          for r in results for st in r["steps"]))})
+    # Plain FP64 path, one query at a time (a subset of the same queries).
+    sub = list(range(min(args.serve_fp64_requests, n_req)))
+    with C.Server(0, slots=1, memory_budget=60 << 30) as srv:
+        t0 = time.perf_counter()
+        res = [srv.wait(srv.submit(*reqs[i], path=C.PATH_FP64)) for i in sub]
+        wall = time.perf_counter() - t0
+    step_ms = np.concatenate([r["step_ms"] for r in res])
+    out["fp64_one_at_a_time"] = {"requests": len(sub), "throughput_req_s": len(sub) / wall,
+                                 "step_ms_p50": pct(step_ms, 50), "step_ms_p99": pct(step_ms, 99)}
+    return out
+
+
 def run_reference(args, rank, world, pg):
     if rank != 0:
         return
@@ -426,6 +485,7 @@ def run_ours(args, rank, world, local, pg):
                           "refine": tm["refine_ms"] / (tm["cull_ms"] + tm["refine_ms"])}}
     cpu = cpu_baseline(vf, ee) if rank == 0 and full else None
     mesh = mesh_section(ctx, stream, rank, args) if args.mesh and full else None
+    serving = serving_section(args) if args.serve and full and world == 1 else None
 
     if rank == 0:
         line = {
@@ -446,6 +506,7 @@ def run_ours(args, rank, world, local, pg):
             "clocks": clk.summary(),
             "gpu_launches": int(tm["launches"]),
             "mesh": mesh,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -8,7 +8,7 @@ and the synthetic workload generators.
 """
 from . import workloads  # noqa: F401
 from ._native import (BROADPHASE_AABB, BROADPHASE_KDOP13, EDGE_EDGE, PATH_CULL_REFINE, PATH_FP64,  # noqa: F401
-                      ROW_WIDTH, VERTEX_EDGE, VERTEX_FACE, VERTEX_VERTEX, CcdError, Context, Mesh,
+                      ROW_WIDTH, VERTEX_EDGE, VERTEX_FACE, VERTEX_VERTEX, CcdError, Context, Mesh, Server,
                       header_functions, load)
 
 __version__ = "0.1.0"

@@ -302,3 +302,121 @@ class Mesh:
         st = MeshStats()
         self.ctx._check(self.lib.ccd_mesh_last_stats(self.handle, ctypes.byref(st)), "ccd_mesh_last_stats")
         return {f: getattr(st, f) for f, _ in MeshStats._fields_}
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("nverts", ctypes.c_int32), ("nfaces", ctypes.c_int32), ("faces", _P), ("steps", ctypes.c_int32),
+                ("frames", _P), ("fixed", _P), ("broadphase_kind", ctypes.c_int32), ("path", ctypes.c_int32),
+                ("outer_eta", ctypes.c_double), ("eta", ctypes.c_double)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("steps", ctypes.c_int32),
+                ("vf_hits", ctypes.POINTER(ctypes.c_int64)), ("ee_hits", ctypes.POINTER(ctypes.c_int64)),
+                ("vf_offsets", ctypes.POINTER(ctypes.c_int64)), ("ee_offsets", ctypes.POINTER(ctypes.c_int64)),
+                ("vf", ctypes.POINTER(ctypes.c_int32)), ("ee", ctypes.POINTER(ctypes.c_int32)),
+                ("vf_t", ctypes.POINTER(ctypes.c_double)), ("ee_t", ctypes.POINTER(ctypes.c_double)),
+                ("step_ms", ctypes.POINTER(ctypes.c_double)), ("queue_ms", ctypes.c_double),
+                ("total_ms", ctypes.c_double), ("error", ctypes.c_char_p)]
+
+
+def _bind_server(L):
+    if getattr(L, "_server_bound", False):
+        return
+    L.ccd_server_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.POINTER(_P)]
+    L.ccd_server_destroy.argtypes = [_P]
+    L.ccd_server_submit.argtypes = [_P, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]
+    L.ccd_server_poll.argtypes = [_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int)]
+    L.ccd_server_wait.argtypes = [_P, ctypes.c_uint64, ctypes.POINTER(RequestResult)]
+    L.ccd_server_release.argtypes = [_P, ctypes.c_uint64]
+    L._server_bound = True
+
+
+def _array(ptr, n, dtype, shape=None):
+    if n == 0:
+        return np.zeros(shape if shape else (0,), dtype)
+    a = np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+    return a.reshape(shape) if shape else a
+
+
+class Server:
+    """Serving engine (ccd_server_*): requests of (mesh, frames) run on
+    `slots` workers with their own contexts, admitted within a device-memory
+    budget; each step is one ccd_mesh_detect between consecutive frames."""
+
+    def __init__(self, device: int = 0, slots: int = 4, memory_budget: int = 60 << 30):
+        self.lib = load()
+        _bind_server(self.lib)
+        h = _P()
+        rc = self.lib.ccd_server_create(device, slots, memory_budget, ctypes.byref(h))
+        if rc != CCD_OK:
+            raise CcdError(f"ccd_server_create: {self.lib.ccd_status_string(rc).decode()}")
+        self.handle = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.ccd_server_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, faces, frames, fixed=None, kind: int = BROADPHASE_KDOP13, path: int = PATH_CULL_REFINE,
+               outer_eta: float = 1e-6, eta: float = 1e-6) -> int:
+        """frames: (steps + 1, 3V) positions; returns a ticket."""
+        f = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+        fr = np.ascontiguousarray(frames, dtype=np.float64)
+        steps = fr.shape[0] - 1
+        nverts = fr.shape[1] // 3
+        fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        req = Request(nverts, f.shape[0], _ptr(f), steps, _ptr(fr), _ptr(fx), kind, path, outer_eta, eta)
+        t = ctypes.c_uint64()
+        rc = self.lib.ccd_server_submit(self.handle, ctypes.byref(req), ctypes.byref(t))
+        if rc != CCD_OK:
+            raise CcdError(f"ccd_server_submit: {self.lib.ccd_status_string(rc).decode()}")
+        self._keep[t.value] = (f, fr, fx)  # frames are read until the request completes
+        return t.value
+
+    def poll(self, ticket: int) -> bool:
+        d = ctypes.c_int(0)
+        rc = self.lib.ccd_server_poll(self.handle, ticket, ctypes.byref(d))
+        if rc != CCD_OK:
+            raise CcdError("ccd_server_poll: unknown ticket")
+        return bool(d.value)
+
+    def wait(self, ticket: int, release: bool = True) -> dict:
+        """Results: per step (vf, vf_t, ee, ee_t) arrays, step_ms, queue_ms,
+        total_ms."""
+        r = RequestResult()
+        rc = self.lib.ccd_server_wait(self.handle, ticket, ctypes.byref(r))
+        if rc != CCD_OK:
+            raise CcdError("ccd_server_wait: unknown ticket")
+        if r.status != CCD_OK:
+            msg = r.error.decode() if r.error else ""
+            self.lib.ccd_server_release(self.handle, ticket)
+            self._keep.pop(ticket, None)
+            raise CcdError(f"request failed: {self.lib.ccd_status_string(r.status).decode()}: {msg}")
+        n = r.steps
+        vfo = _array(r.vf_offsets, n + 1, np.int64)
+        eeo = _array(r.ee_offsets, n + 1, np.int64)
+        vf = _array(r.vf, 4 * int(vfo[-1]), np.int32, (int(vfo[-1]), 4))
+        ee = _array(r.ee, 4 * int(eeo[-1]), np.int32, (int(eeo[-1]), 4))
+        vft = _array(r.vf_t, int(vfo[-1]), np.float64)
+        eet = _array(r.ee_t, int(eeo[-1]), np.float64)
+        out = {"steps": [(vf[vfo[k]:vfo[k + 1]], vft[vfo[k]:vfo[k + 1]], ee[eeo[k]:eeo[k + 1]],
+                          eet[eeo[k]:eeo[k + 1]]) for k in range(n)],
+               "step_ms": _array(r.step_ms, n, np.float64), "queue_ms": r.queue_ms, "total_ms": r.total_ms}
+        if release:
+            self.lib.ccd_server_release(self.handle, ticket)
+            self._keep.pop(ticket, None)
+        return out

@@ -26,15 +26,19 @@ int cuda_fail(ccd_context *ctx, cudaError_t e, const char *what) {
 
 int ensure_stage(ccd_context *ctx, StageBuf &sb, int64_t rows, cudaStream_t s) {
   int64_t cap = std::min<int64_t>(std::max<int64_t>(rows, 1), kStageTileRows);
-  if (sb.cap >= cap) return CCD_OK;
+  // The wavefront solver's scratch (about 3 KB per row) only for batches
+  // large enough to use it.
+  const bool wave = ctx->opt_wave_steps > 0 && rows >= ctx->opt_wave_min_rows;
+  if (sb.cap >= cap && (sb.view.wd != nullptr || !wave)) return CCD_OK;
+  cap = std::max<int64_t>(cap, sb.cap);
   CCD_CUDA(cudaStreamSynchronize(s));
   cudaFree(sb.mem);
   sb = StageBuf{};
   const size_t stage_bytes = ccd::stage_scratch_bytes(cap);
-  CCD_CUDA(cudaMalloc(&sb.mem, stage_bytes + ccd::wave_scratch_bytes(cap)));
+  CCD_CUDA(cudaMalloc(&sb.mem, stage_bytes + (wave ? ccd::wave_scratch_bytes(cap) : 0)));
   sb.cap = cap;
   sb.view = ccd::stage_scratch_view(sb.mem, cap);
-  ccd::attach_wave(sb.view, (char *)sb.mem + stage_bytes);
+  if (wave) ccd::attach_wave(sb.view, (char *)sb.mem + stage_bytes);
   return CCD_OK;
 }
 

@@ -220,7 +220,7 @@ int ccd_mesh_create(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int3
   m->nedges = (int32_t)(topo.rank_edge.size() / 2);
   auto upload = [&](int32_t **dst, const int32_t *src, size_t count) -> int {
     CCD_CUDA(cudaMalloc(dst, std::max<size_t>(count, 1) * sizeof(int32_t)));
-    if (count) CCD_CUDA(cudaMemcpy(*dst, src, count * sizeof(int32_t), cudaMemcpyHostToDevice));
+    if (count) CCD_CUDA(cudaMemcpyAsync(*dst, src, count * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
     return CCD_OK;
   };
   int rc = upload(&m->faces, faces, 3 * (size_t)nfaces);
@@ -231,14 +231,15 @@ int ccd_mesh_create(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int3
   auto alloc = [&]() -> int {
     CCD_CUDA(cudaMalloc(&m->qs, 3 * (size_t)nverts * sizeof(double)));
     CCD_CUDA(cudaMalloc(&m->qe, 3 * (size_t)nverts * sizeof(double)));
-    CCD_CUDA(cudaMemset(m->qs, 0, 3 * (size_t)nverts * sizeof(double)));
-    CCD_CUDA(cudaMemset(m->qe, 0, 3 * (size_t)nverts * sizeof(double)));
+    CCD_CUDA(cudaMemsetAsync(m->qs, 0, 3 * (size_t)nverts * sizeof(double), ctx->stream));
+    CCD_CUDA(cudaMemsetAsync(m->qe, 0, 3 * (size_t)nverts * sizeof(double), ctx->stream));
     CCD_CUDA(cudaMalloc(&m->fixed, (size_t)nverts));
     CCD_CUDA(cudaMalloc(&m->d_eta, sizeof(double)));
     CCD_CUDA(cudaMalloc(&m->d_count, sizeof(uint32_t)));
     return CCD_OK;
   };
   if (!rc) rc = alloc();
+  if (!rc && cudaStreamSynchronize(ctx->stream) != cudaSuccess) rc = cuda_fail(ctx, cudaGetLastError(), "upload");
   if (rc) {
     free_mesh_buffers(m);
     delete m;
@@ -290,7 +291,8 @@ int ccd_mesh_set_fixed(ccd_mesh *m, const uint8_t *fixed) {
     // Normalise to 0/1 on the host.
     std::vector<uint8_t> f(fixed, fixed + m->nv);
     for (auto &x : f) x = x ? 1 : 0;
-    CCD_CUDA(cudaMemcpy(m->fixed, f.data(), (size_t)m->nv, cudaMemcpyHostToDevice));
+    CCD_CUDA(cudaMemcpyAsync(m->fixed, f.data(), (size_t)m->nv, cudaMemcpyHostToDevice, ctx->stream));
+    CCD_CUDA(cudaStreamSynchronize(ctx->stream));  // f is about to go away
   }
   m->has_fixed = fixed != nullptr;
   m->have_cand = m->have_col = false;
@@ -316,9 +318,12 @@ int ccd_broadphase_get(ccd_mesh *m, int32_t *vf, int32_t *ee) {
   if (!m->have_cand) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "no broad phase result on this mesh");
   CCD_CUDA(cudaSetDevice(ctx->device));
   if (vf && m->n_cand[0])
-    CCD_CUDA(cudaMemcpy(vf, m->cand[0], (size_t)m->n_cand[0] * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    CCD_CUDA(cudaMemcpyAsync(vf, m->cand[0], (size_t)m->n_cand[0] * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             ctx->stream));
   if (ee && m->n_cand[1])
-    CCD_CUDA(cudaMemcpy(ee, m->cand[1], (size_t)m->n_cand[1] * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    CCD_CUDA(cudaMemcpyAsync(ee, m->cand[1], (size_t)m->n_cand[1] * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
   return CCD_OK;
 }
 
@@ -440,9 +445,13 @@ int ccd_mesh_get_collisions(ccd_mesh *m, int32_t *vf, double *vf_t, int32_t *ee,
   for (int k = 0; k < 2; k++) {
     const int64_t n = m->n_col[k];
     if (!n) continue;
-    if (st[k]) CCD_CUDA(cudaMemcpy(st[k], m->col[k], (size_t)n * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost));
-    if (tt[k]) CCD_CUDA(cudaMemcpy(tt[k], m->col_t[k], (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (st[k])
+      CCD_CUDA(cudaMemcpyAsync(st[k], m->col[k], (size_t)n * 4 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+    if (tt[k])
+      CCD_CUDA(cudaMemcpyAsync(tt[k], m->col_t[k], (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   }
+  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
   return CCD_OK;
 }
 

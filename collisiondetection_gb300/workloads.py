@@ -282,3 +282,46 @@ def sheet_on_sphere(grid: int = 256, level: int = 6, seed: int = 0, step: int = 
     """Step `step` of cloth_frames(...): (qstart (3V,), qend (3V,), faces)."""
     faces, frames = cloth_frames(grid, level, seed, step + 1, gap, drop, wrinkle, radius)
     return frames[step].copy(), frames[step + 1].copy(), faces
+
+
+_ICO_CACHE = {}
+
+
+def _icosphere_cached(level: int):
+    if level not in _ICO_CACHE:
+        _ICO_CACHE[level] = icosphere(level, 1.0)
+    return _ICO_CACHE[level]
+
+
+def _mean_edge(v, f):
+    e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]])
+    return float(np.linalg.norm(v[e[:, 0]] - v[e[:, 1]], axis=1).mean())
+
+
+def motion_request(tris: int, seed: int, steps: int = 10):
+    """One collision query of the uneven-batch / serving workloads: an
+    icosphere (subdivision level nearest to `tris` triangles) or a pair of
+    grid sheets two edge lengths apart, moved each step by a rigid translation
+    of 0.5-2 mean edge lengths in a random direction plus N(0, 0.1 edge)
+    per-vertex jitter.  Returns (faces (F, 3) int32, frames (steps + 1, 3V))."""
+    rng = np.random.default_rng(seed)
+    if rng.random() < 0.5:
+        level = int(np.clip(np.rint(np.log(max(tris, 20) / 20.0) / np.log(4.0)), 1, 7))
+        v, f = _icosphere_cached(level)
+    else:
+        n = int(max(3, np.rint(np.sqrt(max(tris, 8) / 4.0) + 1)))
+        a, fa = grid_sheet(n, n)
+        edge = 1.0 / (n - 1)
+        b = a + np.array([0.3 * edge, 0.3 * edge, 2.0 * edge])
+        v = np.concatenate([a, b])
+        f = np.concatenate([fa, fa + a.shape[0]]).astype(np.int32)
+    edge = _mean_edge(v, f)
+    frames = np.empty((steps + 1, v.size))
+    pos = v.copy()
+    frames[0] = pos.ravel()
+    for k in range(steps):
+        d = rng.normal(size=3)
+        d *= rng.uniform(0.5, 2.0) * edge / np.linalg.norm(d)
+        pos = pos + d
+        frames[k + 1] = (pos + rng.normal(0.0, 0.1 * edge, pos.shape)).ravel()
+    return np.ascontiguousarray(f, dtype=np.int32), frames

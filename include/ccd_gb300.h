@@ -229,6 +229,60 @@ int ccd_mesh_detect(ccd_mesh *mesh, int broadphase_kind, double outer_eta, doubl
 int ccd_mesh_get_collisions(ccd_mesh *mesh, int32_t *vf, double *vf_t, int32_t *ee, double *ee_t);
 int ccd_mesh_last_stats(const ccd_mesh *mesh, ccd_mesh_stats *out);
 
+/* ------------------------------------------------------------------ serving
+ * No counterpart in the reference (its detection runs in the caller's
+ * thread).  A server runs collision queries for many callers at once on one
+ * device.  A request is a mesh and a sequence of positions, frames 0..steps;
+ * step k is one ccd_mesh_detect between frames k and k+1, which is the
+ * reference's broad phase followed by CTCDNarrowPhase.
+ *
+ * The server has `slots` worker threads, each with its own context and
+ * streams.  Requests wait in submission order and are admitted while the sum
+ * of their estimated device footprints stays within memory_budget bytes. A
+ * request larger than the whole budget runs alone.  An admitted request keeps
+ * its mesh, positions and detection buffers resident for all of its steps.
+ * Requests on different slots overlap on the device.  Results do not depend
+ * on what else is running. */
+typedef struct ccd_server ccd_server;
+
+typedef struct {
+  int32_t nverts, nfaces;
+  const int32_t *faces;    /* [nfaces][3]; copied at submit */
+  int32_t steps;           /* >= 1 */
+  const double *frames;    /* [steps + 1][nverts][3] host memory, read until the request completes */
+  const uint8_t *fixed;    /* nverts flags or NULL; copied at submit */
+  int32_t broadphase_kind; /* ccd_broadphase_kind */
+  int32_t path;            /* ccd_path of the primitive tests */
+  double outer_eta, eta;   /* broad-phase padding, narrow-phase eta */
+} ccd_request;
+
+/* Results of a finished request; the arrays stay valid until
+ * ccd_server_release. Step k's colliding stencils are rows
+ * vf_offsets[k] .. vf_offsets[k + 1] of vf (and likewise ee), in set order,
+ * with the t of their first hitting sub-test. */
+typedef struct {
+  int32_t status; /* ccd_status of the request */
+  int32_t steps;  /* steps run */
+  const int64_t *vf_hits, *ee_hits;       /* [steps] */
+  const int64_t *vf_offsets, *ee_offsets; /* [steps + 1] */
+  const int32_t *vf, *ee;                 /* [total][4] */
+  const double *vf_t, *ee_t;              /* [total] */
+  const double *step_ms;                  /* [steps] wall time of each step */
+  double queue_ms;                        /* submit -> admitted */
+  double total_ms;                        /* submit -> finished */
+  const char *error;                      /* message when status != CCD_OK */
+} ccd_request_result;
+
+int ccd_server_create(int device, int slots, int64_t memory_budget, ccd_server **out);
+/* Finishes the queued and running requests, then frees the server. */
+int ccd_server_destroy(ccd_server *server);
+int ccd_server_submit(ccd_server *server, const ccd_request *request, uint64_t *ticket);
+/* *done = 1 once the request has finished. */
+int ccd_server_poll(ccd_server *server, uint64_t ticket, int *done);
+/* Blocks until the request has finished and describes its results. */
+int ccd_server_wait(ccd_server *server, uint64_t ticket, ccd_request_result *out);
+int ccd_server_release(ccd_server *server, uint64_t ticket);
+
 #ifdef __cplusplus
 }
 #endif
