@@ -45,6 +45,21 @@ int grow(ccd_context *ctx, T **p, int64_t *cap, int64_t need) {
   return CCD_OK;
 }
 
+// Per-kind narrow-phase buffers and stream.
+struct Lane {
+  NarrowScratch ns;
+  cudaStream_t stream = nullptr;  // not owned
+  uint8_t *hit = nullptr;
+  int64_t hit_cap = 0;
+  double *t = nullptr;
+  int64_t t_cap = 0;
+  uint32_t *flags = nullptr, *pos = nullptr;
+  int64_t flags_cap = 0, pos_cap = 0;
+  char *scan_temp = nullptr;
+  int64_t scan_temp_cap = 0;
+  uint32_t *d_count = nullptr;
+};
+
 }  // namespace
 
 struct ccd_mesh {
@@ -62,16 +77,17 @@ struct ccd_mesh {
   int64_t cand_cap[2] = {0, 0};
   int64_t n_cand[2] = {0, 0};
   bool have_cand = false;
-  NarrowScratch ns;
-  // narrow-phase inputs/outputs of the host entry point and of detect
+  // One narrow-phase lane per stencil kind: vertex-face on the context's
+  // stream, edge-edge on the mesh's second stream, so that the two chains
+  // (and their latency-bound root-solver tails) overlap.
+  Lane lane[2];
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  // narrow-phase inputs of the host entry point
   int32_t *in_st = nullptr;
   int64_t in_st_cap = 0;
   double *in_eta = nullptr;
   int64_t in_eta_cap = 0;
-  uint8_t *hit = nullptr;
-  int64_t hit_cap = 0;
-  double *t = nullptr;
-  int64_t t_cap = 0;
   int8_t *which = nullptr;
   int64_t which_cap = 0;
   double *d_eta = nullptr;
@@ -82,11 +98,6 @@ struct ccd_mesh {
   int64_t col_t_cap[2] = {0, 0};
   int64_t n_col[2] = {0, 0};
   bool have_col = false;
-  uint32_t *flags = nullptr, *pos = nullptr;
-  int64_t flags_cap = 0, pos_cap = 0;
-  char *scan_temp = nullptr;
-  int64_t scan_temp_cap = 0;
-  uint32_t *d_count = nullptr;
   ccd_mesh_stats stats{};
 };
 
@@ -94,11 +105,11 @@ namespace {
 
 int mesh_fail(ccd_mesh *m, int code, const std::string &msg) { return fail(m ? m->ctx : nullptr, code, msg); }
 
-int ensure_narrow(ccd_mesh *m, int64_t chunk) {
+int ensure_narrow(ccd_mesh *m, Lane &L, int64_t chunk) {
   ccd_context *ctx = m->ctx;
-  NarrowScratch &n = m->ns;
+  NarrowScratch &n = L.ns;
   if (n.cap >= chunk) return CCD_OK;
-  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+  CCD_CUDA(cudaStreamSynchronize(L.stream));
   void *ptrs[] = {n.prim, n.ve, n.vv, n.eta_prim, n.eta_ve, n.eta_vv, n.h_prim, n.h_ve, n.h_vv,
                   n.t_prim, n.t_ve, n.t_vv, n.surv, n.counters, n.stage.mem};
   for (void *p : ptrs) cudaFree(p);
@@ -122,18 +133,19 @@ int ensure_narrow(ccd_mesh *m, int64_t chunk) {
   return CCD_OK;
 }
 
-// The narrow-phase chain over n device stencils of one kind; results into
-// device arrays hit[n], t[n] (optional), which[n] (optional).
-int narrow_device(ccd_mesh *m, int kind, int path, int64_t n, const int32_t *st, const double *eta, bool eta_per_row,
-                  uint8_t *hit, double *t, int8_t *which) {
+// The narrow-phase chain over n device stencils of one kind, on lane L's
+// stream; results into device arrays hit[n], t[n] (optional), which[n]
+// (optional).
+int narrow_device(ccd_mesh *m, Lane &L, int kind, int path, int64_t n, const int32_t *st, const double *eta,
+                  bool eta_per_row, uint8_t *hit, double *t, int8_t *which) {
   ccd_context *ctx = m->ctx;
   if (n == 0) return CCD_OK;
   const int64_t chunk = std::min<int64_t>(n, kNarrowChunk);
-  int rc = ensure_narrow(m, chunk);
+  int rc = ensure_narrow(m, L, chunk);
   if (rc) return rc;
-  NarrowScratch &ns = m->ns;
+  NarrowScratch &ns = L.ns;
   const int nsub = kind == CCD_VERTEX_FACE ? 3 : 4;
-  cudaStream_t s = ctx->stream;
+  cudaStream_t s = L.stream;
   for (int64_t off = 0; off < n; off += chunk) {
     const int64_t c = std::min<int64_t>(chunk, n - off);
     CCD_CUDA(ccd::gather_stencil_rows(kind, st + 4 * off, c, m->qs, m->qe, eta_per_row ? eta + off : eta,
@@ -187,13 +199,19 @@ int check_eta(ccd_mesh *m, int64_t n, const double *eta, int64_t eta_count) {
 
 void free_mesh_buffers(ccd_mesh *m) {
   void *ptrs[] = {m->faces, m->face_rank, m->rank_triple, m->face_edges, m->rank_edge, m->qs, m->qe, m->fixed,
-                  m->cand[0], m->cand[1], m->in_st, m->in_eta, m->hit, m->t, m->which, m->d_eta,
-                  m->col[0], m->col[1], m->col_t[0], m->col_t[1], m->flags, m->pos, m->scan_temp, m->d_count,
-                  m->ns.prim, m->ns.ve, m->ns.vv, m->ns.eta_prim, m->ns.eta_ve, m->ns.eta_vv, m->ns.h_prim,
-                  m->ns.h_ve, m->ns.h_vv, m->ns.t_prim, m->ns.t_ve, m->ns.t_vv, m->ns.surv, m->ns.counters,
-                  m->ns.stage.mem};
+                  m->cand[0], m->cand[1], m->in_st, m->in_eta, m->which, m->d_eta,
+                  m->col[0], m->col[1], m->col_t[0], m->col_t[1]};
   for (void *p : ptrs) cudaFree(p);
+  for (Lane &L : m->lane) {
+    NarrowScratch &n = L.ns;
+    void *lp[] = {L.hit, L.t, L.flags, L.pos, L.scan_temp, L.d_count, n.prim, n.ve, n.vv, n.eta_prim, n.eta_ve,
+                  n.eta_vv, n.h_prim, n.h_ve, n.h_vv, n.t_prim, n.t_ve, n.t_vv, n.surv, n.counters, n.stage.mem};
+    for (void *p : lp) cudaFree(p);
+  }
   ccd::broadphase_free(m->bp);
+  if (m->fork) cudaEventDestroy(m->fork);
+  if (m->join) cudaEventDestroy(m->join);
+  if (m->side) cudaStreamDestroy(m->side);
 }
 
 }  // namespace
@@ -235,7 +253,10 @@ int ccd_mesh_create(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int3
     CCD_CUDA(cudaMemsetAsync(m->qe, 0, 3 * (size_t)nverts * sizeof(double), ctx->stream));
     CCD_CUDA(cudaMalloc(&m->fixed, (size_t)nverts));
     CCD_CUDA(cudaMalloc(&m->d_eta, sizeof(double)));
-    CCD_CUDA(cudaMalloc(&m->d_count, sizeof(uint32_t)));
+    CCD_CUDA(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+    CCD_CUDA(cudaEventCreateWithFlags(&m->fork, cudaEventDisableTiming));
+    CCD_CUDA(cudaEventCreateWithFlags(&m->join, cudaEventDisableTiming));
+    for (Lane &L : m->lane) CCD_CUDA(cudaMalloc(&L.d_count, sizeof(uint32_t)));
     return CCD_OK;
   };
   if (!rc) rc = alloc();
@@ -366,21 +387,23 @@ int ccd_narrowphase(ccd_mesh *m, int path, int64_t n_vf, const int32_t *vf, cons
     int8_t *which = k ? ee_which : vf_which;
     rc = grow(ctx, &m->in_st, &m->in_st_cap, 4 * n);
     if (!rc) rc = grow(ctx, &m->in_eta, &m->in_eta_cap, eta_count);
-    if (!rc) rc = grow(ctx, &m->hit, &m->hit_cap, n);
-    if (!rc) rc = grow(ctx, &m->t, &m->t_cap, n);
+    Lane &L = m->lane[0];
+    L.stream = ctx->stream;
+    if (!rc) rc = grow(ctx, &L.hit, &L.hit_cap, n);
+    if (!rc) rc = grow(ctx, &L.t, &L.t_cap, n);
     if (!rc) rc = grow(ctx, &m->which, &m->which_cap, n);
     if (rc) return rc;
     CCD_CUDA(cudaMemcpyAsync(m->in_st, st, (size_t)n * 4 * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
     CCD_CUDA(cudaMemcpyAsync(m->in_eta, eta, (size_t)eta_count * sizeof(double), cudaMemcpyHostToDevice,
                              ctx->stream));
-    rc = narrow_device(m, k ? CCD_EDGE_EDGE : CCD_VERTEX_FACE, path, n, m->in_st, m->in_eta, eta_count == n && n != 1,
-                       m->hit, m->t, m->which);
+    rc = narrow_device(m, L, k ? CCD_EDGE_EDGE : CCD_VERTEX_FACE, path, n, m->in_st, m->in_eta,
+                       eta_count == n && n != 1, L.hit, L.t, m->which);
     if (rc) return rc;
-    CCD_CUDA(cudaMemcpyAsync(hit, m->hit, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+    CCD_CUDA(cudaMemcpyAsync(hit, L.hit, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
     if (which) CCD_CUDA(cudaMemcpyAsync(which, m->which, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
     if (t) {
       tbuf.resize((size_t)n);
-      CCD_CUDA(cudaMemcpyAsync(tbuf.data(), m->t, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      CCD_CUDA(cudaMemcpyAsync(tbuf.data(), L.t, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     }
     CCD_CUDA(cudaStreamSynchronize(ctx->stream));
     int64_t hits = 0;
@@ -405,28 +428,41 @@ int ccd_mesh_detect(ccd_mesh *m, int broadphase_kind, double outer_eta, double e
   int rc = run_broadphase(m, broadphase_kind, outer_eta);
   if (rc) return rc;
   CCD_CUDA(cudaMemcpyAsync(m->d_eta, &eta, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  const int64_t nmax = std::max(m->n_cand[0], m->n_cand[1]);
-  rc = grow(ctx, &m->hit, &m->hit_cap, nmax);
-  if (!rc) rc = grow(ctx, &m->t, &m->t_cap, nmax);
-  if (!rc) rc = grow(ctx, &m->flags, &m->flags_cap, nmax);
-  if (!rc) rc = grow(ctx, &m->pos, &m->pos_cap, nmax);
-  if (!rc) rc = grow(ctx, &m->scan_temp, &m->scan_temp_cap, (int64_t)ccd::scan_temp_bytes(nmax));
-  if (rc) return rc;
+  m->lane[0].stream = ctx->stream;
+  m->lane[1].stream = m->side;
   for (int k = 0; k < 2; k++) {
+    Lane &L = m->lane[k];
     const int64_t n = m->n_cand[k];
-    rc = grow(ctx, &m->col[k], &m->col_cap[k], 4 * n);
+    rc = grow(ctx, &L.hit, &L.hit_cap, n);
+    if (!rc) rc = grow(ctx, &L.t, &L.t_cap, n);
+    if (!rc) rc = grow(ctx, &L.flags, &L.flags_cap, n);
+    if (!rc) rc = grow(ctx, &L.pos, &L.pos_cap, n);
+    if (!rc) rc = grow(ctx, &L.scan_temp, &L.scan_temp_cap, (int64_t)ccd::scan_temp_bytes(n));
+    if (!rc) rc = grow(ctx, &m->col[k], &m->col_cap[k], 4 * n);
     if (!rc) rc = grow(ctx, &m->col_t[k], &m->col_t_cap[k], n);
     if (rc) return rc;
-    rc = narrow_device(m, k ? CCD_EDGE_EDGE : CCD_VERTEX_FACE, path, n, m->cand[k], m->d_eta, false, m->hit, m->t,
+  }
+  // Fork: the edge-edge chain runs on the side stream once the broad phase
+  // and eta are in place; join before the counts are read.
+  CCD_CUDA(cudaEventRecord(m->fork, ctx->stream));
+  CCD_CUDA(cudaStreamWaitEvent(m->side, m->fork, 0));
+  for (int k = 0; k < 2; k++) {
+    Lane &L = m->lane[k];
+    const int64_t n = m->n_cand[k];
+    rc = narrow_device(m, L, k ? CCD_EDGE_EDGE : CCD_VERTEX_FACE, path, n, m->cand[k], m->d_eta, false, L.hit, L.t,
                        nullptr);
     if (rc) return rc;
-    CCD_CUDA(ccd::compact_hits(m->cand[k], m->hit, m->t, n, m->flags, m->pos, m->d_count, m->scan_temp,
-                               (size_t)m->scan_temp_cap, m->col[k], m->col_t[k], ctx->stream));
-    uint32_t count = 0;
-    CCD_CUDA(cudaMemcpyAsync(&count, m->d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-    CCD_CUDA(cudaStreamSynchronize(ctx->stream));
-    m->n_col[k] = count;
+    CCD_CUDA(ccd::compact_hits(m->cand[k], L.hit, L.t, n, L.flags, L.pos, L.d_count, L.scan_temp,
+                               (size_t)L.scan_temp_cap, m->col[k], m->col_t[k], L.stream));
   }
+  CCD_CUDA(cudaEventRecord(m->join, m->side));
+  CCD_CUDA(cudaStreamWaitEvent(ctx->stream, m->join, 0));
+  uint32_t counts[2] = {0, 0};
+  for (int k = 0; k < 2; k++)
+    CCD_CUDA(cudaMemcpyAsync(&counts[k], m->lane[k].d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+  m->n_col[0] = counts[0];
+  m->n_col[1] = counts[1];
   m->stats.vf_hits = m->n_col[0];
   m->stats.ee_hits = m->n_col[1];
   m->have_col = true;
