@@ -47,7 +47,20 @@ CCD_HD fb scale(float s, fb a) { return fb{s * a.v, fabsf(s) * a.m}; }  // exact
 struct v3f {
   fb x, y, z;
 };
-CCD_HD v3f ld3f(const double *p) { return v3f{fb_in(p[0]), fb_in(p[1]), fb_in(p[2])}; }
+
+// The reference's difference vectors are formed in FP64 (positions minus
+// positions, velocities minus velocities) before any product.  The stage
+// forms the same FP64 differences, operation for operation, and rounds them
+// to FP32 only then: its error bounds are relative to the differences
+// themselves, not to the absolute coordinates (with coordinates near 1 and
+// edges near 0.01, bounds built from rounded coordinates would exceed the
+// quantities they bound).
+struct d3 {
+  double x, y, z;
+};
+CCD_HD d3 ld3d(const double *p) { return d3{p[0], p[1], p[2]}; }
+CCD_HD d3 operator-(d3 a, d3 b) { return d3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+CCD_HD v3f f3(d3 a) { return v3f{fb_in(a.x), fb_in(a.y), fb_in(a.z)}; }
 CCD_HD v3f operator-(v3f a, v3f b) { return v3f{a.x - b.x, a.y - b.y, a.z - b.z}; }
 CCD_HD v3f operator+(v3f a, v3f b) { return v3f{a.x + b.x, a.y + b.y, a.z + b.z}; }
 CCD_HD fb dotf(v3f a, v3f b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
@@ -180,41 +193,48 @@ CCD_HD void bary_terms(v3f x10, v3f x20, v3f x30, v3f v10, v3f v20, v3f v30, fb 
 // True when vertexFaceCTCD(x, eta) is provably false.  x: as vf_ctcd.
 CCD_HD bool vf_rejects(const double *x, double eta) {
   if (!(fabs(eta) < 1e300)) return false;
-  v3f q0s = ld3f(x), q1s = ld3f(x + 3), q2s = ld3f(x + 6), q3s = ld3f(x + 9);
-  v3f v0 = ld3f(x + 12) - q0s, v1 = ld3f(x + 15) - q1s, v2 = ld3f(x + 18) - q2s, v3 = ld3f(x + 21) - q3s;
+  const d3 q0s = ld3d(x), q1s = ld3d(x + 3), q2s = ld3d(x + 6), q3s = ld3d(x + 9);
+  const d3 v0 = ld3d(x + 12) - q0s, v1 = ld3d(x + 15) - q1s, v2 = ld3d(x + 18) - q2s, v3 = ld3d(x + 21) - q3s;
   fb op[4];
-  plane_terms(q0s - q1s, crossf(q3s - q1s, q2s - q1s), q3s - q1s, v0 - v1, crossf(v3 - v1, v2 - v1), v3 - v1, op);
+  // src/CTCD.cpp:428-435, 443-449, 455-461
+  plane_terms(f3(q0s - q1s), crossf(f3(q3s - q1s), f3(q2s - q1s)), f3(q3s - q1s), f3(v0 - v1),
+              crossf(f3(v3 - v1), f3(v2 - v1)), f3(v3 - v1), op);
   if (surely_negative<3>(op)) return true;
-  plane_terms(q0s - q2s, crossf(q1s - q2s, q3s - q2s), q1s - q2s, v0 - v2, crossf(v1 - v2, v3 - v2), v1 - v2, op);
+  plane_terms(f3(q0s - q2s), crossf(f3(q1s - q2s), f3(q3s - q2s)), f3(q1s - q2s), f3(v0 - v2),
+              crossf(f3(v1 - v2), f3(v3 - v2)), f3(v1 - v2), op);
   if (surely_negative<3>(op)) return true;
-  plane_terms(q0s - q3s, crossf(q2s - q3s, q1s - q3s), q2s - q3s, v0 - v3, crossf(v2 - v3, v1 - v3), v2 - v3, op);
+  plane_terms(f3(q0s - q3s), crossf(f3(q2s - q3s), f3(q1s - q3s)), f3(q2s - q3s), f3(v0 - v3),
+              crossf(f3(v2 - v3), f3(v1 - v3)), f3(v2 - v3), op);
   if (surely_negative<3>(op)) return true;
   fb D[4];
   v3f E, F, G;
-  dist_terms(q0s - q1s, q2s - q1s, q3s - q1s, v0 - v1, v2 - v1, v3 - v1, D, E, F, G);
+  // src/CTCD.cpp:466-472
+  dist_terms(f3(q0s - q1s), f3(q2s - q1s), f3(q3s - q1s), f3(v0 - v1), f3(v2 - v1), f3(v3 - v1), D, E, F, G);
   return surely_apart(D, E, F, G, eta * eta);
 }
 
 // True when edgeEdgeCTCD(x, eta) is provably false.  x: as ee_ctcd.
 CCD_HD bool ee_rejects(const double *x, double eta) {
   if (!(fabs(eta) < 1e300)) return false;
-  v3f q0s = ld3f(x), p0s = ld3f(x + 3), q1s = ld3f(x + 6), p1s = ld3f(x + 9);
-  v3f vq0 = ld3f(x + 12) - q0s, vp0 = ld3f(x + 15) - p0s, vq1 = ld3f(x + 18) - q1s, vp1 = ld3f(x + 21) - p1s;
+  const d3 q0s = ld3d(x), p0s = ld3d(x + 3), q1s = ld3d(x + 6), p1s = ld3d(x + 9);
+  const d3 vq0 = ld3d(x + 12) - q0s, vp0 = ld3d(x + 15) - p0s, vq1 = ld3d(x + 18) - q1s, vp1 = ld3d(x + 21) - p1s;
   fb D[4];
   v3f E, F, G;
-  dist_terms(p0s - p1s, p0s - q0s, p1s - q1s, vp0 - vp1, vp0 - vq0, vp1 - vq1, D, E, F, G);
+  // src/CTCD.cpp:274-286
+  dist_terms(f3(p0s - p1s), f3(p0s - q0s), f3(p1s - q1s), f3(vp0 - vp1), f3(vp0 - vq0), f3(vp1 - vq1), D, E, F, G);
   if (surely_apart(D, E, F, G, eta * eta)) return true;
   fb op[5];
-  v3f x10 = p1s - q1s, v10 = vp1 - vq1;
-  bary_terms(x10, p0s - q0s, q0s - q1s, v10, vp0 - vq0, vq0 - vq1, op);
+  // src/CTCD.cpp:313-346
+  v3f x10 = f3(p1s - q1s), v10 = f3(vp1 - vq1);
+  bary_terms(x10, f3(p0s - q0s), f3(q0s - q1s), v10, f3(vp0 - vq0), f3(vq0 - vq1), op);
   if (surely_negative<4>(op)) return true;
-  bary_terms(x10, q0s - p0s, p0s - q1s, v10, vq0 - vp0, vp0 - vq1, op);
+  bary_terms(x10, f3(q0s - p0s), f3(p0s - q1s), v10, f3(vq0 - vp0), f3(vp0 - vq1), op);
   if (surely_negative<4>(op)) return true;
-  x10 = p0s - q0s;
-  v10 = vp0 - vq0;
-  bary_terms(x10, p1s - q1s, q1s - q0s, v10, vp1 - vq1, vq1 - vq0, op);
+  x10 = f3(p0s - q0s);
+  v10 = f3(vp0 - vq0);
+  bary_terms(x10, f3(p1s - q1s), f3(q1s - q0s), v10, f3(vp1 - vq1), f3(vq1 - vq0), op);
   if (surely_negative<4>(op)) return true;
-  bary_terms(x10, q1s - p1s, p1s - q0s, v10, vq1 - vp1, vp1 - vq0, op);
+  bary_terms(x10, f3(q1s - p1s), f3(p1s - q0s), v10, f3(vq1 - vp1), f3(vp1 - vq0), op);
   return surely_negative<4>(op);
 }
 
@@ -264,10 +284,11 @@ CCD_HD float cross_lower_sq(v3f X0, v3f X1, v3f X2, float a, float h) {
 // (its "<= 0" list is then empty).
 CCD_HD bool ve_rejects(const double *x, double eta) {
   if (!(fabs(eta) < 1e300)) return false;
-  v3f q0s = ld3f(x), q1s = ld3f(x + 3), q2s = ld3f(x + 6);
-  v3f v0 = ld3f(x + 9) - q0s, v1 = ld3f(x + 12) - q1s, v2 = ld3f(x + 15) - q2s;
-  v3f ab = q2s - q1s, ac = q0s - q1s, cb = q2s - q0s;
-  v3f vab = v2 - v1, vac = v0 - v1, vcb = v2 - v0;
+  const d3 q0s = ld3d(x), q1s = ld3d(x + 3), q2s = ld3d(x + 6);
+  const d3 v0 = ld3d(x + 9) - q0s, v1 = ld3d(x + 12) - q1s, v2 = ld3d(x + 15) - q2s;
+  // src/CTCD.cpp:521-534
+  const v3f ab = f3(q2s - q1s), ac = f3(q0s - q1s), cb = f3(q2s - q0s);
+  const v3f vab = f3(v2 - v1), vac = f3(v0 - v1), vcb = f3(v2 - v0);
   fb op[3];
   op[0] = dotf(vab, vac);  // e1: src/CTCD.cpp:536-543
   op[1] = dotf(ac, vab) + dotf(ab, vac);
