@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-sample", type=int, default=2_000_000, help="rows per kind per reference step")
     ap.add_argument("--mesh", type=int, default=1, help="also time the mesh configurations (1) or not (0)")
+    ap.add_argument("--uneven-instances", type=int, default=8,
+                    help="instances of the uneven-batch sample (0: skip; the configuration has 512)")
     ap.add_argument("--serve", type=int, default=1, help="also run the serving loop (1) or not (0)")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0])
@@ -307,6 +309,47 @@ def serving_section(args):
     return out
 
 
+def uneven_section(args):
+    """Uneven batch: independent mesh instances (icospheres and grid-sheet
+    pairs, triangle counts log-uniform in [200, 2e5], rigid + jitter motion)
+    detected in one call on a mesh of instances, against the same instances
+    one call each.  Unit: candidate stencil tests per second."""
+    import collisiondetection_gb300 as C
+    from collisiondetection_gb300 import workloads as W
+
+    n = args.uneven_instances
+    faces, frames, vo, fo = W.uneven_batch(n, seed=0)
+    ctx = C.Context(0)
+    out = {"instances": n, "of_config_instances": 512, "faces": int(faces.shape[0]),
+           "vertices": int(frames.shape[1] // 3)}
+    with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3, instances=(vo, fo)) as m:
+        m.set_positions(frames[0], frames[1])
+        m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6, fetch=False)  # warm-up
+        t0 = time.perf_counter()
+        m.set_positions(frames[0], frames[1])
+        m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6)
+        dt = time.perf_counter() - t0
+        st = m.stats()
+    tests = st["n_vf"] + st["n_ee"]
+    out["one_call"] = {"ms": 1e3 * dt, "stencil_tests": tests, "collisions": st["vf_hits"] + st["ee_hits"],
+                       "value": tests / dt, "unit": "stencil tests/s"}
+    meshes = [C.Mesh(ctx, faces[fo[i]:fo[i + 1]] - vo[i], nverts=int(vo[i + 1] - vo[i])) for i in range(n)]
+    t0 = time.perf_counter()
+    hits = 0
+    for i, mi in enumerate(meshes):
+        a, b = 3 * vo[i], 3 * vo[i + 1]
+        mi.set_positions(frames[0][a:b], frames[1][a:b])
+        vf, vft, ee, eet = mi.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6)
+        hits += vf.shape[0] + ee.shape[0]
+    dt1 = time.perf_counter() - t0
+    for mi in meshes:
+        mi.close()
+    out["per_instance_calls"] = {"ms": 1e3 * dt1, "collisions": hits, "value": tests / dt1,
+                                 "unit": "stencil tests/s"}
+    ctx.close()
+    return out
+
+
 def run_reference(args, rank, world, pg):
     if rank != 0:
         return
@@ -486,6 +529,7 @@ def run_ours(args, rank, world, local, pg):
     cpu = cpu_baseline(vf, ee) if rank == 0 and full else None
     mesh = mesh_section(ctx, stream, rank, args) if args.mesh and full else None
     serving = serving_section(args) if args.serve and full and world == 1 else None
+    uneven = uneven_section(args) if args.uneven_instances and full and world == 1 else None
 
     if rank == 0:
         line = {
@@ -507,6 +551,7 @@ def run_ours(args, rank, world, local, pg):
             "gpu_launches": int(tm["launches"]),
             "mesh": mesh,
             "serving": serving,
+            "uneven_batch": uneven,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

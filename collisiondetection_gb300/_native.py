@@ -81,6 +81,7 @@ def load(path: str = LIB):
     L.ccd_prim_batch_device.argtypes = [_P, ctypes.c_int, ctypes.c_int, _I64, _P, _P, _I64, _P, _P, _P]
     L.ccd_mesh_create.argtypes = [_P, ctypes.c_int32, ctypes.c_int32, _P, ctypes.POINTER(_P)]
     L.ccd_mesh_destroy.argtypes = [_P]
+    L.ccd_mesh_create_instances.argtypes = [_P, ctypes.c_int32, _P, _P, _P, ctypes.POINTER(_P)]
     L.ccd_mesh_set_positions.argtypes = [_P, _P, _P]
     L.ccd_mesh_set_positions_device.argtypes = [_P, _P, _P]
     L.ccd_mesh_set_fixed.argtypes = [_P, _P]
@@ -200,7 +201,10 @@ class Mesh:
     (src/RetrospectiveDetection.h:13) and narrowphase() mirrors
     CTCDNarrowPhase::findCollisions (src/CTCDNarrowPhase.cpp:9-24)."""
 
-    def __init__(self, ctx: Context, faces, qstart=None, qend=None, fixed=None, nverts: int | None = None):
+    def __init__(self, ctx: Context, faces, qstart=None, qend=None, fixed=None, nverts: int | None = None,
+                 instances=None):
+        """instances: optional (vertex_offsets, face_offsets) of independent
+        instances making up the mesh (ccd_mesh_create_instances)."""
         self.ctx = ctx
         self.lib = ctx.lib
         f = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
@@ -210,8 +214,16 @@ class Mesh:
             nverts = np.asarray(qstart).size // 3
         self.nverts, self.nfaces = int(nverts), int(f.shape[0])
         h = _P()
-        ctx._check(self.lib.ccd_mesh_create(ctx.handle, self.nverts, self.nfaces, _ptr(f), ctypes.byref(h)),
-                   "ccd_mesh_create")
+        if instances is None:
+            ctx._check(self.lib.ccd_mesh_create(ctx.handle, self.nverts, self.nfaces, _ptr(f), ctypes.byref(h)),
+                       "ccd_mesh_create")
+        else:
+            vo = np.ascontiguousarray(instances[0], dtype=np.int32)
+            fo = np.ascontiguousarray(instances[1], dtype=np.int32)
+            if vo.size != fo.size or vo[-1] != self.nverts or fo[-1] != self.nfaces:
+                raise ValueError("instance offsets must end at nverts and nfaces")
+            ctx._check(self.lib.ccd_mesh_create_instances(ctx.handle, vo.size - 1, _ptr(vo), _ptr(fo), _ptr(f),
+                                                          ctypes.byref(h)), "ccd_mesh_create_instances")
         self.handle = h
         if qstart is not None:
             self.set_positions(qstart, qend)

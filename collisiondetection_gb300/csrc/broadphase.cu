@@ -21,6 +21,8 @@ constexpr uint64_t kNoKey = ~0ull;
 // sorts after every emitted key when the sort covers one more bit.
 struct KeyBits {
   int fbits, rbits, ebits;
+  int mbits;          // Morton code bits kept (30, fewer when instances and faces need the room)
+  int ibits, ishift;  // instance id above the Morton code: key >> ishift
   uint64_t fmask, rmask, emask;
 };
 
@@ -35,6 +37,11 @@ inline KeyBits key_bits(const MeshTopology &t) {
   k.fbits = bits_for(t.nf - 1);
   k.rbits = bits_for(std::max(t.nranks - 1, 1));
   k.ebits = bits_for(std::max(t.nedges - 1, 1));
+  k.ibits = t.ninst > 1 ? bits_for(t.ninst - 1) : 0;
+  // A shorter Morton code only makes the tree less tight, never the candidate
+  // set different (that depends on the leaf slabs alone).
+  k.mbits = std::min(30, 63 - k.fbits - k.ibits);
+  k.ishift = k.mbits + k.fbits;
   k.fmask = ((uint64_t)1 << k.fbits) - 1;
   k.rmask = ((uint64_t)1 << k.rbits) - 1;
   k.emask = ((uint64_t)1 << k.ebits) - 1;
@@ -126,7 +133,7 @@ __device__ __forceinline__ uint32_t spread10(uint32_t x) {
 }
 
 __global__ void __launch_bounds__(kThreads) morton_keys(int nf, const float *flo, const float *fhi, const float *bounds,
-                                                        KeyBits kb, uint64_t *keys) {
+                                                        const int32_t *face_inst, KeyBits kb, uint64_t *keys) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   uint32_t m = 0;
@@ -139,7 +146,8 @@ __global__ void __launch_bounds__(kThreads) morton_keys(int nf, const float *flo
     uint32_t q = (uint32_t)(u * 1023.0f);
     m |= spread10(q) << (2 - k);
   }
-  keys[f] = ((uint64_t)m << kb.fbits) | (uint32_t)f;
+  const uint64_t inst = face_inst ? (uint64_t)(uint32_t)face_inst[f] : 0;
+  keys[f] = (inst << kb.ishift) | ((uint64_t)(m >> (30 - kb.mbits)) << kb.fbits) | (uint32_t)f;
 }
 
 // Leaf FP32 slabs in Morton order.
@@ -229,6 +237,7 @@ __global__ void __launch_bounds__(kThreads) refit(int n, const int32_t *child, c
 // ------------------------------------------------------------------ traversal
 template <int K>
 __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n, const uint64_t *keys, uint64_t fmask,
+                                                       int ishift, bool multi,
                                                        const int32_t *child, const int32_t *range, const float *llo,
                                                        const float *lhi, const float *nlo, const float *nhi,
                                                        const double *lo64, const double *hi64, uint32_t *pairs,
@@ -243,6 +252,9 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
   }
   const int fa = (int)(keys[s] & fmask);
   const int a0 = topo.faces[3 * fa], a1 = topo.faces[3 * fa + 1], a2 = topo.faces[3 * fa + 2];
+  // Keys are ordered by instance first: a subtree whose first leaf belongs to
+  // a later instance holds no partner of this face.
+  const uint64_t my_inst = keys[s] >> ishift;
   int stack[kStack];
   int sp = 0;
   stack[sp++] = 0;
@@ -258,6 +270,7 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
       if (ch < 0) {
         const int j = ~ch;
         if (j <= s) continue;
+        if (multi && (keys[j] >> ishift) != my_inst) continue;
         bool sep = false;
 #pragma unroll
         for (int k = 0; k < K; k++) sep |= (qhi[k] < llo[(int64_t)k * n + j]) || (lhi[(int64_t)k * n + j] < qlo[k]);
@@ -280,6 +293,7 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
         }
       } else {
         if (range[2 * ch + 1] <= s) continue;
+        if (multi && (keys[range[2 * ch]] >> ishift) > my_inst) continue;
         bool sep = false;
 #pragma unroll
         for (int k = 0; k < K; k++)
@@ -482,10 +496,11 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
     leaf_slabs<3><<<grid_of(nf), kThreads, 0, s>>>(topo, p, ax, b.lo64, b.hi64, flo, fhi, b.bounds);
   BP_CUDA(cudaGetLastError());
   const KeyBits kb = key_bits(topo);
-  morton_keys<<<grid_of(nf), kThreads, 0, s>>>(nf, flo, fhi, b.bounds, kb, b.keys);
+  morton_keys<<<grid_of(nf), kThreads, 0, s>>>(nf, flo, fhi, b.bounds, topo.ninst > 1 ? topo.face_inst : nullptr, kb,
+                                                b.keys);
   BP_CUDA(cudaGetLastError());
-  BP_CUDA(radix_sort_u64(b.keys, (uint64_t *)b.vals, nullptr, nullptr, nf, 0, 30 + kb.fbits, b.temp, b.temp_bytes,
-                         s));
+  BP_CUDA(radix_sort_u64(b.keys, (uint64_t *)b.vals, nullptr, nullptr, nf, 0, kb.ishift + kb.ibits, b.temp,
+                         b.temp_bytes, s));
   if (kdop)
     gather_leaves<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, flo, fhi, b.leaf_lo, b.leaf_hi);
   else
@@ -504,11 +519,13 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   for (;;) {
     BP_CUDA(cudaMemsetAsync(b.counters, 0, 3 * sizeof(unsigned long long), s));  // keeps the error word
     if (kdop)
-      find_pairs<13><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, kb.fmask, b.node_child, b.node_range, b.leaf_lo,
+      find_pairs<13><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, kb.fmask, kb.ishift, topo.ninst > 1,
+                                                      b.node_child, b.node_range, b.leaf_lo,
                                                       b.leaf_hi, b.node_lo, b.node_hi, b.lo64, b.hi64, b.pairs,
                                                       (uint64_t)b.cap_pairs, b.counters);
     else
-      find_pairs<3><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, kb.fmask, b.node_child, b.node_range, b.leaf_lo,
+      find_pairs<3><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, kb.fmask, kb.ishift, topo.ninst > 1,
+                                                     b.node_child, b.node_range, b.leaf_lo,
                                                      b.leaf_hi, b.node_lo, b.node_hi, b.lo64, b.hi64, b.pairs,
                                                      (uint64_t)b.cap_pairs, b.counters);
     BP_CUDA(cudaGetLastError());

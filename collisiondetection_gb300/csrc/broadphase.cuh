@@ -37,6 +37,10 @@ struct MeshTopology {
   const int32_t *rank_triple;  // [nranks][3] sorted triple of each face rank
   const int32_t *face_edges;   // [nf][3] rank of edge (v_i, v_{i+1 mod 3})
   const int32_t *rank_edge;    // [nedges][2] (a <= b) of each edge rank
+  // Independent instances in one mesh (null / 1: a single mesh).  Faces of
+  // different instances are never paired.
+  const int32_t *face_inst;    // [nf] instance of each face
+  int32_t ninst;
 };
 
 // Device buffers of one broad-phase call; grown by the caller.

@@ -68,6 +68,8 @@ struct ccd_mesh {
   int32_t nranks = 0, nedges = 0;
   int32_t *faces = nullptr, *face_rank = nullptr, *rank_triple = nullptr, *face_edges = nullptr,
           *rank_edge = nullptr;
+  int32_t *face_inst = nullptr;  // instance of each face (meshes made of independent instances)
+  int32_t ninst = 1;
   double *qs = nullptr, *qe = nullptr;
   uint8_t *fixed = nullptr;
   bool has_fixed = false;
@@ -173,8 +175,9 @@ int run_broadphase(ccd_mesh *m, int kind, double outer_eta) {
   m->have_cand = false;
   m->have_col = false;
   m->stats = ccd_mesh_stats{};
-  const ccd::MeshTopology topo{m->nv,        m->nf,        m->nranks,    m->nedges,   m->faces,
-                               m->face_rank, m->rank_triple, m->face_edges, m->rank_edge};
+  const ccd::MeshTopology topo{m->nv,         m->nf,         m->nranks,   m->nedges,
+                               m->faces,      m->face_rank,  m->rank_triple, m->face_edges,
+                               m->rank_edge,  m->face_inst,  m->ninst};
   const ccd::BroadphaseParams p{kind, outer_eta, m->qs, m->qe, m->has_fixed ? m->fixed : nullptr};
   cudaError_t err = cudaSuccess;
   int64_t npairs = 0;
@@ -198,7 +201,8 @@ int check_eta(ccd_mesh *m, int64_t n, const double *eta, int64_t eta_count) {
 }
 
 void free_mesh_buffers(ccd_mesh *m) {
-  void *ptrs[] = {m->faces, m->face_rank, m->rank_triple, m->face_edges, m->rank_edge, m->qs, m->qe, m->fixed,
+  void *ptrs[] = {m->faces, m->face_rank, m->rank_triple, m->face_edges, m->rank_edge, m->face_inst, m->qs, m->qe,
+                  m->fixed,
                   m->cand[0], m->cand[1], m->in_st, m->in_eta, m->which, m->d_eta,
                   m->col[0], m->col[1], m->col_t[0], m->col_t[1]};
   for (void *p : ptrs) cudaFree(p);
@@ -218,7 +222,14 @@ void free_mesh_buffers(ccd_mesh *m) {
 
 extern "C" {
 
-int ccd_mesh_create(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int32_t *faces, ccd_mesh **out) {
+}  // extern "C"
+
+namespace {
+
+// Shared by ccd_mesh_create and ccd_mesh_create_instances (face_inst: null, or
+// the instance of each face with ninst > 1 instances).
+int create_mesh(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int32_t *faces,
+                const std::vector<int32_t> *face_inst, int32_t ninst, ccd_mesh **out) {
   if (!ctx || !out) return CCD_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   if (nverts <= 0 || nfaces < 0 || (nfaces > 0 && !faces))
@@ -246,6 +257,10 @@ int ccd_mesh_create(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int3
   if (!rc) rc = upload(&m->rank_triple, topo.rank_triple.data(), topo.rank_triple.size());
   if (!rc) rc = upload(&m->face_edges, topo.face_edges.data(), topo.face_edges.size());
   if (!rc) rc = upload(&m->rank_edge, topo.rank_edge.data(), topo.rank_edge.size());
+  if (!rc && face_inst && ninst > 1) {
+    rc = upload(&m->face_inst, face_inst->data(), face_inst->size());
+    m->ninst = ninst;
+  }
   auto alloc = [&]() -> int {
     CCD_CUDA(cudaMalloc(&m->qs, 3 * (size_t)nverts * sizeof(double)));
     CCD_CUDA(cudaMalloc(&m->qe, 3 * (size_t)nverts * sizeof(double)));
@@ -268,6 +283,46 @@ int ccd_mesh_create(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int3
   }
   *out = m;
   return CCD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ccd_mesh_create(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int32_t *faces, ccd_mesh **out) {
+  return create_mesh(ctx, nverts, nfaces, faces, nullptr, 1, out);
+}
+
+int ccd_mesh_create_instances(ccd_context *ctx, int32_t ninst, const int32_t *vertex_offsets,
+                              const int32_t *face_offsets, const int32_t *faces, ccd_mesh **out) {
+  if (!ctx || !out) return CCD_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (ninst < 1 || !vertex_offsets || !face_offsets)
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "instances need ninst >= 1 and offset arrays");
+  if (vertex_offsets[0] != 0 || face_offsets[0] != 0)
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "offsets must start at 0");
+  if (face_offsets[ninst] > 0 && !faces) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null face array");
+  std::vector<int32_t> inst((size_t)std::max(face_offsets[ninst], 0));
+  for (int32_t i = 0; i < ninst; i++) {
+    if (vertex_offsets[i + 1] <= vertex_offsets[i] || face_offsets[i + 1] < face_offsets[i])
+      return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "offsets must increase (every instance needs a vertex)");
+    for (int32_t f = face_offsets[i]; f < face_offsets[i + 1]; f++) {
+      for (int j = 0; j < 3; j++) {
+        const int32_t v = faces[3 * (int64_t)f + j];
+        if (v < vertex_offsets[i] || v >= vertex_offsets[i + 1])
+          return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "a face uses a vertex outside its instance");
+      }
+      inst[(size_t)f] = i;
+    }
+  }
+  const int32_t nverts = vertex_offsets[ninst], nfaces = face_offsets[ninst];
+  // The broad phase's sort key holds the instance, a Morton code of at least
+  // 12 bits and the face index in 63 bits.
+  int fbits = 1, ibits = 0;
+  while (fbits < 62 && ((int64_t)1 << fbits) <= (int64_t)std::max(nfaces - 1, 0)) fbits++;
+  while (ninst > 1 && ((int64_t)1 << ibits) <= (int64_t)(ninst - 1)) ibits++;
+  if (12 + fbits + ibits > 63) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "too many faces and instances for the sort key");
+  return create_mesh(ctx, nverts, nfaces, faces, &inst, ninst, out);
 }
 
 int ccd_mesh_destroy(ccd_mesh *m) {

@@ -47,7 +47,12 @@ constexpr int kStageThreads = 128;
 // the batch size below which the pool kernel alone solves (the wavefront pays
 // a global-memory round trip per step, which only a large batch hides).
 constexpr int kWaveSteps = 48;
-constexpr int kPoolBudget = 128;
+// 0: the pool kernel finishes every job it resumes.  Handing long solves to
+// the one-per-warp finish only pays when few remain: on near-degenerate
+// polynomials (coplanar edges of flat sheets) about 1% of the solves run
+// through all 20 shifts, 12-15 thousand steps each, and the pool's lane
+// packing beats one busy lane per warp by about 9x there.
+constexpr int kPoolBudget = 0;
 constexpr int64_t kWaveMinRows = (int64_t)1 << 18;
 // Job lists: one per (working phase, current degree 3..6).
 constexpr int kWaveBins = 16;

@@ -325,3 +325,22 @@ def motion_request(tris: int, seed: int, steps: int = 10):
         pos = pos + d
         frames[k + 1] = (pos + rng.normal(0.0, 0.1 * edge, pos.shape)).ravel()
     return np.ascontiguousarray(f, dtype=np.int32), frames
+
+
+def uneven_batch(n_instances: int = 512, lo: float = 200.0, hi: float = 2e5, seed: int = 0, steps: int = 1):
+    """Uneven batch of independent collision queries: `n_instances` motion
+    requests (motion_request) with triangle counts log-uniform in [lo, hi],
+    concatenated.  Returns (faces (F, 3) int32 with global vertex indices,
+    frames (steps + 1, 3V), vertex_offsets, face_offsets)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), n_instances)).astype(int)
+    faces, frames, vo, fo = [], [], [0], [0]
+    for i, t in enumerate(sizes):
+        f, fr = motion_request(int(t), 100000 + seed * 10000 + i, steps=steps)
+        faces.append(f + vo[-1])
+        frames.append(fr.reshape(steps + 1, -1, 3))
+        vo.append(vo[-1] + fr.shape[1] // 3)
+        fo.append(fo[-1] + f.shape[0])
+    return (np.ascontiguousarray(np.concatenate(faces), dtype=np.int32),
+            np.ascontiguousarray(np.concatenate(frames, axis=1).reshape(steps + 1, -1)),
+            np.array(vo, np.int32), np.array(fo, np.int32))

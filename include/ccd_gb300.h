@@ -96,7 +96,7 @@ int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
  *                    default 262144
  *   "pool_budget"    further steps the unfinished polynomials get, many per
  *                    warp, before the last ones are finished one per warp
- *                    (0: no limit); default 128
+ *                    (0: no limit); default 0
  * Unknown names and out-of-range values return CCD_ERR_INVALID_ARGUMENT. */
 int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value);
 /* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
@@ -183,6 +183,17 @@ typedef struct {
 /* faces: nfaces x 3 vertex indices in [0, nverts).  Topology is fixed for the
  * mesh's lifetime; positions change per step. */
 int ccd_mesh_create(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int32_t *faces, ccd_mesh **out);
+/* A mesh made of independent instances (no counterpart in the reference: it
+ * is many reference meshes, each with its own broad and narrow phase, run as
+ * one).  Instance i owns vertices vertex_offsets[i] .. vertex_offsets[i+1] - 1
+ * and faces face_offsets[i] .. face_offsets[i+1] - 1; faces hold global
+ * vertex indices and may only use their own instance's vertices.  The broad
+ * phase never pairs faces of different instances, so every result is the
+ * concatenation, in instance order, of what each instance gives alone (with
+ * its vertex indices shifted by its offset).  Positions are [V][3] for all
+ * instances together. */
+int ccd_mesh_create_instances(ccd_context *ctx, int32_t ninst, const int32_t *vertex_offsets,
+                              const int32_t *face_offsets, const int32_t *faces, ccd_mesh **out);
 int ccd_mesh_destroy(ccd_mesh *mesh);
 /* Start and end positions of the step (History entries at t = 0 and 1), host
  * memory; blocks until copied. */

@@ -172,3 +172,63 @@ def test_edge_cases(ctx):
             m.narrowphase(np.array([[0, 1, 2, 3]]), 1e-6, np.zeros((0, 4)), 1e-6)
         with pytest.raises(C.CcdError):
             m.narrowphase(np.array([[0, 1, 2, 0]]), [1e-6, 1e-6], np.zeros((0, 4)), 1e-6)
+
+
+def _concat(scenes):
+    faces, qs, qe, fixed, vo, fo = [], [], [], [], [0], [0]
+    for s_qs, s_qe, s_f, s_fx in scenes:
+        faces.append(np.asarray(s_f, np.int32) + vo[-1])
+        qs.append(np.asarray(s_qs).ravel())
+        qe.append(np.asarray(s_qe).ravel())
+        fixed.append(np.asarray(s_fx, np.uint8))
+        vo.append(vo[-1] + np.asarray(s_qs).size // 3)
+        fo.append(fo[-1] + len(s_f))
+    return (np.concatenate(faces), np.concatenate(qs), np.concatenate(qe), np.concatenate(fixed),
+            np.array(vo, np.int32), np.array(fo, np.int32))
+
+
+@pytest.mark.parametrize("label", ["kdop", "aabb"])
+def test_instances_equal_each_instance_alone(ctx, golden, label):
+    # Three reference scenes and a second copy of the two-sphere scene at the
+    # same coordinates (instances overlap in space but are never paired).
+    names = ["test12", "spheres", "prob3", "spheres"]
+    scenes = [_scene(golden, n)[:4] for n in names]
+    scenes = [(qs, qe, f, fx) for qs, qe, f, fx in scenes]
+    f, qs, qe, fixed, vo, fo = _concat(scenes)
+    eta = 1e-6
+    with C.Mesh(ctx, f, qs, qe, instances=(vo, fo)) as m:
+        for use_fixed in (False, True):
+            m.set_fixed(fixed if use_fixed else None)
+            vf, ee = m.broadphase(KINDS[label], eta)
+            want_vf, want_ee = [], []
+            for i, (s_qs, s_qe, s_f, s_fx) in enumerate(scenes):
+                with C.Mesh(ctx, s_f, s_qs, s_qe, s_fx if use_fixed else None) as single:
+                    a, b = single.broadphase(KINDS[label], eta)
+                want_vf.append(a + vo[i])
+                want_ee.append(b + vo[i])
+            np.testing.assert_array_equal(vf, np.concatenate(want_vf))
+            np.testing.assert_array_equal(ee, np.concatenate(want_ee))
+        m.set_fixed(None)
+        vf, vft, ee, eet = m.detect(KINDS[label], eta, eta)
+        want = [[], [], [], []]
+        for i, (s_qs, s_qe, s_f, _) in enumerate(scenes):
+            with C.Mesh(ctx, s_f, s_qs, s_qe) as single:
+                a, at, b, bt = single.detect(KINDS[label], eta, eta)
+            want[0].append(a + vo[i])
+            want[1].append(at)
+            want[2].append(b + vo[i])
+            want[3].append(bt)
+        np.testing.assert_array_equal(vf, np.concatenate(want[0]))
+        np.testing.assert_array_equal(vft, np.concatenate(want[1]))
+        np.testing.assert_array_equal(ee, np.concatenate(want[2]))
+        np.testing.assert_array_equal(eet, np.concatenate(want[3]))
+
+
+def test_instances_reject_foreign_vertices(ctx):
+    tri = np.array([[0, 1, 2], [3, 4, 5]], np.int32)
+    pos = np.zeros(18)
+    with pytest.raises(C.CcdError):  # face 1 of instance 0 uses instance 1's vertices
+        C.Mesh(ctx, tri, pos, pos, instances=(np.array([0, 3, 6]), np.array([0, 2, 2])))
+    with C.Mesh(ctx, tri, pos, pos, instances=(np.array([0, 3, 6]), np.array([0, 1, 2]))) as m:
+        vf, ee = m.broadphase(C.BROADPHASE_KDOP13, 1e-6)
+        assert vf.shape == (0, 4) and ee.shape == (0, 4)  # coincident, but different instances
