@@ -333,17 +333,16 @@ def uneven_section(args):
     tests = st["n_vf"] + st["n_ee"]
     out["one_call"] = {"ms": 1e3 * dt, "stencil_tests": tests, "collisions": st["vf_hits"] + st["ee_hits"],
                        "value": tests / dt, "unit": "stencil tests/s"}
-    meshes = [C.Mesh(ctx, faces[fo[i]:fo[i + 1]] - vo[i], nverts=int(vo[i + 1] - vo[i])) for i in range(n)]
-    t0 = time.perf_counter()
-    hits = 0
-    for i, mi in enumerate(meshes):
-        a, b = 3 * vo[i], 3 * vo[i + 1]
-        mi.set_positions(frames[0][a:b], frames[1][a:b])
-        vf, vft, ee, eet = mi.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6)
-        hits += vf.shape[0] + ee.shape[0]
-    dt1 = time.perf_counter() - t0
-    for mi in meshes:
-        mi.close()
+    # One mesh at a time (created and freed outside the timed steps).
+    hits, dt1 = 0, 0.0
+    for i in range(n):
+        with C.Mesh(ctx, faces[fo[i]:fo[i + 1]] - vo[i], nverts=int(vo[i + 1] - vo[i])) as mi:
+            a, b = 3 * vo[i], 3 * vo[i + 1]
+            t0 = time.perf_counter()
+            mi.set_positions(frames[0][a:b], frames[1][a:b])
+            vf, vft, ee, eet = mi.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6)
+            dt1 += time.perf_counter() - t0
+            hits += vf.shape[0] + ee.shape[0]
     out["per_instance_calls"] = {"ms": 1e3 * dt1, "collisions": hits, "value": tests / dt1,
                                  "unit": "stencil tests/s"}
     ctx.close()
