@@ -150,18 +150,88 @@ __global__ void __launch_bounds__(kThreads) morton_keys(int nf, const float *flo
   keys[f] = (inst << kb.ishift) | ((uint64_t)(m >> (30 - kb.mbits)) << kb.fbits) | (uint32_t)f;
 }
 
-// Leaf FP32 slabs in Morton order.
+// FP32 slab boxes of the tree, one contiguous record per leaf or node: lower
+// bounds at [0, K), upper bounds at [H, H + K), H = 16 for the 13-DOP (128 B,
+// one cache line per record) and 4 for the AABB (32 B); a slab test reads
+// whole records with 16-byte loads.
+template <int K>
+struct BoxLayout {
+  static constexpr int H = K > 4 ? 16 : 4;  // floats per half
+  static constexpr int S = 2 * H;           // floats per record
+  static constexpr int V = H / 4;           // float4 per half
+};
+
+template <int K>
+__device__ __forceinline__ void load_box(const float *rec, float (&lo)[K], float (&hi)[K]) {
+  typedef BoxLayout<K> L;
+  const float4 *q = reinterpret_cast<const float4 *>(rec);
+  float tmp[L::S];
+#pragma unroll
+  for (int v = 0; v < 2 * L::V; v++) {
+    const float4 x = __ldg(q + v);
+    tmp[4 * v] = x.x;
+    tmp[4 * v + 1] = x.y;
+    tmp[4 * v + 2] = x.z;
+    tmp[4 * v + 3] = x.w;
+  }
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    lo[k] = tmp[k];
+    hi[k] = tmp[L::H + k];
+  }
+}
+
+// The same through L2 (records written by other blocks of the same launch).
+template <int K>
+__device__ __forceinline__ void load_box_cg(const float *rec, float (&lo)[K], float (&hi)[K]) {
+  typedef BoxLayout<K> L;
+  const float4 *q = reinterpret_cast<const float4 *>(rec);
+  float tmp[L::S];
+#pragma unroll
+  for (int v = 0; v < 2 * L::V; v++) {
+    const float4 x = __ldcg(q + v);
+    tmp[4 * v] = x.x;
+    tmp[4 * v + 1] = x.y;
+    tmp[4 * v + 2] = x.z;
+    tmp[4 * v + 3] = x.w;
+  }
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    lo[k] = tmp[k];
+    hi[k] = tmp[L::H + k];
+  }
+}
+
+template <int K>
+__device__ __forceinline__ void store_box_cg(float *rec, const float (&lo)[K], const float (&hi)[K]) {
+  typedef BoxLayout<K> L;
+  float tmp[L::S];
+#pragma unroll
+  for (int k = 0; k < L::S; k++) tmp[k] = 0.0f;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    tmp[k] = lo[k];
+    tmp[L::H + k] = hi[k];
+  }
+  float4 *q = reinterpret_cast<float4 *>(rec);
+#pragma unroll
+  for (int v = 0; v < 2 * L::V; v++) __stcg(q + v, make_float4(tmp[4 * v], tmp[4 * v + 1], tmp[4 * v + 2], tmp[4 * v + 3]));
+}
+
+// Leaf boxes in Morton order.
 template <int K>
 __global__ void __launch_bounds__(kThreads) gather_leaves(int nf, const uint64_t *keys, uint64_t fmask,
-                                                          const float *flo, const float *fhi, float *llo, float *lhi) {
+                                                          const float *flo, const float *fhi, float *leaf_box) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nf) return;
   const int f = (int)(keys[s] & fmask);
+  float lo[K], hi[K];
 #pragma unroll
   for (int k = 0; k < K; k++) {
-    llo[(int64_t)k * nf + s] = flo[(int64_t)k * nf + f];
-    lhi[(int64_t)k * nf + s] = fhi[(int64_t)k * nf + f];
+    lo[k] = flo[(int64_t)k * nf + f];
+    hi[k] = fhi[(int64_t)k * nf + f];
   }
+  store_box_cg<K>(leaf_box + (int64_t)s * BoxLayout<K>::S, lo, hi);
 }
 
 // ------------------------------------------------------------------ LBVH (Karras 2012)
@@ -205,8 +275,9 @@ __global__ void __launch_bounds__(kThreads) build_lbvh(int n, const uint64_t *ke
 // Bottom-up FP32 slab unions; the second child to arrive at a node builds it.
 template <int K>
 __global__ void __launch_bounds__(kThreads) refit(int n, const int32_t *child, const int32_t *parent, uint32_t *arrive,
-                                                  const float *llo, const float *lhi, float *nlo, float *nhi,
+                                                  const float *leaf_box, float *node_box,
                                                   unsigned long long *counters) {
+  typedef BoxLayout<K> L;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   int node = parent[(n - 1) + s];
@@ -221,35 +292,40 @@ __global__ void __launch_bounds__(kThreads) refit(int n, const int32_t *child, c
     if (atomicAdd(&arrive[node], 1u) == 0) return;
     __threadfence();
     const int c0 = child[2 * node], c1 = child[2 * node + 1];
+    float lo0[K], hi0[K], lo1[K], hi1[K];
+    if (c0 >= 0)
+      load_box_cg<K>(node_box + (int64_t)c0 * L::S, lo0, hi0);
+    else
+      load_box_cg<K>(leaf_box + (int64_t)(~c0) * L::S, lo0, hi0);
+    if (c1 >= 0)
+      load_box_cg<K>(node_box + (int64_t)c1 * L::S, lo1, hi1);
+    else
+      load_box_cg<K>(leaf_box + (int64_t)(~c1) * L::S, lo1, hi1);
 #pragma unroll
     for (int k = 0; k < K; k++) {
-      const float lo0 = c0 >= 0 ? __ldcg(&nlo[(int64_t)k * (n - 1) + c0]) : llo[(int64_t)k * n + ~c0];
-      const float hi0 = c0 >= 0 ? __ldcg(&nhi[(int64_t)k * (n - 1) + c0]) : lhi[(int64_t)k * n + ~c0];
-      const float lo1 = c1 >= 0 ? __ldcg(&nlo[(int64_t)k * (n - 1) + c1]) : llo[(int64_t)k * n + ~c1];
-      const float hi1 = c1 >= 0 ? __ldcg(&nhi[(int64_t)k * (n - 1) + c1]) : lhi[(int64_t)k * n + ~c1];
-      __stcg(&nlo[(int64_t)k * (n - 1) + node], fminf(lo0, lo1));
-      __stcg(&nhi[(int64_t)k * (n - 1) + node], fmaxf(hi0, hi1));
+      lo0[k] = fminf(lo0[k], lo1[k]);
+      hi0[k] = fmaxf(hi0[k], hi1[k]);
     }
+    store_box_cg<K>(node_box + (int64_t)node * L::S, lo0, hi0);
     node = parent[node];
   }
 }
 
 // ------------------------------------------------------------------ traversal
-template <int K>
+// COUNT: also count the slab tests (leaf and node), for the traversal's
+// algorithmic bytes; a separate variant so that timed runs carry no counter.
+template <int K, bool COUNT>
 __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n, const uint64_t *keys, uint64_t fmask,
                                                        int ishift, bool multi,
-                                                       const int32_t *child, const int32_t *range, const float *llo,
-                                                       const float *lhi, const float *nlo, const float *nhi,
-                                                       const double *lo64, const double *hi64, uint32_t *pairs,
+                                                       const int32_t *child, const int32_t *range, const float *leaf_box,
+                                                       const float *node_box, const double *lo64, const double *hi64,
+                                                       uint32_t *pairs,
                                                        uint64_t cap, unsigned long long *counters) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n || n < 2) return;
+  typedef BoxLayout<K> L;
   float qlo[K], qhi[K];
-#pragma unroll
-  for (int k = 0; k < K; k++) {
-    qlo[k] = llo[(int64_t)k * n + s];
-    qhi[k] = lhi[(int64_t)k * n + s];
-  }
+  load_box<K>(leaf_box + (int64_t)s * L::S, qlo, qhi);
   const int fa = (int)(keys[s] & fmask);
   const int a0 = topo.faces[3 * fa], a1 = topo.faces[3 * fa + 1], a2 = topo.faces[3 * fa + 2];
   // Keys are ordered by instance first: a subtree whose first leaf belongs to
@@ -258,6 +334,7 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
   int stack[kStack];
   int sp = 0;
   stack[sp++] = 0;
+  unsigned long long tests = 0;
   // A valid tree is visited at most once per node (n - 1 internal nodes).
   for (int visits = 0; sp > 0; visits++) {
     if (visits >= n) {
@@ -271,9 +348,14 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
         const int j = ~ch;
         if (j <= s) continue;
         if (multi && (keys[j] >> ishift) != my_inst) continue;
+        if (COUNT) tests++;
         bool sep = false;
+        {
+          float blo[K], bhi[K];
+          load_box<K>(leaf_box + (int64_t)j * L::S, blo, bhi);
 #pragma unroll
-        for (int k = 0; k < K; k++) sep |= (qhi[k] < llo[(int64_t)k * n + j]) || (lhi[(int64_t)k * n + j] < qlo[k]);
+          for (int k = 0; k < K; k++) sep |= (qhi[k] < blo[k]) || (bhi[k] < qlo[k]);
+        }
         if (sep) continue;
         // The reference's exact FP64 test (KDOPBroadPhase.cpp:132-137).
         const int fb = (int)(keys[j] & fmask);
@@ -294,10 +376,14 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
       } else {
         if (range[2 * ch + 1] <= s) continue;
         if (multi && (keys[range[2 * ch]] >> ishift) > my_inst) continue;
+        if (COUNT) tests++;
         bool sep = false;
+        {
+          float blo[K], bhi[K];
+          load_box<K>(node_box + (int64_t)ch * L::S, blo, bhi);
 #pragma unroll
-        for (int k = 0; k < K; k++)
-          sep |= (qhi[k] < nlo[(int64_t)k * (n - 1) + ch]) || (nhi[(int64_t)k * (n - 1) + ch] < qlo[k]);
+          for (int k = 0; k < K; k++) sep |= (qhi[k] < blo[k]) || (bhi[k] < qlo[k]);
+        }
         if (sep) continue;
         if (sp < kStack)
           stack[sp++] = ch;
@@ -306,6 +392,7 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
       }
     }
   }
+  if (COUNT && tests) atomicAdd(&counters[4], tests);
 }
 
 // ------------------------------------------------------------------ stencils
@@ -410,7 +497,7 @@ Axes make_axes() {
 }  // namespace
 
 void broadphase_free(BroadphaseBuffers &b) {
-  void *ptrs[] = {b.lo64, b.hi64, b.leaf_lo, b.leaf_hi, b.node_lo, b.node_hi, b.node_child, b.node_range, b.parent,
+  void *ptrs[] = {b.lo64, b.hi64, b.face_lo, b.face_hi, b.leaf_box, b.node_box, b.node_child, b.node_range, b.parent,
                   b.arrive, b.keys, b.keys_alt, b.vals, b.vals_alt, b.bounds, b.counters, b.pairs, b.vf_keys,
                   b.ee_keys, b.flags, b.scan, b.temp};
   for (void *p : ptrs) cudaFree(p);
@@ -431,7 +518,7 @@ void broadphase_free(BroadphaseBuffers &b) {
 // candidate face pairs exceed 2^27.
 int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, BroadphaseBuffers &b, int32_t **vf_out,
                    int64_t *vf_cap, int32_t **ee_out, int64_t *ee_cap, int64_t *n_vf, int64_t *n_ee,
-                   int64_t *n_pairs, int num_sms, cudaStream_t s, cudaError_t *err) {
+                   int64_t *n_pairs, int64_t *slab_tests, int num_sms, cudaStream_t s, cudaError_t *err) {
   (void)num_sms;
   *n_vf = *n_ee = *n_pairs = 0;
   const int nf = topo.nf;
@@ -443,10 +530,10 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
     const size_t F = (size_t)nf;
     BP_CUDA(cudaMalloc(&b.lo64, 13 * F * sizeof(double)));
     BP_CUDA(cudaMalloc(&b.hi64, 13 * F * sizeof(double)));
-    BP_CUDA(cudaMalloc(&b.leaf_lo, 2 * 13 * F * sizeof(float)));  // [sorted | face-indexed]
-    BP_CUDA(cudaMalloc(&b.leaf_hi, 2 * 13 * F * sizeof(float)));
-    BP_CUDA(cudaMalloc(&b.node_lo, 13 * F * sizeof(float)));
-    BP_CUDA(cudaMalloc(&b.node_hi, 13 * F * sizeof(float)));
+    BP_CUDA(cudaMalloc(&b.face_lo, 13 * F * sizeof(float)));  // [axis][face]
+    BP_CUDA(cudaMalloc(&b.face_hi, 13 * F * sizeof(float)));
+    BP_CUDA(cudaMalloc(&b.leaf_box, 32 * F * sizeof(float)));  // [sorted leaf][record]
+    BP_CUDA(cudaMalloc(&b.node_box, 32 * F * sizeof(float)));  // [node][record]
     BP_CUDA(cudaMalloc(&b.node_child, 2 * F * sizeof(int32_t)));
     BP_CUDA(cudaMalloc(&b.node_range, 2 * F * sizeof(int32_t)));
     BP_CUDA(cudaMalloc(&b.parent, 2 * F * sizeof(int32_t)));
@@ -454,7 +541,7 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
     BP_CUDA(cudaMalloc(&b.keys, F * sizeof(uint64_t)));
     BP_CUDA(cudaMalloc(&b.vals, F * sizeof(uint64_t)));  // second Morton key buffer
     BP_CUDA(cudaMalloc(&b.bounds, 8 * sizeof(float)));
-    BP_CUDA(cudaMalloc(&b.counters, 4 * sizeof(unsigned long long)));
+    BP_CUDA(cudaMalloc(&b.counters, 8 * sizeof(unsigned long long)));
     b.cap_faces = nf;
   }
   // Pair-sized buffers; grown when a traversal reports more pairs.
@@ -482,7 +569,8 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   int rc = ensure_pairs(std::max<int64_t>(b.cap_pairs, std::min<int64_t>(std::max<int64_t>(8 * (int64_t)nf, 4096), kMaxPairs)));
   if (rc) return rc;
 
-  float *flo = b.leaf_lo + 13 * (size_t)nf, *fhi = b.leaf_hi + 13 * (size_t)nf;
+  if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[0], s));
+  float *flo = b.face_lo, *fhi = b.face_hi;
   const Axes ax = make_axes();
   {
     // centre bounds as order-preserving ints: +inf for minima, -inf for maxima
@@ -502,45 +590,57 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   BP_CUDA(radix_sort_u64(b.keys, (uint64_t *)b.vals, nullptr, nullptr, nf, 0, kb.ishift + kb.ibits, b.temp,
                          b.temp_bytes, s));
   if (kdop)
-    gather_leaves<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, flo, fhi, b.leaf_lo, b.leaf_hi);
+    gather_leaves<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, flo, fhi, b.leaf_box);
   else
-    gather_leaves<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, flo, fhi, b.leaf_lo, b.leaf_hi);
+    gather_leaves<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, flo, fhi, b.leaf_box);
   build_lbvh<<<grid_of(nf - 1), kThreads, 0, s>>>(nf, b.keys, b.node_child, b.node_range, b.parent);
   BP_CUDA(cudaMemsetAsync(b.arrive, 0, (size_t)nf * sizeof(uint32_t), s));
-  BP_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(unsigned long long), s));
+  BP_CUDA(cudaMemsetAsync(b.counters, 0, 8 * sizeof(unsigned long long), s));
   if (kdop)
-    refit<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.node_child, b.parent, b.arrive, b.leaf_lo, b.leaf_hi, b.node_lo,
-                                               b.node_hi, b.counters);
+    refit<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.node_child, b.parent, b.arrive, b.leaf_box, b.node_box,
+                                               b.counters);
   else
-    refit<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.node_child, b.parent, b.arrive, b.leaf_lo, b.leaf_hi, b.node_lo,
-                                              b.node_hi, b.counters);
+    refit<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.node_child, b.parent, b.arrive, b.leaf_box, b.node_box,
+                                              b.counters);
   BP_CUDA(cudaGetLastError());
 
+  if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[1], s));
+  auto traverse = [&]() {
+    const bool multi = topo.ninst > 1;
+#define BP_FIND(KK, CC)                                                                                           \
+  find_pairs<KK, CC><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, kb.fmask, kb.ishift, multi, b.node_child, \
+                                                      b.node_range, b.leaf_box, b.node_box,                     \
+                                                      b.lo64, b.hi64, b.pairs, (uint64_t)b.cap_pairs, b.counters)
+    if (kdop && p.count_tests) BP_FIND(13, true);
+    else if (kdop) BP_FIND(13, false);
+    else if (p.count_tests) BP_FIND(3, true);
+    else BP_FIND(3, false);
+#undef BP_FIND
+  };
   for (;;) {
-    BP_CUDA(cudaMemsetAsync(b.counters, 0, 3 * sizeof(unsigned long long), s));  // keeps the error word
-    if (kdop)
-      find_pairs<13><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, kb.fmask, kb.ishift, topo.ninst > 1,
-                                                      b.node_child, b.node_range, b.leaf_lo,
-                                                      b.leaf_hi, b.node_lo, b.node_hi, b.lo64, b.hi64, b.pairs,
-                                                      (uint64_t)b.cap_pairs, b.counters);
-    else
-      find_pairs<3><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, kb.fmask, kb.ishift, topo.ninst > 1,
-                                                     b.node_child, b.node_range, b.leaf_lo,
-                                                     b.leaf_hi, b.node_lo, b.node_hi, b.lo64, b.hi64, b.pairs,
-                                                     (uint64_t)b.cap_pairs, b.counters);
+    // pairs, vf, ee and the slab-test count; keeps the error word
+    BP_CUDA(cudaMemsetAsync(b.counters, 0, 3 * sizeof(unsigned long long), s));
+    BP_CUDA(cudaMemsetAsync(b.counters + 4, 0, sizeof(unsigned long long), s));
+    traverse();
     BP_CUDA(cudaGetLastError());
-    unsigned long long hc[4];
+    if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[2], s));
+    unsigned long long hc[5];
     BP_CUDA(cudaMemcpyAsync(hc, b.counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
     BP_CUDA(cudaStreamSynchronize(s));
     if (hc[3]) return 3;
     *n_pairs = hc[0];
+    if (slab_tests) *slab_tests = (int64_t)hc[4];
     if ((int64_t)hc[0] <= b.cap_pairs) break;
     if ((int64_t)hc[0] > kMaxPairs) return 4;
     rc = ensure_pairs(std::min<int64_t>(2 * (int64_t)hc[0], kMaxPairs));  // the tree stays valid; only the pair buffers grow
     if (rc) return rc;
   }
   const int64_t np = *n_pairs;
-  if (np == 0) return 0;
+  if (np == 0) {
+    if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[3], s));
+    BP_CUDA(cudaStreamSynchronize(s));
+    return 0;
+  }
   stencil_keys<<<grid_of(np), kThreads, 0, s>>>(topo, kb, p.fixed, b.pairs, np, b.vf_keys, b.ee_keys);
   BP_CUDA(cudaGetLastError());
   // Sort, mark the first of each run of equal keys, scan, decode.
@@ -568,6 +668,7 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
     }
     BP_CUDA(cudaGetLastError());
   }
+  if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[3], s));
   BP_CUDA(cudaStreamSynchronize(s));
   return 0;
 }

@@ -48,8 +48,9 @@ struct BroadphaseBuffers {
   int64_t cap_faces = 0, cap_pairs = 0;
   // per face / node
   double *lo64 = nullptr, *hi64 = nullptr;        // [13][nf]
-  float *leaf_lo = nullptr, *leaf_hi = nullptr;   // [13][nf]   by sorted position
-  float *node_lo = nullptr, *node_hi = nullptr;   // [13][nf-1] internal nodes
+  float *face_lo = nullptr, *face_hi = nullptr;   // [13][nf]   outward-rounded FP32 slabs by face
+  float *leaf_box = nullptr;                      // [nf][32]   slab records by sorted position
+  float *node_box = nullptr;                      // [nf-1][32] internal nodes
   int32_t *node_child = nullptr;                  // [nf-1][2]  >= 0 internal, < 0 leaf ~s
   int32_t *node_range = nullptr;                  // [nf-1][2]  first, last sorted leaf
   int32_t *parent = nullptr;                      // [2 nf]     internal then leaves
@@ -57,7 +58,7 @@ struct BroadphaseBuffers {
   uint64_t *keys = nullptr, *keys_alt = nullptr;  // [max(nf, 9 pairs)]
   uint32_t *vals = nullptr, *vals_alt = nullptr;  // [2 nf]: second Morton key buffer
   float *bounds = nullptr;                        // [6]
-  unsigned long long *counters = nullptr;         // [4] pairs, vf, ee, overflow
+  unsigned long long *counters = nullptr;         // [8] pairs, vf, ee, overflow, slab tests
   uint32_t *pairs = nullptr;                      // [cap_pairs][2]
   uint64_t *vf_keys = nullptr, *ee_keys = nullptr;
   uint32_t *flags = nullptr, *scan = nullptr;
@@ -70,6 +71,8 @@ struct BroadphaseParams {
   double eta;
   const double *qs, *qe;  // [nv][3]
   const uint8_t *fixed;   // [nv] or null
+  bool count_tests;       // count the traversal's slab tests (a slower, counting variant)
+  cudaEvent_t ev[4];      // optional (all null or all set): start, before / after the traversal, end
 };
 
 // Runs the candidate search; on return (stream synchronised) n_vf / n_ee
@@ -77,7 +80,7 @@ struct BroadphaseParams {
 // the reference's order.  The output arrays are grown as needed.
 int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, BroadphaseBuffers &buf, int32_t **vf_out,
                    int64_t *vf_cap, int32_t **ee_out, int64_t *ee_cap, int64_t *n_vf, int64_t *n_ee,
-                   int64_t *n_pairs, int num_sms, cudaStream_t s, cudaError_t *err);
+                   int64_t *n_pairs, int64_t *slab_tests, int num_sms, cudaStream_t s, cudaError_t *err);
 
 void broadphase_free(BroadphaseBuffers &buf);
 

@@ -293,6 +293,9 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
   } else if (key == "pool_budget") {
     if (value < 0 || value > (1 << 20)) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "pool_budget must be in [0, 2^20]");
     ctx->opt_pool_budget = (int)value;
+  } else if (key == "count_slab_tests") {
+    if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "count_slab_tests must be 0 or 1");
+    ctx->opt_count_tests = (int)value;
   } else if (key == "wave_min_rows") {
     if (value < 0) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "wave_min_rows must be >= 0");
     ctx->opt_wave_min_rows = value;

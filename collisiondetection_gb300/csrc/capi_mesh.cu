@@ -85,6 +85,7 @@ struct ccd_mesh {
   Lane lane[2];
   cudaStream_t side = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  cudaEvent_t bp_ev[4] = {nullptr, nullptr, nullptr, nullptr};  // broad-phase timing (profiling)
   // narrow-phase inputs of the host entry point
   int32_t *in_st = nullptr;
   int64_t in_st_cap = 0;
@@ -178,15 +179,28 @@ int run_broadphase(ccd_mesh *m, int kind, double outer_eta) {
   const ccd::MeshTopology topo{m->nv,         m->nf,         m->nranks,   m->nedges,
                                m->faces,      m->face_rank,  m->rank_triple, m->face_edges,
                                m->rank_edge,  m->face_inst,  m->ninst};
-  const ccd::BroadphaseParams p{kind, outer_eta, m->qs, m->qe, m->has_fixed ? m->fixed : nullptr};
+  ccd::BroadphaseParams p{kind, outer_eta, m->qs, m->qe, m->has_fixed ? m->fixed : nullptr,
+                          ctx->opt_count_tests != 0, {nullptr, nullptr, nullptr, nullptr}};
+  const bool timed = ctx->profiling && m->nf >= 2;
+  if (timed) {
+    for (int k = 0; k < 4; k++) {
+      if (!m->bp_ev[k]) CCD_CUDA(cudaEventCreate(&m->bp_ev[k]));
+      p.ev[k] = m->bp_ev[k];
+    }
+  }
   cudaError_t err = cudaSuccess;
-  int64_t npairs = 0;
+  int64_t npairs = 0, tests = 0;
   const int rc = ccd::broadphase_run(topo, p, m->bp, &m->cand[0], &m->cand_cap[0], &m->cand[1], &m->cand_cap[1],
-                                     &m->n_cand[0], &m->n_cand[1], &npairs, ctx->num_sms, ctx->stream, &err);
+                                     &m->n_cand[0], &m->n_cand[1], &npairs, &tests, ctx->num_sms, ctx->stream, &err);
   if (rc == 2) return cuda_fail(ctx, err, "broadphase");
   if (rc == 3) return mesh_fail(m, CCD_ERR_CUDA, "broadphase: malformed tree (traversal beyond its size)");
   if (rc == 4) return mesh_fail(m, CCD_ERR_OUT_OF_MEMORY, "broadphase: more than 2^27 overlapping face pairs");
   m->stats.face_pairs = npairs;
+  m->stats.slab_tests = p.count_tests ? tests : -1;
+  if (timed) {
+    CCD_CUDA(cudaEventElapsedTime(&m->stats.broadphase_ms, p.ev[0], p.ev[3]));
+    CCD_CUDA(cudaEventElapsedTime(&m->stats.traversal_ms, p.ev[1], p.ev[2]));
+  }
   m->stats.n_vf = m->n_cand[0];
   m->stats.n_ee = m->n_cand[1];
   m->have_cand = true;
@@ -213,6 +227,8 @@ void free_mesh_buffers(ccd_mesh *m) {
     for (void *p : lp) cudaFree(p);
   }
   ccd::broadphase_free(m->bp);
+  for (cudaEvent_t e : m->bp_ev)
+    if (e) cudaEventDestroy(e);
   if (m->fork) cudaEventDestroy(m->fork);
   if (m->join) cudaEventDestroy(m->join);
   if (m->side) cudaStreamDestroy(m->side);
@@ -426,10 +442,10 @@ int ccd_narrowphase(ccd_mesh *m, int path, int64_t n_vf, const int32_t *vf, cons
       if (st[i] < 0 || st[i] >= m->nv) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "stencil vertex out of range");
   }
   CCD_CUDA(cudaSetDevice(ctx->device));
+  m->stats = ccd_mesh_stats{};
   m->stats.n_vf = n_vf;
   m->stats.n_ee = n_ee;
-  m->stats.vf_hits = m->stats.ee_hits = 0;
-  m->stats.face_pairs = 0;
+  m->stats.slab_tests = -1;
   std::vector<double> tbuf;
   for (int k = 0; k < 2; k++) {
     const int64_t n = k ? n_ee : n_vf;

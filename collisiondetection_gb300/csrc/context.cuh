@@ -80,6 +80,7 @@ struct ccd_context {
   int opt_wave_steps = ccd::kWaveSteps;
   int64_t opt_wave_min_rows = ccd::kWaveMinRows;
   int opt_pool_budget = ccd::kPoolBudget;
+  int opt_count_tests = 0;
   std::string err;
 };
 

@@ -94,6 +94,8 @@ int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
  *                    solver only); default 48, at most 4096
  *   "wave_min_rows"  smallest batch (rows) that uses those lock-step steps;
  *                    default 262144
+ *   "count_slab_tests" 1: the broad phase counts its traversal's slab tests
+ *                    (ccd_mesh_stats.slab_tests; a slower variant); default 0
  *   "pool_budget"    further steps the unfinished polynomials get, many per
  *                    warp, before the last ones are finished one per warp
  *                    (0: no limit); default 0
@@ -178,6 +180,9 @@ typedef struct {
   int64_t n_ee;       /* edge-edge stencils tested (candidates) */
   int64_t vf_hits;    /* colliding vertex-face stencils */
   int64_t ee_hits;    /* colliding edge-edge stencils */
+  int64_t slab_tests; /* traversal slab tests (leaf and node), or -1 unless counting is on */
+  float broadphase_ms; /* device time of the broad phase, traversal_ms of its tree */
+  float traversal_ms;  /* traversal (both 0 unless the context's profiling is on) */
 } ccd_mesh_stats;
 
 /* faces: nfaces x 3 vertex indices in [0, nverts).  Topology is fixed for the

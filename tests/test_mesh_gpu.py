@@ -232,3 +232,21 @@ def test_instances_reject_foreign_vertices(ctx):
     with C.Mesh(ctx, tri, pos, pos, instances=(np.array([0, 3, 6]), np.array([0, 1, 2]))) as m:
         vf, ee = m.broadphase(C.BROADPHASE_KDOP13, 1e-6)
         assert vf.shape == (0, 4) and ee.shape == (0, 4)  # coincident, but different instances
+
+
+def test_slab_test_counting_and_broadphase_timing(ctx, golden):
+    qs, qe, f, _, meta = _scene(golden, "spheres")
+    with C.Mesh(ctx, f, qs, qe) as m:
+        vf0, ee0 = m.broadphase(C.BROADPHASE_KDOP13, meta["eta"])
+        assert m.stats()["slab_tests"] == -1
+        ctx.set_option("count_slab_tests", 1)
+        ctx.set_profiling(True)
+        vf1, ee1 = m.broadphase(C.BROADPHASE_KDOP13, meta["eta"])
+        st = m.stats()
+        ctx.set_profiling(False)
+        ctx.set_option("count_slab_tests", 0)
+        np.testing.assert_array_equal(vf0, vf1)  # counting changes nothing but the count
+        np.testing.assert_array_equal(ee0, ee1)
+        # at least one slab test per reported pair, at most one per (leaf, node)
+        assert st["face_pairs"] <= st["slab_tests"] <= f.shape[0] * (2 * f.shape[0])
+        assert 0 < st["traversal_ms"] <= st["broadphase_ms"]
