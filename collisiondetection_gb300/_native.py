@@ -19,6 +19,8 @@ CCD_OK = 0
 VERTEX_FACE, EDGE_EDGE, VERTEX_EDGE, VERTEX_VERTEX = 0, 1, 2, 3
 PATH_FP64, PATH_CULL_REFINE = 0, 1
 BROADPHASE_KDOP13, BROADPHASE_AABB = 0, 1
+DISTANCE_VERTEX_FACE, DISTANCE_EDGE_EDGE = 0, 1    # ccd_distance_batch
+DISTANCE_VERTEX_PLANE, DISTANCE_LINE_LINE = 0, 1   # ccd_distance_less_than_batch
 ROW_WIDTH = {VERTEX_FACE: 24, EDGE_EDGE: 24, VERTEX_EDGE: 18, VERTEX_VERTEX: 12}
 
 _P = ctypes.c_void_p
@@ -93,6 +95,12 @@ def load(path: str = LIB):
                                   ctypes.POINTER(_I64), ctypes.POINTER(_I64)]
     L.ccd_mesh_get_collisions.argtypes = [_P, _P, _P, _P, _P]
     L.ccd_mesh_last_stats.argtypes = [_P, ctypes.POINTER(MeshStats)]
+    L.ccd_distance_batch.argtypes = [_P, ctypes.c_int, _I64, _P, _P, _P]
+    L.ccd_distance_batch_device.argtypes = [_P, ctypes.c_int, _I64, _P, _P, _P]
+    L.ccd_distance_less_than_batch.argtypes = [_P, ctypes.c_int, _I64, _P, _P, _I64, _P]
+    L.ccd_mesh_self_distance.argtypes = [_P, _P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64),
+                                         ctypes.POINTER(_I64)]
+    L.ccd_self_distance.argtypes = [_P, ctypes.c_int32, _P, ctypes.c_int32, _P, _P, ctypes.POINTER(ctypes.c_double)]
     _lib = L
     return L
 
@@ -180,6 +188,44 @@ class Context:
         self._check(self.lib.ccd_prim_batch(self.handle, kind, path, n, _ptr(rows), _ptr(eta), eta.size, _ptr(hit),
                                             _ptr(t)), "ccd_prim_batch")
         return hit, t
+
+    def distance(self, kind: int, rows, want_bary: bool = True):
+        """Distance::vertexFaceDistance (DISTANCE_VERTEX_FACE) or
+        edgeEdgeDistance (DISTANCE_EDGE_EDGE) per row of 12 doubles
+        (ccd_distance_batch).  Returns (vec [n][3], bary [n][3|4] or None)."""
+        rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 12)
+        n = rows.shape[0]
+        vec = np.zeros((n, 3))
+        bary = np.zeros((n, 3 if kind == DISTANCE_VERTEX_FACE else 4)) if want_bary else None
+        self._check(self.lib.ccd_distance_batch(self.handle, kind, n, _ptr(rows), _ptr(vec), _ptr(bary)),
+                    "ccd_distance_batch")
+        return vec, bary
+
+    def distance_device(self, kind: int, n: int, rows_ptr: int, vec_ptr: int, bary_ptr: int | None = None):
+        """Device-memory form (ccd_distance_batch_device); asynchronous."""
+        self._check(self.lib.ccd_distance_batch_device(self.handle, kind, n, rows_ptr, vec_ptr, bary_ptr),
+                    "ccd_distance_batch_device")
+
+    def distance_less_than(self, kind: int, rows, eta):
+        """Distance::vertexPlaneDistanceLessThan (DISTANCE_VERTEX_PLANE) or
+        lineLineDistanceLessThan (DISTANCE_LINE_LINE) per row; uint8 [n]."""
+        rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 12)
+        n = rows.shape[0]
+        eta = np.ascontiguousarray(np.atleast_1d(np.asarray(eta, dtype=np.float64)))
+        out = np.zeros(n, np.uint8)
+        self._check(self.lib.ccd_distance_less_than_batch(self.handle, kind, n, _ptr(rows), _ptr(eta), eta.size,
+                                                          _ptr(out)), "ccd_distance_less_than_batch")
+        return out
+
+    def self_distance(self, verts, faces, fixed=None) -> float:
+        """Distance::meshSelfDistance(verts, faces, fixedVerts) (ccd_self_distance)."""
+        verts = np.ascontiguousarray(verts, dtype=np.float64).ravel()
+        faces = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+        fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8).ravel()
+        d = ctypes.c_double()
+        self._check(self.lib.ccd_self_distance(self.handle, verts.size // 3, _ptr(verts), faces.shape[0], _ptr(faces),
+                                               _ptr(fx), ctypes.byref(d)), "ccd_self_distance")
+        return d.value
 
     def prim_batch_device(self, kind: int, n: int, rows_ptr: int, eta_ptr: int, eta_count: int, hit_ptr: int,
                           t_ptr: int, status_ptr: int | None = None, path: int = PATH_CULL_REFINE):
@@ -310,6 +356,28 @@ class Mesh:
         self.ctx._check(self.lib.ccd_mesh_get_collisions(self.handle, _ptr(vf), _ptr(vft), _ptr(ee), _ptr(eet)),
                         "ccd_mesh_get_collisions")
         return vf, vft, ee, eet
+
+    def candidates(self):
+        """The stencils of the mesh's last broad phase (also the one
+        self_distance runs), without running a new one."""
+        st = self.stats()
+        vf = np.zeros((st["n_vf"], 4), np.int32)
+        ee = np.zeros((st["n_ee"], 4), np.int32)
+        self.ctx._check(self.lib.ccd_broadphase_get(self.handle, _ptr(vf), _ptr(ee)), "ccd_broadphase_get")
+        return vf, ee
+
+    def self_distance(self, verts):
+        """Distance::meshSelfDistance on this mesh's faces and fixed flags at
+        positions verts (ccd_mesh_self_distance; verts become the mesh's start
+        and end positions).  Returns (distance, n_vf, n_ee): the stencil
+        counts are the ones the reference prints."""
+        v = np.ascontiguousarray(verts, dtype=np.float64).ravel()
+        if v.size != 3 * self.nverts:
+            raise ValueError("verts must hold nverts x 3 doubles")
+        d, nvf, nee = ctypes.c_double(), _I64(), _I64()
+        self.ctx._check(self.lib.ccd_mesh_self_distance(self.handle, _ptr(v), ctypes.byref(d), ctypes.byref(nvf),
+                                                        ctypes.byref(nee)), "ccd_mesh_self_distance")
+        return d.value, nvf.value, nee.value
 
     def stats(self) -> dict:
         st = MeshStats()

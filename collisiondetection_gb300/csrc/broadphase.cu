@@ -3,8 +3,11 @@
 
 #include <algorithm>
 
+#include <string.h>
+
 #include "broadphase.cuh"
 #include "ccd_common.h"
+#include "ccd_distance.h"
 #include "radix_sort.cuh"
 
 namespace ccd {
@@ -494,6 +497,196 @@ Axes make_axes() {
   return ax;
 }
 
+// ------------------------------------------------------------------ closest vertex pair
+// The vertex scan of Distance::meshSelfDistance (src/Distance.cpp:21-34):
+// the least (x_i - x_v).squaredNorm() over vertices i and vertices v of a face
+// that does not contain i.  A pair (i, v) qualifies exactly when some face
+// incident to v misses i; a vertex in no face is never the far end v.
+
+// Vertex -> face incidence (CSR): each face once per distinct vertex.
+__global__ void __launch_bounds__(kThreads) incidence_count(int nf, const int32_t *faces, uint32_t *count) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int a = faces[3 * f], b = faces[3 * f + 1], c = faces[3 * f + 2];
+  atomicAdd(&count[a], 1u);
+  if (b != a) atomicAdd(&count[b], 1u);
+  if (c != a && c != b) atomicAdd(&count[c], 1u);
+}
+
+__global__ void __launch_bounds__(kThreads) incidence_fill(int nf, const int32_t *faces, const uint32_t *off,
+                                                           uint32_t *cursor, int32_t *list) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int a = faces[3 * f], b = faces[3 * f + 1], c = faces[3 * f + 2];
+  list[off[a] + atomicAdd(&cursor[a], 1u)] = f;
+  if (b != a) list[off[b] + atomicAdd(&cursor[b], 1u)] = f;
+  if (c != a && c != b) list[off[c] + atomicAdd(&cursor[c], 1u)] = f;
+}
+
+__device__ __forceinline__ bool finite3(const double *x) {
+  return isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]);
+}
+
+// Point boxes (outward-rounded FP32) of the vertices that can be a far end:
+// in some face and with finite coordinates (a non-finite coordinate makes
+// every squared distance NaN or infinite, which never lowers the reference's
+// running minimum).  Other vertices get the empty box [+inf, -inf], which no
+// test passes.
+__global__ void __launch_bounds__(kThreads) point_slabs(int nv, const double *x, const uint32_t *degree, float *flo,
+                                                        float *fhi, float *bounds) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  float cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+  if (v < nv) {
+    const double *p = x + 3 * (int64_t)v;
+    const bool far_end = degree[v] > 0 && finite3(p);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const float lo = far_end ? __double2float_rd(p[k]) : INFINITY;
+      const float hi = far_end ? __double2float_ru(p[k]) : -INFINITY;
+      flo[(int64_t)k * nv + v] = lo;
+      fhi[(int64_t)k * nv + v] = hi;
+      if (far_end) cmin[k] = cmax[k] = 0.5f * (lo + hi);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      cmin[k] = fminf(cmin[k], __shfl_xor_sync(0xffffffffu, cmin[k], o));
+      cmax[k] = fmaxf(cmax[k], __shfl_xor_sync(0xffffffffu, cmax[k], o));
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+    for (int k = 0; k < 3; k++) {
+      if (cmin[k] <= cmax[k]) {
+        atomicMin((int *)&bounds[k], __float_as_int(cmin[k]) >= 0 ? __float_as_int(cmin[k])
+                                                                   : (int)(0x80000000u - (unsigned)__float_as_int(cmin[k])));
+        atomicMax((int *)&bounds[3 + k], __float_as_int(cmax[k]) >= 0 ? __float_as_int(cmax[k])
+                                                                       : (int)(0x80000000u - (unsigned)__float_as_int(cmax[k])));
+      }
+    }
+  }
+}
+
+// Does some face incident to v miss vertex i?  (Mesh::vertexOfFace,
+// src/Mesh.cpp:5-11, negated, over v's faces.)
+__device__ __forceinline__ bool far_end_of(int i, int v, const uint32_t *off, const int32_t *list,
+                                           const int32_t *faces) {
+  const uint32_t e = off[v + 1];
+  for (uint32_t k = off[v]; k < e; k++) {
+    const int f = list[k];
+    if (faces[3 * f] != i && faces[3 * f + 1] != i && faces[3 * f + 2] != i) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ double sq_dist(const double *a, const double *b) {
+  return vertex_distance_sq(v3d{a[0], a[1], a[2]}, v3d{b[0], b[1], b[2]});
+}
+
+// Lowers *best (the bits of a non-negative double) to d, one atomic per warp.
+__device__ __forceinline__ void warp_min_to(double d, unsigned long long *best) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_xor_sync(0xffffffffu, b, o);
+    b = other < b ? other : b;
+  }
+  if ((threadIdx.x & 31) == 0 && b < __ldcg(best)) atomicMin(best, b);
+}
+
+constexpr int kSeedReach = 4;
+
+// A first bound: each vertex against its Morton-order neighbours.
+__global__ void __launch_bounds__(kThreads) pair_seed(int n, const uint64_t *keys, uint64_t vmask, const double *x,
+                                                      const uint32_t *off, const int32_t *list, const int32_t *faces,
+                                                      unsigned long long *best) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  double local = INFINITY;
+  if (s < n) {
+    const int i = (int)(keys[s] & vmask);
+    const double *xi = x + 3 * (int64_t)i;
+    if (finite3(xi)) {
+      for (int d = -kSeedReach; d <= kSeedReach; d++) {
+        const int j = s + d;
+        if (d == 0 || j < 0 || j >= n) continue;
+        const int v = (int)(keys[j] & vmask);
+        const double dd = sq_dist(xi, x + 3 * (int64_t)v);
+        if (dd < local && off[v + 1] > off[v] && far_end_of(i, v, off, list, faces)) local = dd;
+      }
+    }
+  }
+  warp_min_to(local, best);
+}
+
+// Every vertex i against the tree of far-end vertices, pruned by the running
+// global minimum.  A node is skipped when a lower bound of its squared
+// distance to x_i exceeds the minimum by a relative 2^-40, far more than the
+// rounding of the FP64 squared distances (a few ulps) -- so no pair whose
+// FP64 squared distance is at most the final minimum is ever skipped.
+__global__ void __launch_bounds__(kThreads) pair_search(int n, const uint64_t *keys, uint64_t vmask, const double *x,
+                                                        const uint32_t *off, const int32_t *list, const int32_t *faces,
+                                                        const int32_t *child, const float *leaf_box,
+                                                        const float *node_box, unsigned long long *best,
+                                                        unsigned long long *counters) {
+  typedef BoxLayout<3> L;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n || n < 2) return;
+  const int i = (int)(keys[s] & vmask);
+  const double *xi = x + 3 * (int64_t)i;
+  if (!finite3(xi)) return;
+  float qlo[3], qhi[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    qlo[k] = __double2float_rd(xi[k]);
+    qhi[k] = __double2float_ru(xi[k]);
+  }
+  const double keep = 1.0 - 0x1p-40;
+  double cur = __longlong_as_double((long long)__ldcg(best));
+  int stack[kStack];
+  int sp = 0;
+  stack[sp++] = 0;  // root
+  int64_t visits = 0;
+  while (sp > 0) {
+    if (cur == 0.0) return;  // nothing lies below zero
+    const int node = stack[--sp];
+    if (++visits > 4 * (int64_t)n) {
+      atomicOr(&counters[3], 2ull);
+      return;
+    }
+    if ((visits & 7) == 0) cur = fmin(cur, __longlong_as_double((long long)__ldcg(best)));
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const int ch = child[2 * node + c];
+      float blo[3], bhi[3];
+      if (ch >= 0)
+        load_box<3>(node_box + (int64_t)ch * L::S, blo, bhi);
+      else
+        load_box<3>(leaf_box + (int64_t)(~ch) * L::S, blo, bhi);
+      float lb = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const float g = fmaxf(0.0f, fmaxf(__fsub_rd(blo[k], qhi[k]), __fsub_rd(qlo[k], bhi[k])));
+        lb = __fadd_rd(lb, __fmul_rd(g, g));
+      }
+      if ((double)lb * keep > cur) continue;
+      if (ch >= 0) {
+        if (sp >= kStack) {
+          atomicOr(&counters[3], 1ull);
+          return;
+        }
+        stack[sp++] = ch;
+        continue;
+      }
+      const int v = (int)(keys[~ch] & vmask);
+      if (v == i) continue;
+      const double dd = sq_dist(xi, x + 3 * (int64_t)v);
+      if (dd < cur && far_end_of(i, v, off, list, faces)) {
+        cur = dd;
+        atomicMin(best, (unsigned long long)__double_as_longlong(dd));
+      }
+    }
+  }
+}
+
 }  // namespace
 
 void broadphase_free(BroadphaseBuffers &b) {
@@ -670,6 +863,90 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   }
   if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[3], s));
   BP_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+
+void point_tree_free(PointTreeBuffers &b) {
+  void *ptrs[] = {b.pt_lo, b.pt_hi, b.leaf_box, b.node_box, b.node_child, b.node_range, b.parent, b.arrive, b.keys,
+                  b.keys_alt, b.degree, b.off, b.list, b.bounds, b.counters, b.temp};
+  for (void *p : ptrs) cudaFree(p);
+  b = PointTreeBuffers{};
+}
+
+// Returns 0 on success, 2 on a CUDA error (*err), 3 on a malformed tree.
+int closest_vertex_pair(int nv, int nf, const int32_t *faces, const double *x, PointTreeBuffers &b, double *d2,
+                        cudaStream_t s, cudaError_t *err) {
+  *d2 = INFINITY;
+  if (nv < 2 || nf < 1) return 0;
+  if (b.cap_verts < nv || b.cap_faces < nf) {
+    point_tree_free(b);
+    const size_t V = (size_t)nv, F = (size_t)nf;
+    BP_CUDA(cudaMalloc(&b.pt_lo, 3 * V * sizeof(float)));
+    BP_CUDA(cudaMalloc(&b.pt_hi, 3 * V * sizeof(float)));
+    BP_CUDA(cudaMalloc(&b.leaf_box, 8 * V * sizeof(float)));
+    BP_CUDA(cudaMalloc(&b.node_box, 8 * V * sizeof(float)));
+    BP_CUDA(cudaMalloc(&b.node_child, 2 * V * sizeof(int32_t)));
+    BP_CUDA(cudaMalloc(&b.node_range, 2 * V * sizeof(int32_t)));
+    BP_CUDA(cudaMalloc(&b.parent, 2 * V * sizeof(int32_t)));
+    BP_CUDA(cudaMalloc(&b.arrive, V * sizeof(uint32_t)));
+    BP_CUDA(cudaMalloc(&b.keys, V * sizeof(uint64_t)));
+    BP_CUDA(cudaMalloc(&b.keys_alt, V * sizeof(uint64_t)));
+    BP_CUDA(cudaMalloc(&b.degree, V * sizeof(uint32_t)));
+    BP_CUDA(cudaMalloc(&b.off, (V + 1) * sizeof(uint32_t)));
+    BP_CUDA(cudaMalloc(&b.list, 3 * F * sizeof(int32_t)));
+    BP_CUDA(cudaMalloc(&b.bounds, 8 * sizeof(float)));
+    BP_CUDA(cudaMalloc(&b.counters, 8 * sizeof(unsigned long long)));
+    b.temp_bytes = std::max(radix_sort_temp_bytes(nv), scan_temp_bytes(nv));
+    BP_CUDA(cudaMalloc(&b.temp, b.temp_bytes));
+    b.cap_verts = nv;
+    b.cap_faces = nf;
+  }
+  // Incidence lists.
+  BP_CUDA(cudaMemsetAsync(b.degree, 0, (size_t)nv * sizeof(uint32_t), s));
+  incidence_count<<<grid_of(nf), kThreads, 0, s>>>(nf, faces, b.degree);
+  BP_CUDA(cudaGetLastError());
+  BP_CUDA(exclusive_scan_u32(b.degree, b.off, nv, b.off + nv, b.temp, b.temp_bytes, s));
+  BP_CUDA(cudaMemsetAsync(b.degree, 0, (size_t)nv * sizeof(uint32_t), s));
+  incidence_fill<<<grid_of(nf), kThreads, 0, s>>>(nf, faces, b.off, b.degree, b.list);
+  BP_CUDA(cudaGetLastError());
+  // Point tree over the far-end vertices.
+  {
+    const int pinf = 0x7f800000, ninf = (int)(0x80000000u - 0xff800000u);
+    int hb[6] = {pinf, pinf, pinf, ninf, ninf, ninf};
+    BP_CUDA(cudaMemcpyAsync(b.bounds, hb, sizeof(hb), cudaMemcpyHostToDevice, s));
+    // counters[0]: the minimum's bits (+inf); [3]: error word
+    unsigned long long hc[8] = {0x7ff0000000000000ull, 0, 0, 0, 0, 0, 0, 0};
+    BP_CUDA(cudaMemcpyAsync(b.counters, hc, sizeof(hc), cudaMemcpyHostToDevice, s));
+  }
+  point_slabs<<<grid_of(nv), kThreads, 0, s>>>(nv, x, b.degree, b.pt_lo, b.pt_hi, b.bounds);
+  BP_CUDA(cudaGetLastError());
+  KeyBits kb{};
+  kb.fbits = bits_for(nv - 1);
+  kb.mbits = std::min(30, 63 - kb.fbits);
+  kb.ishift = kb.mbits + kb.fbits;
+  kb.fmask = ((uint64_t)1 << kb.fbits) - 1;
+  morton_keys<<<grid_of(nv), kThreads, 0, s>>>(nv, b.pt_lo, b.pt_hi, b.bounds, nullptr, kb, b.keys);
+  BP_CUDA(cudaGetLastError());
+  BP_CUDA(radix_sort_u64(b.keys, b.keys_alt, nullptr, nullptr, nv, 0, kb.ishift, b.temp, b.temp_bytes, s));
+  gather_leaves<3><<<grid_of(nv), kThreads, 0, s>>>(nv, b.keys, kb.fmask, b.pt_lo, b.pt_hi, b.leaf_box);
+  build_lbvh<<<grid_of(nv - 1), kThreads, 0, s>>>(nv, b.keys, b.node_child, b.node_range, b.parent);
+  BP_CUDA(cudaMemsetAsync(b.arrive, 0, (size_t)nv * sizeof(uint32_t), s));
+  refit<3><<<grid_of(nv), kThreads, 0, s>>>(nv, b.node_child, b.parent, b.arrive, b.leaf_box, b.node_box,
+                                            b.counters);
+  BP_CUDA(cudaGetLastError());
+  // Seed the bound, then search.
+  pair_seed<<<grid_of(nv), kThreads, 0, s>>>(nv, b.keys, kb.fmask, x, b.off, b.list, faces, b.counters);
+  pair_search<<<grid_of(nv), kThreads, 0, s>>>(nv, b.keys, kb.fmask, x, b.off, b.list, faces, b.node_child,
+                                               b.leaf_box, b.node_box, b.counters, b.counters);
+  BP_CUDA(cudaGetLastError());
+  unsigned long long hc[4];
+  BP_CUDA(cudaMemcpyAsync(hc, b.counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  BP_CUDA(cudaStreamSynchronize(s));
+  if (hc[3]) return 3;
+  double d;
+  memcpy(&d, &hc[0], sizeof(d));
+  *d2 = d;
   return 0;
 }
 

@@ -84,4 +84,33 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
 
 void broadphase_free(BroadphaseBuffers &buf);
 
+// Device buffers of the closest-vertex-pair search; grown by the caller.
+struct PointTreeBuffers {
+  int64_t cap_verts = 0, cap_faces = 0;
+  float *pt_lo = nullptr, *pt_hi = nullptr;       // [3][nv] outward-rounded FP32 points (empty for non-far ends)
+  float *leaf_box = nullptr, *node_box = nullptr; // [nv][8] point-tree records (AABB layout)
+  int32_t *node_child = nullptr, *node_range = nullptr, *parent = nullptr;
+  uint32_t *arrive = nullptr;
+  uint64_t *keys = nullptr, *keys_alt = nullptr;  // Morton code << vbits | vertex
+  uint32_t *degree = nullptr;                     // [nv] faces per vertex
+  uint32_t *off = nullptr;                        // [nv + 1] incidence offsets
+  int32_t *list = nullptr;                        // [<= 3 nf] faces of each vertex
+  float *bounds = nullptr;
+  unsigned long long *counters = nullptr;         // [0] minimum (bits of a double), [3] error word
+  void *temp = nullptr;
+  size_t temp_bytes = 0;
+};
+
+// The vertex scan of Distance::meshSelfDistance (src/Distance.cpp:21-34):
+// *d2 = the least squared distance (x_i - x_v).squaredNorm(), in the
+// reference's FP64 arithmetic, over vertex pairs (i, v) where some face
+// contains v but not i; +inf when there is none.  x is [nv][3] on the device.
+// Exact: a point LBVH with conservative FP32 bounds prunes only pairs whose
+// FP64 squared distance exceeds the running minimum.  Returns 0, 2 on a CUDA
+// error (*err), 3 on a malformed tree.
+int closest_vertex_pair(int nv, int nf, const int32_t *faces, const double *x, PointTreeBuffers &buf, double *d2,
+                        cudaStream_t s, cudaError_t *err);
+
+void point_tree_free(PointTreeBuffers &buf);
+
 }  // namespace ccd

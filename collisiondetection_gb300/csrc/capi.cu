@@ -245,6 +245,7 @@ int ccd_context_destroy(ccd_context *ctx) {
   cudaFree(ctx->stage.mem);
   cudaFree(ctx->d_surv);
   cudaFree(ctx->d_counters);
+  cudaFree(ctx->dist_mem);
   cudaFreeHost(ctx->h_counters);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;

@@ -4,12 +4,14 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <new>
 #include <string>
 #include <vector>
 
 #include "broadphase.cuh"
 #include "context.cuh"
+#include "distance.cuh"
 #include "mesh.cuh"
 #include "radix_sort.cuh"
 
@@ -74,6 +76,7 @@ struct ccd_mesh {
   uint8_t *fixed = nullptr;
   bool has_fixed = false;
   ccd::BroadphaseBuffers bp;
+  ccd::PointTreeBuffers pt;  // closest-vertex-pair search (self distance)
   // candidates of the last broad phase: [0] vertex-face, [1] edge-edge
   int32_t *cand[2] = {nullptr, nullptr};
   int64_t cand_cap[2] = {0, 0};
@@ -171,14 +174,16 @@ int narrow_device(ccd_mesh *m, Lane &L, int kind, int path, int64_t n, const int
   return CCD_OK;
 }
 
-int run_broadphase(ccd_mesh *m, int kind, double outer_eta) {
+// whole: one mesh even when it is made of instances (faces of different
+// instances are paired too).
+int run_broadphase(ccd_mesh *m, int kind, double outer_eta, bool whole = false) {
   ccd_context *ctx = m->ctx;
   m->have_cand = false;
   m->have_col = false;
   m->stats = ccd_mesh_stats{};
   const ccd::MeshTopology topo{m->nv,         m->nf,         m->nranks,   m->nedges,
                                m->faces,      m->face_rank,  m->rank_triple, m->face_edges,
-                               m->rank_edge,  m->face_inst,  m->ninst};
+                               m->rank_edge,  whole ? nullptr : m->face_inst,  whole ? 1 : m->ninst};
   ccd::BroadphaseParams p{kind, outer_eta, m->qs, m->qe, m->has_fixed ? m->fixed : nullptr,
                           ctx->opt_count_tests != 0, {nullptr, nullptr, nullptr, nullptr}};
   const bool timed = ctx->profiling && m->nf >= 2;
@@ -227,6 +232,7 @@ void free_mesh_buffers(ccd_mesh *m) {
     for (void *p : lp) cudaFree(p);
   }
   ccd::broadphase_free(m->bp);
+  ccd::point_tree_free(m->pt);
   for (cudaEvent_t e : m->bp_ev)
     if (e) cudaEventDestroy(e);
   if (m->fork) cudaEventDestroy(m->fork);
@@ -560,6 +566,64 @@ int ccd_mesh_get_collisions(ccd_mesh *m, int32_t *vf, double *vf_t, int32_t *ee,
   }
   CCD_CUDA(cudaStreamSynchronize(ctx->stream));
   return CCD_OK;
+}
+
+int ccd_mesh_self_distance(ccd_mesh *m, const double *verts, double *distance, int64_t *n_vf, int64_t *n_ee) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  if (!distance) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null distance");
+  int rc = ccd_mesh_set_positions(m, verts, verts);  // the motionless step of src/Distance.cpp:38-39
+  if (rc) return rc;
+  // 1. the vertex scan (src/Distance.cpp:21-35)
+  cudaError_t err = cudaSuccess;
+  double d2 = INFINITY;
+  rc = ccd::closest_vertex_pair(m->nv, m->nf, m->faces, m->qs, m->pt, &d2, ctx->stream, &err);
+  if (rc == 2) return cuda_fail(ctx, err, "closest vertex pair");
+  if (rc == 3) return mesh_fail(m, CCD_ERR_CUDA, "closest vertex pair: malformed tree");
+  const double closest = std::sqrt(d2);
+  // 2. candidates of the AABB broad phase padded by that distance
+  //    (src/Distance.cpp:41-46).  With no qualifying vertex pair every face
+  //    holds every vertex, so every face pair shares a vertex and there is
+  //    no candidate; the broad phase is skipped then.
+  int64_t nvf = 0, nee = 0;
+  if (std::isfinite(closest)) {
+    rc = run_broadphase(m, CCD_BROADPHASE_AABB, closest, /*whole=*/true);
+    if (rc) return rc;
+    nvf = m->n_cand[0];
+    nee = m->n_cand[1];
+  } else {
+    m->stats = ccd_mesh_stats{};
+    m->n_cand[0] = m->n_cand[1] = 0;
+    m->have_cand = true;
+  }
+  // 3. the least stencil distance (src/Distance.cpp:48-64)
+  unsigned long long *best = m->pt.counters ? m->pt.counters + 2 : nullptr;
+  double result = INFINITY;
+  if (nvf + nee > 0 && best) {
+    const unsigned long long inf = 0x7ff0000000000000ull;
+    CCD_CUDA(cudaMemcpyAsync(best, &inf, sizeof(inf), cudaMemcpyHostToDevice, ctx->stream));
+    CCD_CUDA(ccd::launch_stencil_distance_min(m->qs, m->cand[0], nvf, m->cand[1], nee, best, ctx->num_sms,
+                                              ctx->stream));
+    unsigned long long bits = inf;
+    CCD_CUDA(cudaMemcpyAsync(&bits, best, sizeof(bits), cudaMemcpyDeviceToHost, ctx->stream));
+    CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+    memcpy(&result, &bits, sizeof(result));
+  }
+  *distance = result;
+  if (n_vf) *n_vf = nvf;
+  if (n_ee) *n_ee = nee;
+  return CCD_OK;
+}
+
+int ccd_self_distance(ccd_context *ctx, int32_t nverts, const double *verts, int32_t nfaces, const int32_t *faces,
+                      const uint8_t *fixed, double *distance) {
+  ccd_mesh *m = nullptr;
+  int rc = ccd_mesh_create(ctx, nverts, nfaces, faces, &m);
+  if (rc) return rc;
+  if (fixed) rc = ccd_mesh_set_fixed(m, fixed);
+  if (!rc) rc = ccd_mesh_self_distance(m, verts, distance, nullptr, nullptr);
+  ccd_mesh_destroy(m);
+  return rc;
 }
 
 int ccd_mesh_last_stats(const ccd_mesh *m, ccd_mesh_stats *out) {

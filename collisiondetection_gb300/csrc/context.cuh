@@ -68,6 +68,9 @@ struct ccd_context {
   int64_t surv_cap = 0;
   ccd::BatchCounters *d_counters = nullptr;
   ccd::BatchCounters *h_counters = nullptr;
+  // scratch of the distance entry points
+  void *dist_mem = nullptr;
+  size_t dist_cap = 0;
   bool pending_stats = false;
   ccd_batch_stats last{};
   // per-kernel timing

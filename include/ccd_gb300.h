@@ -245,6 +245,52 @@ int ccd_mesh_detect(ccd_mesh *mesh, int broadphase_kind, double outer_eta, doubl
 int ccd_mesh_get_collisions(ccd_mesh *mesh, int32_t *vf, double *vf_t, int32_t *ee, double *ee_t);
 int ccd_mesh_last_stats(const ccd_mesh *mesh, ccd_mesh_stats *out);
 
+/* ------------------------------------------------------------------ distances
+ * The static queries of the reference's Distance class (include/Distance.h),
+ * in FP64 with the reference's operation order: results are bit-identical.
+ * Rows are 12 doubles, the reference's argument points in order:
+ *   vertex-face, vertex-plane  p q0 q1 q2
+ *   edge-edge, line-line       p0 p1 q0 q1 */
+typedef enum {
+  CCD_DISTANCE_VERTEX_FACE = 0, /* Distance::vertexFaceDistance (include/Distance.h:31-113) */
+  CCD_DISTANCE_EDGE_EDGE = 1    /* Distance::edgeEdgeDistance (include/Distance.h:117-170) */
+} ccd_distance_kind;
+
+typedef enum {
+  CCD_DISTANCE_VERTEX_PLANE = 0, /* Distance::vertexPlaneDistanceLessThan (include/Distance.h:13-19) */
+  CCD_DISTANCE_LINE_LINE = 1     /* Distance::lineLineDistanceLessThan (include/Distance.h:21-27) */
+} ccd_distance_predicate;
+
+/* Per row: vec [n][3] the returned vector (closest point of the face or
+ * segment minus p, or the shortest vector between the segments; its norm is
+ * the distance); bary the barycentric coordinates the reference writes
+ * through its reference arguments, [n][3] (q0, q1, q2) for vertex-face,
+ * [n][4] (p0, p1, q0, q1) for edge-edge, or NULL.  Host memory. */
+int ccd_distance_batch(ccd_context *ctx, int kind, int64_t n, const double *rows, double *vec, double *bary);
+/* The same on device memory, enqueued on the context's stream. */
+int ccd_distance_batch_device(ccd_context *ctx, int kind, int64_t n, const double *rows, double *vec, double *bary);
+/* Per row: out[i] = 1 if the predicate holds for eta (eta_count 1 shared value
+ * or n, one per row).  Host memory. */
+int ccd_distance_less_than_batch(ccd_context *ctx, int kind, int64_t n, const double *rows, const double *eta,
+                                 int64_t eta_count, uint8_t *out);
+
+/* Distance::meshSelfDistance (src/Distance.cpp:12-66) on this mesh's faces
+ * and fixed flags (ccd_mesh_set_fixed) at positions verts ([nverts][3] host
+ * memory, which become both the start and end positions of the mesh):
+ *   1. d = the least distance between a vertex i and a vertex of a face that
+ *      does not contain i;
+ *   2. the AABB broad phase with outer_eta = d on the motionless step;
+ *   3. *distance = the least norm of vertexFaceDistance / edgeEdgeDistance
+ *      over its stencils (+inf when there are none).
+ * n_vf / n_ee (optional) receive the numbers of stencils checked, which the
+ * reference prints.  The candidates stay available to ccd_broadphase_get.
+ * A mesh made of instances is measured as the one mesh they form together. */
+int ccd_mesh_self_distance(ccd_mesh *mesh, const double *verts, double *distance, int64_t *n_vf, int64_t *n_ee);
+/* The same for a mesh given by value, as the reference's static call takes
+ * it: faces [nfaces][3], fixed nverts flags or NULL. */
+int ccd_self_distance(ccd_context *ctx, int32_t nverts, const double *verts, int32_t nfaces, const int32_t *faces,
+                      const uint8_t *fixed, double *distance);
+
 /* ------------------------------------------------------------------ serving
  * No counterpart in the reference (its detection runs in the caller's
  * thread).  A server runs collision queries for many callers at once on one

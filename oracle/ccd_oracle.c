@@ -1340,3 +1340,161 @@ void oracle_narrowphase(int nverts, const double *qstart, const double *qend, in
   np_worker(&jobs[0]);
   for (int w = 1; w < nthreads; w++) pthread_join(th[w], NULL);
 }
+
+/* ------------------------------------------------------------ Distance (include/Distance.h, src/Distance.cpp) */
+/* Distance::clamp (include/Distance.h:182-185). */
+static double dclamp(double u) { return smin(1.0, smax(u, 0.0)); }
+
+/* Distance::vertexFaceDistance (include/Distance.h:31-113). */
+static vec3 vf_distance(vec3 p, vec3 q0, vec3 q1, vec3 q2, double *b) {
+  vec3 ab = vsub(q1, q0), ac = vsub(q2, q0), ap = vsub(p, q0);
+  double d1 = vdot(ab, ap), d2 = vdot(ac, ap);
+  if (d1 <= 0 && d2 <= 0) {
+    b[0] = 1.0; b[1] = 0.0; b[2] = 0.0;
+    return vsub(q0, p);
+  }
+  vec3 bp = vsub(p, q1);
+  double d3 = vdot(ab, bp), d4 = vdot(ac, bp);
+  if (d3 >= 0 && d4 <= d3) {
+    b[0] = 0.0; b[1] = 1.0; b[2] = 0.0;
+    return vsub(q1, p);
+  }
+  double vc = d1 * d4 - d3 * d2;
+  if ((vc <= 0) && (d1 >= 0) && (d3 <= 0)) {
+    double v = d1 / (d1 - d3);
+    b[0] = 1.0 - v; b[1] = v; b[2] = 0;
+    return vsub(vadd(q0, vscale(v, ab)), p);
+  }
+  vec3 cp = vsub(p, q2);
+  double d5 = vdot(ab, cp), d6 = vdot(ac, cp);
+  if (d6 >= 0 && d5 <= d6) {
+    b[0] = 0; b[1] = 0; b[2] = 1.0;
+    return vsub(q2, p);
+  }
+  double vb = d5 * d2 - d1 * d6;
+  if ((vb <= 0) && (d2 >= 0) && (d6 <= 0)) {
+    double w = d2 / (d2 - d6);
+    b[0] = 1 - w; b[1] = 0; b[2] = w;
+    return vsub(vadd(q0, vscale(w, ac)), p);
+  }
+  double va = d3 * d6 - d5 * d4;
+  if ((va <= 0) && (d4 - d3 >= 0) && (d5 - d6 >= 0)) {
+    double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+    b[0] = 0; b[1] = 1.0 - w; b[2] = w;
+    return vsub(vadd(q1, vscale(w, vsub(q2, q1))), p);
+  }
+  double denom = 1.0 / (va + vb + vc);
+  double v = vb * denom, w = vc * denom;
+  double u = 1.0 - v - w;
+  b[0] = u; b[1] = v; b[2] = w;
+  return vsub(vadd(vadd(vscale(u, q0), vscale(v, q1)), vscale(w, q2)), p);
+}
+
+/* Distance::edgeEdgeDistance (include/Distance.h:117-170). */
+static vec3 ee_distance(vec3 p0, vec3 p1, vec3 q0, vec3 q1, double *bary) {
+  vec3 d1 = vsub(p1, p0), d2 = vsub(q1, q0), r = vsub(p0, q0);
+  double a = vdot(d1, d1), e = vdot(d2, d2), f = vdot(d2, r);
+  double s, t;
+  double c = vdot(d1, r), b = vdot(d1, d2);
+  double denom = a * e - b * b;
+  if (denom != 0.0)
+    s = dclamp((b * f - c * e) / denom);
+  else
+    s = 0;
+  double tnom = b * s + f;
+  if (tnom < 0 || e == 0) {
+    t = 0;
+    if (a == 0) s = 0;
+    else s = dclamp(-c / a);
+  } else if (tnom > e) {
+    t = 1.0;
+    if (a == 0) s = 0;
+    else s = dclamp((b - c) / a);
+  } else {
+    t = tnom / e;
+  }
+  vec3 c1 = vadd(p0, vscale(s, d1)), c2 = vadd(q0, vscale(t, d2));
+  bary[0] = 1.0 - s; bary[1] = s; bary[2] = 1.0 - t; bary[3] = t;
+  return vsub(c2, c1);
+}
+
+void oracle_distance_batch(int kind, int64_t n, const double *rows, double *vec, double *bary) {
+  for (int64_t i = 0; i < n; i++) {
+    const double *x = rows + 12 * i;
+    double b[4];
+    vec3 r = kind == 0 ? vf_distance(v3(x), v3(x + 3), v3(x + 6), v3(x + 9), b)
+                       : ee_distance(v3(x), v3(x + 3), v3(x + 6), v3(x + 9), b);
+    vec[3 * i] = r.x; vec[3 * i + 1] = r.y; vec[3 * i + 2] = r.z;
+    if (bary)
+      for (int k = 0; k < (kind == 0 ? 3 : 4); k++) bary[(kind == 0 ? 3 : 4) * i + k] = b[k];
+  }
+}
+
+/* Distance::vertexPlaneDistanceLessThan / lineLineDistanceLessThan
+ * (include/Distance.h:13-27). */
+void oracle_distance_less_than(int kind, int64_t n, const double *rows, const double *eta, int eta_per_row,
+                               uint8_t *out) {
+  for (int64_t i = 0; i < n; i++) {
+    const double *x = rows + 12 * i;
+    double e = eta[eta_per_row ? i : 0];
+    vec3 a = v3(x), b = v3(x + 3), c = v3(x + 6), d = v3(x + 9);
+    vec3 cr;
+    double s;
+    if (kind == 0) {
+      cr = vcross(vsub(c, b), vsub(d, b));
+      s = vdot(cr, vsub(a, b));
+    } else {
+      cr = vcross(vsub(b, a), vsub(d, c));
+      s = vdot(cr, vsub(c, a));
+    }
+    out[i] = (uint8_t)(s * s < e * e * vdot(cr, cr));
+  }
+}
+
+/* Distance::meshSelfDistance (src/Distance.cpp:12-66). */
+double oracle_mesh_self_distance(int nverts, const double *verts, int nfaces, const int32_t *faces,
+                                 const uint8_t *fixed, int64_t *n_vf, int64_t *n_ee) {
+  double closest = INFINITY;
+  for (int i = 0; i < nverts; i++) {
+    for (int j = 0; j < nfaces; j++) {
+      const int32_t *fj = faces + 3 * (int64_t)j;
+      if (fj[0] == i || fj[1] == i || fj[2] == i) continue; /* Mesh::vertexOfFace (src/Mesh.cpp:5-11) */
+      for (int k = 0; k < 3; k++) {
+        vec3 d = vsub(v3(verts + 3 * (int64_t)i), v3(verts + 3 * (int64_t)fj[k]));
+        double dist = vdot(d, d);
+        if (dist < closest) closest = dist;
+      }
+    }
+  }
+  closest = sqrt(closest);
+  int64_t nvf = 0, nee = 0;
+  if (oracle_broadphase(1, nverts, verts, verts, nfaces, faces, closest, fixed, &nvf, &nee) != 0) return NAN;
+  int32_t *vf = (int32_t *)malloc((size_t)(4 * nvf + 1) * sizeof(int32_t));
+  int32_t *ee = (int32_t *)malloc((size_t)(4 * nee + 1) * sizeof(int32_t));
+  if (!vf || !ee) {
+    free(vf);
+    free(ee);
+    return NAN;
+  }
+  oracle_broadphase_get(vf, ee);
+  closest = INFINITY;
+  for (int64_t i = 0; i < nvf; i++) {
+    const int32_t *s = vf + 4 * i;
+    double b[3];
+    double dist = vnorm(vf_distance(v3(verts + 3 * (int64_t)s[0]), v3(verts + 3 * (int64_t)s[1]),
+                                    v3(verts + 3 * (int64_t)s[2]), v3(verts + 3 * (int64_t)s[3]), b));
+    if (dist < closest) closest = dist;
+  }
+  for (int64_t i = 0; i < nee; i++) {
+    const int32_t *s = ee + 4 * i;
+    double b[4];
+    double dist = vnorm(ee_distance(v3(verts + 3 * (int64_t)s[0]), v3(verts + 3 * (int64_t)s[1]),
+                                    v3(verts + 3 * (int64_t)s[2]), v3(verts + 3 * (int64_t)s[3]), b));
+    if (dist < closest) closest = dist;
+  }
+  free(vf);
+  free(ee);
+  if (n_vf) *n_vf = nvf;
+  if (n_ee) *n_ee = nee;
+  return closest;
+}

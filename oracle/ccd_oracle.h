@@ -57,6 +57,19 @@ void oracle_narrowphase(int nverts, const double *qstart, const double *qend, in
                         uint8_t *ee_hit, double *vf_t, double *ee_t, int8_t *vf_which, int8_t *ee_which,
                         int nthreads);
 
+/* Distance (include/Distance.h): rows of 12 doubles, (p, q0, q1, q2) for
+ * kind 0 and (p0, p1, q0, q1) for kind 1.  oracle_distance_batch:
+ * vertexFaceDistance (0) / edgeEdgeDistance (1), vec [n][3], bary [n][3|4] or
+ * NULL.  oracle_distance_less_than: vertexPlaneDistanceLessThan (0) /
+ * lineLineDistanceLessThan (1). */
+void oracle_distance_batch(int kind, int64_t n, const double *rows, double *vec, double *bary);
+void oracle_distance_less_than(int kind, int64_t n, const double *rows, const double *eta, int eta_per_row,
+                               uint8_t *out);
+/* Distance::meshSelfDistance (src/Distance.cpp:12-66), its O(V F) vertex scan
+ * included; n_vf / n_ee receive the stencil counts it checks (may be NULL). */
+double oracle_mesh_self_distance(int nverts, const double *verts, int nfaces, const int32_t *faces,
+                                 const uint8_t *fixed, int64_t *n_vf, int64_t *n_ee);
+
 /* Stencil canonical forms (src/Stencils.h): writes the canonical 4-tuple. */
 void oracle_vf_canon(int p, int q0, int q1, int q2, int32_t *out);
 void oracle_ee_canon(int p0, int p1, int q0, int q1, int32_t *out);

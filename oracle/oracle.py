@@ -42,6 +42,31 @@ class _Lib:
             fn.argtypes = [_P, ctypes.c_double, _P]
             fn.restype = ctypes.c_int
 
+    def _distance_setup(self):
+        L, pre = self.lib, self.prefix
+        getattr(L, f"{pre}_distance_batch").argtypes = [ctypes.c_int, _I64, _P, _P, _P]
+        getattr(L, f"{pre}_distance_less_than").argtypes = [ctypes.c_int, _I64, _P, _P, ctypes.c_int, _P]
+
+    def distance(self, kind: int, rows):
+        """Distance::vertexFaceDistance (0) / edgeEdgeDistance (1) per row of
+        12 doubles; returns (vec [n][3], bary [n][3|4])."""
+        rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 12)
+        n = rows.shape[0]
+        vec = np.zeros((n, 3))
+        bary = np.zeros((n, 3 if kind == 0 else 4))
+        getattr(self.lib, f"{self.prefix}_distance_batch")(kind, n, _ptr(rows), _ptr(vec), _ptr(bary))
+        return vec, bary
+
+    def distance_less_than(self, kind: int, rows, eta):
+        """vertexPlaneDistanceLessThan (0) / lineLineDistanceLessThan (1)."""
+        rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 12)
+        n = rows.shape[0]
+        eta_a = np.ascontiguousarray(np.atleast_1d(np.asarray(eta, dtype=np.float64)))
+        per = 1 if eta_a.size == n and n != 1 else 0
+        out = np.zeros(n, np.uint8)
+        getattr(self.lib, f"{self.prefix}_distance_less_than")(kind, n, _ptr(rows), _ptr(eta_a), per, _ptr(out))
+        return out
+
     def prim(self, kind: str, x, eta: float):
         """One primitive test; returns (hit, t or None)."""
         x = np.ascontiguousarray(x, dtype=np.float64).ravel()
@@ -64,6 +89,19 @@ class Oracle(_Lib):
         L.oracle_broadphase_face_pairs.restype = ctypes.c_int64
         L.oracle_narrowphase.argtypes = [ctypes.c_int, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P,
                                          ctypes.c_int]
+        L.oracle_mesh_self_distance.argtypes = [ctypes.c_int, _P, ctypes.c_int, _P, _P, _P, _P]
+        L.oracle_mesh_self_distance.restype = ctypes.c_double
+        self._distance_setup()
+
+    def mesh_self_distance(self, verts, faces, fixed=None):
+        """Distance::meshSelfDistance; returns (distance, n_vf, n_ee)."""
+        verts = np.ascontiguousarray(verts, dtype=np.float64).ravel()
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        nvf, nee = ctypes.c_int64(), ctypes.c_int64()
+        d = self.lib.oracle_mesh_self_distance(verts.size // 3, _ptr(verts), faces.shape[0], _ptr(faces), _ptr(fx),
+                                               ctypes.byref(nvf), ctypes.byref(nee))
+        return float(d), int(nvf.value), int(nee.value)
 
     def batch(self, kind: int, x, eta, nthreads: int = 1):
         """kind 0..3 (VF, EE, VE, VV); eta scalar or per-row.  Returns
@@ -125,6 +163,16 @@ class Reference(_Lib):
                                      _P]
         L.ref_broadphase_get.argtypes = [_P, _P]
         L.ref_narrowphase.argtypes = [ctypes.c_int, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P]
+        L.ref_mesh_self_distance.argtypes = [ctypes.c_int, _P, ctypes.c_int, _P, _P]
+        L.ref_mesh_self_distance.restype = ctypes.c_double
+        self._distance_setup()
+
+    def mesh_self_distance(self, verts, faces, fixed=None) -> float:
+        verts = np.ascontiguousarray(verts, dtype=np.float64).ravel()
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        return float(self.lib.ref_mesh_self_distance(verts.size // 3, _ptr(verts), faces.shape[0], _ptr(faces),
+                                                     _ptr(fx)))
 
     @staticmethod
     def available() -> bool:

@@ -2,7 +2,7 @@
 //
 // extern "C" wrapper over the reference library's own, unmodified sources
 // (src/CTCD.cpp, src/History.cpp, src/Mesh.cpp, src/KDOPBroadPhase.cpp,
-// src/AABBBroadPhase.cpp, src/CTCDNarrowPhase.cpp), compiled by
+// src/AABBBroadPhase.cpp, src/CTCDNarrowPhase.cpp, src/Distance.cpp), compiled by
 // oracle/Makefile against the project-written Eigen-API subset.  It exists so
 // that tests/golden/make_golden.py can pin the C restatement (ccd_oracle.c)
 // against the reference itself.  The reference tree is only present in the
@@ -14,6 +14,7 @@
 
 #include "CTCD.h"
 #include "CTCDNarrowPhase.h"
+#include "Distance.h"
 #include "History.h"
 #include "KDOPBroadPhase.h"
 #include "Mesh.h"
@@ -141,6 +142,45 @@ void ref_narrowphase(int nverts, const double *qstart, const double *qend, int64
     vf_hit[i] = (uint8_t)ovf.count(VertexFaceStencil(vf[4 * i], vf[4 * i + 1], vf[4 * i + 2], vf[4 * i + 3]));
   for (int64_t i = 0; i < n_ee; i++)
     ee_hit[i] = (uint8_t)oee.count(EdgeEdgeStencil(ee[4 * i], ee[4 * i + 1], ee[4 * i + 2], ee[4 * i + 3]));
+}
+
+// ---------------------------------------------------------------- distances
+// Distance::vertexFaceDistance (kind 0) / edgeEdgeDistance (kind 1) over rows
+// of 12 doubles; vec [n][3], bary [n][3|4].
+void ref_distance_batch(int kind, int64_t n, const double *x, double *vec, double *bary) {
+  for (int64_t i = 0; i < n; i++) {
+    const double *r = x + 12 * i;
+    Vector3d v;
+    if (kind == 0) {
+      double *b = bary + 3 * i;
+      v = Distance::vertexFaceDistance(v3(r), v3(r + 3), v3(r + 6), v3(r + 9), b[0], b[1], b[2]);
+    } else {
+      double *b = bary + 4 * i;
+      v = Distance::edgeEdgeDistance(v3(r), v3(r + 3), v3(r + 6), v3(r + 9), b[0], b[1], b[2], b[3]);
+    }
+    for (int k = 0; k < 3; k++) vec[3 * i + k] = v[k];
+  }
+}
+
+// Distance::vertexPlaneDistanceLessThan (kind 0) / lineLineDistanceLessThan (kind 1).
+void ref_distance_less_than(int kind, int64_t n, const double *x, const double *eta, int eta_per_row, uint8_t *out) {
+  for (int64_t i = 0; i < n; i++) {
+    const double *r = x + 12 * i;
+    const double e = eta_per_row ? eta[i] : eta[0];
+    out[i] = (uint8_t)(kind == 0 ? Distance::vertexPlaneDistanceLessThan(v3(r), v3(r + 3), v3(r + 6), v3(r + 9), e)
+                                 : Distance::lineLineDistanceLessThan(v3(r), v3(r + 3), v3(r + 6), v3(r + 9), e));
+  }
+}
+
+// Distance::meshSelfDistance (src/Distance.cpp:12-66); fixed may be NULL.
+double ref_mesh_self_distance(int nverts, const double *q, int nfaces, const int32_t *faces, const uint8_t *fixed) {
+  Mesh m;
+  build_mesh(nverts, q, nfaces, faces, m);
+  std::set<int> fixedVerts;
+  if (fixed)
+    for (int i = 0; i < nverts; i++)
+      if (fixed[i]) fixedVerts.insert(i);
+  return Distance::meshSelfDistance(vecx(nverts, q), m.faces, fixedVerts);
 }
 
 }  // extern "C"

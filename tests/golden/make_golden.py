@@ -13,15 +13,24 @@ the reference's example meshes, and writes:
   pairs meshes/test1.obj -> test2.obj and meshes/V0_prob3_402.obj ->
   V1_prob3_402.obj, with digests of the reference's k-DOP and AABB candidate
   sets and its CTCD narrow-phase result.
+* ``distances.npz`` / ``distances.json`` -- the reference's Distance class:
+  vertexFaceDistance / edgeEdgeDistance vectors and barycentric coordinates
+  and the two distance predicates on seeded and hand-built rows, and
+  meshSelfDistance (with the stencil counts it prints) on the meshes above, on
+  meshes/V0_prob11_835.obj, on a small sheet over a sphere and on hand-built
+  small meshes.
 
-Only runs where the reference tree exists:  python tests/golden/make_golden.py
+Only runs where the reference tree exists:
+    python tests/golden/make_golden.py [--only distances]
 """
 from __future__ import annotations
 
 import hashlib
 import json
 import os
+import re
 import sys
+import tempfile
 
 import numpy as np
 
@@ -111,11 +120,139 @@ def edge_cases(kind: int) -> np.ndarray:
     return np.array(rows, np.float64)
 
 
+def distance_rows(kind: int) -> np.ndarray:
+    """Seeded and hand-built rows (12 doubles) for one Distance query kind:
+    0 = (p, q0, q1, q2), 1 = (p0, p1, q0, q1)."""
+    rng = np.random.default_rng(5000 + kind)
+    rows = [rng.uniform(-1, 1, size=(600, 12)), rng.normal(0, 1e-3, size=(100, 12)) + rng.uniform(0, 1, (1, 12))]
+    tri = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float)
+    if kind == 0:
+        # every Voronoi region of a triangle, above, on and below its plane
+        for x in (-0.5, 0.0, 0.25, 0.5, 1.0, 1.5):
+            for y in (-0.5, 0.0, 0.25, 0.5, 1.0, 1.5):
+                for z in (-1.0, 0.0, 1e-9, 1.0):
+                    rows.append(np.concatenate([[x, y, z], tri.ravel()])[None])
+        degenerate = [
+            [[0.3, 0.3, 1], [0, 0, 0], [1, 1, 1], [2, 2, 2]],    # collinear triangle
+            [[0.3, 0.3, 1], [1, 1, 1], [1, 1, 1], [1, 1, 1]],    # all three vertices coincide
+            [[1, 1, 1], [1, 1, 1], [1, 1, 1], [1, 1, 1]],        # everything coincides
+            [[0.2, 0.2, 0], [0, 0, 0], [1, 0, 0], [0, 1, 0]],    # p inside the triangle
+            [[0.5, 0, 0], [0, 0, 0], [1, 0, 0], [0, 1, 0]],      # p on an edge
+            [[1, 0, 0], [0, 0, 0], [1, 0, 0], [0, 1, 0]],        # p on a vertex
+            [[0.5, 0.5, 0.5], [0, 0, 0], [1, 0, 0], [1, 0, 0]],  # two coincident vertices
+        ]
+    else:
+        degenerate = [
+            [[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0]],        # parallel (denominator 0)
+            [[0, 0, 0], [1, 0, 0], [2, 0, 0], [3, 0, 0]],        # collinear, apart
+            [[0, 0, 0], [2, 0, 0], [1, 0, 0], [3, 0, 0]],        # collinear, overlapping
+            [[0, 0, 0], [0, 0, 0], [1, 1, 1], [2, 0, 1]],        # first edge a point
+            [[0, 0, 0], [1, 0, 0], [1, 1, 1], [1, 1, 1]],        # second edge a point
+            [[1, 1, 1], [1, 1, 1], [1, 1, 1], [1, 1, 1]],        # both points, coincident
+            [[0, 0, 0], [1, 0, 0], [0.5, -1, 0], [0.5, 1, 0]],   # crossing
+            [[0, 0, 0], [1, 0, 0], [0.5, -1, 1], [0.5, 1, 1]],   # skew, closest inside both
+            [[0, 0, 0], [1, 0, 0], [2, -1, 1], [2, 1, 1]],       # skew, clamped
+            [[0, 0, 0], [1, 0, 0], [-2, 1, 0], [-1, 1, 1e-12]],  # nearly parallel
+        ]
+    rows.append(np.array(degenerate, float).reshape(-1, 12))
+    base = rng.uniform(0, 1, size=(50, 12))
+    rows += [base * 1e6, base * 1e-6, base + 1e4]
+    nonfinite = base[:4].copy()
+    nonfinite[0, 0] = np.nan
+    nonfinite[1, 4] = np.inf
+    nonfinite[2, 9] = -np.inf
+    nonfinite[3, :] = np.nan
+    rows.append(nonfinite)
+    return np.concatenate(rows).astype(np.float64)
+
+
+def small_meshes():
+    """Hand-built small meshes for meshSelfDistance: (verts [V][3], faces)."""
+    out = {}
+    out["one_triangle"] = (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float), np.array([[0, 1, 2]], np.int32))
+    out["two_triangles"] = (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.2, 0.2, 0.5], [1.2, 0.2, 0.5],
+                                      [0.2, 1.2, 0.6]], float), np.array([[0, 1, 2], [3, 4, 5]], np.int32))
+    out["shared_edge"] = (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0.1]], float),
+                          np.array([[0, 1, 2], [1, 3, 2]], np.int32))
+    out["coincident_copies"] = (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]] * 2, float),
+                                np.array([[0, 1, 2], [3, 4, 5]], np.int32))
+    out["isolated_vertex"] = (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.3, 0.3, 0.01]], float),
+                              np.array([[0, 1, 2]], np.int32))
+    out["repeated_index"] = (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float),
+                             np.array([[0, 0, 1], [2, 3, 3]], np.int32))
+    return out
+
+
+def stdout_of(fn, *args):
+    """Runs fn(*args) and returns (its result, what it wrote to file
+    descriptor 1): the reference prints its stencil counts there."""
+    sys.stdout.flush()
+    saved = os.dup(1)
+    with tempfile.TemporaryFile() as tmp:
+        os.dup2(tmp.fileno(), 1)
+        try:
+            result = fn(*args)
+        finally:
+            os.dup2(saved, 1)
+            os.close(saved)
+        tmp.seek(0)
+        text = tmp.read().decode()
+    return result, text
+
+
+def distance_fixtures(ref) -> None:
+    arrays, meta = {}, {"queries": {}, "self_distance": {}}
+    for kind in (0, 1):
+        rows = distance_rows(kind)
+        vec, bary = ref.distance(kind, rows)
+        eta = np.random.default_rng(6000 + kind).uniform(0, 0.5, rows.shape[0])
+        less = ref.distance_less_than(kind, rows, eta)
+        arrays[f"rows{kind}"] = rows
+        arrays[f"vec{kind}"] = vec
+        arrays[f"bary{kind}"] = bary
+        arrays[f"eta{kind}"] = eta
+        arrays[f"less{kind}"] = less
+        meta["queries"][str(kind)] = {"rows": int(rows.shape[0]), "less_true": int(less.sum())}
+    meshes = {}
+    qs, _, f = W.two_spheres(seed=1)
+    meshes["spheres"] = (qs.reshape(-1, 3), f)
+    v0, f0 = load_obj(os.path.join(REF_TREE, "meshes", "test1.obj"))
+    meshes["test1"] = (v0, f0)
+    v0, f0 = load_obj(os.path.join(REF_TREE, "meshes", "V0_prob3_402.obj"))
+    meshes["prob3"] = (v0, f0)
+    v0, f0 = load_obj(os.path.join(REF_TREE, "meshes", "V0_prob11_835.obj"))
+    meshes["prob11"] = (v0, f0)
+    f, frames = W.cloth_frames(grid=24, level=2, seed=3, steps=1)
+    meshes["cloth"] = (frames[0].reshape(-1, 3), f)
+    meshes.update(small_meshes())
+    for name, (v, f) in meshes.items():
+        v = np.ascontiguousarray(v, np.float64)
+        f = np.ascontiguousarray(f, np.int32)
+        arrays[f"mesh_{name}_verts"] = v
+        arrays[f"mesh_{name}_faces"] = f
+        fixed = np.zeros(v.shape[0], np.uint8)
+        fixed[: v.shape[0] // 2] = 1
+        arrays[f"mesh_{name}_fixed"] = fixed
+        entry = {}
+        for label, fx in (("free", None), ("fixed", fixed)):
+            d, text = stdout_of(ref.mesh_self_distance, v, f, fx)
+            m = re.search(r"Checking (\d+) vertex-face and (\d+) edge-edge stencils", text)
+            entry[label] = {"distance_hex": float(d).hex(), "distance": d,
+                            "n_vf": int(m.group(1)), "n_ee": int(m.group(2))}
+        meta["self_distance"][name] = entry
+    np.savez_compressed(os.path.join(HERE, "distances.npz"), **arrays)
+    with open(os.path.join(HERE, "distances.json"), "w") as fh:
+        json.dump(meta, fh, indent=1, sort_keys=True)
+
+
 def main() -> None:
     if not os.path.isdir(REF_TREE):
         sys.exit(f"reference tree not found at {REF_TREE}")
     O.build(ref=True)
     ref = O.Reference()
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "distances":
+        distance_fixtures(ref)
+        return
 
     kat = []
     for name, pts in KAT:
@@ -173,6 +310,7 @@ def main() -> None:
     np.savez_compressed(os.path.join(HERE, "meshes.npz"), **arrays)
     with open(os.path.join(HERE, "meshes.json"), "w") as fh:
         json.dump(meta, fh, indent=1, sort_keys=True)
+    distance_fixtures(ref)
     print("wrote", sorted(os.listdir(HERE)))
 
 

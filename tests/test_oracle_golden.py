@@ -86,3 +86,34 @@ def test_stencil_canonical_forms(oracle):
     assert list(r) == [2, 8, 4, 9]
     oracle.lib.oracle_ee_canon(1, 4, 8, 2, r)
     assert list(r) == [1, 4, 2, 8]
+
+
+def _same_bits(a, b):
+    """Equal bit for bit, NaN matching any NaN."""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return (a.view(np.uint64) == b.view(np.uint64)) | (np.isnan(a) & np.isnan(b))
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_distance_queries_bit_exact(oracle, golden_dir, kind):
+    g = np.load(os.path.join(golden_dir, "distances.npz"))
+    rows = g[f"rows{kind}"]
+    vec, bary = oracle.distance(kind, rows)
+    assert _same_bits(vec, g[f"vec{kind}"]).all()
+    assert _same_bits(bary, g[f"bary{kind}"]).all()
+    less = oracle.distance_less_than(kind, rows, g[f"eta{kind}"])
+    np.testing.assert_array_equal(less, g[f"less{kind}"])
+    assert 0 < less.sum() < less.size
+
+
+@pytest.mark.parametrize("mesh", ["spheres", "test1", "prob3", "prob11", "cloth", "one_triangle", "two_triangles",
+                                  "shared_edge", "coincident_copies", "isolated_vertex", "repeated_index"])
+def test_mesh_self_distance(oracle, golden_dir, mesh):
+    meta = json.load(open(os.path.join(golden_dir, "distances.json")))["self_distance"][mesh]
+    g = np.load(os.path.join(golden_dir, "distances.npz"))
+    v, f, fixed = g[f"mesh_{mesh}_verts"], g[f"mesh_{mesh}_faces"], g[f"mesh_{mesh}_fixed"]
+    for label, fx in (("free", None), ("fixed", fixed)):
+        d, nvf, nee = oracle.mesh_self_distance(v, f, fx)
+        exp = meta[label]
+        assert float(d).hex() == exp["distance_hex"]
+        assert (nvf, nee) == (exp["n_vf"], exp["n_ee"])
