@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--mesh", type=int, default=1, help="also time the mesh configurations (1) or not (0)")
     ap.add_argument("--uneven-instances", type=int, default=8,
                     help="instances of the uneven-batch sample (0: skip; the configuration has 512)")
+    ap.add_argument("--distance", type=int, default=1,
+                    help="also time meshSelfDistance and the closest-point batches (1) or not (0)")
     ap.add_argument("--serve", type=int, default=1, help="also run the serving loop (1) or not (0)")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0])
@@ -275,6 +277,106 @@ def mesh_section(ctx, stream, rank, args):
         bp, nph = oracle_steps(frames, faces, 1e-6, idx)
         out["cloth_on_sphere_kdop"]["cpu_oracle"] = {"broadphase_ms": bp, "narrowphase_ms": nph, "sample_steps": idx,
                                                     "cores": {"broadphase": 1, "narrowphase": threads}}
+    return out
+
+
+def distance_section(ctx, stream, rank, args):
+    """Distance::meshSelfDistance (src/Distance.cpp:12-66) and the closest-point
+    batch kernels.
+
+    self_distance: wall time of ccd_mesh_self_distance (positions copied from
+    host memory, the vertex scan on a point tree, the AABB broad phase, the
+    stencil minimum, result read back) on the two-sphere start frame (2,560
+    faces) and on one sheet-on-sphere frame (211,970 faces).  The oracle is
+    timed beside it on one core: the whole call on the spheres; on the sheet,
+    its O(V F) vertex scan over a bounded sample of vertices, scaled to all of
+    them, plus its broad phase and stencil stage at the same padding.
+
+    closest_point_batch: 10M vertex-face + 10M edge-edge rows of 12 doubles
+    resident in HBM through ccd_distance_batch_device (vectors and barycentric
+    coordinates out), timed with CUDA events on the launching stream; HBM
+    roofline with 96 B in + 24 B vector + 24 (32) B barycentrics per row."""
+    import torch
+
+    import collisiondetection_gb300 as C
+    from collisiondetection_gb300 import workloads as W
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    orc = O.Oracle()
+    out = {}
+    qs, _, f_sph = W.two_spheres(seed=1)
+    f_cl, frames = W.cloth_frames(grid=args.cloth_grid, level=args.cloth_level, seed=0, steps=2)
+    cases = (("two_spheres", qs.reshape(-1, 3), f_sph), ("cloth_on_sphere", frames[1].reshape(-1, 3), f_cl))
+    for name, v, f in cases:
+        v = np.ascontiguousarray(v, np.float64)
+        with C.Mesh(ctx, f, nverts=v.shape[0]) as m:
+            for _ in range(3):
+                m.self_distance(v)
+            dts = []
+            for _ in range(10):
+                t0 = time.perf_counter()
+                d, nvf, nee = m.self_distance(v)
+                dts.append(time.perf_counter() - t0)
+            eta = m.stats()["self_distance_eta"]
+        entry = {"faces": int(f.shape[0]), "vertices": int(v.shape[0]), "distance": d, "padding": eta,
+                 "stencils": {"vf": nvf, "ee": nee}, "ms": 1e3 * statistics.median(dts),
+                 "ms_min": 1e3 * min(dts)}
+        if rank == 0:
+            nv = v.shape[0]
+            if f.shape[0] <= 10_000:
+                t0 = time.perf_counter()
+                d_ref, _, _ = orc.mesh_self_distance(v, f)
+                entry["cpu_oracle"] = {"ms": 1e3 * (time.perf_counter() - t0), "cores": 1, "sample": "whole call",
+                                       "same_result": float(d_ref).hex() == float(d).hex()}
+            else:
+                sample = max(1, nv // 128)
+                t0 = time.perf_counter()
+                orc.vertex_scan(v, f, 0, sample)
+                scan_ms = 1e3 * (time.perf_counter() - t0) * nv / sample
+                t0 = time.perf_counter()
+                vf, ee = orc.broadphase(1, v.ravel(), v.ravel(), f, eta)
+                orc.distance(0, v[vf].reshape(-1, 12))
+                orc.distance(1, v[ee].reshape(-1, 12))
+                rest_ms = 1e3 * (time.perf_counter() - t0)
+                entry["cpu_oracle"] = {"ms": scan_ms + rest_ms, "vertex_scan_ms": scan_ms,
+                                       "broadphase_and_stencils_ms": rest_ms, "cores": 1,
+                                       "sample": f"vertex scan over {sample} of {nv} vertices, scaled"}
+        out[name] = entry
+    # closest-point batch throughput, rows resident in HBM
+    n = 10_000_000
+    g = torch.Generator(device="cuda").manual_seed(7)
+    peak, src = measured_peaks()
+    batch = {}
+    total_ms, total_bytes = 0.0, 0
+    for kind, label, nb in ((C.DISTANCE_VERTEX_FACE, "vertex_face", 3), (C.DISTANCE_EDGE_EDGE, "edge_edge", 4)):
+        rows = torch.rand((n, 12), generator=g, device="cuda", dtype=torch.float64)
+        vec = torch.empty((n, 3), device="cuda", dtype=torch.float64)
+        bary = torch.empty((n, nb), device="cuda", dtype=torch.float64)
+        for _ in range(3):
+            ctx.distance_device(kind, n, rows.data_ptr(), vec.data_ptr(), bary.data_ptr())
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 5
+        e0.record(stream)
+        for _ in range(reps):
+            ctx.distance_device(kind, n, rows.data_ptr(), vec.data_ptr(), bary.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        nbytes = n * (96 + 24 + 8 * nb)
+        batch[label] = {"rows": n, "ms_per_launch": ms, "rows_per_s": n / (ms / 1e3),
+                        "achieved_gbs": nbytes / (ms / 1e3) / 1e9}
+        total_ms += ms
+        total_bytes += nbytes
+        del rows, vec, bary
+    batch["roofline"] = {"kernel": "distance_rows<0|1>", "bound": "hbm", "achieved": total_bytes / (total_ms / 1e3) / 1e9,
+                         "peak": peak, "unit": "GB/s", "frac": total_bytes / (total_ms / 1e3) / 1e9 / peak,
+                         "peak_source": f"{src} hbm_gbs",
+                         "note": "inputs (0.96 GB per kind) larger than L2; algorithmic bytes per row "
+                                 "96 in + 24 vector + 24 (32) barycentrics"}
+    out["closest_point_batch"] = batch
     return out
 
 
@@ -551,6 +653,7 @@ def run_ours(args, rank, world, local, pg):
                           "refine": tm["refine_ms"] / (tm["cull_ms"] + tm["refine_ms"])}}
     cpu = cpu_baseline(vf, ee) if rank == 0 and full else None
     mesh = mesh_section(ctx, stream, rank, args) if args.mesh and full else None
+    distance = distance_section(ctx, stream, rank, args) if args.distance and full else None
     serving = serving_section(args) if args.serve and full and world == 1 else None
     uneven = uneven_section(args) if args.uneven_instances and full and world == 1 else None
 
@@ -573,6 +676,7 @@ def run_ours(args, rank, world, local, pg):
             "clocks": clk.summary(),
             "gpu_launches": int(tm["launches"]),
             "mesh": mesh,
+            "distance": distance,
             "serving": serving,
             "uneven_batch": uneven,
         }

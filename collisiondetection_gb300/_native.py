@@ -39,7 +39,8 @@ class BatchStats(ctypes.Structure):
 class MeshStats(ctypes.Structure):
     _fields_ = [("face_pairs", ctypes.c_int64), ("n_vf", ctypes.c_int64), ("n_ee", ctypes.c_int64),
                 ("vf_hits", ctypes.c_int64), ("ee_hits", ctypes.c_int64), ("slab_tests", ctypes.c_int64),
-                ("broadphase_ms", ctypes.c_float), ("traversal_ms", ctypes.c_float)]
+                ("broadphase_ms", ctypes.c_float), ("traversal_ms", ctypes.c_float),
+                ("self_distance_eta", ctypes.c_double)]
 
 
 class BatchTimings(ctypes.Structure):

@@ -596,6 +596,7 @@ int ccd_mesh_self_distance(ccd_mesh *m, const double *verts, double *distance, i
     m->n_cand[0] = m->n_cand[1] = 0;
     m->have_cand = true;
   }
+  m->stats.self_distance_eta = closest;
   // 3. the least stencil distance (src/Distance.cpp:48-64)
   unsigned long long *best = m->pt.counters ? m->pt.counters + 2 : nullptr;
   double result = INFINITY;

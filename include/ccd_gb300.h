@@ -183,6 +183,8 @@ typedef struct {
   int64_t slab_tests; /* traversal slab tests (leaf and node), or -1 unless counting is on */
   float broadphase_ms; /* device time of the broad phase, traversal_ms of its tree */
   float traversal_ms;  /* traversal (both 0 unless the context's profiling is on) */
+  double self_distance_eta; /* ccd_mesh_self_distance: its broad phase's padding, the least
+                               qualifying vertex distance (+inf if none); 0 otherwise */
 } ccd_mesh_stats;
 
 /* faces: nfaces x 3 vertex indices in [0, nverts).  Topology is fixed for the

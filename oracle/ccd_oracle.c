@@ -1498,3 +1498,24 @@ double oracle_mesh_self_distance(int nverts, const double *verts, int nfaces, co
   if (n_ee) *n_ee = nee;
   return closest;
 }
+
+/* The vertex scan of Distance::meshSelfDistance (src/Distance.cpp:21-34)
+ * restricted to vertices i in [i0, i1): the least squared distance found
+ * there (the CPU baseline times it on a bounded sample of vertices). */
+double oracle_vertex_scan(int nverts, const double *verts, int nfaces, const int32_t *faces, int i0, int i1) {
+  double closest = INFINITY;
+  if (i0 < 0) i0 = 0;
+  if (i1 > nverts) i1 = nverts;
+  for (int i = i0; i < i1; i++) {
+    for (int j = 0; j < nfaces; j++) {
+      const int32_t *fj = faces + 3 * (int64_t)j;
+      if (fj[0] == i || fj[1] == i || fj[2] == i) continue;
+      for (int k = 0; k < 3; k++) {
+        vec3 d = vsub(v3(verts + 3 * (int64_t)i), v3(verts + 3 * (int64_t)fj[k]));
+        double dist = vdot(d, d);
+        if (dist < closest) closest = dist;
+      }
+    }
+  }
+  return closest;
+}

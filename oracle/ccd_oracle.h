@@ -70,6 +70,9 @@ void oracle_distance_less_than(int kind, int64_t n, const double *rows, const do
 double oracle_mesh_self_distance(int nverts, const double *verts, int nfaces, const int32_t *faces,
                                  const uint8_t *fixed, int64_t *n_vf, int64_t *n_ee);
 
+/* That vertex scan alone over vertices [i0, i1): the least squared distance. */
+double oracle_vertex_scan(int nverts, const double *verts, int nfaces, const int32_t *faces, int i0, int i1);
+
 /* Stencil canonical forms (src/Stencils.h): writes the canonical 4-tuple. */
 void oracle_vf_canon(int p, int q0, int q1, int q2, int32_t *out);
 void oracle_ee_canon(int p0, int p1, int q0, int q1, int32_t *out);

@@ -91,7 +91,15 @@ class Oracle(_Lib):
                                          ctypes.c_int]
         L.oracle_mesh_self_distance.argtypes = [ctypes.c_int, _P, ctypes.c_int, _P, _P, _P, _P]
         L.oracle_mesh_self_distance.restype = ctypes.c_double
+        L.oracle_vertex_scan.argtypes = [ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_int, ctypes.c_int]
+        L.oracle_vertex_scan.restype = ctypes.c_double
         self._distance_setup()
+
+    def vertex_scan(self, verts, faces, i0: int, i1: int) -> float:
+        """meshSelfDistance's O(V F) vertex scan over vertices [i0, i1)."""
+        verts = np.ascontiguousarray(verts, dtype=np.float64).ravel()
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        return float(self.lib.oracle_vertex_scan(verts.size // 3, _ptr(verts), faces.shape[0], _ptr(faces), i0, i1))
 
     def mesh_self_distance(self, verts, faces, fixed=None):
         """Distance::meshSelfDistance; returns (distance, n_vf, n_ee)."""
