@@ -618,6 +618,11 @@ int ccd_mesh_self_distance(ccd_mesh *m, const double *verts, double *distance, i
 
 int ccd_self_distance(ccd_context *ctx, int32_t nverts, const double *verts, int32_t nfaces, const int32_t *faces,
                       const uint8_t *fixed, double *distance) {
+  if (!ctx || !distance) return CCD_ERR_INVALID_ARGUMENT;
+  if (nverts == 0 && nfaces == 0) {  // no vertex pair and no stencil, as in the reference
+    *distance = INFINITY;
+    return CCD_OK;
+  }
   ccd_mesh *m = nullptr;
   int rc = ccd_mesh_create(ctx, nverts, nfaces, faces, &m);
   if (rc) return rc;

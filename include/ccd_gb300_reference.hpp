@@ -105,6 +105,82 @@ inline bool vertexVertexCTCD(const Eigen::Vector3d &q1start, const Eigen::Vector
   return hit != 0;
 }
 
+// ------------------------------------------------------------------ Distance statics
+// The reference's Distance class (include/Distance.h) with the same
+// signatures, evaluated on the device with bit-identical results.  Reference
+// arguments written in order, so aliased outputs (meshSelfDistance passes
+// t, t, t) end with the same value as in the reference.
+inline Eigen::Vector3d vertexFaceDistance(const Eigen::Vector3d &p, const Eigen::Vector3d &q0,
+                                          const Eigen::Vector3d &q1, const Eigen::Vector3d &q2, double &q0bary,
+                                          double &q1bary, double &q2bary) {
+  double x[12], v[3], b[3];
+  put(x, p), put(x + 3, q0), put(x + 6, q1), put(x + 9, q2);
+  check(default_context(), ccd_distance_batch(default_context(), CCD_DISTANCE_VERTEX_FACE, 1, x, v, b),
+        "ccd_distance_batch");
+  q0bary = b[0];
+  q1bary = b[1];
+  q2bary = b[2];
+  return Eigen::Vector3d(v[0], v[1], v[2]);
+}
+
+inline Eigen::Vector3d edgeEdgeDistance(const Eigen::Vector3d &p0, const Eigen::Vector3d &p1,
+                                        const Eigen::Vector3d &q0, const Eigen::Vector3d &q1, double &p0bary,
+                                        double &p1bary, double &q0bary, double &q1bary) {
+  double x[12], v[3], b[4];
+  put(x, p0), put(x + 3, p1), put(x + 6, q0), put(x + 9, q1);
+  check(default_context(), ccd_distance_batch(default_context(), CCD_DISTANCE_EDGE_EDGE, 1, x, v, b),
+        "ccd_distance_batch");
+  p0bary = b[0];
+  p1bary = b[1];
+  q0bary = b[2];
+  q1bary = b[3];
+  return Eigen::Vector3d(v[0], v[1], v[2]);
+}
+
+inline bool vertexPlaneDistanceLessThan(const Eigen::Vector3d &p, const Eigen::Vector3d &q0,
+                                        const Eigen::Vector3d &q1, const Eigen::Vector3d &q2, double eta) {
+  double x[12];
+  uint8_t out = 0;
+  put(x, p), put(x + 3, q0), put(x + 6, q1), put(x + 9, q2);
+  check(default_context(),
+        ccd_distance_less_than_batch(default_context(), CCD_DISTANCE_VERTEX_PLANE, 1, x, &eta, 1, &out),
+        "ccd_distance_less_than_batch");
+  return out != 0;
+}
+
+inline bool lineLineDistanceLessThan(const Eigen::Vector3d &p0, const Eigen::Vector3d &p1,
+                                     const Eigen::Vector3d &q0, const Eigen::Vector3d &q1, double eta) {
+  double x[12];
+  uint8_t out = 0;
+  put(x, p0), put(x + 3, p1), put(x + 6, q0), put(x + 9, q1);
+  check(default_context(),
+        ccd_distance_less_than_batch(default_context(), CCD_DISTANCE_LINE_LINE, 1, x, &eta, 1, &out),
+        "ccd_distance_less_than_batch");
+  return out != 0;
+}
+
+// Distance::meshSelfDistance (src/Distance.cpp:12-66).  The reference also
+// prints the numbers of stencils it checks; ccd_mesh_self_distance returns
+// them instead.
+inline double meshSelfDistance(const Eigen::VectorXd &verts, const Eigen::Matrix3Xi &faces,
+                               const std::set<int> &fixedVerts) {
+  const int nv = (int)(verts.size() / 3), nf = (int)faces.cols();
+  std::vector<double> x((size_t)3 * nv);
+  for (int i = 0; i < 3 * nv; i++) x[(size_t)i] = verts[i];
+  std::vector<int32_t> f((size_t)3 * nf);
+  for (int c = 0; c < nf; c++)
+    for (int j = 0; j < 3; j++) f[(size_t)3 * c + j] = faces.coeff(j, c);
+  std::vector<uint8_t> fixed((size_t)nv, 0);
+  for (std::set<int>::const_iterator it = fixedVerts.begin(); it != fixedVerts.end(); ++it)
+    if (*it >= 0 && *it < nv) fixed[(size_t)*it] = 1;
+  double d = 0;
+  check(default_context(),
+        ccd_self_distance(default_context(), nv, x.data(), nf, f.data(), fixedVerts.empty() ? nullptr : fixed.data(),
+                          &d),
+        "ccd_self_distance");
+  return d;
+}
+
 // ------------------------------------------------------------------ meshes
 // A device mesh that follows the faces of the reference Mesh it is given:
 // re-created when the topology changes, positions uploaded on every call.

@@ -1,8 +1,8 @@
 """The header-only C++ adapters (include/ccd_gb300_reference.hpp) compile
 against the reference's own headers (CTCD.h, History.h, Mesh.h, Stencils.h,
-RetrospectiveDetection.h) and the Eigen API subset: the classes derive from
-the reference's BroadPhase / NarrowPhase and the CTCD forwarders keep the
-CTCD statics' signatures.  Needs the reference tree (skipped without it)."""
+RetrospectiveDetection.h, Distance.h) and the Eigen API subset: the classes
+derive from the reference's BroadPhase / NarrowPhase and the CTCD and Distance
+forwarders keep the statics' signatures.  Needs the reference tree (skipped without it)."""
 import os
 import shutil
 import subprocess
@@ -14,6 +14,7 @@ REF_TREE = os.environ.get("CCD_REFERENCE_TREE", "/root/reference")
 
 CHECK = r'''
 #include "ccd_gb300_reference.hpp"
+#include "Distance.h"
 #include <type_traits>
 static_assert(std::is_base_of<BroadPhase, ccd_gb300::GpuKDOPBroadPhase>::value, "k-DOP adapter");
 static_assert(std::is_base_of<BroadPhase, ccd_gb300::GpuAABBBroadPhase>::value, "AABB adapter");
@@ -23,6 +24,14 @@ static_assert(std::is_same<decltype(&CTCD::vertexFaceCTCD), decltype(&ccd_gb300:
 static_assert(std::is_same<decltype(&CTCD::edgeEdgeCTCD), decltype(&ccd_gb300::edgeEdgeCTCD)>::value, "ee");
 static_assert(std::is_same<decltype(&CTCD::vertexEdgeCTCD), decltype(&ccd_gb300::vertexEdgeCTCD)>::value, "ve");
 static_assert(std::is_same<decltype(&CTCD::vertexVertexCTCD), decltype(&ccd_gb300::vertexVertexCTCD)>::value, "vv");
+// ... and the Distance statics'.
+static_assert(std::is_same<decltype(&Distance::vertexFaceDistance), decltype(&ccd_gb300::vertexFaceDistance)>::value, "vfd");
+static_assert(std::is_same<decltype(&Distance::edgeEdgeDistance), decltype(&ccd_gb300::edgeEdgeDistance)>::value, "eed");
+static_assert(std::is_same<decltype(&Distance::vertexPlaneDistanceLessThan),
+                           decltype(&ccd_gb300::vertexPlaneDistanceLessThan)>::value, "vpl");
+static_assert(std::is_same<decltype(&Distance::lineLineDistanceLessThan),
+                           decltype(&ccd_gb300::lineLineDistanceLessThan)>::value, "lll");
+static_assert(std::is_same<decltype(&Distance::meshSelfDistance), decltype(&ccd_gb300::meshSelfDistance)>::value, "msd");
 int main() { return 0; }
 '''
 
