@@ -18,7 +18,7 @@ HEADER = os.path.join(ROOT, "include", "ccd_gb300.h")
 CCD_OK = 0
 VERTEX_FACE, EDGE_EDGE, VERTEX_EDGE, VERTEX_VERTEX = 0, 1, 2, 3
 PATH_FP64, PATH_CULL_REFINE = 0, 1
-BROADPHASE_KDOP13, BROADPHASE_AABB = 0, 1
+BROADPHASE_KDOP13, BROADPHASE_AABB, BROADPHASE_TRIVIAL = 0, 1, 2
 DISTANCE_VERTEX_FACE, DISTANCE_EDGE_EDGE = 0, 1    # ccd_distance_batch
 DISTANCE_VERTEX_PLANE, DISTANCE_LINE_LINE = 0, 1   # ccd_distance_less_than_batch
 ROW_WIDTH = {VERTEX_FACE: 24, EDGE_EDGE: 24, VERTEX_EDGE: 18, VERTEX_VERTEX: 12}

@@ -360,17 +360,19 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
           for (int k = 0; k < K; k++) sep |= (qhi[k] < blo[k]) || (bhi[k] < qlo[k]);
         }
         if (sep) continue;
-        // The reference's exact FP64 test (KDOPBroadPhase.cpp:132-137).
+        // Mesh::neighboringFaces (src/Mesh.cpp:13-20) first: most leaf pairs
+        // whose slabs overlap are adjacent faces, and this integer test spares
+        // them the FP64 one (FP64 compares run at 1/64 of the FP32 rate).
         const int fb = (int)(keys[j] & fmask);
-        for (int k = 0; k < K && !sep; k++)
-          sep = (hi64[(int64_t)k * topo.nf + fa] < lo64[(int64_t)k * topo.nf + fb]) ||
-                (hi64[(int64_t)k * topo.nf + fb] < lo64[(int64_t)k * topo.nf + fa]);
-        if (sep) continue;
-        // Mesh::neighboringFaces (src/Mesh.cpp:13-20).
         const int b0 = topo.faces[3 * fb], b1 = topo.faces[3 * fb + 1], b2 = topo.faces[3 * fb + 2];
         if (a0 == b0 || a0 == b1 || a0 == b2 || a1 == b0 || a1 == b1 || a1 == b2 || a2 == b0 || a2 == b1 ||
             a2 == b2)
           continue;
+        // The reference's exact FP64 test (KDOPBroadPhase.cpp:132-137).
+        for (int k = 0; k < K && !sep; k++)
+          sep = (hi64[(int64_t)k * topo.nf + fa] < lo64[(int64_t)k * topo.nf + fb]) ||
+                (hi64[(int64_t)k * topo.nf + fb] < lo64[(int64_t)k * topo.nf + fa]);
+        if (sep) continue;
         const unsigned long long idx = atomicAdd(&counters[0], 1ull);
         if (idx < cap) {
           pairs[2 * (int64_t)idx] = (uint32_t)fa;
@@ -495,6 +497,56 @@ Axes make_axes() {
     ax.a[k][2] = z / nrm;
   }
   return ax;
+}
+
+// ------------------------------------------------------------------ trivial candidates
+// TrivialBroadPhase::findCollisionCandidates (src/TrivialBroadPhase.cpp:4-53)
+// in set order without a sort.  Vertex-face stencils are the pairs (vertex i,
+// face rank r) with i not in r's sorted triple, in (i, r) order -- the set
+// order of (p, q0, q1, q2), each distinct triple once.  Edge-edge stencils are
+// the pairs of edge ranks (a < b) whose edges share no vertex, in (a, b) order
+// -- the set order of (p0, p1, q0, q1), since the smaller-ranked edge has the
+// smaller first vertex.  A chunk of the index space is flagged, scanned and
+// written out at its running offset.
+__device__ __forceinline__ bool all_fixed4(const uint8_t *fixed, int a, int b, int c, int d) {
+  return fixed && fixed[a] && fixed[b] && fixed[c] && fixed[d];
+}
+
+__global__ void __launch_bounds__(kThreads) trivial_flags(MeshTopology topo, const uint8_t *fixed, int which,
+                                                          int64_t begin, int64_t count, uint32_t *flags) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int64_t idx = begin + t;
+  bool keep;
+  if (which == 0) {
+    const int i = (int)(idx / topo.nranks), r = (int)(idx % topo.nranks);
+    const int a = topo.rank_triple[3 * r], b = topo.rank_triple[3 * r + 1], c = topo.rank_triple[3 * r + 2];
+    keep = i != a && i != b && i != c && !all_fixed4(fixed, i, a, b, c);
+  } else {
+    const int ea = (int)(idx / topo.nedges), eb = (int)(idx % topo.nedges);
+    const int a0 = topo.rank_edge[2 * ea], a1 = topo.rank_edge[2 * ea + 1];
+    const int b0 = topo.rank_edge[2 * eb], b1 = topo.rank_edge[2 * eb + 1];
+    keep = ea < eb && a0 != b0 && a0 != b1 && a1 != b0 && a1 != b1 && !all_fixed4(fixed, a0, a1, b0, b1);
+  }
+  flags[t] = keep ? 1u : 0u;
+}
+
+__global__ void __launch_bounds__(kThreads) trivial_emit(MeshTopology topo, int which, int64_t begin, int64_t count,
+                                                         const uint32_t *flags, const uint32_t *pos, int64_t base,
+                                                         int32_t *out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= count || !flags[t]) return;
+  const int64_t idx = begin + t;
+  int4 st;
+  if (which == 0) {
+    const int i = (int)(idx / topo.nranks), r = (int)(idx % topo.nranks);
+    st = make_int4(i, topo.rank_triple[3 * r], topo.rank_triple[3 * r + 1], topo.rank_triple[3 * r + 2]);
+  } else {
+    const int ea = (int)(idx / topo.nedges), eb = (int)(idx % topo.nedges);
+    st = make_int4(topo.rank_edge[2 * ea], topo.rank_edge[2 * ea + 1], topo.rank_edge[2 * eb],
+                   topo.rank_edge[2 * eb + 1]);
+  }
+  reinterpret_cast<int4 *>(out)[base + pos[t]] = st;
 }
 
 // ------------------------------------------------------------------ closest vertex pair
@@ -948,6 +1000,64 @@ int closest_vertex_pair(int nv, int nf, const int32_t *faces, const double *x, P
   memcpy(&d, &hc[0], sizeof(d));
   *d2 = d;
   return 0;
+}
+
+
+// Returns 0, 2 on a CUDA error (*err), 4 when a stencil list would pass 2^31.
+int trivial_candidates(const MeshTopology &topo, const uint8_t *fixed, int32_t **vf_out, int64_t *vf_cap,
+                       int32_t **ee_out, int64_t *ee_cap, int64_t *n_vf, int64_t *n_ee, cudaStream_t s,
+                       cudaError_t *err) {
+  *n_vf = *n_ee = 0;
+  const int64_t space[2] = {(int64_t)topo.nv * topo.nranks, (int64_t)topo.nedges * topo.nedges};
+  const int64_t chunk = std::min<int64_t>(std::max(space[0], space[1]), (int64_t)1 << 26);
+  if (chunk <= 0) return 0;
+  uint32_t *flags = nullptr, *pos = nullptr, *total = nullptr;
+  void *temp = nullptr;
+  const size_t temp_bytes = scan_temp_bytes(chunk);
+  int rc = 0;
+  auto run = [&]() -> int {
+    BP_CUDA(cudaMalloc(&flags, (size_t)chunk * sizeof(uint32_t)));
+    BP_CUDA(cudaMalloc(&pos, (size_t)chunk * sizeof(uint32_t)));
+    BP_CUDA(cudaMalloc(&total, sizeof(uint32_t)));
+    BP_CUDA(cudaMalloc(&temp, temp_bytes));
+    for (int which = 0; which < 2; which++) {
+      int32_t **out = which == 0 ? vf_out : ee_out;
+      int64_t *cap = which == 0 ? vf_cap : ee_cap;
+      // pass 0 counts, pass 1 writes
+      int64_t n = 0;
+      for (int pass = 0; pass < 2; pass++) {
+        if (pass == 1) {
+          if (n >= ((int64_t)1 << 31)) return 4;
+          BP_CUDA(grow(out, cap, 4 * std::max<int64_t>(n, 1)));
+        }
+        int64_t base = 0;
+        for (int64_t begin = 0; begin < space[which]; begin += chunk) {
+          const int64_t count = std::min(chunk, space[which] - begin);
+          const unsigned grid = (unsigned)((count + kThreads - 1) / kThreads);
+          trivial_flags<<<grid, kThreads, 0, s>>>(topo, fixed, which, begin, count, flags);
+          BP_CUDA(cudaGetLastError());
+          BP_CUDA(exclusive_scan_u32(flags, pos, count, total, temp, temp_bytes, s));
+          if (pass == 1) {
+            trivial_emit<<<grid, kThreads, 0, s>>>(topo, which, begin, count, flags, pos, base, *out);
+            BP_CUDA(cudaGetLastError());
+          }
+          uint32_t h = 0;
+          BP_CUDA(cudaMemcpyAsync(&h, total, sizeof(h), cudaMemcpyDeviceToHost, s));
+          BP_CUDA(cudaStreamSynchronize(s));
+          base += h;
+        }
+        n = base;
+      }
+      *(which == 0 ? n_vf : n_ee) = n;
+    }
+    return 0;
+  };
+  rc = run();
+  cudaFree(flags);
+  cudaFree(pos);
+  cudaFree(total);
+  cudaFree(temp);
+  return rc;
 }
 
 }  // namespace ccd

@@ -84,6 +84,16 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
 
 void broadphase_free(BroadphaseBuffers &buf);
 
+// TrivialBroadPhase::findCollisionCandidates (src/TrivialBroadPhase.cpp:4-53):
+// every vertex-face stencil of a vertex and a face without it and every
+// edge-edge stencil of two edges without a common vertex, minus stencils
+// whose four vertices are all fixed; positions and padding are not used.
+// Same outputs as broadphase_run (synchronised on return).  Returns 0, 2 on
+// a CUDA error (*err), 4 when a list would reach 2^31 stencils.
+int trivial_candidates(const MeshTopology &topo, const uint8_t *fixed, int32_t **vf_out, int64_t *vf_cap,
+                       int32_t **ee_out, int64_t *ee_cap, int64_t *n_vf, int64_t *n_ee, cudaStream_t s,
+                       cudaError_t *err);
+
 // Device buffers of the closest-vertex-pair search; grown by the caller.
 struct PointTreeBuffers {
   int64_t cap_verts = 0, cap_faces = 0;

@@ -195,6 +195,18 @@ int run_broadphase(ccd_mesh *m, int kind, double outer_eta, bool whole = false) 
   }
   cudaError_t err = cudaSuccess;
   int64_t npairs = 0, tests = 0;
+  if (kind == CCD_BROADPHASE_TRIVIAL) {
+    if (topo.ninst > 1) return mesh_fail(m, CCD_ERR_INVALID_ARGUMENT, "the trivial broad phase takes single meshes");
+    const int trc = ccd::trivial_candidates(topo, p.fixed, &m->cand[0], &m->cand_cap[0], &m->cand[1],
+                                            &m->cand_cap[1], &m->n_cand[0], &m->n_cand[1], ctx->stream, &err);
+    if (trc == 2) return cuda_fail(ctx, err, "trivial broadphase");
+    if (trc == 4) return mesh_fail(m, CCD_ERR_OUT_OF_MEMORY, "trivial broadphase: 2^31 or more stencils");
+    m->stats.slab_tests = -1;
+    m->stats.n_vf = m->n_cand[0];
+    m->stats.n_ee = m->n_cand[1];
+    m->have_cand = true;
+    return CCD_OK;
+  }
   const int rc = ccd::broadphase_run(topo, p, m->bp, &m->cand[0], &m->cand_cap[0], &m->cand[1], &m->cand_cap[1],
                                      &m->n_cand[0], &m->n_cand[1], &npairs, &tests, ctx->num_sms, ctx->stream, &err);
   if (rc == 2) return cuda_fail(ctx, err, "broadphase");
@@ -400,7 +412,7 @@ int ccd_mesh_set_fixed(ccd_mesh *m, const uint8_t *fixed) {
 int ccd_broadphase(ccd_mesh *m, int kind, double outer_eta, int64_t *n_vf, int64_t *n_ee) {
   if (!m) return CCD_ERR_INVALID_ARGUMENT;
   ccd_context *ctx = m->ctx;
-  if (kind != CCD_BROADPHASE_KDOP13 && kind != CCD_BROADPHASE_AABB)
+  if (kind != CCD_BROADPHASE_KDOP13 && kind != CCD_BROADPHASE_AABB && kind != CCD_BROADPHASE_TRIVIAL)
     return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown broadphase kind");
   CCD_CUDA(cudaSetDevice(ctx->device));
   int rc = run_broadphase(m, kind, outer_eta);
@@ -497,7 +509,8 @@ int ccd_mesh_detect(ccd_mesh *m, int broadphase_kind, double outer_eta, double e
                     int64_t *ee_hits) {
   if (!m) return CCD_ERR_INVALID_ARGUMENT;
   ccd_context *ctx = m->ctx;
-  if (broadphase_kind != CCD_BROADPHASE_KDOP13 && broadphase_kind != CCD_BROADPHASE_AABB)
+  if (broadphase_kind != CCD_BROADPHASE_KDOP13 && broadphase_kind != CCD_BROADPHASE_AABB &&
+      broadphase_kind != CCD_BROADPHASE_TRIVIAL)
     return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown broadphase kind");
   if (path != CCD_PATH_FP64 && path != CCD_PATH_CULL_REFINE)
     return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown path");

@@ -147,7 +147,8 @@ void worker_loop(ccd_server *s, int slot) {
 int check_request(const ccd_request *r) {
   if (!r || r->nverts <= 0 || r->nfaces < 0 || r->steps < 1 || !r->frames || (r->nfaces > 0 && !r->faces))
     return CCD_ERR_INVALID_ARGUMENT;
-  if (r->broadphase_kind != CCD_BROADPHASE_KDOP13 && r->broadphase_kind != CCD_BROADPHASE_AABB)
+  if (r->broadphase_kind != CCD_BROADPHASE_KDOP13 && r->broadphase_kind != CCD_BROADPHASE_AABB &&
+      r->broadphase_kind != CCD_BROADPHASE_TRIVIAL)
     return CCD_ERR_INVALID_ARGUMENT;
   if (r->path != CCD_PATH_FP64 && r->path != CCD_PATH_CULL_REFINE) return CCD_ERR_INVALID_ARGUMENT;
   return CCD_OK;

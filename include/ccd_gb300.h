@@ -170,7 +170,13 @@ typedef struct ccd_mesh ccd_mesh;
 
 typedef enum {
   CCD_BROADPHASE_KDOP13 = 0, /* KDOPBroadPhase (src/KDOPBroadPhase.cpp) */
-  CCD_BROADPHASE_AABB = 1    /* AABBBroadPhase (src/AABBBroadPhase.cpp) */
+  CCD_BROADPHASE_AABB = 1,   /* AABBBroadPhase (src/AABBBroadPhase.cpp) */
+  /* TrivialBroadPhase (src/TrivialBroadPhase.cpp:4-53), the brute-force
+   * verifier: every stencil of a vertex and a face without it and of two
+   * edges without a common vertex (all-fixed ones excepted), whatever the
+   * positions and padding.  O(V F + E^2) stencils: for small meshes; single
+   * meshes only (not ccd_mesh_create_instances). */
+  CCD_BROADPHASE_TRIVIAL = 2
 } ccd_broadphase_kind;
 
 /* Counters of the most recent broad/narrow phase call on a mesh. */

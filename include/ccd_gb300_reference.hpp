@@ -263,6 +263,8 @@ class GpuBroadPhase : public BroadPhase {
 
 typedef GpuBroadPhase<CCD_BROADPHASE_KDOP13> GpuKDOPBroadPhase;
 typedef GpuBroadPhase<CCD_BROADPHASE_AABB> GpuAABBBroadPhase;
+// TrivialBroadPhase (src/TrivialBroadPhase.cpp): the brute-force verifier.
+typedef GpuBroadPhase<CCD_BROADPHASE_TRIVIAL> GpuTrivialBroadPhase;
 
 // ------------------------------------------------------------------ narrow phase
 class GpuCTCDNarrowPhase : public NarrowPhase {

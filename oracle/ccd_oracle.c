@@ -1107,9 +1107,50 @@ static int cmp_sweep(const void *a, const void *b) {
   return ((const sweep_key *)a)->face - ((const sweep_key *)b)->face;
 }
 
+/* TrivialBroadPhase::findCollisionCandidates (src/TrivialBroadPhase.cpp:4-53):
+ * every vertex with every face that does not contain it, every pair of face
+ * edges without a common vertex, minus all-fixed stencils.  Positions and
+ * padding are not used. */
+static int trivial_candidates(int nverts, int nfaces, const int32_t *faces, const uint8_t *fixed) {
+#define FIXED(v) (fixed && fixed[(v)])
+  int rc = 0;
+  int32_t r[4];
+  for (int i = 0; i < nverts && !rc; i++) {
+    for (int j = 0; j < nfaces && !rc; j++) {
+      const int32_t *F = faces + 3 * (size_t)j;
+      if (F[0] == i || F[1] == i || F[2] == i) continue;
+      if (FIXED(i) && FIXED(F[0]) && FIXED(F[1]) && FIXED(F[2])) continue;
+      oracle_vf_canon(i, F[0], F[1], F[2], r);
+      rc |= i4_push(&g_vf, r);
+    }
+  }
+  for (int64_t e1 = 0; e1 < 3 * (int64_t)nfaces && !rc; e1++) {
+    for (int64_t e2 = e1 + 1; e2 < 3 * (int64_t)nfaces && !rc; e2++) {
+      const int64_t f1 = e1 / 3, f2 = e2 / 3;
+      const int a = faces[3 * f1 + e1 % 3], b = faces[3 * f1 + (e1 + 1) % 3];
+      const int c = faces[3 * f2 + e2 % 3], d = faces[3 * f2 + (e2 + 1) % 3];
+      if (a == c || a == d || b == c || b == d) continue;
+      if (FIXED(a) && FIXED(b) && FIXED(c) && FIXED(d)) continue;
+      oracle_ee_canon(a, b, c, d, r);
+      rc |= i4_push(&g_ee, r);
+    }
+  }
+#undef FIXED
+  return rc;
+}
+
 int oracle_broadphase(int kind, int nverts, const double *qstart, const double *qend, int nfaces,
                       const int32_t *faces, double eta, const uint8_t *fixed, int64_t *n_vf, int64_t *n_ee) {
-  (void)nverts;
+  if (kind == 2) {
+    g_vf.n = g_ee.n = 0;
+    g_pairs = 0;
+    if (trivial_candidates(nverts, nfaces, faces, fixed)) return -1;
+    i4_sort_unique(&g_vf);
+    i4_sort_unique(&g_ee);
+    *n_vf = g_vf.n;
+    *n_ee = g_ee.n;
+    return 0;
+  }
   int K = (kind == 0) ? 13 : 3;
   /* The 13 k-DOP directions, normalised as the reference does (KDOPBroadPhase.cpp:12-31). */
   static const double dirs[13][3] = {{1, 0, 0},  {0, 1, 0},  {0, 0, 1},  {1, 1, 0},  {1, -1, 0},

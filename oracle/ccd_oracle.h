@@ -36,7 +36,9 @@ void oracle_batch(int kind, int64_t n, const double *x, const double *eta, int e
                   int nthreads);
 
 /* Swept-primitive candidate search.  kind 0 = 13-DOP (KDOPBroadPhase),
- * 1 = AABB (AABBBroadPhase).  faces is F x 3 (row per face), fixed is NULL or
+ * 1 = AABB (AABBBroadPhase), 2 = TrivialBroadPhase (every stencil of a
+ * vertex and a face without it and of two edges without a common vertex;
+ * positions and eta unused).  faces is F x 3 (row per face), fixed is NULL or
  * one byte per vertex.  Results are held until oracle_broadphase_get copies
  * them out (VF rows p,q0,q1,q2; EE rows p0,p1,q0,q1), in the reference's
  * std::set order.  Returns 0, or -1 on allocation failure. */

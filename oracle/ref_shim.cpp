@@ -2,7 +2,8 @@
 //
 // extern "C" wrapper over the reference library's own, unmodified sources
 // (src/CTCD.cpp, src/History.cpp, src/Mesh.cpp, src/KDOPBroadPhase.cpp,
-// src/AABBBroadPhase.cpp, src/CTCDNarrowPhase.cpp, src/Distance.cpp), compiled by
+// src/AABBBroadPhase.cpp, src/TrivialBroadPhase.cpp, src/CTCDNarrowPhase.cpp,
+// src/Distance.cpp), compiled by
 // oracle/Makefile against the project-written Eigen-API subset.  It exists so
 // that tests/golden/make_golden.py can pin the C restatement (ccd_oracle.c)
 // against the reference itself.  The reference tree is only present in the
@@ -18,6 +19,7 @@
 #include "History.h"
 #include "KDOPBroadPhase.h"
 #include "Mesh.h"
+#include "TrivialBroadPhase.h"
 
 using Eigen::Vector3d;
 
@@ -83,7 +85,8 @@ static Eigen::VectorXd vecx(int nverts, const double *q) {
   return v;
 }
 
-// Runs KDOPBroadPhase (kind 0) or AABBBroadPhase (kind 1) on the 2-entry
+// Runs KDOPBroadPhase (kind 0), AABBBroadPhase (kind 1) or TrivialBroadPhase
+// (kind 2) on the 2-entry
 // history (qstart at t=0, qend at t=1).  fixed may be NULL.  Results are kept
 // until ref_broadphase_get copies them out, in std::set iteration order.
 void ref_broadphase(int kind, int nverts, const double *qstart, const double *qend, int nfaces, const int32_t *faces,
@@ -100,6 +103,9 @@ void ref_broadphase(int kind, int nverts, const double *qstart, const double *qe
   std::set<EdgeEdgeStencil> ees;
   if (kind == 0) {
     KDOPBroadPhase bp;
+    bp.findCollisionCandidates(h, m, eta, vfs, ees, fixedVerts);
+  } else if (kind == 2) {
+    TrivialBroadPhase bp;
     bp.findCollisionCandidates(h, m, eta, vfs, ees, fixedVerts);
   } else {
     ref_aabb_candidates(h, m, eta, vfs, ees, fixedVerts);

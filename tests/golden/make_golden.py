@@ -19,9 +19,11 @@ the reference's example meshes, and writes:
   meshSelfDistance (with the stencil counts it prints) on the meshes above, on
   meshes/V0_prob11_835.obj, on a small sheet over a sphere and on hand-built
   small meshes.
+* ``trivial.json`` -- digests of TrivialBroadPhase's candidate sets on the
+  meshes of ``meshes.npz``, free and with fixed vertices.
 
 Only runs where the reference tree exists:
-    python tests/golden/make_golden.py [--only distances]
+    python tests/golden/make_golden.py [--only distances|trivial]
 """
 from __future__ import annotations
 
@@ -245,13 +247,33 @@ def distance_fixtures(ref) -> None:
         json.dump(meta, fh, indent=1, sort_keys=True)
 
 
+def trivial_fixtures(ref) -> None:
+    """Digests of TrivialBroadPhase's candidate sets (src/TrivialBroadPhase.cpp)
+    on the fixture meshes, free and with their fixed vertices."""
+    g = np.load(os.path.join(HERE, "meshes.npz"))
+    meta = {}
+    for name in ("test12", "prob3", "spheres"):
+        qs, qe, f, fixed = g[f"{name}_qstart"], g[f"{name}_qend"], g[f"{name}_faces"], g[f"{name}_fixed"]
+        entry = {}
+        for label, fx in (("free", None), ("fixed", fixed)):
+            vf, ee = ref.broadphase(2, qs, qe, f, 1e-6, fx)
+            entry[label] = {"n_vf": int(vf.shape[0]), "n_ee": int(ee.shape[0]), "digest": digest(vf, ee)}
+        meta[name] = entry
+    with open(os.path.join(HERE, "trivial.json"), "w") as fh:
+        json.dump(meta, fh, indent=1, sort_keys=True)
+
+
 def main() -> None:
     if not os.path.isdir(REF_TREE):
         sys.exit(f"reference tree not found at {REF_TREE}")
     O.build(ref=True)
     ref = O.Reference()
-    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "distances":
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only == "distances":
         distance_fixtures(ref)
+        return
+    if only == "trivial":
+        trivial_fixtures(ref)
         return
 
     kat = []
@@ -311,6 +333,7 @@ def main() -> None:
     with open(os.path.join(HERE, "meshes.json"), "w") as fh:
         json.dump(meta, fh, indent=1, sort_keys=True)
     distance_fixtures(ref)
+    trivial_fixtures(ref)
     print("wrote", sorted(os.listdir(HERE)))
 
 

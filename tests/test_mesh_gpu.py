@@ -250,3 +250,64 @@ def test_slab_test_counting_and_broadphase_timing(ctx, golden):
         # at least one slab test per reported pair, at most one per (leaf, node)
         assert st["face_pairs"] <= st["slab_tests"] <= f.shape[0] * (2 * f.shape[0])
         assert 0 < st["traversal_ms"] <= st["broadphase_ms"]
+
+
+# ------------------------------------------------------------------ TrivialBroadPhase
+@pytest.mark.parametrize("mesh", ["test12", "prob3", "spheres"])
+def test_trivial_broadphase_matches_reference(ctx, golden_dir, mesh):
+    meta = json.load(open(os.path.join(golden_dir, "trivial.json")))[mesh]
+    g = np.load(os.path.join(golden_dir, "meshes.npz"))
+    qs, qe, f, fixed = g[f"{mesh}_qstart"], g[f"{mesh}_qend"], g[f"{mesh}_faces"], g[f"{mesh}_fixed"]
+    with C.Mesh(ctx, f, qs, qe) as m:
+        for label, fx in (("free", None), ("fixed", fixed)):
+            m.set_fixed(fx)
+            vf, ee = m.broadphase(C.BROADPHASE_TRIVIAL, 1e-6)
+            exp = meta[label]
+            assert (vf.shape[0], ee.shape[0]) == (exp["n_vf"], exp["n_ee"])
+            assert digest(vf, ee) == exp["digest"]
+
+
+@pytest.mark.parametrize("case", ["spheres", "cloth"])
+def test_tree_broadphases_against_every_stencil(ctx, oracle, case):
+    """The k-DOP and AABB trees against the trivial broad phase (every stencil
+    of the mesh), with the narrow phase's eta equal to the padding.  Every
+    collision the trees find is found with every stencil too, with the same t,
+    and so is every vertex-face collision.  The reference's edge-edge test
+    measures the distance between the edges' lines, so it also reports nearly
+    collinear edges far apart (along a row of the wrinkled sheet: 114 such
+    hits; one on the spheres); only the broad phase keeps those out, so the
+    extra hits are edge-edge stencils the trees never propose.  The trivial
+    result itself is the oracle's."""
+    if case == "spheres":
+        qs, qe, f = W.two_spheres(seed=2, level=2)
+    else:
+        f, frames = W.cloth_frames(grid=20, level=2, seed=4, steps=6)
+        qs, qe = frames[4], frames[5]
+    eta = 1e-3
+    with C.Mesh(ctx, f, qs, qe) as m:
+        tvf, tvft, tee, teet = m.detect(C.BROADPHASE_TRIVIAL, eta, eta)
+        assert tvf.shape[0] + tee.shape[0] > 0
+        cvf, cee = oracle.broadphase(2, qs, qe, f, eta)
+        r = oracle.narrowphase(qs, qe, cvf, eta, cee, eta, nthreads=os.cpu_count() or 1)
+        np.testing.assert_array_equal(tvf, cvf[r["vf_hit"] == 1])
+        np.testing.assert_array_equal(tee, cee[r["ee_hit"] == 1])
+        for kind in (C.BROADPHASE_KDOP13, C.BROADPHASE_AABB):
+            vf, vft, ee, eet = m.detect(kind, eta, eta)
+            cand_vf, cand_ee = m.broadphase(kind, eta)
+            for got, t_got, every, t_every, cand in ((vf, vft, tvf, tvft, cand_vf), (ee, eet, tee, teet, cand_ee)):
+                pos = {tuple(x): i for i, x in enumerate(every)}
+                assert all(tuple(x) in pos for x in got)
+                np.testing.assert_array_equal(t_got, t_every[[pos[tuple(x)] for x in got]])
+                extra = set(pos) - set(map(tuple, got))
+                assert not (extra & set(map(tuple, cand)))
+            assert vf.shape[0] == tvf.shape[0]  # no vertex-face hit is left out in either scene
+
+
+def test_trivial_broadphase_rejects_instances(ctx):
+    v, f = W.icosphere(1, 0.5)
+    vv = np.concatenate([v, v + 2.0])
+    ff = np.concatenate([f, f + v.shape[0]]).astype(np.int32)
+    with C.Mesh(ctx, ff, vv.ravel(), vv.ravel(), instances=([0, v.shape[0], vv.shape[0]],
+                                                          [0, f.shape[0], ff.shape[0]])) as m:
+        with pytest.raises(C.CcdError):
+            m.broadphase(C.BROADPHASE_TRIVIAL, 1e-6)

@@ -117,3 +117,14 @@ def test_mesh_self_distance(oracle, golden_dir, mesh):
         exp = meta[label]
         assert float(d).hex() == exp["distance_hex"]
         assert (nvf, nee) == (exp["n_vf"], exp["n_ee"])
+
+
+@pytest.mark.parametrize("mesh,label", [("test12", "free"), ("test12", "fixed"), ("prob3", "free"),
+                                        ("prob3", "fixed"), ("spheres", "fixed")])
+def test_trivial_broadphase(oracle, golden_dir, mesh, label):
+    meta = json.load(open(os.path.join(golden_dir, "trivial.json")))[mesh][label]
+    g = np.load(os.path.join(golden_dir, "meshes.npz"))
+    qs, qe, f, fixed = g[f"{mesh}_qstart"], g[f"{mesh}_qend"], g[f"{mesh}_faces"], g[f"{mesh}_fixed"]
+    vf, ee = oracle.broadphase(2, qs, qe, f, 1e-6, fixed if label == "fixed" else None)
+    assert (vf.shape[0], ee.shape[0]) == (meta["n_vf"], meta["n_ee"])
+    assert _digest(vf, ee) == meta["digest"]

@@ -18,6 +18,7 @@ CHECK = r'''
 #include <type_traits>
 static_assert(std::is_base_of<BroadPhase, ccd_gb300::GpuKDOPBroadPhase>::value, "k-DOP adapter");
 static_assert(std::is_base_of<BroadPhase, ccd_gb300::GpuAABBBroadPhase>::value, "AABB adapter");
+static_assert(std::is_base_of<BroadPhase, ccd_gb300::GpuTrivialBroadPhase>::value, "trivial adapter");
 static_assert(std::is_base_of<NarrowPhase, ccd_gb300::GpuCTCDNarrowPhase>::value, "narrow-phase adapter");
 // The forwarders take exactly the CTCD statics' argument lists.
 static_assert(std::is_same<decltype(&CTCD::vertexFaceCTCD), decltype(&ccd_gb300::vertexFaceCTCD)>::value, "vf");
