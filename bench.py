@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--uneven-instances", type=int, default=8,
                     help="instances of the uneven-batch sample (0: skip; the configuration has 512)")
     ap.add_argument("--distance", type=int, default=1,
-                    help="also time meshSelfDistance and the closest-point batches (1) or not (0)")
+                    help="also time meshSelfDistance, the closest-point batches and the penalty forces (1) or not (0)")
     ap.add_argument("--serve", type=int, default=1, help="also run the serving loop (1) or not (0)")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0])
@@ -380,6 +380,46 @@ def distance_section(ctx, stream, rank, args):
     return out
 
 
+def penalty_section(ctx, rank, args):
+    """PenaltyGroup::addForce (src/PenaltyGroup.cpp:34-52) on one group made of
+    every k-DOP candidate of one sheet-on-sphere frame (211,970 faces) at a
+    padding of 0.005 (about a third of the sheet's spacing): wall time of
+    ccd_penalty_group_force (positions, velocities, forces and stencils from
+    host memory, forces and fired flags back), with the oracle's sequential
+    restatement timed beside it on one core."""
+    import collisiondetection_gb300 as C
+    from collisiondetection_gb300 import workloads as W
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    f, frames = W.cloth_frames(grid=args.cloth_grid, level=args.cloth_level, seed=0, steps=50)
+    q = frames[40]
+    v = (frames[41] - frames[39]) / 2
+    eta = 0.005
+    with C.Mesh(ctx, f, q, q) as m:
+        vf, ee = m.broadphase(C.BROADPHASE_KDOP13, eta)
+    F0 = np.zeros_like(q)
+    args_ = (q, v, F0, vf, ee, eta, 1e-6, 1.0, 0.1, 1e-3)
+    for _ in range(2):
+        ctx.penalty_group_force(*args_)
+    dts = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        F, vfire, efire, _used = ctx.penalty_group_force(*args_)
+        dts.append(time.perf_counter() - t0)
+    out = {"faces": int(f.shape[0]), "stencils": {"vf": int(vf.shape[0]), "ee": int(ee.shape[0])},
+           "fired": {"vf": int(vfire.sum()), "ee": int(efire.sum())}, "ms": 1e3 * statistics.median(dts),
+           "stencils_per_s": (vf.shape[0] + ee.shape[0]) / statistics.median(dts)}
+    if rank == 0:
+        orc = O.Oracle()
+        t0 = time.perf_counter()
+        Fr = orc.penalty_group_force(*args_)[0]
+        out["cpu_oracle"] = {"ms": 1e3 * (time.perf_counter() - t0), "cores": 1, "sample": "whole group",
+                             "same_forces": bool(np.array_equal(Fr.view(np.uint64), F.view(np.uint64)))}
+    return out
+
+
 def serving_section(args):
     """Serving loop: Poisson arrivals of collision queries (mesh + 10 steps of
     seeded rigid + jitter motion, triangle counts log-uniform in [1e3, 5e5])
@@ -654,6 +694,7 @@ def run_ours(args, rank, world, local, pg):
     cpu = cpu_baseline(vf, ee) if rank == 0 and full else None
     mesh = mesh_section(ctx, stream, rank, args) if args.mesh and full else None
     distance = distance_section(ctx, stream, rank, args) if args.distance and full else None
+    penalty = penalty_section(ctx, rank, args) if args.distance and full else None
     serving = serving_section(args) if args.serve and full and world == 1 else None
     uneven = uneven_section(args) if args.uneven_instances and full and world == 1 else None
 
@@ -677,6 +718,7 @@ def run_ours(args, rank, world, local, pg):
             "gpu_launches": int(tm["launches"]),
             "mesh": mesh,
             "distance": distance,
+            "penalty": penalty,
             "serving": serving,
             "uneven_batch": uneven,
         }

@@ -102,6 +102,9 @@ def load(path: str = LIB):
     L.ccd_mesh_self_distance.argtypes = [_P, _P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64),
                                          ctypes.POINTER(_I64)]
     L.ccd_self_distance.argtypes = [_P, ctypes.c_int32, _P, ctypes.c_int32, _P, _P, ctypes.POINTER(ctypes.c_double)]
+    L.ccd_penalty_group_force.argtypes = [_P, ctypes.c_int32, _P, _P, _I64, _P, _P, _I64, _P, _P, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P,
+                                          _P, _P, ctypes.POINTER(ctypes.c_int)]
     _lib = L
     return L
 
@@ -227,6 +230,26 @@ class Context:
         self._check(self.lib.ccd_self_distance(self.handle, verts.size // 3, _ptr(verts), faces.shape[0], _ptr(faces),
                                                _ptr(fx), ctypes.byref(d)), "ccd_self_distance")
         return d.value
+
+    def penalty_group_force(self, q, v, F, vf, ee, outer_eta: float, inner_eta: float, stiffness: float,
+                            cor: float, dt: float, vf_isnew=None, ee_isnew=None):
+        """PenaltyGroup::addForce (ccd_penalty_group_force).  Returns
+        (F_out, vf_fired, ee_fired, newused); F is not modified."""
+        q = np.ascontiguousarray(q, dtype=np.float64).ravel()
+        v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+        Fo = np.ascontiguousarray(F, dtype=np.float64).ravel().copy()
+        vf = np.ascontiguousarray(vf, dtype=np.int32).reshape(-1, 4)
+        ee = np.ascontiguousarray(ee, dtype=np.int32).reshape(-1, 4)
+        vn = None if vf_isnew is None else np.ascontiguousarray(vf_isnew, dtype=np.uint8)
+        en = None if ee_isnew is None else np.ascontiguousarray(ee_isnew, dtype=np.uint8)
+        vfire = np.zeros(vf.shape[0], np.uint8)
+        efire = np.zeros(ee.shape[0], np.uint8)
+        used = ctypes.c_int(0)
+        self._check(self.lib.ccd_penalty_group_force(self.handle, q.size // 3, _ptr(q), _ptr(v), vf.shape[0], _ptr(vf),
+                                                     _ptr(vn), ee.shape[0], _ptr(ee), _ptr(en), outer_eta, inner_eta,
+                                                     stiffness, cor, dt, _ptr(Fo), _ptr(vfire), _ptr(efire),
+                                                     ctypes.byref(used)), "ccd_penalty_group_force")
+        return Fo, vfire, efire, bool(used.value)
 
     def prim_batch_device(self, kind: int, n: int, rows_ptr: int, eta_ptr: int, eta_count: int, hit_ptr: int,
                           t_ptr: int, status_ptr: int | None = None, path: int = PATH_CULL_REFINE):

@@ -299,6 +299,28 @@ int ccd_mesh_self_distance(ccd_mesh *mesh, const double *verts, double *distance
 int ccd_self_distance(ccd_context *ctx, int32_t nverts, const double *verts, int32_t nfaces, const int32_t *faces,
                       const uint8_t *fixed, double *distance);
 
+/* ------------------------------------------------------------------ penalty forces
+ * PenaltyGroup::addForce (src/PenaltyGroup.cpp:34-52) for one group, with
+ * the potentials of VertexFacePenaltyPotential::addForce and
+ * EdgeEdgePenaltyPotential::addForce (src/PenaltyPotential.cpp:7-64): each
+ * stencil whose primitives are closer than outer_eta (and not closer than
+ * inner_eta) pushes them apart with stiffness (times cor when they are
+ * separating); F += dt * (sum of the group's forces).  Bit-identical to the
+ * reference: each vertex's forces are summed in the reference's order (the
+ * vertex-face stencils in the order given, then the edge-edge ones).
+ *   q, v, F     [nverts][3] positions, velocities, forces (F in and out)
+ *   vf, ee      [n][4] stencils in the group's order (canonicalised as the
+ *               stencil constructors do); *_isnew the stencils' isnew flags
+ *               (NULL: none new)
+ *   *_fired     optional [n] outputs: 1 where the stencil's potential fired
+ *   newused     optional: 1 if a new stencil fired (the return value of
+ *               PenaltyGroup::addForce)
+ * Host memory; blocks until done. */
+int ccd_penalty_group_force(ccd_context *ctx, int32_t nverts, const double *q, const double *v, int64_t n_vf,
+                            const int32_t *vf, const uint8_t *vf_isnew, int64_t n_ee, const int32_t *ee,
+                            const uint8_t *ee_isnew, double outer_eta, double inner_eta, double stiffness, double cor,
+                            double dt, double *F, uint8_t *vf_fired, uint8_t *ee_fired, int *newused);
+
 /* ------------------------------------------------------------------ serving
  * No counterpart in the reference (its detection runs in the caller's
  * thread).  A server runs collision queries for many callers at once on one

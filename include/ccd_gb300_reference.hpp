@@ -181,6 +181,72 @@ inline double meshSelfDistance(const Eigen::VectorXd &verts, const Eigen::Matrix
   return d;
 }
 
+// ------------------------------------------------------------------ penalty groups
+// PenaltyGroup (src/PenaltyGroup.h) with the same interface; addForce runs on
+// the device (ccd_penalty_group_force) with bit-identical forces.
+class GpuPenaltyGroup {
+ public:
+  GpuPenaltyGroup(double dt, double outerEta, double innerEta, double stiffness, double CoR)
+      : nextstep_(1), dt_(dt), outerEta_(outerEta), innerEta_(innerEta), stiffness_(stiffness), CoR_(CoR) {}
+
+  void addVFStencil(VertexFaceStencil stencil) {
+    vf_.push_back(stencil);
+    groupStencil_.insert(stencil.p);
+    groupStencil_.insert(stencil.q0);
+    groupStencil_.insert(stencil.q1);
+    groupStencil_.insert(stencil.q2);
+  }
+  void addEEStencil(EdgeEdgeStencil stencil) {
+    ee_.push_back(stencil);
+    groupStencil_.insert(stencil.p0);
+    groupStencil_.insert(stencil.p1);
+    groupStencil_.insert(stencil.q0);
+    groupStencil_.insert(stencil.q1);
+  }
+  bool addForce(const Eigen::VectorXd &q, const Eigen::VectorXd &v, Eigen::VectorXd &F) {
+    const int nv = (int)(q.size() / 3);
+    std::vector<int32_t> vf(4 * vf_.size()), ee(4 * ee_.size());
+    std::vector<uint8_t> vfn(vf_.size()), een(ee_.size());
+    for (size_t i = 0; i < vf_.size(); i++) {
+      vf[4 * i] = vf_[i].p, vf[4 * i + 1] = vf_[i].q0, vf[4 * i + 2] = vf_[i].q1, vf[4 * i + 3] = vf_[i].q2;
+      vfn[i] = vf_[i].isnew ? 1 : 0;
+    }
+    for (size_t i = 0; i < ee_.size(); i++) {
+      ee[4 * i] = ee_[i].p0, ee[4 * i + 1] = ee_[i].p1, ee[4 * i + 2] = ee_[i].q0, ee[4 * i + 3] = ee_[i].q1;
+      een[i] = ee_[i].isnew ? 1 : 0;
+    }
+    std::vector<double> qq(q.data(), q.data() + 3 * nv), vv(v.data(), v.data() + 3 * nv),
+        ff(F.data(), F.data() + 3 * nv);
+    int used = 0;
+    check(default_context(),
+          ccd_penalty_group_force(default_context(), nv, qq.data(), vv.data(), (int64_t)vf_.size(), vf.data(),
+                                  vfn.data(), (int64_t)ee_.size(), ee.data(), een.data(), outerEta_, innerEta_,
+                                  stiffness_, CoR_, dt_, ff.data(), nullptr, nullptr, &used),
+          "ccd_penalty_group_force");
+    for (int i = 0; i < 3 * nv; i++) F[i] = ff[(size_t)i];
+    return used != 0;
+  }
+  void incrementTimeStep() { nextstep_++; }
+  double nextFireTime() const { return nextstep_ * dt_; }
+  void rollback() {
+    nextstep_ = 1;
+    for (size_t i = 0; i < vf_.size(); i++) vf_[i].isnew = false;
+    for (size_t i = 0; i < ee_.size(); i++) ee_[i].isnew = false;
+  }
+  double getDt() { return dt_; }
+  double getOuterEta() { return outerEta_; }
+  const std::set<int> &getGroupStencil() { return groupStencil_; }
+
+ private:
+  GpuPenaltyGroup(const GpuPenaltyGroup &);
+  GpuPenaltyGroup &operator=(const GpuPenaltyGroup &);
+  std::vector<VertexFaceStencil> vf_;
+  std::vector<EdgeEdgeStencil> ee_;
+  std::set<int> groupStencil_;
+  int nextstep_;
+  double dt_, outerEta_, innerEta_, stiffness_, CoR_;
+};
+
 // ------------------------------------------------------------------ meshes
 // A device mesh that follows the faces of the reference Mesh it is given:
 // re-created when the topology changes, positions uploaded on every call.

@@ -1560,3 +1560,85 @@ double oracle_vertex_scan(int nverts, const double *verts, int nfaces, const int
   }
   return closest;
 }
+
+/* ------------------------------------------------------------ penalty forces (src/PenaltyPotential.cpp, src/PenaltyGroup.cpp) */
+static void add3(double *g, vec3 a) { g[0] = g[0] + a.x; g[1] = g[1] + a.y; g[2] = g[2] + a.z; }
+static void sub3(double *g, vec3 a) { g[0] = g[0] - a.x; g[1] = g[1] - a.y; g[2] = g[2] - a.z; }
+
+/* VertexFacePenaltyPotential::addForce (src/PenaltyPotential.cpp:7-34). */
+static int vf_penalty(const double *q, const double *v, double *G, const int32_t *st, double oe, double ie,
+                      double stiffness, double cor) {
+  int32_t s[4];
+  oracle_vf_canon(st[0], st[1], st[2], st[3], s);
+  vec3 p = v3(q + 3 * (size_t)s[0]), q0 = v3(q + 3 * (size_t)s[1]), q1 = v3(q + 3 * (size_t)s[2]),
+       q2 = v3(q + 3 * (size_t)s[3]);
+  vec3 c = vcross(vsub(q1, q0), vsub(q2, q0));
+  if (!(vdot(c, vsub(p, q0)) * vdot(c, vsub(p, q0)) < oe * oe * vdot(c, c))) return 0;
+  double b[3];
+  vec3 cv = vf_distance(p, q0, q1, q2, b);
+  double dist = vnorm(cv);
+  if (dist >= oe || dist < ie) return 0;
+  vec3 vp = v3(v + 3 * (size_t)s[0]);
+  vec3 nvp = {-vp.x, -vp.y, -vp.z};
+  vec3 relvel = vadd(vadd(vadd(nvp, vscale(b[0], v3(v + 3 * (size_t)s[1]))), vscale(b[1], v3(v + 3 * (size_t)s[2]))),
+                     vscale(b[2], v3(v + 3 * (size_t)s[3])));
+  if (vdot(relvel, cv) > 0) stiffness *= cor;
+  double k = stiffness * (oe - dist) / (oe - ie);
+  vec3 sc = vscale(k, cv);
+  vec3 lf = {sc.x / dist, sc.y / dist, sc.z / dist};
+  sub3(G + 3 * (size_t)s[0], lf);
+  add3(G + 3 * (size_t)s[1], vscale(b[0], lf));
+  add3(G + 3 * (size_t)s[2], vscale(b[1], lf));
+  add3(G + 3 * (size_t)s[3], vscale(b[2], lf));
+  return 1;
+}
+
+/* EdgeEdgePenaltyPotential::addForce (src/PenaltyPotential.cpp:36-64). */
+static int ee_penalty(const double *q, const double *v, double *G, const int32_t *st, double oe, double ie,
+                      double stiffness, double cor) {
+  int32_t s[4];
+  oracle_ee_canon(st[0], st[1], st[2], st[3], s);
+  vec3 p0 = v3(q + 3 * (size_t)s[0]), p1 = v3(q + 3 * (size_t)s[1]), q0 = v3(q + 3 * (size_t)s[2]),
+       q1 = v3(q + 3 * (size_t)s[3]);
+  vec3 c = vcross(vsub(p1, p0), vsub(q1, q0));
+  if (!(vdot(c, vsub(q0, p0)) * vdot(c, vsub(q0, p0)) < oe * oe * vdot(c, c))) return 0;
+  double b[4];
+  vec3 cv = ee_distance(p0, p1, q0, q1, b);
+  double dist = vnorm(cv);
+  if (dist >= oe || dist < ie) return 0;
+  vec3 relvel = vadd(vadd(vsub(vscale(-b[0], v3(v + 3 * (size_t)s[0])), vscale(b[1], v3(v + 3 * (size_t)s[1]))),
+                          vscale(b[2], v3(v + 3 * (size_t)s[2]))),
+                     vscale(b[3], v3(v + 3 * (size_t)s[3])));
+  if (vdot(relvel, cv) > 0) stiffness *= cor;
+  double k = stiffness * (oe - dist) / (oe - ie);
+  vec3 sc = vscale(k, cv);
+  vec3 lf = {sc.x / dist, sc.y / dist, sc.z / dist};
+  sub3(G + 3 * (size_t)s[0], vscale(b[0], lf));
+  sub3(G + 3 * (size_t)s[1], vscale(b[1], lf));
+  add3(G + 3 * (size_t)s[2], vscale(b[2], lf));
+  add3(G + 3 * (size_t)s[3], vscale(b[3], lf));
+  return 1;
+}
+
+/* PenaltyGroup::addForce (src/PenaltyGroup.cpp:34-52). */
+int oracle_penalty_group_force(int nverts, const double *q, const double *v, int64_t n_vf, const int32_t *vf,
+                               const uint8_t *vf_isnew, int64_t n_ee, const int32_t *ee, const uint8_t *ee_isnew,
+                               double outer_eta, double inner_eta, double stiffness, double cor, double dt,
+                               double *F, uint8_t *vf_fired, uint8_t *ee_fired) {
+  double *G = (double *)calloc((size_t)3 * (nverts > 0 ? nverts : 1), sizeof(double));
+  if (!G) return -1;
+  int newused = 0;
+  for (int64_t i = 0; i < n_vf; i++) {
+    int fired = vf_penalty(q, v, G, vf + 4 * i, outer_eta, inner_eta, stiffness, cor);
+    if (vf_fired) vf_fired[i] = (uint8_t)fired;
+    newused |= fired && vf_isnew && vf_isnew[i];
+  }
+  for (int64_t i = 0; i < n_ee; i++) {
+    int fired = ee_penalty(q, v, G, ee + 4 * i, outer_eta, inner_eta, stiffness, cor);
+    if (ee_fired) ee_fired[i] = (uint8_t)fired;
+    newused |= fired && ee_isnew && ee_isnew[i];
+  }
+  for (int64_t i = 0; i < 3 * (int64_t)nverts; i++) F[i] = F[i] + G[i] * dt;
+  free(G);
+  return newused;
+}

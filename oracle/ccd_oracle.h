@@ -75,6 +75,15 @@ double oracle_mesh_self_distance(int nverts, const double *verts, int nfaces, co
 /* That vertex scan alone over vertices [i0, i1): the least squared distance. */
 double oracle_vertex_scan(int nverts, const double *verts, int nfaces, const int32_t *faces, int i0, int i1);
 
+/* PenaltyGroup::addForce (src/PenaltyGroup.cpp:34-52) with the potentials of
+ * src/PenaltyPotential.cpp:7-64: F += dt * group force; *_fired (may be NULL)
+ * receive the per-stencil flags; returns newused (or -1 on allocation
+ * failure). */
+int oracle_penalty_group_force(int nverts, const double *q, const double *v, int64_t n_vf, const int32_t *vf,
+                               const uint8_t *vf_isnew, int64_t n_ee, const int32_t *ee, const uint8_t *ee_isnew,
+                               double outer_eta, double inner_eta, double stiffness, double cor, double dt,
+                               double *F, uint8_t *vf_fired, uint8_t *ee_fired);
+
 /* Stencil canonical forms (src/Stencils.h): writes the canonical 4-tuple. */
 void oracle_vf_canon(int p, int q0, int q1, int q2, int32_t *out);
 void oracle_ee_canon(int p0, int p1, int q0, int q1, int32_t *out);

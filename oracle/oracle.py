@@ -46,6 +46,28 @@ class _Lib:
         L, pre = self.lib, self.prefix
         getattr(L, f"{pre}_distance_batch").argtypes = [ctypes.c_int, _I64, _P, _P, _P]
         getattr(L, f"{pre}_distance_less_than").argtypes = [ctypes.c_int, _I64, _P, _P, ctypes.c_int, _P]
+        fn = getattr(L, f"{pre}_penalty_group_force")
+        fn.argtypes = [ctypes.c_int, _P, _P, _I64, _P, _P, _I64, _P, _P] + [ctypes.c_double] * 5 + [_P, _P, _P]
+        fn.restype = ctypes.c_int
+
+    def penalty_group_force(self, q, v, F, vf, ee, outer_eta, inner_eta, stiffness, cor, dt, vf_isnew=None,
+                            ee_isnew=None):
+        """PenaltyGroup::addForce; returns (F_out, vf_fired, ee_fired, newused)."""
+        q = np.ascontiguousarray(q, dtype=np.float64).ravel()
+        v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+        Fo = np.ascontiguousarray(F, dtype=np.float64).ravel().copy()
+        vf = np.ascontiguousarray(vf, dtype=np.int32).reshape(-1, 4)
+        ee = np.ascontiguousarray(ee, dtype=np.int32).reshape(-1, 4)
+        vn = None if vf_isnew is None else np.ascontiguousarray(vf_isnew, dtype=np.uint8)
+        en = None if ee_isnew is None else np.ascontiguousarray(ee_isnew, dtype=np.uint8)
+        vfire = np.zeros(vf.shape[0], np.uint8)
+        efire = np.zeros(ee.shape[0], np.uint8)
+        fn = getattr(self.lib, f"{self.prefix}_penalty_group_force")
+        used = fn(q.size // 3, _ptr(q), _ptr(v), vf.shape[0], _ptr(vf), _ptr(vn), ee.shape[0], _ptr(ee), _ptr(en),
+                  outer_eta, inner_eta, stiffness, cor, dt, _ptr(Fo), _ptr(vfire), _ptr(efire))
+        if used < 0:
+            raise MemoryError("penalty_group_force failed")
+        return Fo, vfire, efire, bool(used)
 
     def distance(self, kind: int, rows):
         """Distance::vertexFaceDistance (0) / edgeEdgeDistance (1) per row of

@@ -3,7 +3,7 @@
 // extern "C" wrapper over the reference library's own, unmodified sources
 // (src/CTCD.cpp, src/History.cpp, src/Mesh.cpp, src/KDOPBroadPhase.cpp,
 // src/AABBBroadPhase.cpp, src/TrivialBroadPhase.cpp, src/CTCDNarrowPhase.cpp,
-// src/Distance.cpp), compiled by
+// src/Distance.cpp, src/PenaltyPotential.cpp, src/PenaltyGroup.cpp), compiled by
 // oracle/Makefile against the project-written Eigen-API subset.  It exists so
 // that tests/golden/make_golden.py can pin the C restatement (ccd_oracle.c)
 // against the reference itself.  The reference tree is only present in the
@@ -16,6 +16,8 @@
 #include "CTCD.h"
 #include "CTCDNarrowPhase.h"
 #include "Distance.h"
+#include "PenaltyGroup.h"
+#include "PenaltyPotential.h"
 #include "History.h"
 #include "KDOPBroadPhase.h"
 #include "Mesh.h"
@@ -187,6 +189,37 @@ double ref_mesh_self_distance(int nverts, const double *q, int nfaces, const int
     for (int i = 0; i < nverts; i++)
       if (fixed[i]) fixedVerts.insert(i);
   return Distance::meshSelfDistance(vecx(nverts, q), m.faces, fixedVerts);
+}
+
+// ---------------------------------------------------------------- penalty forces
+// PenaltyGroup::addForce on one group built from the given stencils (with
+// their isnew flags); F is updated in place; *_fired from the potentials'
+// own addForce on a scratch vector.  Returns newused.
+int ref_penalty_group_force(int nverts, const double *q, const double *v, int64_t n_vf, const int32_t *vf,
+                            const uint8_t *vf_isnew, int64_t n_ee, const int32_t *ee, const uint8_t *ee_isnew,
+                            double outer_eta, double inner_eta, double stiffness, double cor, double dt, double *F,
+                            uint8_t *vf_fired, uint8_t *ee_fired) {
+  Eigen::VectorXd Q = vecx(nverts, q), Vv = vecx(nverts, v), FF = vecx(nverts, F), scratch(3 * nverts);
+  PenaltyGroup g(dt, outer_eta, inner_eta, stiffness, cor);
+  for (int64_t i = 0; i < n_vf; i++) {
+    VertexFaceStencil st(vf[4 * i], vf[4 * i + 1], vf[4 * i + 2], vf[4 * i + 3]);
+    st.isnew = vf_isnew ? vf_isnew[i] != 0 : false;
+    g.addVFStencil(st);
+    scratch.setZero();
+    vf_fired[i] = (uint8_t)VertexFacePenaltyPotential::addForce(Q, Vv, scratch, st, outer_eta, inner_eta, stiffness,
+                                                                 cor);
+  }
+  for (int64_t i = 0; i < n_ee; i++) {
+    EdgeEdgeStencil st(ee[4 * i], ee[4 * i + 1], ee[4 * i + 2], ee[4 * i + 3]);
+    st.isnew = ee_isnew ? ee_isnew[i] != 0 : false;
+    g.addEEStencil(st);
+    scratch.setZero();
+    ee_fired[i] = (uint8_t)EdgeEdgePenaltyPotential::addForce(Q, Vv, scratch, st, outer_eta, inner_eta, stiffness,
+                                                               cor);
+  }
+  const bool used = g.addForce(Q, Vv, FF);
+  for (int i = 0; i < 3 * nverts; i++) F[i] = FF[i];
+  return used ? 1 : 0;
 }
 
 }  // extern "C"

@@ -21,9 +21,15 @@ the reference's example meshes, and writes:
   small meshes.
 * ``trivial.json`` -- digests of TrivialBroadPhase's candidate sets on the
   meshes of ``meshes.npz``, free and with fixed vertices.
+* ``penalty.npz`` / ``penalty.json`` -- PenaltyGroup::addForce on three
+  groups (two spheres in contact, a sheet on a sphere, hand-built stencils
+  with repeated and coincident vertices), in shuffled group order with
+  non-canonical and repeated stencils, with and without new stencils: the
+  forces, the per-stencil fired flags (from the potentials' own addForce) and
+  the returned newused flag.
 
 Only runs where the reference tree exists:
-    python tests/golden/make_golden.py [--only distances|trivial]
+    python tests/golden/make_golden.py [--only distances|trivial|penalty]
 """
 from __future__ import annotations
 
@@ -263,6 +269,70 @@ def trivial_fixtures(ref) -> None:
         json.dump(meta, fh, indent=1, sort_keys=True)
 
 
+def penalty_scenes():
+    """Groups for PenaltyGroup::addForce: (q, v, F, vf, vf_isnew, ee, ee_isnew,
+    outer_eta, inner_eta, stiffness, cor, dt)."""
+    rng = np.random.default_rng(90)
+    scenes = {}
+
+    def jumble(st, kind):
+        """Group order shuffled, a tenth of the stencils written
+        non-canonically, a few listed twice."""
+        st = st[rng.permutation(st.shape[0])].copy()
+        pick = rng.random(st.shape[0]) < 0.1
+        if kind == 0:
+            st[pick, 1:] = st[pick][:, [2, 3, 1]]
+        else:
+            st[pick] = st[pick][:, [3, 2, 1, 0]]
+        return np.concatenate([st, st[: max(1, st.shape[0] // 50)]])
+
+    qs, qe, f = W.two_spheres(seed=1)
+    q = qs + 0.62 * (qe - qs)
+    vf, ee = O.Oracle().broadphase(0, q, q, f, 0.05)
+    v = (qe - qs) + rng.normal(0, 0.05, qs.shape)
+    scenes["spheres"] = (q, v, rng.normal(0, 1, qs.shape), jumble(vf, 0), None, jumble(ee, 1), None,
+                         0.05, 1e-4, 10.0, 0.1, 1e-3)
+    f2, frames = W.cloth_frames(grid=24, level=2, seed=6, steps=30)
+    q = frames[28]
+    vf, ee = O.Oracle().broadphase(0, q, q, f2, 0.02)
+    v = (frames[29] - frames[27]) / 2 + rng.normal(0, 1e-3, q.shape)
+    scenes["cloth"] = (q, v, np.zeros(q.shape), jumble(vf, 0), None, jumble(ee, 1), None, 0.02, 0.0, 1.0, 0.5, 0.01)
+    # hand-built: repeated vertices, coincident points, both signs of relative velocity
+    q = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.2, 0.2, 0.01], [0.2, 0.2, 0.01], [0.3, 0.3, -0.005],
+                  [0.5, -0.5, 0.002], [0.5, 0.5, 0.002], [1, 1, 0]], float)
+    v = rng.normal(0, 1, q.shape)
+    vf = np.array([[3, 0, 1, 2], [4, 2, 1, 0], [5, 0, 1, 2], [3, 0, 0, 1], [3, 0, 1, 2], [8, 0, 1, 2]], np.int32)
+    ee = np.array([[6, 7, 0, 1], [0, 1, 6, 7], [1, 0, 7, 6], [3, 4, 0, 1], [0, 2, 1, 8], [6, 7, 2, 8]], np.int32)
+    scenes["hand"] = (q.ravel(), v.ravel(), np.full(q.size, -0.0), vf, None, ee, None, 0.05, 1e-3, 2.0, 0.25, 0.5)
+    out = {}
+    for name, sc in scenes.items():
+        q, v, F, vf, _, ee, _, oe, ie, k, cor, dt = sc
+        vfn = rng.integers(0, 2, vf.shape[0]).astype(np.uint8)
+        een = (rng.random(ee.shape[0]) < 0.05).astype(np.uint8)
+        out[name] = (np.ascontiguousarray(q, np.float64).ravel(), np.ascontiguousarray(v, np.float64).ravel(),
+                     np.ascontiguousarray(F, np.float64).ravel(), vf, vfn, ee, een, oe, ie, k, cor, dt)
+    return out
+
+
+def penalty_fixtures(ref) -> None:
+    arrays, meta = {}, {}
+    for name, (q, v, F, vf, vfn, ee, een, oe, ie, k, cor, dt) in penalty_scenes().items():
+        for label, (vn, en) in (("new", (vfn, een)), ("old", (None, None))):
+            Fo, vfire, efire, used = ref.penalty_group_force(q, v, F, vf, ee, oe, ie, k, cor, dt, vn, en)
+            arrays[f"{name}_{label}_F"] = Fo
+            arrays[f"{name}_{label}_vf_fired"] = vfire
+            arrays[f"{name}_{label}_ee_fired"] = efire
+            meta[f"{name}_{label}"] = {"newused": bool(used), "vf_fired": int(vfire.sum()),
+                                       "ee_fired": int(efire.sum())}
+        for key, val in (("q", q), ("v", v), ("F0", F), ("vf", vf), ("vf_isnew", vfn), ("ee", ee),
+                         ("ee_isnew", een)):
+            arrays[f"{name}_{key}"] = val
+        meta[name] = {"outer_eta": oe, "inner_eta": ie, "stiffness": k, "cor": cor, "dt": dt}
+    np.savez_compressed(os.path.join(HERE, "penalty.npz"), **arrays)
+    with open(os.path.join(HERE, "penalty.json"), "w") as fh:
+        json.dump(meta, fh, indent=1, sort_keys=True)
+
+
 def main() -> None:
     if not os.path.isdir(REF_TREE):
         sys.exit(f"reference tree not found at {REF_TREE}")
@@ -274,6 +344,9 @@ def main() -> None:
         return
     if only == "trivial":
         trivial_fixtures(ref)
+        return
+    if only == "penalty":
+        penalty_fixtures(ref)
         return
 
     kat = []
@@ -334,6 +407,7 @@ def main() -> None:
         json.dump(meta, fh, indent=1, sort_keys=True)
     distance_fixtures(ref)
     trivial_fixtures(ref)
+    penalty_fixtures(ref)
     print("wrote", sorted(os.listdir(HERE)))
 
 

@@ -128,3 +128,19 @@ def test_trivial_broadphase(oracle, golden_dir, mesh, label):
     vf, ee = oracle.broadphase(2, qs, qe, f, 1e-6, fixed if label == "fixed" else None)
     assert (vf.shape[0], ee.shape[0]) == (meta["n_vf"], meta["n_ee"])
     assert _digest(vf, ee) == meta["digest"]
+
+
+@pytest.mark.parametrize("scene", ["spheres", "cloth", "hand"])
+def test_penalty_group_force(oracle, golden_dir, scene):
+    meta = json.load(open(os.path.join(golden_dir, "penalty.json")))
+    g = np.load(os.path.join(golden_dir, "penalty.npz"))
+    p = meta[scene]
+    for label, use_new in (("new", True), ("old", False)):
+        F, vfire, efire, used = oracle.penalty_group_force(
+            g[f"{scene}_q"], g[f"{scene}_v"], g[f"{scene}_F0"], g[f"{scene}_vf"], g[f"{scene}_ee"], p["outer_eta"],
+            p["inner_eta"], p["stiffness"], p["cor"], p["dt"],
+            g[f"{scene}_vf_isnew"] if use_new else None, g[f"{scene}_ee_isnew"] if use_new else None)
+        assert _same_bits(F, g[f"{scene}_{label}_F"]).all()
+        np.testing.assert_array_equal(vfire, g[f"{scene}_{label}_vf_fired"])
+        np.testing.assert_array_equal(efire, g[f"{scene}_{label}_ee_fired"])
+        assert used == meta[f"{scene}_{label}"]["newused"]

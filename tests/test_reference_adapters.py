@@ -15,6 +15,7 @@ REF_TREE = os.environ.get("CCD_REFERENCE_TREE", "/root/reference")
 CHECK = r'''
 #include "ccd_gb300_reference.hpp"
 #include "Distance.h"
+#include "PenaltyGroup.h"
 #include <type_traits>
 static_assert(std::is_base_of<BroadPhase, ccd_gb300::GpuKDOPBroadPhase>::value, "k-DOP adapter");
 static_assert(std::is_base_of<BroadPhase, ccd_gb300::GpuAABBBroadPhase>::value, "AABB adapter");
@@ -33,7 +34,16 @@ static_assert(std::is_same<decltype(&Distance::vertexPlaneDistanceLessThan),
 static_assert(std::is_same<decltype(&Distance::lineLineDistanceLessThan),
                            decltype(&ccd_gb300::lineLineDistanceLessThan)>::value, "lll");
 static_assert(std::is_same<decltype(&Distance::meshSelfDistance), decltype(&ccd_gb300::meshSelfDistance)>::value, "msd");
-int main() { return 0; }
+// GpuPenaltyGroup keeps PenaltyGroup's interface (src/PenaltyGroup.h).
+static bool (ccd_gb300::GpuPenaltyGroup::*add_force)(const Eigen::VectorXd &, const Eigen::VectorXd &,
+                                                       Eigen::VectorXd &) = &ccd_gb300::GpuPenaltyGroup::addForce;
+static bool (PenaltyGroup::*ref_add_force)(const Eigen::VectorXd &, const Eigen::VectorXd &, Eigen::VectorXd &) =
+    &PenaltyGroup::addForce;
+static void (ccd_gb300::GpuPenaltyGroup::*add_vf)(VertexFaceStencil) = &ccd_gb300::GpuPenaltyGroup::addVFStencil;
+static void (PenaltyGroup::*ref_add_vf)(VertexFaceStencil) = &PenaltyGroup::addVFStencil;
+static double (ccd_gb300::GpuPenaltyGroup::*next_fire)() const = &ccd_gb300::GpuPenaltyGroup::nextFireTime;
+static double (PenaltyGroup::*ref_next_fire)() const = &PenaltyGroup::nextFireTime;
+int main() { return add_force && ref_add_force && add_vf && ref_add_vf && next_fire && ref_next_fire ? 0 : 1; }
 '''
 
 
