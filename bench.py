@@ -408,9 +408,39 @@ def penalty_section(ctx, rank, args):
         t0 = time.perf_counter()
         F, vfire, efire, _used = ctx.penalty_group_force(*args_)
         dts.append(time.perf_counter() - t0)
+    # the same group resident on the device (ccd_penalty_group_force_device)
+    import torch
+
+    d = {k: torch.from_numpy(np.ascontiguousarray(a)).cuda() for k, a in (("q", q), ("v", v), ("vf", vf), ("ee", ee))}
+    dF = torch.zeros(q.size, dtype=torch.float64, device="cuda")
+    dvf = torch.zeros(vf.shape[0], dtype=torch.uint8, device="cuda")
+    dee = torch.zeros(ee.shape[0], dtype=torch.uint8, device="cuda")
+
+    def dev_call():
+        ctx.penalty_group_force_device(q.size // 3, d["q"].data_ptr(), d["v"].data_ptr(), vf.shape[0],
+                                       d["vf"].data_ptr(), ee.shape[0], d["ee"].data_ptr(), eta, 1e-6, 1.0, 0.1, 1e-3,
+                                       dF.data_ptr(), dvf.data_ptr(), dee.data_ptr())
+
+    for _ in range(2):
+        dev_call()
+    torch.cuda.synchronize()
+    ddts = []
+    for _ in range(5):
+        dF.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev_call()
+        ctx.synchronize()
+        ddts.append(time.perf_counter() - t0)
+    same_dev = bool(np.array_equal(dF.cpu().numpy().view(np.uint64), F.view(np.uint64)))
     out = {"faces": int(f.shape[0]), "stencils": {"vf": int(vf.shape[0]), "ee": int(ee.shape[0])},
-           "fired": {"vf": int(vfire.sum()), "ee": int(efire.sum())}, "ms": 1e3 * statistics.median(dts),
-           "stencils_per_s": (vf.shape[0] + ee.shape[0]) / statistics.median(dts)}
+           "fired": {"vf": int(vfire.sum()), "ee": int(efire.sum())},
+           "host_memory": {"ms": 1e3 * statistics.median(dts),
+                           "stencils_per_s": (vf.shape[0] + ee.shape[0]) / statistics.median(dts),
+                           "entry_point": "ccd_penalty_group_force (pageable host buffers, 0.42 GB of stencils in)"},
+           "device_memory": {"ms": 1e3 * statistics.median(ddts),
+                             "stencils_per_s": (vf.shape[0] + ee.shape[0]) / statistics.median(ddts),
+                             "entry_point": "ccd_penalty_group_force_device", "same_forces": same_dev}}
     if rank == 0:
         orc = O.Oracle()
         t0 = time.perf_counter()

@@ -105,6 +105,7 @@ def load(path: str = LIB):
     L.ccd_penalty_group_force.argtypes = [_P, ctypes.c_int32, _P, _P, _I64, _P, _P, _I64, _P, _P, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P,
                                           _P, _P, ctypes.POINTER(ctypes.c_int)]
+    L.ccd_penalty_group_force_device.argtypes = L.ccd_penalty_group_force.argtypes
     _lib = L
     return L
 
@@ -250,6 +251,19 @@ class Context:
                                                      stiffness, cor, dt, _ptr(Fo), _ptr(vfire), _ptr(efire),
                                                      ctypes.byref(used)), "ccd_penalty_group_force")
         return Fo, vfire, efire, bool(used.value)
+
+    def penalty_group_force_device(self, nverts: int, q_ptr: int, v_ptr: int, n_vf: int, vf_ptr: int, n_ee: int,
+                                   ee_ptr: int, outer_eta: float, inner_eta: float, stiffness: float, cor: float,
+                                   dt: float, F_ptr: int, vf_fired_ptr: int, ee_fired_ptr: int,
+                                   vf_isnew_ptr: int | None = None, ee_isnew_ptr: int | None = None) -> bool:
+        """Device-memory form (ccd_penalty_group_force_device); returns newused."""
+        used = ctypes.c_int(0)
+        self._check(self.lib.ccd_penalty_group_force_device(self.handle, nverts, q_ptr, v_ptr, n_vf, vf_ptr,
+                                                            vf_isnew_ptr, n_ee, ee_ptr, ee_isnew_ptr, outer_eta,
+                                                            inner_eta, stiffness, cor, dt, F_ptr, vf_fired_ptr,
+                                                            ee_fired_ptr, ctypes.byref(used)),
+                    "ccd_penalty_group_force_device")
+        return bool(used.value)
 
     def prim_batch_device(self, kind: int, n: int, rows_ptr: int, eta_ptr: int, eta_count: int, hit_ptr: int,
                           t_ptr: int, status_ptr: int | None = None, path: int = PATH_CULL_REFINE):

@@ -320,6 +320,16 @@ int ccd_penalty_group_force(ccd_context *ctx, int32_t nverts, const double *q, c
                             const int32_t *vf, const uint8_t *vf_isnew, int64_t n_ee, const int32_t *ee,
                             const uint8_t *ee_isnew, double outer_eta, double inner_eta, double stiffness, double cor,
                             double dt, double *F, uint8_t *vf_fired, uint8_t *ee_fired, int *newused);
+/* The same on device memory (q, v, F, stencils, flags; the fired arrays are
+ * required here), on the context's stream; returns once newused is known
+ * (the force kernels may still run; ccd_context_synchronize waits).  A
+ * stencil vertex out of range fails the call with CCD_ERR_INVALID_ARGUMENT
+ * (F is then left untouched). */
+int ccd_penalty_group_force_device(ccd_context *ctx, int32_t nverts, const double *q, const double *v, int64_t n_vf,
+                                   const int32_t *vf, const uint8_t *vf_isnew, int64_t n_ee, const int32_t *ee,
+                                   const uint8_t *ee_isnew, double outer_eta, double inner_eta, double stiffness,
+                                   double cor, double dt, double *F, uint8_t *vf_fired, uint8_t *ee_fired,
+                                   int *newused);
 
 /* ------------------------------------------------------------------ serving
  * No counterpart in the reference (its detection runs in the caller's

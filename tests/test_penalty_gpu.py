@@ -81,3 +81,38 @@ def test_penalty_edge_cases(ctx, oracle):
     assert _same_bits(F, Fr).all() and not used and vfire.size == 0
     with pytest.raises(C.CcdError):
         ctx.penalty_group_force(q, v, F0, [[0, 1, 2, 7]], np.zeros((0, 4)), 0.05, 0.0, 1.0, 0.5, 0.1)
+
+
+def test_penalty_device_entry_point(ctx, golden_dir):
+    torch = pytest.importorskip("torch")
+    meta = json.load(open(os.path.join(golden_dir, "penalty.json")))
+    g = np.load(os.path.join(golden_dir, "penalty.npz"))
+    scene = "spheres"
+    p = meta[scene]
+    dev = {k: torch.from_numpy(np.ascontiguousarray(g[f"{scene}_{k}"])).cuda()
+           for k in ("q", "v", "F0", "vf", "ee", "vf_isnew", "ee_isnew")}
+    n_vf, n_ee = dev["vf"].shape[0], dev["ee"].shape[0]
+    vfire = torch.zeros(n_vf, dtype=torch.uint8, device="cuda")
+    efire = torch.zeros(n_ee, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    used = ctx.penalty_group_force_device(dev["q"].numel() // 3, dev["q"].data_ptr(), dev["v"].data_ptr(), n_vf,
+                                          dev["vf"].data_ptr(), n_ee, dev["ee"].data_ptr(), p["outer_eta"],
+                                          p["inner_eta"], p["stiffness"], p["cor"], p["dt"], dev["F0"].data_ptr(),
+                                          vfire.data_ptr(), efire.data_ptr(), dev["vf_isnew"].data_ptr(),
+                                          dev["ee_isnew"].data_ptr())
+    ctx.synchronize()
+    assert _same_bits(dev["F0"].cpu().numpy(), g[f"{scene}_new_F"]).all()
+    np.testing.assert_array_equal(vfire.cpu().numpy(), g[f"{scene}_new_vf_fired"])
+    np.testing.assert_array_equal(efire.cpu().numpy(), g[f"{scene}_new_ee_fired"])
+    assert used == meta[f"{scene}_new"]["newused"]
+    # an index out of range is caught by the kernel's own check, F stays as it was
+    before = dev["F0"].clone()
+    bad = dev["vf"][:4].clone()
+    bad[2, 3] = dev["q"].numel() // 3 + 5
+    with pytest.raises(C.CcdError):
+        ctx.penalty_group_force_device(dev["q"].numel() // 3, dev["q"].data_ptr(), dev["v"].data_ptr(), 4,
+                                       bad.data_ptr(), 0, dev["ee"].data_ptr(), p["outer_eta"], p["inner_eta"],
+                                       p["stiffness"], p["cor"], p["dt"], dev["F0"].data_ptr(), vfire.data_ptr(),
+                                       efire.data_ptr())
+    ctx.synchronize()
+    assert torch.equal(before, dev["F0"])
