@@ -89,6 +89,7 @@ def load(path: str = LIB):
     L.ccd_mesh_set_positions.argtypes = [_P, _P, _P]
     L.ccd_mesh_set_positions_device.argtypes = [_P, _P, _P]
     L.ccd_mesh_set_fixed.argtypes = [_P, _P]
+    L.ccd_mesh_set_history.argtypes = [_P, _P, _P, _P]
     L.ccd_broadphase.argtypes = [_P, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]
     L.ccd_broadphase_get.argtypes = [_P, _P, _P]
     L.ccd_narrowphase.argtypes = [_P, ctypes.c_int, _I64, _P, _P, _I64, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P]
@@ -342,6 +343,17 @@ class Mesh:
     def set_positions_device(self, qstart_ptr: int, qend_ptr: int):
         self.ctx._check(self.lib.ccd_mesh_set_positions_device(self.handle, qstart_ptr, qend_ptr),
                         "ccd_mesh_set_positions_device")
+
+    def set_history(self, offsets, times, positions):
+        """A multi-entry History (ccd_mesh_set_history): vertex v's entries
+        are offsets[v] .. offsets[v+1]-1 of times and positions ([E][3])."""
+        off = np.ascontiguousarray(offsets, dtype=np.int32).ravel()
+        tt = np.ascontiguousarray(times, dtype=np.float64).ravel()
+        pp = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        if off.size != self.nverts + 1 or tt.size != off[-1] or pp.shape[0] != off[-1]:
+            raise ValueError("offsets must hold nverts + 1 values and the arrays offsets[-1] entries")
+        self.ctx._check(self.lib.ccd_mesh_set_history(self.handle, _ptr(off), _ptr(tt), _ptr(pp)),
+                        "ccd_mesh_set_history")
 
     def set_fixed(self, fixed):
         fx = None

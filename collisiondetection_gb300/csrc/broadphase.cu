@@ -74,8 +74,11 @@ __global__ void __launch_bounds__(kThreads) leaf_slabs(MeshTopology topo, Broadp
     }
     for (int j = 0; j < 3; j++) {
       const int v = topo.faces[3 * f + j];
-      for (int e = 0; e < 2; e++) {
-        const double *pos = (e ? p.qe : p.qs) + 3 * (int64_t)v;
+      // every History entry of the vertex (src/KDOPBroadPhase.cpp:60-70): the
+      // two of a step, or the entries of a multi-entry history
+      const int e0 = p.hoff ? p.hoff[v] : 0, e1 = p.hoff ? p.hoff[v + 1] : 2;
+      for (int e = e0; e < e1; e++) {
+        const double *pos = p.hoff ? p.hpos + 3 * (int64_t)e : (e ? p.qe : p.qs) + 3 * (int64_t)v;
         const double px = pos[0], py = pos[1], pz = pos[2];
 #pragma unroll
         for (int k = 0; k < K; k++) {

@@ -69,7 +69,9 @@ struct BroadphaseBuffers {
 struct BroadphaseParams {
   int kind;
   double eta;
-  const double *qs, *qe;  // [nv][3]
+  const double *qs, *qe;  // [nv][3]: a two-entry history (start, end) ...
+  const int32_t *hoff;    // ... or, when non-null, every entry: vertex v's are hoff[v] .. hoff[v+1]-1
+  const double *hpos;     // [entries][3]
   const uint8_t *fixed;   // [nv] or null
   bool count_tests;       // count the traversal's slab tests (a slower, counting variant)
   cudaEvent_t ev[4];      // optional (all null or all set): start, before / after the traversal, end

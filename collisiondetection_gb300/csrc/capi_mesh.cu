@@ -32,6 +32,10 @@ struct NarrowScratch {
   double *t_prim = nullptr, *t_ve = nullptr, *t_vv = nullptr;
   int32_t *surv = nullptr;
   ccd::BatchCounters *counters = nullptr;
+  // per-segment results of a multi-entry history
+  uint8_t *seg_hit = nullptr;
+  double *seg_t = nullptr;
+  int8_t *seg_which = nullptr;
   StageBuf stage;
 };
 
@@ -60,6 +64,10 @@ struct Lane {
   char *scan_temp = nullptr;
   int64_t scan_temp_cap = 0;
   uint32_t *d_count = nullptr;
+  // segments per stencil and their offsets (multi-entry history)
+  uint32_t *seg_cnt = nullptr, *seg_off = nullptr;
+  int64_t seg_cnt_cap = 0, seg_off_cap = 0;
+  std::vector<uint32_t> h_seg_off;
 };
 
 }  // namespace
@@ -73,6 +81,13 @@ struct ccd_mesh {
   int32_t *face_inst = nullptr;  // instance of each face (meshes made of independent instances)
   int32_t ninst = 1;
   double *qs = nullptr, *qe = nullptr;
+  // A multi-entry History (ccd_mesh_set_history), used instead of qs / qe
+  // while has_history is set: vertex v's entries are hist_off[v] ..
+  // hist_off[v+1]-1 of hist_time / hist_pos.
+  int32_t *hist_off = nullptr;
+  double *hist_time = nullptr, *hist_pos = nullptr;
+  int64_t hist_cap = 0;
+  bool has_history = false;
   uint8_t *fixed = nullptr;
   bool has_fixed = false;
   ccd::BroadphaseBuffers bp;
@@ -117,7 +132,7 @@ int ensure_narrow(ccd_mesh *m, Lane &L, int64_t chunk) {
   if (n.cap >= chunk) return CCD_OK;
   CCD_CUDA(cudaStreamSynchronize(L.stream));
   void *ptrs[] = {n.prim, n.ve, n.vv, n.eta_prim, n.eta_ve, n.eta_vv, n.h_prim, n.h_ve, n.h_vv,
-                  n.t_prim, n.t_ve, n.t_vv, n.surv, n.counters, n.stage.mem};
+                  n.t_prim, n.t_ve, n.t_vv, n.surv, n.counters, n.stage.mem, n.seg_hit, n.seg_t, n.seg_which};
   for (void *p : ptrs) cudaFree(p);
   n = NarrowScratch{};
   const size_t c = (size_t)chunk, c4 = 4 * (size_t)chunk;
@@ -135,7 +150,80 @@ int ensure_narrow(ccd_mesh *m, Lane &L, int64_t chunk) {
   CCD_CUDA(cudaMalloc(&n.t_vv, c4 * sizeof(double)));
   CCD_CUDA(cudaMalloc(&n.surv, c4 * sizeof(int32_t)));
   CCD_CUDA(cudaMalloc(&n.counters, sizeof(ccd::BatchCounters)));
+  CCD_CUDA(cudaMalloc(&n.seg_hit, c));
+  CCD_CUDA(cudaMalloc(&n.seg_t, c * sizeof(double)));
+  CCD_CUDA(cudaMalloc(&n.seg_which, c));
   n.cap = chunk;
+  return CCD_OK;
+}
+
+// The chain three batches (primitive, vertex-edge, vertex-vertex) over c rows
+// already gathered in L.ns, then the per-row first hit.
+int run_chain(ccd_mesh *m, Lane &L, int kind, int path, int64_t c, uint8_t *hit, double *t, int8_t *which) {
+  ccd_context *ctx = m->ctx;
+  NarrowScratch &ns = L.ns;
+  const int nsub = kind == CCD_VERTEX_FACE ? 3 : 4;
+  cudaStream_t s = L.stream;
+  const ccd::PrimBatch bp{kind, c, ns.prim, ns.eta_prim, true, ns.h_prim, ns.t_prim, nullptr, ns.counters};
+  int rc = enqueue_batch(ctx, bp, path, ns.surv, ns.stage, s, nullptr);
+  if (rc) return rc;
+  const ccd::PrimBatch bve{CCD_VERTEX_EDGE, nsub * c, ns.ve, ns.eta_ve, true, ns.h_ve, ns.t_ve, nullptr,
+                           ns.counters};
+  rc = enqueue_batch(ctx, bve, path, ns.surv, ns.stage, s, nullptr);
+  if (rc) return rc;
+  const ccd::PrimBatch bvv{CCD_VERTEX_VERTEX, nsub * c, ns.vv, ns.eta_vv, true, ns.h_vv, ns.t_vv, nullptr,
+                           ns.counters};
+  rc = enqueue_batch(ctx, bvv, CCD_PATH_FP64, ns.surv, ns.stage, s, nullptr);
+  if (rc) return rc;
+  CCD_CUDA(ccd::combine_chain(kind, c, ns.h_prim, ns.t_prim, ns.h_ve, ns.t_ve, ns.h_vv, ns.t_vv, hit, t, which, s));
+  return CCD_OK;
+}
+
+// The narrow phase over a multi-entry history: every segment of each
+// stencil's stitched common history runs the chain; stencils are taken in
+// chunks of at most kNarrowChunk segments.
+int narrow_device_history(ccd_mesh *m, Lane &L, int kind, int path, int64_t n, const int32_t *st, const double *eta,
+                          bool eta_per_row, uint8_t *hit, double *t, int8_t *which) {
+  ccd_context *ctx = m->ctx;
+  cudaStream_t s = L.stream;
+  int rc = grow(ctx, &L.seg_cnt, &L.seg_cnt_cap, n);
+  if (!rc) rc = grow(ctx, &L.seg_off, &L.seg_off_cap, n + 1);
+  if (!rc) rc = grow(ctx, &L.scan_temp, &L.scan_temp_cap, (int64_t)ccd::scan_temp_bytes(n));
+  if (rc) return rc;
+  CCD_CUDA(ccd::history_segment_counts(kind, st, n, m->hist_off, m->hist_time, m->hist_pos, L.seg_cnt, s));
+  CCD_CUDA(ccd::exclusive_scan_u32(L.seg_cnt, L.seg_off, n, L.seg_off + n, L.scan_temp, (size_t)L.scan_temp_cap, s));
+  L.h_seg_off.resize((size_t)n + 1);
+  CCD_CUDA(cudaMemcpyAsync(L.h_seg_off.data(), L.seg_off, ((size_t)n + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                           s));
+  CCD_CUDA(cudaStreamSynchronize(s));
+  const uint32_t *so = L.h_seg_off.data();
+  for (int64_t i = 0; i < n; i++) {
+    if (so[i + 1] < so[i]) return mesh_fail(m, CCD_ERR_INVALID_ARGUMENT, "2^32 or more history segments");
+    if ((int64_t)(so[i + 1] - so[i]) > kNarrowChunk)
+      return mesh_fail(m, CCD_ERR_INVALID_ARGUMENT, "a stencil's stitched history has more than 2^20 segments");
+  }
+  int64_t i0 = 0;
+  while (i0 < n) {
+    // the longest run of stencils whose segments fit one chunk
+    int64_t i1 = i0;
+    while (i1 < n && (int64_t)(so[i1 + 1] - so[i0]) <= kNarrowChunk) i1++;
+    const int64_t segs = (int64_t)(so[i1] - so[i0]);
+    if (segs > 0) {
+      rc = ensure_narrow(m, L, std::min<int64_t>(kNarrowChunk, std::max<int64_t>(segs, 1)));
+      if (rc) return rc;
+      NarrowScratch &ns = L.ns;
+      CCD_CUDA(ccd::gather_history_rows(kind, st + 4 * i0, i1 - i0, L.seg_off + i0, so[i0], m->hist_off,
+                                        m->hist_time, m->hist_pos, eta_per_row ? eta + i0 : eta, eta_per_row ? 1 : 0,
+                                        ns.prim, ns.ve, ns.vv, ns.eta_prim, ns.eta_ve, ns.eta_vv, s));
+      rc = run_chain(m, L, kind, path, segs, ns.seg_hit, ns.seg_t, ns.seg_which);
+      if (rc) return rc;
+    }
+    CCD_CUDA(ccd::reduce_history_segments(i1 - i0, L.seg_off + i0, so[i0], L.ns.seg_hit, L.ns.seg_t, L.ns.seg_which,
+                                          hit + i0, t ? t + i0 : nullptr, which ? which + i0 : nullptr, s));
+    // the next chunk reuses the row buffers: wait for this one's kernels
+    CCD_CUDA(cudaStreamSynchronize(s));
+    i0 = i1;
+  }
   return CCD_OK;
 }
 
@@ -146,30 +234,19 @@ int narrow_device(ccd_mesh *m, Lane &L, int kind, int path, int64_t n, const int
                   bool eta_per_row, uint8_t *hit, double *t, int8_t *which) {
   ccd_context *ctx = m->ctx;
   if (n == 0) return CCD_OK;
+  if (m->has_history) return narrow_device_history(m, L, kind, path, n, st, eta, eta_per_row, hit, t, which);
   const int64_t chunk = std::min<int64_t>(n, kNarrowChunk);
   int rc = ensure_narrow(m, L, chunk);
   if (rc) return rc;
   NarrowScratch &ns = L.ns;
-  const int nsub = kind == CCD_VERTEX_FACE ? 3 : 4;
   cudaStream_t s = L.stream;
   for (int64_t off = 0; off < n; off += chunk) {
     const int64_t c = std::min<int64_t>(chunk, n - off);
     CCD_CUDA(ccd::gather_stencil_rows(kind, st + 4 * off, c, m->qs, m->qe, eta_per_row ? eta + off : eta,
                                       eta_per_row ? 1 : 0, ns.prim, ns.ve, ns.vv, ns.eta_prim, ns.eta_ve, ns.eta_vv,
                                       s));
-    const ccd::PrimBatch bp{kind, c, ns.prim, ns.eta_prim, true, ns.h_prim, ns.t_prim, nullptr, ns.counters};
-    rc = enqueue_batch(ctx, bp, path, ns.surv, ns.stage, s, nullptr);
+    rc = run_chain(m, L, kind, path, c, hit + off, t ? t + off : nullptr, which ? which + off : nullptr);
     if (rc) return rc;
-    const ccd::PrimBatch bve{CCD_VERTEX_EDGE, nsub * c, ns.ve, ns.eta_ve, true, ns.h_ve, ns.t_ve, nullptr,
-                             ns.counters};
-    rc = enqueue_batch(ctx, bve, path, ns.surv, ns.stage, s, nullptr);
-    if (rc) return rc;
-    const ccd::PrimBatch bvv{CCD_VERTEX_VERTEX, nsub * c, ns.vv, ns.eta_vv, true, ns.h_vv, ns.t_vv, nullptr,
-                             ns.counters};
-    rc = enqueue_batch(ctx, bvv, CCD_PATH_FP64, ns.surv, ns.stage, s, nullptr);
-    if (rc) return rc;
-    CCD_CUDA(ccd::combine_chain(kind, c, ns.h_prim, ns.t_prim, ns.h_ve, ns.t_ve, ns.h_vv, ns.t_vv, hit + off,
-                                t ? t + off : nullptr, which ? which + off : nullptr, s));
   }
   return CCD_OK;
 }
@@ -184,8 +261,15 @@ int run_broadphase(ccd_mesh *m, int kind, double outer_eta, bool whole = false) 
   const ccd::MeshTopology topo{m->nv,         m->nf,         m->nranks,   m->nedges,
                                m->faces,      m->face_rank,  m->rank_triple, m->face_edges,
                                m->rank_edge,  whole ? nullptr : m->face_inst,  whole ? 1 : m->ninst};
-  ccd::BroadphaseParams p{kind, outer_eta, m->qs, m->qe, m->has_fixed ? m->fixed : nullptr,
-                          ctx->opt_count_tests != 0, {nullptr, nullptr, nullptr, nullptr}};
+  ccd::BroadphaseParams p{kind,
+                          outer_eta,
+                          m->qs,
+                          m->qe,
+                          m->has_history ? m->hist_off : nullptr,
+                          m->has_history ? m->hist_pos : nullptr,
+                          m->has_fixed ? m->fixed : nullptr,
+                          ctx->opt_count_tests != 0,
+                          {nullptr, nullptr, nullptr, nullptr}};
   const bool timed = ctx->profiling && m->nf >= 2;
   if (timed) {
     for (int k = 0; k < 4; k++) {
@@ -233,13 +317,14 @@ int check_eta(ccd_mesh *m, int64_t n, const double *eta, int64_t eta_count) {
 
 void free_mesh_buffers(ccd_mesh *m) {
   void *ptrs[] = {m->faces, m->face_rank, m->rank_triple, m->face_edges, m->rank_edge, m->face_inst, m->qs, m->qe,
-                  m->fixed,
+                  m->hist_off, m->hist_time, m->hist_pos, m->fixed,
                   m->cand[0], m->cand[1], m->in_st, m->in_eta, m->which, m->d_eta,
                   m->col[0], m->col[1], m->col_t[0], m->col_t[1]};
   for (void *p : ptrs) cudaFree(p);
   for (Lane &L : m->lane) {
     NarrowScratch &n = L.ns;
-    void *lp[] = {L.hit, L.t, L.flags, L.pos, L.scan_temp, L.d_count, n.prim, n.ve, n.vv, n.eta_prim, n.eta_ve,
+    void *lp[] = {L.hit, L.t, L.flags, L.pos, L.scan_temp, L.d_count, L.seg_cnt, L.seg_off, n.seg_hit, n.seg_t,
+                  n.seg_which, n.prim, n.ve, n.vv, n.eta_prim, n.eta_ve,
                   n.eta_vv, n.h_prim, n.h_ve, n.h_vv, n.t_prim, n.t_ve, n.t_vv, n.surv, n.counters, n.stage.mem};
     for (void *p : lp) cudaFree(p);
   }
@@ -377,6 +462,7 @@ int ccd_mesh_set_positions(ccd_mesh *m, const double *qstart, const double *qend
   CCD_CUDA(cudaMemcpyAsync(m->qs, qstart, bytes, cudaMemcpyHostToDevice, ctx->stream));
   CCD_CUDA(cudaMemcpyAsync(m->qe, qend, bytes, cudaMemcpyHostToDevice, ctx->stream));
   CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+  m->has_history = false;
   m->have_cand = m->have_col = false;
   return CCD_OK;
 }
@@ -389,6 +475,43 @@ int ccd_mesh_set_positions_device(ccd_mesh *m, const double *qstart, const doubl
   const size_t bytes = 3 * (size_t)m->nv * sizeof(double);
   CCD_CUDA(cudaMemcpyAsync(m->qs, qstart, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
   CCD_CUDA(cudaMemcpyAsync(m->qe, qend, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  m->has_history = false;
+  m->have_cand = m->have_col = false;
+  return CCD_OK;
+}
+
+int ccd_mesh_set_history(ccd_mesh *m, const int32_t *offsets, const double *times, const double *positions) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  if (!offsets || !times || !positions) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null history");
+  if (offsets[0] != 0) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "history offsets must start at 0");
+  for (int32_t v = 0; v < m->nv; v++)
+    if (offsets[v + 1] <= offsets[v])
+      return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "every vertex needs at least one history entry");
+  const int64_t ne = offsets[m->nv];
+  for (int32_t v = 0; v < m->nv; v++)
+    for (int32_t e = offsets[v] + 1; e < offsets[v + 1]; e++)
+      if (!(times[e - 1] <= times[e]))
+        return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "history times must be non-decreasing per vertex");
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  if (m->hist_cap < ne || !m->hist_off) {
+    CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+    cudaFree(m->hist_time);
+    cudaFree(m->hist_pos);
+    m->hist_time = m->hist_pos = nullptr;
+    m->hist_cap = 0;
+    CCD_CUDA(cudaMalloc(&m->hist_time, (size_t)ne * sizeof(double)));
+    CCD_CUDA(cudaMalloc(&m->hist_pos, (size_t)ne * 3 * sizeof(double)));
+    m->hist_cap = ne;
+    if (!m->hist_off) CCD_CUDA(cudaMalloc(&m->hist_off, ((size_t)m->nv + 1) * sizeof(int32_t)));
+  }
+  CCD_CUDA(cudaMemcpyAsync(m->hist_off, offsets, ((size_t)m->nv + 1) * sizeof(int32_t), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  CCD_CUDA(cudaMemcpyAsync(m->hist_time, times, (size_t)ne * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CCD_CUDA(cudaMemcpyAsync(m->hist_pos, positions, (size_t)ne * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+  m->has_history = true;
   m->have_cand = m->have_col = false;
   return CCD_OK;
 }

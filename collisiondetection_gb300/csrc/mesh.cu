@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <numeric>
 
+#include "ccd_common.h"
 #include "mesh.cuh"
 #include "radix_sort.cuh"
 
@@ -85,29 +86,18 @@ __device__ __forceinline__ void canonical(int kind, int *v) {
   }
 }
 
-__global__ void __launch_bounds__(kThreads) gather_rows(int kind, const int32_t *st, int64_t n, const double *qs,
-                                                        const double *qe, const double *eta, int eta_per_row,
-                                                        double *prim, double *ve, double *vv, double *eta_prim,
-                                                        double *eta_ve, double *eta_vv) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int v[4] = {st[4 * i], st[4 * i + 1], st[4 * i + 2], st[4 * i + 3]};
-  canonical(kind, v);
-  double P0[12], P1[12];
-  for (int a = 0; a < 4; a++)
-    for (int c = 0; c < 3; c++) {
-      const double s = qs[3 * (int64_t)v[a] + c], e = qe[3 * (int64_t)v[a] + c];
-      P0[3 * a + c] = (1.0 * s + 0.0 * e) / 1.0;  // History::stitchCommonHistory, two entries
-      P1[3 * a + c] = e;
-    }
-  const double et = eta_per_row ? eta[i] : eta[0];
+// The rows of one segment's chain (start points P0, end points P1 of the
+// four stencil vertices, 12 doubles each) at row index i: the primitive row,
+// then the vertex-edge triples and vertex-vertex pairs in chain order.
+__device__ __forceinline__ void write_rows(int kind, const double *P0, const double *P1, double et, int64_t i,
+                                           double *prim, double *ve, double *vv, double *eta_prim, double *eta_ve,
+                                           double *eta_vv) {
   double *r = prim + 24 * i;
   for (int k = 0; k < 12; k++) {
     r[k] = P0[k];
     r[12 + k] = P1[k];
   }
   eta_prim[i] = et;
-  // Vertex-edge and vertex-vertex argument triples / pairs in chain order.
   const int nsub = kind == 0 ? 3 : 4;
   for (int c = 0; c < nsub; c++) {
     int a, b0, b1, w0, w1;
@@ -143,6 +133,134 @@ __global__ void __launch_bounds__(kThreads) gather_rows(int kind, const int32_t 
     eta_ve[nsub * i + c] = et;
     eta_vv[nsub * i + c] = et;
   }
+}
+
+__global__ void __launch_bounds__(kThreads) gather_rows(int kind, const int32_t *st, int64_t n, const double *qs,
+                                                        const double *qe, const double *eta, int eta_per_row,
+                                                        double *prim, double *ve, double *vv, double *eta_prim,
+                                                        double *eta_ve, double *eta_vv) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int v[4] = {st[4 * i], st[4 * i + 1], st[4 * i + 2], st[4 * i + 3]};
+  canonical(kind, v);
+  double P0[12], P1[12];
+  for (int a = 0; a < 4; a++)
+    for (int c = 0; c < 3; c++) {
+      const double s = qs[3 * (int64_t)v[a] + c], e = qe[3 * (int64_t)v[a] + c];
+      P0[3 * a + c] = (1.0 * s + 0.0 * e) / 1.0;  // History::stitchCommonHistory, two entries
+      P1[3 * a + c] = e;
+    }
+  write_rows(kind, P0, P1, eta_per_row ? eta[i] : eta[0], i, prim, ve, vv, eta_prim, eta_ve, eta_vv);
+}
+
+// History::stitchCommonHistory (src/History.cpp:98-140) over the four stencil
+// vertices of a multi-entry history: one call of next() per stitched entry,
+// in the reference's loop order and arithmetic.  The loop is capped at the
+// total number of entries (each stitched entry passes at least one of them).
+struct Stitcher {
+  const double *t, *p;
+  int it[4], end[4];
+  double cur;
+  int budget;
+
+  __device__ Stitcher(const int *v, const int32_t *off, const double *times, const double *pos) : t(times), p(pos) {
+    budget = 1;
+    for (int i = 0; i < 4; i++) {
+      it[i] = off[v[i]];
+      end[i] = off[v[i] + 1];
+      budget += end[i] - it[i];
+    }
+    cur = 0.0;
+  }
+
+  // Writes the entry at the current time (12 doubles) and advances; false
+  // once the reference's loop would have ended.
+  __device__ bool next(double *pos) {
+    if (!(cur <= 1.0) || budget-- <= 0) return false;
+    double newtime = INFINITY;
+    for (int i = 0; i < 4; i++) {
+      int nx = it[i] + 1;
+      while (nx < end[i] && t[nx] <= cur) {
+        nx++;
+        it[i]++;
+      }
+      const double *o = p + 3 * (int64_t)it[i];
+      if (nx == end[i]) {
+        for (int k = 0; k < 3; k++) pos[3 * i + k] = o[k];
+      } else {
+        const double *nw = p + 3 * (int64_t)nx;
+        const double dt = t[nx] - t[it[i]];
+        const double a = cur - t[it[i]];
+        const double b = t[nx] - cur;
+        for (int k = 0; k < 3; k++) pos[3 * i + k] = (b * o[k] + a * nw[k]) / dt;
+        newtime = smin(newtime, t[nx]);
+      }
+    }
+    cur = newtime;
+    return true;
+  }
+};
+
+// Segments (stitched entries - 1) of each stencil's common history.
+__global__ void __launch_bounds__(kThreads) segment_counts(int kind, const int32_t *st, int64_t n,
+                                                           const int32_t *off, const double *times,
+                                                           const double *pos, uint32_t *count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int v[4] = {st[4 * i], st[4 * i + 1], st[4 * i + 2], st[4 * i + 3]};
+  canonical(kind, v);
+  Stitcher sh(v, off, times, pos);
+  double P[12];
+  uint32_t entries = 0;
+  while (sh.next(P)) entries++;
+  count[i] = entries > 0 ? entries - 1 : 0;
+}
+
+// The chain rows of every segment of stencils [0, n): stencil i's segments
+// are rows seg_off[i] - base .. seg_off[i+1] - base - 1.
+__global__ void __launch_bounds__(kThreads) gather_segment_rows(int kind, const int32_t *st, int64_t n,
+                                                                const uint32_t *seg_off, uint32_t base,
+                                                                const int32_t *off, const double *times,
+                                                                const double *pos, const double *eta,
+                                                                int eta_per_row, double *prim, double *ve, double *vv,
+                                                                double *eta_prim, double *eta_ve, double *eta_vv) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int v[4] = {st[4 * i], st[4 * i + 1], st[4 * i + 2], st[4 * i + 3]};
+  canonical(kind, v);
+  const double et = eta_per_row ? eta[i] : eta[0];
+  Stitcher sh(v, off, times, pos);
+  double P[2][12];
+  int cur = 0;
+  int64_t row = (int64_t)seg_off[i] - base;
+  const int64_t last = (int64_t)seg_off[i + 1] - base;
+  if (!sh.next(P[0])) return;
+  while (row < last && sh.next(P[cur ^ 1])) {
+    write_rows(kind, P[cur], P[cur ^ 1], et, row, prim, ve, vv, eta_prim, eta_ve, eta_vv);
+    cur ^= 1;
+    row++;
+  }
+}
+
+// A stencil collides when the chain of one of its segments does; its t and
+// sub-test are those of the first such segment (CTCDNarrowPhase.cpp:33-36).
+__global__ void __launch_bounds__(kThreads) reduce_segments(int64_t n, const uint32_t *seg_off, uint32_t base,
+                                                            const uint8_t *seg_hit, const double *seg_t,
+                                                            const int8_t *seg_which, uint8_t *hit, double *t,
+                                                            int8_t *which) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int8_t w = -1;
+  double tt = 0.0;
+  for (int64_t s = (int64_t)seg_off[i] - base; s < (int64_t)seg_off[i + 1] - base; s++)
+    if (seg_hit[s]) {
+      w = seg_which[s];
+      tt = seg_t[s];
+      break;
+    }
+  hit[i] = w >= 0;
+  if (w >= 0 && t) t[i] = tt;
+  if (which) which[i] = w;
 }
 
 __global__ void __launch_bounds__(kThreads) combine(int nsub, int64_t n, const uint8_t *h_prim, const double *t_prim,
@@ -206,6 +324,33 @@ cudaError_t gather_stencil_rows(int kind, const int32_t *stencils, int64_t n, co
   if (n <= 0) return cudaSuccess;
   gather_rows<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(
       kind, stencils, n, qs, qe, eta, eta_per_row, prim, ve, vv, eta_prim, eta_ve, eta_vv);
+  return cudaGetLastError();
+}
+
+cudaError_t history_segment_counts(int kind, const int32_t *stencils, int64_t n, const int32_t *off,
+                                   const double *times, const double *pos, uint32_t *count, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  segment_counts<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(kind, stencils, n, off, times, pos,
+                                                                                count);
+  return cudaGetLastError();
+}
+
+cudaError_t gather_history_rows(int kind, const int32_t *stencils, int64_t n, const uint32_t *seg_off,
+                                uint32_t base, const int32_t *off, const double *times, const double *pos,
+                                const double *eta, int eta_per_row, double *prim, double *ve, double *vv,
+                                double *eta_prim, double *eta_ve, double *eta_vv, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  gather_segment_rows<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(
+      kind, stencils, n, seg_off, base, off, times, pos, eta, eta_per_row, prim, ve, vv, eta_prim, eta_ve, eta_vv);
+  return cudaGetLastError();
+}
+
+cudaError_t reduce_history_segments(int64_t n, const uint32_t *seg_off, uint32_t base, const uint8_t *seg_hit,
+                                    const double *seg_t, const int8_t *seg_which, uint8_t *hit, double *t,
+                                    int8_t *which, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  reduce_segments<<<(unsigned)((n + kThreads - 1) / kThreads), kThreads, 0, s>>>(n, seg_off, base, seg_hit, seg_t,
+                                                                                 seg_which, hit, t, which);
   return cudaGetLastError();
 }
 

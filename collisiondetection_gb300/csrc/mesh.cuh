@@ -31,6 +31,25 @@ cudaError_t gather_stencil_rows(int kind, const int32_t *stencils, int64_t n, co
                                 const double *eta, int eta_per_row, double *prim, double *ve, double *vv,
                                 double *eta_prim, double *eta_ve, double *eta_vv, cudaStream_t s);
 
+// A multi-entry History: vertex v's entries are off[v] .. off[v+1]-1 of times
+// and pos ([entries][3]).  The narrow phase runs its chain on every segment of
+// each stencil's stitched common history (History::stitchCommonHistory,
+// src/History.cpp:98-140; CTCDNarrowPhase.cpp:24-72, 74-135):
+//   history_segment_counts: count[i] = segments of stencil i;
+//   gather_history_rows: the chain rows of stencils [0, n), stencil i's
+//     segments at rows seg_off[i] - base .. seg_off[i+1] - base - 1;
+//   reduce_history_segments: per stencil, the first segment whose chain hits
+//     (hit, t, which as combine_chain gives them per segment).
+cudaError_t history_segment_counts(int kind, const int32_t *stencils, int64_t n, const int32_t *off,
+                                   const double *times, const double *pos, uint32_t *count, cudaStream_t s);
+cudaError_t gather_history_rows(int kind, const int32_t *stencils, int64_t n, const uint32_t *seg_off,
+                                uint32_t base, const int32_t *off, const double *times, const double *pos,
+                                const double *eta, int eta_per_row, double *prim, double *ve, double *vv,
+                                double *eta_prim, double *eta_ve, double *eta_vv, cudaStream_t s);
+cudaError_t reduce_history_segments(int64_t n, const uint32_t *seg_off, uint32_t base, const uint8_t *seg_hit,
+                                    const double *seg_t, const int8_t *seg_which, uint8_t *hit, double *t,
+                                    int8_t *which, cudaStream_t s);
+
 // First hit along the reference's chain: primitive, then the vertex-edge
 // tests, then the vertex-vertex tests (src/CTCDNarrowPhase.cpp:43-69, 92-129).
 // which: 0 primitive, 1 vertex-edge, 2 vertex-vertex, -1 miss.

@@ -344,3 +344,39 @@ def uneven_batch(n_instances: int = 512, lo: float = 200.0, hi: float = 2e5, see
     return (np.ascontiguousarray(np.concatenate(faces), dtype=np.int32),
             np.ascontiguousarray(np.concatenate(frames, axis=1).reshape(steps + 1, -1)),
             np.array(vo, np.int32), np.array(fo, np.int32))
+
+
+def multi_entry_history(q0, q1, seed: int, active: float = 0.3, max_entries: int = 6, jitter: float = 0.02,
+                        pool: int = 16):
+    """A History with extra entries between its start (t = 0, q0) and end
+    (t = 1, q1), shaped like the ones the active-layers loop leaves: a
+    fraction `active` of the vertices gets 1..max_entries intermediate
+    entries at times drawn from a shared pool (so that vertices share entry
+    times, as the vertices of one penalty group do), at the straight-line
+    position plus N(0, jitter) noise.  Returns (offsets [V+1] int32, times [E],
+    positions [E][3])."""
+    rng = np.random.default_rng(seed)
+    q0 = np.asarray(q0, np.float64).reshape(-1, 3)
+    q1 = np.asarray(q1, np.float64).reshape(-1, 3)
+    nv = q0.shape[0]
+    times_pool = np.sort(rng.uniform(0.02, 0.98, pool))
+    offsets = np.zeros(nv + 1, np.int32)
+    times, positions = [], []
+    for v in range(nv):
+        ts = [0.0]
+        if rng.random() < active:
+            k = int(rng.integers(1, max_entries + 1))
+            ts += sorted(rng.choice(times_pool, size=min(k, pool), replace=False).tolist())
+        ts.append(1.0)
+        for t in ts:
+            p = (1.0 - t) * q0[v] + t * q1[v]
+            if 0.0 < t < 1.0:
+                p = p + rng.normal(0.0, jitter, 3)
+            elif t == 1.0:
+                p = q1[v]
+            else:
+                p = q0[v]
+            times.append(t)
+            positions.append(p)
+        offsets[v + 1] = offsets[v] + len(ts)
+    return offsets, np.array(times, np.float64), np.array(positions, np.float64)

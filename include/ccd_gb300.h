@@ -213,6 +213,19 @@ int ccd_mesh_destroy(ccd_mesh *mesh);
 int ccd_mesh_set_positions(ccd_mesh *mesh, const double *qstart, const double *qend);
 /* The same from device memory; enqueued on the context's stream. */
 int ccd_mesh_set_positions_device(ccd_mesh *mesh, const double *qstart, const double *qend);
+/* A History with any number of entries per vertex (src/History.h; what
+ * History::getVertexHistory(v) holds for every v): vertex v's entries are
+ * offsets[v] .. offsets[v+1]-1 of times[] and positions[] ([entries][3]), in
+ * time order, normally from time 0 (History's constructor) to time 1
+ * (finishHistory) with the entries addHistory put between.  offsets has
+ * nverts + 1 values, offsets[0] = 0, at least one entry per vertex.  Until
+ * the next ccd_mesh_set_positions it replaces the two-entry step: the broad
+ * phases take their slabs over every entry (src/KDOPBroadPhase.cpp:60-70),
+ * and the narrow phase runs its chain on every segment of each stencil's
+ * stitched common history (History::stitchCommonHistory,
+ * src/History.cpp:98-140); a stencil collides when one segment does, and
+ * its t is that segment's.  Host memory; blocks until copied. */
+int ccd_mesh_set_history(ccd_mesh *mesh, const int32_t *offsets, const double *times, const double *positions);
 /* fixedVerts as nverts bytes (non-zero = fixed), or NULL for none. */
 int ccd_mesh_set_fixed(ccd_mesh *mesh, const uint8_t *fixed);
 

@@ -1139,8 +1139,23 @@ static int trivial_candidates(int nverts, int nfaces, const int32_t *faces, cons
   return rc;
 }
 
+static int broadphase_impl(int kind, int nverts, const double *qstart, const double *qend, const int32_t *hoff,
+                           const double *hpos, int nfaces, const int32_t *faces, double eta, const uint8_t *fixed,
+                           int64_t *n_vf, int64_t *n_ee);
+
 int oracle_broadphase(int kind, int nverts, const double *qstart, const double *qend, int nfaces,
                       const int32_t *faces, double eta, const uint8_t *fixed, int64_t *n_vf, int64_t *n_ee) {
+  return broadphase_impl(kind, nverts, qstart, qend, NULL, NULL, nfaces, faces, eta, fixed, n_vf, n_ee);
+}
+
+int oracle_broadphase_history(int kind, int nverts, const int32_t *offsets, const double *positions, int nfaces,
+                              const int32_t *faces, double eta, const uint8_t *fixed, int64_t *n_vf, int64_t *n_ee) {
+  return broadphase_impl(kind, nverts, NULL, NULL, offsets, positions, nfaces, faces, eta, fixed, n_vf, n_ee);
+}
+
+static int broadphase_impl(int kind, int nverts, const double *qstart, const double *qend, const int32_t *hoff,
+                           const double *hpos, int nfaces, const int32_t *faces, double eta, const uint8_t *fixed,
+                           int64_t *n_vf, int64_t *n_ee) {
   if (kind == 2) {
     g_vf.n = g_ee.n = 0;
     g_pairs = 0;
@@ -1182,8 +1197,10 @@ int oracle_broadphase(int kind, int nverts, const double *qstart, const double *
     }
     for (int j = 0; j < 3; j++) {
       int vtx = faces[3 * f + j];
-      for (int e = 0; e < 2; e++) {
-        vec3 pos = v3((e == 0 ? qstart : qend) + 3 * (size_t)vtx);
+      /* every History entry of the vertex (KDOPBroadPhase.cpp:60-70) */
+      int e0 = hoff ? hoff[vtx] : 0, e1 = hoff ? hoff[vtx + 1] : 2;
+      for (int e = e0; e < e1; e++) {
+        vec3 pos = hoff ? v3(hpos + 3 * (size_t)e) : v3((e == 0 ? qstart : qend) + 3 * (size_t)vtx);
         for (int k = 0; k < K; k++) {
           double s = (kind == 0) ? vdot(pos, axis[k]) : (k == 0 ? pos.x : (k == 1 ? pos.y : pos.z));
           L[k] = smin(s - eta, L[k]);
@@ -1274,14 +1291,24 @@ static void stitched_start(const double *qs, const double *qe, int v, double *ou
 }
 
 /* CTCDNarrowPhase::checkVFS (src/CTCDNarrowPhase.cpp:24-72). */
+static int chain_vf(const double *P0, const double *P1, double eta, double *t);
+static int chain_ee(const double *P0, const double *P1, double eta, double *t);
+
 static int check_vf_stencil(const double *qs, const double *qe, const int32_t *st, double eta, double *t) {
-  double P0[12], P1[12], x[24];
+  double P0[12], P1[12];
   for (int i = 0; i < 4; i++) {
     stitched_start(qs, qe, st[i], P0 + 3 * i);
     memcpy(P1 + 3 * i, qe + 3 * (size_t)st[i], 3 * sizeof(double));
   }
-  memcpy(x, P0, sizeof P0);
-  memcpy(x + 12, P1, sizeof P1);
+  return chain_vf(P0, P1, eta, t);
+}
+
+/* The chain of CTCDNarrowPhase::checkVFS (src/CTCDNarrowPhase.cpp:33-69) on
+ * one segment: 0 vertex-face, 1 vertex-edge, 2 vertex-vertex hit, -1 none. */
+static int chain_vf(const double *P0, const double *P1, double eta, double *t) {
+  double x[24];
+  memcpy(x, P0, 12 * sizeof(double));
+  memcpy(x + 12, P1, 12 * sizeof(double));
   if (oracle_vf(x, eta, t)) return 0;
   for (int edge = 0; edge < 3; edge++) {
     int i1 = 1 + (edge % 3), i2 = 1 + ((edge + 1) % 3);
@@ -1305,15 +1332,22 @@ static int check_vf_stencil(const double *qs, const double *qe, const int32_t *s
 
 /* CTCDNarrowPhase::checkEES (src/CTCDNarrowPhase.cpp:74-135). */
 static int check_ee_stencil(const double *qs, const double *qe, const int32_t *st, double eta, double *t) {
-  static const int ve[4][3] = {{0, 2, 3}, {1, 2, 3}, {2, 0, 1}, {3, 0, 1}};
-  static const int vv[4][2] = {{0, 2}, {0, 3}, {1, 2}, {1, 3}};
-  double P0[12], P1[12], x[24];
+  double P0[12], P1[12];
   for (int i = 0; i < 4; i++) {
     stitched_start(qs, qe, st[i], P0 + 3 * i);
     memcpy(P1 + 3 * i, qe + 3 * (size_t)st[i], 3 * sizeof(double));
   }
-  memcpy(x, P0, sizeof P0);
-  memcpy(x + 12, P1, sizeof P1);
+  return chain_ee(P0, P1, eta, t);
+}
+
+/* The chain of CTCDNarrowPhase::checkEES (src/CTCDNarrowPhase.cpp:84-129) on
+ * one segment. */
+static int chain_ee(const double *P0, const double *P1, double eta, double *t) {
+  static const int ve[4][3] = {{0, 2, 3}, {1, 2, 3}, {2, 0, 1}, {3, 0, 1}};
+  static const int vv[4][2] = {{0, 2}, {0, 3}, {1, 2}, {1, 3}};
+  double x[24];
+  memcpy(x, P0, 12 * sizeof(double));
+  memcpy(x + 12, P1, 12 * sizeof(double));
   if (oracle_ee(x, eta, t)) return 0;
   for (int c = 0; c < 4; c++) {
     for (int j = 0; j < 3; j++) {
@@ -1641,4 +1675,86 @@ int oracle_penalty_group_force(int nverts, const double *q, const double *v, int
   for (int64_t i = 0; i < 3 * (int64_t)nverts; i++) F[i] = F[i] + G[i] * dt;
   free(G);
   return newused;
+}
+
+
+/* ------------------------------------------------------------ multi-entry history */
+/* History::stitchCommonHistory (src/History.cpp:98-140) over the four
+ * vertices v of a history given as offsets / times / positions: writes the
+ * stitched entries' positions (12 doubles each) into out (room for cap) and
+ * returns their number. */
+static int stitch4(const int32_t *off, const double *times, const double *pos, const int32_t *v, double *out,
+                   int cap) {
+  int it[4], end[4], n = 0;
+  for (int i = 0; i < 4; i++) {
+    it[i] = off[v[i]];
+    end[i] = off[v[i] + 1];
+  }
+  double curtime = 0;
+  while (curtime <= 1.0 && n < cap) {
+    double newtime = INFINITY;
+    double *e = out + 12 * (size_t)n;
+    for (int i = 0; i < 4; i++) {
+      int next = it[i] + 1;
+      while (next != end[i] && times[next] <= curtime) {
+        ++next;
+        ++it[i];
+      }
+      const double *oldpos = pos + 3 * (size_t)it[i];
+      if (next == end[i]) {
+        for (int k = 0; k < 3; k++) e[3 * i + k] = oldpos[k];
+      } else {
+        const double *newpos = pos + 3 * (size_t)next;
+        double dt = times[next] - times[it[i]];
+        double a = curtime - times[it[i]];
+        double b = times[next] - curtime;
+        for (int k = 0; k < 3; k++) e[3 * i + k] = (b * oldpos[k] + a * newpos[k]) / dt;
+        newtime = smin(newtime, times[next]);
+      }
+    }
+    n++;
+    curtime = newtime;
+  }
+  return n;
+}
+
+/* CTCDNarrowPhase::findCollisions (src/CTCDNarrowPhase.cpp:9-135) on a
+ * multi-entry history: each stencil's chain on every segment of its stitched
+ * common history; hit / t / which of the first segment that hits. */
+int oracle_narrowphase_history(int nverts, const int32_t *offsets, const double *times, const double *positions,
+                               int64_t n_vf, const int32_t *vf, const double *vf_eta, int64_t n_ee, const int32_t *ee,
+                               const double *ee_eta, uint8_t *vf_hit, uint8_t *ee_hit, double *vf_t, double *ee_t,
+                               int8_t *vf_which, int8_t *ee_which) {
+  int maxe = 0;
+  for (int v = 0; v < nverts; v++)
+    if (offsets[v + 1] - offsets[v] > maxe) maxe = offsets[v + 1] - offsets[v];
+  const int cap = 4 * maxe + 2;
+  double *buf = (double *)malloc((size_t)cap * 12 * sizeof(double));
+  if (!buf) return -1;
+  for (int kind = 0; kind < 2; kind++) {
+    const int64_t n = kind == 0 ? n_vf : n_ee;
+    for (int64_t i = 0; i < n; i++) {
+      const int32_t *raw = (kind == 0 ? vf : ee) + 4 * i;
+      int32_t st[4];
+      if (kind == 0)
+        oracle_vf_canon(raw[0], raw[1], raw[2], raw[3], st);
+      else
+        oracle_ee_canon(raw[0], raw[1], raw[2], raw[3], st);
+      const int ne = stitch4(offsets, times, positions, st, buf, cap);
+      const double eta = (kind == 0 ? vf_eta : ee_eta)[i];
+      int w = -1;
+      double t = 0;
+      for (int sgm = 0; sgm + 1 < ne && w < 0; sgm++)
+        w = kind == 0 ? chain_vf(buf + 12 * (size_t)sgm, buf + 12 * (size_t)(sgm + 1), eta, &t)
+                      : chain_ee(buf + 12 * (size_t)sgm, buf + 12 * (size_t)(sgm + 1), eta, &t);
+      uint8_t *hit = kind == 0 ? vf_hit : ee_hit;
+      double *tt = kind == 0 ? vf_t : ee_t;
+      int8_t *wh = kind == 0 ? vf_which : ee_which;
+      hit[i] = (uint8_t)(w >= 0);
+      if (w >= 0 && tt) tt[i] = t;
+      if (wh) wh[i] = (int8_t)w;
+    }
+  }
+  free(buf);
+  return 0;
 }

@@ -84,6 +84,18 @@ int oracle_penalty_group_force(int nverts, const double *q, const double *v, int
                                double outer_eta, double inner_eta, double stiffness, double cor, double dt,
                                double *F, uint8_t *vf_fired, uint8_t *ee_fired);
 
+/* The same two phases on a multi-entry History (src/History.h): vertex v's
+ * entries are offsets[v] .. offsets[v+1]-1 of times / positions ([E][3]).
+ * The broad phase takes slabs over every entry; the narrow phase runs its
+ * chain on every segment of each stencil's stitched common history
+ * (History::stitchCommonHistory) and reports the first segment that hits. */
+int oracle_broadphase_history(int kind, int nverts, const int32_t *offsets, const double *positions, int nfaces,
+                              const int32_t *faces, double eta, const uint8_t *fixed, int64_t *n_vf, int64_t *n_ee);
+int oracle_narrowphase_history(int nverts, const int32_t *offsets, const double *times, const double *positions,
+                               int64_t n_vf, const int32_t *vf, const double *vf_eta, int64_t n_ee, const int32_t *ee,
+                               const double *ee_eta, uint8_t *vf_hit, uint8_t *ee_hit, double *vf_t, double *ee_t,
+                               int8_t *vf_which, int8_t *ee_which);
+
 /* Stencil canonical forms (src/Stencils.h): writes the canonical 4-tuple. */
 void oracle_vf_canon(int p, int q0, int q1, int q2, int32_t *out);
 void oracle_ee_canon(int p0, int p1, int q0, int q1, int32_t *out);

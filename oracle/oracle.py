@@ -115,7 +115,49 @@ class Oracle(_Lib):
         L.oracle_mesh_self_distance.restype = ctypes.c_double
         L.oracle_vertex_scan.argtypes = [ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_int, ctypes.c_int]
         L.oracle_vertex_scan.restype = ctypes.c_double
+        L.oracle_broadphase_history.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int, _P,
+                                                ctypes.c_double, _P, _P, _P]
+        L.oracle_broadphase_history.restype = ctypes.c_int
+        L.oracle_narrowphase_history.argtypes = [ctypes.c_int, _P, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P, _P,
+                                                 _P, _P, _P]
+        L.oracle_narrowphase_history.restype = ctypes.c_int
         self._distance_setup()
+
+    def broadphase_history(self, kind: int, offsets, times, positions, faces, eta: float, fixed=None):
+        """The broad phase on a multi-entry history (slabs over every entry)."""
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        pos = np.ascontiguousarray(positions, dtype=np.float64)
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        nvf, nee = ctypes.c_int64(), ctypes.c_int64()
+        rc = self.lib.oracle_broadphase_history(kind, off.size - 1, _ptr(off), _ptr(pos), faces.shape[0],
+                                                _ptr(faces), eta, _ptr(fx), ctypes.byref(nvf), ctypes.byref(nee))
+        if rc != 0:
+            raise MemoryError("oracle_broadphase_history failed")
+        vf = np.zeros((nvf.value, 4), np.int32)
+        ee = np.zeros((nee.value, 4), np.int32)
+        self.lib.oracle_broadphase_get(_ptr(vf), _ptr(ee))
+        return vf, ee
+
+    def narrowphase_history(self, offsets, times, positions, vf, vf_eta, ee, ee_eta):
+        """CTCDNarrowPhase on a multi-entry history: dict of hit / t / which."""
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        tt = np.ascontiguousarray(times, dtype=np.float64)
+        pos = np.ascontiguousarray(positions, dtype=np.float64)
+        vf = np.ascontiguousarray(vf, dtype=np.int32).reshape(-1, 4)
+        ee = np.ascontiguousarray(ee, dtype=np.int32).reshape(-1, 4)
+        vfe = np.ascontiguousarray(np.broadcast_to(np.asarray(vf_eta, np.float64), (vf.shape[0],)))
+        eee = np.ascontiguousarray(np.broadcast_to(np.asarray(ee_eta, np.float64), (ee.shape[0],)))
+        out = {"vf_hit": np.zeros(vf.shape[0], np.uint8), "ee_hit": np.zeros(ee.shape[0], np.uint8),
+               "vf_t": np.full(vf.shape[0], np.nan), "ee_t": np.full(ee.shape[0], np.nan),
+               "vf_which": np.zeros(vf.shape[0], np.int8), "ee_which": np.zeros(ee.shape[0], np.int8)}
+        rc = self.lib.oracle_narrowphase_history(off.size - 1, _ptr(off), _ptr(tt), _ptr(pos), vf.shape[0], _ptr(vf),
+                                                 _ptr(vfe), ee.shape[0], _ptr(ee), _ptr(eee), _ptr(out["vf_hit"]),
+                                                 _ptr(out["ee_hit"]), _ptr(out["vf_t"]), _ptr(out["ee_t"]),
+                                                 _ptr(out["vf_which"]), _ptr(out["ee_which"]))
+        if rc != 0:
+            raise MemoryError("oracle_narrowphase_history failed")
+        return out
 
     def vertex_scan(self, verts, faces, i0: int, i1: int) -> float:
         """meshSelfDistance's O(V F) vertex scan over vertices [i0, i1)."""
@@ -195,7 +237,38 @@ class Reference(_Lib):
         L.ref_narrowphase.argtypes = [ctypes.c_int, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P]
         L.ref_mesh_self_distance.argtypes = [ctypes.c_int, _P, ctypes.c_int, _P, _P]
         L.ref_mesh_self_distance.restype = ctypes.c_double
+        L.ref_broadphase_history.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, _P, ctypes.c_int, _P,
+                                             ctypes.c_double, _P, _P, _P]
+        L.ref_narrowphase_history.argtypes = [ctypes.c_int, _P, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P]
         self._distance_setup()
+
+    def broadphase_history(self, kind: int, offsets, times, positions, faces, eta: float, fixed=None):
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        tt = np.ascontiguousarray(times, dtype=np.float64)
+        pos = np.ascontiguousarray(positions, dtype=np.float64)
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        nvf, nee = ctypes.c_int64(), ctypes.c_int64()
+        self.lib.ref_broadphase_history(kind, off.size - 1, _ptr(off), _ptr(tt), _ptr(pos), faces.shape[0],
+                                        _ptr(faces), eta, _ptr(fx), ctypes.byref(nvf), ctypes.byref(nee))
+        vf = np.zeros((nvf.value, 4), np.int32)
+        ee = np.zeros((nee.value, 4), np.int32)
+        self.lib.ref_broadphase_get(_ptr(vf), _ptr(ee))
+        return vf, ee
+
+    def narrowphase_history(self, offsets, times, positions, vf, vf_eta, ee, ee_eta):
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        tt = np.ascontiguousarray(times, dtype=np.float64)
+        pos = np.ascontiguousarray(positions, dtype=np.float64)
+        vf = np.ascontiguousarray(vf, dtype=np.int32).reshape(-1, 4)
+        ee = np.ascontiguousarray(ee, dtype=np.int32).reshape(-1, 4)
+        vfe = np.ascontiguousarray(np.broadcast_to(np.asarray(vf_eta, np.float64), (vf.shape[0],)))
+        eee = np.ascontiguousarray(np.broadcast_to(np.asarray(ee_eta, np.float64), (ee.shape[0],)))
+        vh = np.zeros(vf.shape[0], np.uint8)
+        eh = np.zeros(ee.shape[0], np.uint8)
+        self.lib.ref_narrowphase_history(off.size - 1, _ptr(off), _ptr(tt), _ptr(pos), vf.shape[0], _ptr(vf),
+                                         _ptr(vfe), ee.shape[0], _ptr(ee), _ptr(eee), _ptr(vh), _ptr(eh))
+        return vh, eh
 
     def mesh_self_distance(self, verts, faces, fixed=None) -> float:
         verts = np.ascontiguousarray(verts, dtype=np.float64).ravel()

@@ -191,6 +191,74 @@ double ref_mesh_self_distance(int nverts, const double *q, int nfaces, const int
   return Distance::meshSelfDistance(vecx(nverts, q), m.faces, fixedVerts);
 }
 
+// ---------------------------------------------------------------- multi-entry history
+// A History built through the reference's own API: the constructor takes each
+// vertex's first entry (time 0), addHistory the others in order.
+static History *make_history(int nverts, const int32_t *off, const double *times, const double *pos) {
+  Eigen::VectorXd q0(3 * nverts);
+  for (int v = 0; v < nverts; v++)
+    for (int k = 0; k < 3; k++) q0[3 * v + k] = pos[3 * (size_t)off[v] + k];
+  History *h = new History(q0);
+  for (int v = 0; v < nverts; v++)
+    for (int e = off[v] + 1; e < off[v + 1]; e++) h->addHistory(v, times[e], v3(pos + 3 * (size_t)e));
+  return h;
+}
+
+void ref_broadphase_history(int kind, int nverts, const int32_t *off, const double *times, const double *pos,
+                            int nfaces, const int32_t *faces, double eta, const uint8_t *fixed, int64_t *n_vf,
+                            int64_t *n_ee) {
+  History *h = make_history(nverts, off, times, pos);
+  Mesh m;
+  std::vector<double> q0(3 * (size_t)nverts);
+  for (int v = 0; v < nverts; v++)
+    for (int k = 0; k < 3; k++) q0[3 * (size_t)v + k] = pos[3 * (size_t)off[v] + k];
+  build_mesh(nverts, q0.data(), nfaces, faces, m);
+  std::set<int> fixedVerts;
+  if (fixed)
+    for (int i = 0; i < nverts; i++)
+      if (fixed[i]) fixedVerts.insert(i);
+  std::set<VertexFaceStencil> vfs;
+  std::set<EdgeEdgeStencil> ees;
+  if (kind == 0) {
+    KDOPBroadPhase bp;
+    bp.findCollisionCandidates(*h, m, eta, vfs, ees, fixedVerts);
+  } else {
+    ref_aabb_candidates(*h, m, eta, vfs, ees, fixedVerts);
+  }
+  delete h;
+  g_vf.clear();
+  g_ee.clear();
+  for (std::set<VertexFaceStencil>::const_iterator it = vfs.begin(); it != vfs.end(); ++it) {
+    g_vf.push_back(it->p); g_vf.push_back(it->q0); g_vf.push_back(it->q1); g_vf.push_back(it->q2);
+  }
+  for (std::set<EdgeEdgeStencil>::const_iterator it = ees.begin(); it != ees.end(); ++it) {
+    g_ee.push_back(it->p0); g_ee.push_back(it->p1); g_ee.push_back(it->q0); g_ee.push_back(it->q1);
+  }
+  *n_vf = (int64_t)(g_vf.size() / 4);
+  *n_ee = (int64_t)(g_ee.size() / 4);
+}
+
+void ref_narrowphase_history(int nverts, const int32_t *off, const double *times, const double *pos, int64_t n_vf,
+                             const int32_t *vf, const double *vf_eta, int64_t n_ee, const int32_t *ee,
+                             const double *ee_eta, uint8_t *vf_hit, uint8_t *ee_hit) {
+  History *h = make_history(nverts, off, times, pos);
+  std::set<std::pair<VertexFaceStencil, double> > cvf;
+  std::set<std::pair<EdgeEdgeStencil, double> > cee;
+  for (int64_t i = 0; i < n_vf; i++)
+    cvf.insert(std::make_pair(VertexFaceStencil(vf[4 * i], vf[4 * i + 1], vf[4 * i + 2], vf[4 * i + 3]), vf_eta[i]));
+  for (int64_t i = 0; i < n_ee; i++)
+    cee.insert(std::make_pair(EdgeEdgeStencil(ee[4 * i], ee[4 * i + 1], ee[4 * i + 2], ee[4 * i + 3]), ee_eta[i]));
+  std::set<VertexFaceStencil> ovf;
+  std::set<EdgeEdgeStencil> oee;
+  CTCDNarrowPhase np;
+  np.findCollisions(*h, cvf, cee, ovf, oee);
+  delete h;
+  for (int64_t i = 0; i < n_vf; i++)
+    vf_hit[i] = (uint8_t)ovf.count(VertexFaceStencil(vf[4 * i], vf[4 * i + 1], vf[4 * i + 2], vf[4 * i + 3]));
+  for (int64_t i = 0; i < n_ee; i++)
+    ee_hit[i] = (uint8_t)oee.count(EdgeEdgeStencil(ee[4 * i], ee[4 * i + 1], ee[4 * i + 2], ee[4 * i + 3]));
+}
+
 // ---------------------------------------------------------------- penalty forces
 // PenaltyGroup::addForce on one group built from the given stencils (with
 // their isnew flags); F is updated in place; *_fired from the potentials'

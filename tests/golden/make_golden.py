@@ -27,9 +27,13 @@ the reference's example meshes, and writes:
   non-canonical and repeated stencils, with and without new stencils: the
   forces, the per-stencil fired flags (from the potentials' own addForce) and
   the returned newused flag.
+* ``history.npz`` / ``history.json`` -- multi-entry histories (built with
+  History's constructor and addHistory) for the two spheres, a sheet on a
+  sphere and two hand-built triangles: k-DOP and AABB candidate digests, free
+  and with fixed vertices, and CTCDNarrowPhase's colliding stencils.
 
 Only runs where the reference tree exists:
-    python tests/golden/make_golden.py [--only distances|trivial|penalty]
+    python tests/golden/make_golden.py [--only distances|trivial|penalty|history]
 """
 from __future__ import annotations
 
@@ -333,6 +337,45 @@ def penalty_fixtures(ref) -> None:
         json.dump(meta, fh, indent=1, sort_keys=True)
 
 
+def history_fixtures(ref) -> None:
+    """KDOPBroadPhase / AABBBroadPhase candidate digests and CTCDNarrowPhase
+    results on multi-entry histories built through History's own API."""
+    scenes = {}
+    qs, qe, f = W.two_spheres(seed=1)
+    scenes["spheres"] = (W.multi_entry_history(qs, qe, seed=5), f, 1e-3)
+    f2, frames = W.cloth_frames(grid=24, level=2, seed=6, steps=30)
+    scenes["cloth"] = (W.multi_entry_history(frames[26], frames[28], seed=6, active=0.5, max_entries=10,
+                                             jitter=0.004), f2, 2e-3)
+    # vertices whose histories start late / hold one entry only / repeat a time
+    q0 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.2, 0.2, 0.3], [1.2, 0.2, 0.3], [0.2, 1.2, 0.3]], float)
+    q1 = q0.copy()
+    q1[3:, 2] -= 0.6  # the upper triangle passes through the lower one
+    off, tt, pp = W.multi_entry_history(q0, q1, seed=7, active=1.0, max_entries=4, jitter=0.01, pool=3)
+    scenes["hand"] = ((off, tt, pp), np.array([[0, 1, 2], [3, 4, 5]], np.int32), 1e-2)
+    arrays, meta = {}, {}
+    for name, ((off, tt, pp), f, eta) in scenes.items():
+        arrays[f"{name}_offsets"], arrays[f"{name}_times"], arrays[f"{name}_positions"] = off, tt, pp
+        arrays[f"{name}_faces"] = f
+        fixed = np.zeros(off.size - 1, np.uint8)
+        fixed[: (off.size - 1) // 2] = 1
+        arrays[f"{name}_fixed"] = fixed
+        entry = {"eta": eta}
+        for kind, label in ((0, "kdop"), (1, "aabb")):
+            for fx_label, fx in (("", None), ("_fixed", fixed)):
+                vf, ee = ref.broadphase_history(kind, off, tt, pp, f, eta, fx)
+                entry[f"{label}{fx_label}"] = {"n_vf": int(vf.shape[0]), "n_ee": int(ee.shape[0]),
+                                               "digest": digest(vf, ee)}
+        vf, ee = ref.broadphase_history(0, off, tt, pp, f, eta)
+        vh, eh = ref.narrowphase_history(off, tt, pp, vf, eta, ee, eta)
+        arrays[f"{name}_hit_vf"] = vf[vh.astype(bool)]
+        arrays[f"{name}_hit_ee"] = ee[eh.astype(bool)]
+        entry["narrow"] = {"n_vf_hit": int(vh.sum()), "n_ee_hit": int(eh.sum()), "digest": digest(vh, eh)}
+        meta[name] = entry
+    np.savez_compressed(os.path.join(HERE, "history.npz"), **arrays)
+    with open(os.path.join(HERE, "history.json"), "w") as fh:
+        json.dump(meta, fh, indent=1, sort_keys=True)
+
+
 def main() -> None:
     if not os.path.isdir(REF_TREE):
         sys.exit(f"reference tree not found at {REF_TREE}")
@@ -347,6 +390,9 @@ def main() -> None:
         return
     if only == "penalty":
         penalty_fixtures(ref)
+        return
+    if only == "history":
+        history_fixtures(ref)
         return
 
     kat = []
@@ -408,6 +454,7 @@ def main() -> None:
     distance_fixtures(ref)
     trivial_fixtures(ref)
     penalty_fixtures(ref)
+    history_fixtures(ref)
     print("wrote", sorted(os.listdir(HERE)))
 
 

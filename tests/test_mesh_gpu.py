@@ -311,3 +311,74 @@ def test_trivial_broadphase_rejects_instances(ctx):
                                                           [0, f.shape[0], ff.shape[0]])) as m:
         with pytest.raises(C.CcdError):
             m.broadphase(C.BROADPHASE_TRIVIAL, 1e-6)
+
+
+# ------------------------------------------------------------------ multi-entry History
+@pytest.mark.parametrize("scene", ["spheres", "cloth", "hand"])
+def test_multi_entry_history_matches_reference(ctx, oracle, golden_dir, scene):
+    meta = json.load(open(os.path.join(golden_dir, "history.json")))[scene]
+    g = np.load(os.path.join(golden_dir, "history.npz"))
+    off, tt, pp = g[f"{scene}_offsets"], g[f"{scene}_times"], g[f"{scene}_positions"]
+    f, fixed, eta = g[f"{scene}_faces"], g[f"{scene}_fixed"], meta["eta"]
+    with C.Mesh(ctx, f, nverts=off.size - 1) as m:
+        m.set_history(off, tt, pp)
+        for label in ("kdop", "aabb"):
+            for fx_label, fx in (("", None), ("_fixed", fixed)):
+                m.set_fixed(fx)
+                vf, ee = m.broadphase(KINDS[label], eta)
+                exp = meta[f"{label}{fx_label}"]
+                assert (vf.shape[0], ee.shape[0]) == (exp["n_vf"], exp["n_ee"])
+                assert digest(vf, ee) == exp["digest"]
+        m.set_fixed(None)
+        hvf, hvft, hee, heet = m.detect(C.BROADPHASE_KDOP13, eta, eta)
+        np.testing.assert_array_equal(hvf, g[f"{scene}_hit_vf"])
+        np.testing.assert_array_equal(hee, g[f"{scene}_hit_ee"])
+        # contact times and sub-tests against the oracle
+        vf, ee = m.broadphase(C.BROADPHASE_KDOP13, eta)
+        out = m.narrowphase(vf, eta, ee, eta)
+        ref = oracle.narrowphase_history(off, tt, pp, vf, eta, ee, eta)
+        for k in ("vf", "ee"):
+            np.testing.assert_array_equal(out[f"{k}_hit"], ref[f"{k}_hit"])
+            np.testing.assert_array_equal(out[f"{k}_which"], ref[f"{k}_which"])
+            h = ref[f"{k}_hit"] == 1
+            rel = np.abs(out[f"{k}_t"][h] - ref[f"{k}_t"][h]) / np.maximum(np.abs(ref[f"{k}_t"][h]), 1e-300)
+            assert not h.any() or rel.max() <= TOL
+
+
+def test_two_entry_history_equals_a_step(ctx):
+    """A history of two entries per vertex (t = 0 and 1) gives exactly what
+    the step of ccd_mesh_set_positions gives, and set_positions afterwards
+    returns to the step."""
+    qs, qe, f = W.two_spheres(seed=3)
+    nv = qs.size // 3
+    off = np.arange(0, 2 * nv + 1, 2, dtype=np.int32)
+    tt = np.tile([0.0, 1.0], nv)
+    pp = np.stack([qs.reshape(-1, 3), qe.reshape(-1, 3)], axis=1).reshape(-1, 3)
+    with C.Mesh(ctx, f, qs, qe) as m:
+        step = m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6)
+        m.set_history(off, tt, pp)
+        hist = m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6)
+        m.set_positions(qs, qe)
+        again = m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6)
+    for a, b, c in zip(step, hist, again):
+        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(a, c)
+    assert step[0].shape[0] + step[2].shape[0] > 0
+
+
+def test_history_rejects_bad_input(ctx):
+    v, f = W.icosphere(1, 0.5)
+    nv = v.shape[0]
+    with C.Mesh(ctx, f, nverts=nv) as m:
+        off = np.arange(0, 2 * nv + 1, 2, dtype=np.int32)
+        tt = np.tile([0.0, 1.0], nv)
+        pp = np.repeat(v, 2, axis=0)
+        bad_t = tt.copy()
+        bad_t[1] = -1.0  # decreasing
+        with pytest.raises(C.CcdError):
+            m.set_history(off, bad_t, pp)
+        empty = off.copy()
+        empty[1:] -= 2  # vertex 0 without entries
+        empty[0] = 0
+        with pytest.raises(C.CcdError):
+            m.set_history(empty, tt[: empty[-1]], pp[: empty[-1]])

@@ -144,3 +144,22 @@ def test_penalty_group_force(oracle, golden_dir, scene):
         np.testing.assert_array_equal(vfire, g[f"{scene}_{label}_vf_fired"])
         np.testing.assert_array_equal(efire, g[f"{scene}_{label}_ee_fired"])
         assert used == meta[f"{scene}_{label}"]["newused"]
+
+
+@pytest.mark.parametrize("scene", ["spheres", "cloth", "hand"])
+def test_multi_entry_history(oracle, golden_dir, scene):
+    meta = json.load(open(os.path.join(golden_dir, "history.json")))[scene]
+    g = np.load(os.path.join(golden_dir, "history.npz"))
+    off, tt, pp = g[f"{scene}_offsets"], g[f"{scene}_times"], g[f"{scene}_positions"]
+    f, fixed, eta = g[f"{scene}_faces"], g[f"{scene}_fixed"], meta["eta"]
+    for kind, label in ((0, "kdop"), (1, "aabb")):
+        for fx_label, fx in (("", None), ("_fixed", fixed)):
+            vf, ee = oracle.broadphase_history(kind, off, tt, pp, f, eta, fx)
+            exp = meta[f"{label}{fx_label}"]
+            assert (vf.shape[0], ee.shape[0]) == (exp["n_vf"], exp["n_ee"])
+            assert _digest(vf, ee) == exp["digest"]
+    vf, ee = oracle.broadphase_history(0, off, tt, pp, f, eta)
+    out = oracle.narrowphase_history(off, tt, pp, vf, eta, ee, eta)
+    assert _digest(out["vf_hit"], out["ee_hit"]) == meta["narrow"]["digest"]
+    np.testing.assert_array_equal(vf[out["vf_hit"] == 1], g[f"{scene}_hit_vf"])
+    np.testing.assert_array_equal(ee[out["ee_hit"] == 1], g[f"{scene}_hit_ee"])
