@@ -90,6 +90,7 @@ def load(path: str = LIB):
     L.ccd_mesh_set_positions_device.argtypes = [_P, _P, _P]
     L.ccd_mesh_set_fixed.argtypes = [_P, _P]
     L.ccd_mesh_set_history.argtypes = [_P, _P, _P, _P]
+    L.ccd_narrowphase_separating_plane.argtypes = [_P, _I64, _P, _P, _I64, _I64, _P, _P, _I64, _P, _P, _P, _P]
     L.ccd_broadphase.argtypes = [_P, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_I64), ctypes.POINTER(_I64)]
     L.ccd_broadphase_get.argtypes = [_P, _P, _P]
     L.ccd_narrowphase.argtypes = [_P, ctypes.c_int, _I64, _P, _P, _I64, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P]
@@ -388,6 +389,21 @@ class Mesh:
                                                  _ptr(eee), eee.size, _ptr(out["vf_hit"]), _ptr(out["ee_hit"]),
                                                  _ptr(out["vf_t"]), _ptr(out["ee_t"]), _ptr(out["vf_which"]),
                                                  _ptr(out["ee_which"])), "ccd_narrowphase")
+        return out
+
+    def narrowphase_separating_plane(self, vf, vf_eta, ee, ee_eta):
+        """SeparatingPlaneNarrowPhase::findCollisions per stencil
+        (ccd_narrowphase_separating_plane): dict of vf_hit / ee_hit and
+        vf_status / ee_status (1 where the reference's search stalls)."""
+        vf, ee = _stencils(vf), _stencils(ee)
+        vfe = np.ascontiguousarray(np.atleast_1d(np.asarray(vf_eta, np.float64)))
+        eee = np.ascontiguousarray(np.atleast_1d(np.asarray(ee_eta, np.float64)))
+        nv, ne = vf.shape[0], ee.shape[0]
+        out = {"vf_hit": np.zeros(nv, np.uint8), "ee_hit": np.zeros(ne, np.uint8),
+               "vf_status": np.zeros(nv, np.uint8), "ee_status": np.zeros(ne, np.uint8)}
+        self.ctx._check(self.lib.ccd_narrowphase_separating_plane(
+            self.handle, nv, _ptr(vf), _ptr(vfe), vfe.size, ne, _ptr(ee), _ptr(eee), eee.size, _ptr(out["vf_hit"]),
+            _ptr(out["ee_hit"]), _ptr(out["vf_status"]), _ptr(out["ee_status"])), "ccd_narrowphase_separating_plane")
         return out
 
     def detect(self, kind: int = BROADPHASE_KDOP13, outer_eta: float = 1e-6, eta: float = 1e-6,

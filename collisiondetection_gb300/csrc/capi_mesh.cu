@@ -10,10 +10,12 @@
 #include <vector>
 
 #include "broadphase.cuh"
+#include "ccd_common.h"
 #include "context.cuh"
 #include "distance.cuh"
 #include "mesh.cuh"
 #include "radix_sort.cuh"
+#include "separating.cuh"
 
 using namespace ccd_capi;
 
@@ -88,6 +90,10 @@ struct ccd_mesh {
   double *hist_time = nullptr, *hist_pos = nullptr;
   int64_t hist_cap = 0;
   bool has_history = false;
+  double hist_min_gap = 1.0;  // History::computeMinimumGap of the history set
+  // the two-entry step as a history, for the separating-plane narrow phase
+  int32_t *step_off = nullptr;
+  double *step_time = nullptr, *step_pos = nullptr;
   uint8_t *fixed = nullptr;
   bool has_fixed = false;
   ccd::BroadphaseBuffers bp;
@@ -317,7 +323,7 @@ int check_eta(ccd_mesh *m, int64_t n, const double *eta, int64_t eta_count) {
 
 void free_mesh_buffers(ccd_mesh *m) {
   void *ptrs[] = {m->faces, m->face_rank, m->rank_triple, m->face_edges, m->rank_edge, m->face_inst, m->qs, m->qe,
-                  m->hist_off, m->hist_time, m->hist_pos, m->fixed,
+                  m->hist_off, m->hist_time, m->hist_pos, m->step_off, m->step_time, m->step_pos, m->fixed,
                   m->cand[0], m->cand[1], m->in_st, m->in_eta, m->which, m->d_eta,
                   m->col[0], m->col[1], m->col_t[0], m->col_t[1]};
   for (void *p : ptrs) cudaFree(p);
@@ -511,6 +517,11 @@ int ccd_mesh_set_history(ccd_mesh *m, const int32_t *offsets, const double *time
   CCD_CUDA(cudaMemcpyAsync(m->hist_pos, positions, (size_t)ne * 3 * sizeof(double), cudaMemcpyHostToDevice,
                            ctx->stream));
   CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+  // History::computeMinimumGap (src/History.cpp:82-96), in its loop order
+  double gap_min = 1.0;
+  for (int32_t v = 0; v < m->nv; v++)
+    for (int32_t e = offsets[v] + 1; e < offsets[v + 1]; e++) gap_min = ccd::smin(times[e] - times[e - 1], gap_min);
+  m->hist_min_gap = gap_min;
   m->has_history = true;
   m->have_cand = m->have_col = false;
   return CCD_OK;
@@ -624,6 +635,62 @@ int ccd_narrowphase(ccd_mesh *m, int path, int64_t n_vf, const int32_t *vf, cons
       if (t && hit[i]) t[i] = tbuf[(size_t)i];
     }
     (k ? m->stats.ee_hits : m->stats.vf_hits) = hits;
+  }
+  return CCD_OK;
+}
+
+int ccd_narrowphase_separating_plane(ccd_mesh *m, int64_t n_vf, const int32_t *vf, const double *vf_eta,
+                                     int64_t vf_eta_count, int64_t n_ee, const int32_t *ee, const double *ee_eta,
+                                     int64_t ee_eta_count, uint8_t *vf_hit, uint8_t *ee_hit, uint8_t *vf_status,
+                                     uint8_t *ee_status) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  if (n_vf < 0 || n_ee < 0 || (n_vf && (!vf || !vf_hit)) || (n_ee && (!ee || !ee_hit)))
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null buffer or negative size");
+  int rc = check_eta(m, n_vf, vf_eta, vf_eta_count);
+  if (!rc) rc = check_eta(m, n_ee, ee_eta, ee_eta_count);
+  if (rc) return rc;
+  for (int k = 0; k < 2; k++) {
+    const int32_t *st = k == 0 ? vf : ee;
+    const int64_t n = k == 0 ? n_vf : n_ee;
+    for (int64_t i = 0; i < 4 * n; i++)
+      if (st[i] < 0 || st[i] >= m->nv) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "stencil vertex out of range");
+  }
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  ccd::HistoryView hv{m->hist_off, m->hist_time, m->hist_pos};
+  double gap = m->hist_min_gap;
+  if (!m->has_history) {
+    // the two-entry step: entries at 0 and 1, so the minimum gap is 1
+    if (!m->step_off) {
+      CCD_CUDA(cudaMalloc(&m->step_off, ((size_t)m->nv + 1) * sizeof(int32_t)));
+      CCD_CUDA(cudaMalloc(&m->step_time, 2 * (size_t)m->nv * sizeof(double)));
+      CCD_CUDA(cudaMalloc(&m->step_pos, 6 * (size_t)m->nv * sizeof(double)));
+    }
+    CCD_CUDA(ccd::launch_two_entry_view(m->nv, m->qs, m->qe, m->step_off, m->step_time, m->step_pos, s));
+    hv = ccd::HistoryView{m->step_off, m->step_time, m->step_pos};
+    gap = ccd::smin(1.0 - 0.0, 1.0);
+  }
+  const double eps = gap / 4.0;
+  for (int k = 0; k < 2; k++) {
+    const int64_t n = k == 0 ? n_vf : n_ee;
+    if (n == 0) continue;
+    const int32_t *st = k == 0 ? vf : ee;
+    const double *eta = k == 0 ? vf_eta : ee_eta;
+    const int64_t ec = k == 0 ? vf_eta_count : ee_eta_count;
+    Lane &L = m->lane[0];
+    rc = grow(ctx, &m->in_st, &m->in_st_cap, 4 * n);
+    if (!rc) rc = grow(ctx, &m->in_eta, &m->in_eta_cap, ec);
+    if (!rc) rc = grow(ctx, &L.hit, &L.hit_cap, 2 * n);
+    if (rc) return rc;
+    CCD_CUDA(cudaMemcpyAsync(m->in_st, st, (size_t)n * 16, cudaMemcpyHostToDevice, s));
+    CCD_CUDA(cudaMemcpyAsync(m->in_eta, eta, (size_t)ec * sizeof(double), cudaMemcpyHostToDevice, s));
+    CCD_CUDA(ccd::launch_separating_plane(k, hv, m->in_st, n, m->in_eta, ec == n && n != 1 ? 1 : 0, eps, L.hit,
+                                          L.hit + n, s));
+    CCD_CUDA(cudaMemcpyAsync(k == 0 ? vf_hit : ee_hit, L.hit, (size_t)n, cudaMemcpyDeviceToHost, s));
+    uint8_t *status = k == 0 ? vf_status : ee_status;
+    if (status) CCD_CUDA(cudaMemcpyAsync(status, L.hit + n, (size_t)n, cudaMemcpyDeviceToHost, s));
+    CCD_CUDA(cudaStreamSynchronize(s));
   }
   return CCD_OK;
 }

@@ -254,6 +254,21 @@ int ccd_narrowphase(ccd_mesh *mesh, int path, int64_t n_vf, const int32_t *vf, c
                     uint8_t *vf_hit, uint8_t *ee_hit, double *vf_t, double *ee_t, int8_t *vf_which,
                     int8_t *ee_which);
 
+/* SeparatingPlaneNarrowPhase::findCollisions (src/SeparatingPlaneNarrowPhase.cpp:
+ * 11-278), the narrow phase the reference's velocity filter uses, over caller
+ * stencils in host memory, on the mesh's history (ccd_mesh_set_history, or
+ * the two-entry step): hit[i] = 1 if stencil i collides, by the reference's
+ * separating-plane interval search with eps = History::computeMinimumGap()/4
+ * and the CTCD chain on its short intervals.  Bit-identical to the
+ * reference where it terminates.  On some inputs the reference's recursion
+ * never ends (an interval ending exactly at a history entry time stops
+ * shrinking) and it overflows its stack; such a stencil is stopped here with
+ * status 1 (optional [n] outputs, 0 otherwise) and hit 0. */
+int ccd_narrowphase_separating_plane(ccd_mesh *mesh, int64_t n_vf, const int32_t *vf, const double *vf_eta,
+                                     int64_t vf_eta_count, int64_t n_ee, const int32_t *ee, const double *ee_eta,
+                                     int64_t ee_eta_count, uint8_t *vf_hit, uint8_t *ee_hit, uint8_t *vf_status,
+                                     uint8_t *ee_status);
+
 /* One detection step on the device, as the reference's callers chain it
  * (example/AlecTest.cpp:97-111): broad phase with outer_eta, then the narrow
  * phase over every candidate with eta.  Writes the numbers of colliding

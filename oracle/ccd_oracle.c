@@ -13,6 +13,7 @@
 
 #include <math.h>
 #include <pthread.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -1757,4 +1758,231 @@ int oracle_narrowphase_history(int nverts, const int32_t *offsets, const double 
   }
   free(buf);
   return 0;
+}
+
+/* ------------------------------------------------------------ separating-plane narrow phase
+ * SeparatingPlaneNarrowPhase (src/SeparatingPlaneNarrowPhase.cpp) on a
+ * multi-entry history given as offsets / times / positions. */
+typedef struct {
+  const int32_t *off;
+  const double *t, *p;
+} hist_view;
+
+/* History::getPosAtTime (src/History.cpp:54-80): binary halving while the
+ * range holds 10 or more entries, then a forward scan. */
+static void pos_at_time(hist_view h, int v, double time, vec3 *pos, int *idx) {
+  const int base = h.off[v], size = h.off[v + 1] - h.off[v];
+  int start = 0, end = size - 1;
+  while (end - start >= 10) {
+    int mid = (start + end) / 2;
+    if (h.t[base + mid] < time)
+      start = mid;
+    else
+      end = mid;
+  }
+  int next = start;
+  while (next < size && h.t[base + next] <= time) next++;
+  int prev = next - 1;
+  if (prev < 0) prev = 0; /* the reference reads before the first entry here; not reached from [0, 1] */
+  if (next == size) {
+    *pos = v3(h.p + 3 * (size_t)(base + prev));
+    *idx = prev;
+    return;
+  }
+  double dt = h.t[base + next] - h.t[base + prev];
+  double alpha = (time - h.t[base + prev]) / dt;
+  *pos = vadd(vscale(1.0 - alpha, v3(h.p + 3 * (size_t)(base + prev))), vscale(alpha, v3(h.p + 3 * (size_t)(base + next))));
+  *idx = prev;
+}
+
+/* History::computeMinimumGap (src/History.cpp:82-96). */
+static double minimum_gap(hist_view h, int nverts) {
+  double result = 1.0;
+  for (int i = 0; i < nverts; i++)
+    for (int j = h.off[i] + 1; j < h.off[i + 1]; j++) {
+      double gap = h.t[j] - h.t[j - 1];
+      result = smin(gap, result);
+    }
+  return result;
+}
+
+/* SeparatingPlaneNarrowPhase::planeIntersect (:264-277). */
+static double plane_intersect(vec3 planePos, vec3 planeVel, vec3 planeNormal, vec3 ptOld, vec3 ptNew, double ptdt,
+                              double eta) {
+  double numerator = 0.5 * eta - vdot(vsub(ptOld, planePos), planeNormal);
+  double denom = -vdot(planeVel, planeNormal);
+  if (ptdt != 0.0) denom += vdot(vsub(ptNew, ptOld), planeNormal) / ptdt;
+  return numerator / denom;
+}
+
+/* SeparatingPlaneNarrowPhase::planeTrajectoryIntersect (:217-262); startidx
+ * relative to the vertex's entries. */
+static double plane_trajectory(hist_view h, int v, int startidx, int forward, vec3 planePos, vec3 planeVel,
+                               vec3 planeNormal, vec3 ptstart, double timestart, double eta) {
+  const int base = h.off[v], size = h.off[v + 1] - h.off[v];
+  const double *T = h.t + base;
+  const double *P = h.p + 3 * (size_t)base;
+  double dt = forward ? T[startidx] - timestart : timestart - T[startidx];
+  vec3 newpos = v3(P + 3 * startidx);
+  double t = plane_intersect(planePos, vscale(forward ? 1.0 : -1.0, planeVel), planeNormal, ptstart, newpos, dt, eta);
+  if (t >= 0 && t <= dt) return t;
+  if (forward) {
+    for (int i = startidx; i < size; i++) {
+      if (i == size - 1) return INFINITY;
+      int next = i + 1;
+      vec3 newplanepos = vadd(planePos, vscale(T[i] - timestart, planeVel));
+      double dti = T[next] - T[i];
+      double ti = plane_intersect(newplanepos, planeVel, planeNormal, v3(P + 3 * i), v3(P + 3 * next), dti, eta);
+      if (ti >= 0 && ti <= dti) return T[i] + ti - timestart;
+    }
+  } else {
+    for (int i = startidx; i >= 0; i--) {
+      if (i == 0) return INFINITY;
+      int prev = i - 1;
+      vec3 newplanepos = vsub(planePos, vscale(timestart - T[i], planeVel));
+      vec3 nvel = {-planeVel.x, -planeVel.y, -planeVel.z};
+      double dti = T[i] - T[prev];
+      double ti = plane_intersect(newplanepos, nvel, planeNormal, v3(P + 3 * i), v3(P + 3 * prev), dti, eta);
+      if (ti >= 0 && ti <= dti) return timestart - (T[i] - ti);
+    }
+  }
+  return INFINITY;
+}
+
+/* SeparatingPlaneNarrowPhase::checkInterval (:47-215); type 0 vertex-face,
+ * 1 edge-edge; v the canonical stencil.
+ *
+ * Every child interval is at most half its parent, so a recursion that
+ * terminates is at most about 1,076 levels deep (halving 1.0 that often
+ * reaches 0, and an empty interval is a leaf).  Deeper means a stall: an
+ * interval that ends exactly at a history entry time never passes the leaf
+ * test (its two ends lie in different entries), and once halving stops
+ * shrinking it (adjacent doubles) the upper child equals its parent.  The
+ * reference then recurses until its stack overflows.  Here depth 1,100 (or
+ * 2^20 calls) stops the stencil and reports it through *capped. */
+static int check_interval(int type, hist_view h, const int32_t *v, double eta, double mint, double maxt, double eps,
+                          int64_t *frames, int *capped, int depth) {
+  if (*capped) return 0;
+  if (++*frames > (1 << 20) || depth > 1100) {
+    *capped = 1;
+    return 0;
+  }
+  if (maxt < mint) return 0;
+  if (maxt - mint < 3 * eps) {
+    int ok = 1;
+    vec3 oldpos[4], newpos[4];
+    for (int i = 0; i < 4; i++) {
+      int oldidx, newidx;
+      pos_at_time(h, v[i], mint, &oldpos[i], &oldidx);
+      pos_at_time(h, v[i], maxt, &newpos[i], &newidx);
+      if (oldidx != newidx) {
+        ok = 0;
+        break;
+      }
+    }
+    if (ok) {
+      double P0[12], P1[12], t;
+      for (int i = 0; i < 4; i++) {
+        P0[3 * i] = oldpos[i].x; P0[3 * i + 1] = oldpos[i].y; P0[3 * i + 2] = oldpos[i].z;
+        P1[3 * i] = newpos[i].x; P1[3 * i + 1] = newpos[i].y; P1[3 * i + 2] = newpos[i].z;
+      }
+      return (type == 0 ? chain_vf(P0, P1, eta, &t) : chain_ee(P0, P1, eta, &t)) >= 0;
+    }
+  }
+  double midt = 0.5 * (mint + maxt);
+  vec3 midpos[4];
+  int mididx[4];
+  for (int i = 0; i < 4; i++) pos_at_time(h, v[i], midt, &midpos[i], &mididx[i]);
+  double b[4] = {0, 0, 0, 0};
+  vec3 closest = type == 0 ? vf_distance(midpos[0], midpos[1], midpos[2], midpos[3], b)
+                           : ee_distance(midpos[0], midpos[1], midpos[2], midpos[3], b);
+  double distsq = vdot(closest, closest);
+  if (distsq < eta * eta) return 1;
+  vec3 prevpos[4], nextpos[4];
+  double dts[4];
+  for (int i = 0; i < 4; i++) {
+    const int base = h.off[v[i]];
+    prevpos[i] = v3(h.p + 3 * (size_t)(base + mididx[i]));
+    nextpos[i] = v3(h.p + 3 * (size_t)(base + mididx[i] + 1));
+    dts[i] = h.t[base + mididx[i] + 1] - h.t[base + mididx[i]];
+  }
+  vec3 planepos, planevel;
+  if (type == 0) {
+    planepos = vscale(0.5, vadd(vadd(vadd(midpos[0], vscale(b[0], midpos[1])), vscale(b[1], midpos[2])),
+                                vscale(b[2], midpos[3])));
+    vec3 d0 = vsub(nextpos[0], prevpos[0]), s0 = {d0.x / dts[0], d0.y / dts[0], d0.z / dts[0]};
+    vec3 acc = s0;
+    for (int i = 1; i < 4; i++) {
+      vec3 d = vscale(b[i - 1], vsub(nextpos[i], prevpos[i]));
+      vec3 q = {d.x / dts[i], d.y / dts[i], d.z / dts[i]};
+      acc = vadd(acc, q);
+    }
+    planevel = vscale(0.5, acc);
+  } else {
+    planepos = vscale(0.5, vadd(vadd(vadd(vscale(b[0], midpos[0]), vscale(b[1], midpos[1])), vscale(b[2], midpos[2])),
+                                vscale(b[3], midpos[3])));
+    vec3 acc = {0, 0, 0};
+    for (int i = 0; i < 4; i++) {
+      vec3 d = vscale(b[i], vsub(nextpos[i], prevpos[i]));
+      vec3 q = {d.x / dts[i], d.y / dts[i], d.z / dts[i]};
+      acc = i == 0 ? q : vadd(acc, q);
+    }
+    planevel = vscale(0.5, acc);
+  }
+  double nrm = vnorm(closest);
+  closest.x = closest.x / nrm;
+  closest.y = closest.y / nrm;
+  closest.z = closest.z / nrm;
+  double t = INFINITY;
+  for (int vert = 0; vert < 4; vert++) {
+    double sign = (vert == 0 || (vert == 1 && type == 1)) ? -1.0 : 1.0;
+    t = smin(t, plane_trajectory(h, v[vert], mididx[vert], 0, planepos, planevel, vscale(sign, closest),
+                                 midpos[vert], midt, eta));
+  }
+  if (t < 1.0) {
+    double newmaxt = midt - smax(0.0, t - eps);
+    if (check_interval(type, h, v, eta, mint, newmaxt, eps, frames, capped, depth + 1)) return 1;
+  }
+  t = INFINITY;
+  for (int vert = 0; vert < 4; vert++) {
+    double sign = (vert == 0 || (vert == 1 && type == 1)) ? -1.0 : 1.0;
+    t = smin(t, plane_trajectory(h, v[vert], mididx[vert] + 1, 1, planepos, planevel, vscale(sign, closest),
+                                 midpos[vert], midt, eta));
+  }
+  if (t < 1.0) {
+    double newmint = midt + smax(0.0, t - eps);
+    if (check_interval(type, h, v, eta, newmint, maxt, eps, frames, capped, depth + 1)) return 1;
+  }
+  return 0;
+}
+
+/* SeparatingPlaneNarrowPhase::findCollisions (:11-25): hit flags per
+ * stencil; returns the number of stencils whose recursion hit the cap. */
+int64_t oracle_separating_plane(int nverts, const int32_t *offsets, const double *times, const double *positions,
+                                int64_t n_vf, const int32_t *vf, const double *vf_eta, int64_t n_ee,
+                                const int32_t *ee, const double *ee_eta, uint8_t *vf_hit, uint8_t *ee_hit,
+                                uint8_t *vf_status, uint8_t *ee_status) {
+  hist_view h = {offsets, times, positions};
+  const double eps = minimum_gap(h, nverts) / 4.0;
+  int64_t capped_total = 0;
+  for (int kind = 0; kind < 2; kind++) {
+    const int64_t n = kind == 0 ? n_vf : n_ee;
+    for (int64_t i = 0; i < n; i++) {
+      const int32_t *raw = (kind == 0 ? vf : ee) + 4 * i;
+      int32_t st[4];
+      if (kind == 0)
+        oracle_vf_canon(raw[0], raw[1], raw[2], raw[3], st);
+      else
+        oracle_ee_canon(raw[0], raw[1], raw[2], raw[3], st);
+      int64_t frames = 0;
+      int capped = 0;
+      const int hit =
+          check_interval(kind, h, st, (kind == 0 ? vf_eta : ee_eta)[i], 0.0, 1.0, eps, &frames, &capped, 0);
+      (kind == 0 ? vf_hit : ee_hit)[i] = (uint8_t)(hit && !capped);
+      uint8_t *status = kind == 0 ? vf_status : ee_status;
+      if (status) status[i] = (uint8_t)capped;
+      capped_total += capped;
+    }
+  }
+  return capped_total;
 }

@@ -96,6 +96,16 @@ int oracle_narrowphase_history(int nverts, const int32_t *offsets, const double 
                                const double *ee_eta, uint8_t *vf_hit, uint8_t *ee_hit, double *vf_t, double *ee_t,
                                int8_t *vf_which, int8_t *ee_which);
 
+/* SeparatingPlaneNarrowPhase::findCollisions (src/SeparatingPlaneNarrowPhase.cpp)
+ * on a multi-entry history: hit flags per stencil; *_status (may be NULL)
+ * 1 where the stencil's interval recursion stalled (the reference recurses
+ * until its stack overflows there) and was stopped, hit then 0.  Returns
+ * the number of such stencils. */
+int64_t oracle_separating_plane(int nverts, const int32_t *offsets, const double *times, const double *positions,
+                                int64_t n_vf, const int32_t *vf, const double *vf_eta, int64_t n_ee,
+                                const int32_t *ee, const double *ee_eta, uint8_t *vf_hit, uint8_t *ee_hit,
+                                uint8_t *vf_status, uint8_t *ee_status);
+
 /* Stencil canonical forms (src/Stencils.h): writes the canonical 4-tuple. */
 void oracle_vf_canon(int p, int q0, int q1, int q2, int32_t *out);
 void oracle_ee_canon(int p0, int p1, int q0, int q1, int32_t *out);

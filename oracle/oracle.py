@@ -121,6 +121,8 @@ class Oracle(_Lib):
         L.oracle_narrowphase_history.argtypes = [ctypes.c_int, _P, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P, _P,
                                                  _P, _P, _P]
         L.oracle_narrowphase_history.restype = ctypes.c_int
+        L.oracle_separating_plane.argtypes = [ctypes.c_int, _P, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P]
+        L.oracle_separating_plane.restype = ctypes.c_int64
         self._distance_setup()
 
     def broadphase_history(self, kind: int, offsets, times, positions, faces, eta: float, fixed=None):
@@ -158,6 +160,25 @@ class Oracle(_Lib):
         if rc != 0:
             raise MemoryError("oracle_narrowphase_history failed")
         return out
+
+    def separating_plane(self, offsets, times, positions, vf, vf_eta, ee, ee_eta):
+        """SeparatingPlaneNarrowPhase on a multi-entry history: (vf_hit,
+        ee_hit, vf_status, ee_status); status 1 marks a stalled recursion."""
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        tt = np.ascontiguousarray(times, dtype=np.float64)
+        pos = np.ascontiguousarray(positions, dtype=np.float64)
+        vf = np.ascontiguousarray(vf, dtype=np.int32).reshape(-1, 4)
+        ee = np.ascontiguousarray(ee, dtype=np.int32).reshape(-1, 4)
+        vfe = np.ascontiguousarray(np.broadcast_to(np.asarray(vf_eta, np.float64), (vf.shape[0],)))
+        eee = np.ascontiguousarray(np.broadcast_to(np.asarray(ee_eta, np.float64), (ee.shape[0],)))
+        vh = np.zeros(vf.shape[0], np.uint8)
+        eh = np.zeros(ee.shape[0], np.uint8)
+        vs = np.zeros(vf.shape[0], np.uint8)
+        es = np.zeros(ee.shape[0], np.uint8)
+        self.lib.oracle_separating_plane(off.size - 1, _ptr(off), _ptr(tt), _ptr(pos), vf.shape[0], _ptr(vf),
+                                         _ptr(vfe), ee.shape[0], _ptr(ee), _ptr(eee), _ptr(vh), _ptr(eh), _ptr(vs),
+                                         _ptr(es))
+        return vh, eh, vs, es
 
     def vertex_scan(self, verts, faces, i0: int, i1: int) -> float:
         """meshSelfDistance's O(V F) vertex scan over vertices [i0, i1)."""
@@ -240,6 +261,7 @@ class Reference(_Lib):
         L.ref_broadphase_history.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, _P, ctypes.c_int, _P,
                                              ctypes.c_double, _P, _P, _P]
         L.ref_narrowphase_history.argtypes = [ctypes.c_int, _P, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P]
+        L.ref_separating_plane.argtypes = [ctypes.c_int, _P, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P]
         self._distance_setup()
 
     def broadphase_history(self, kind: int, offsets, times, positions, faces, eta: float, fixed=None):
@@ -268,6 +290,20 @@ class Reference(_Lib):
         eh = np.zeros(ee.shape[0], np.uint8)
         self.lib.ref_narrowphase_history(off.size - 1, _ptr(off), _ptr(tt), _ptr(pos), vf.shape[0], _ptr(vf),
                                          _ptr(vfe), ee.shape[0], _ptr(ee), _ptr(eee), _ptr(vh), _ptr(eh))
+        return vh, eh
+
+    def separating_plane(self, offsets, times, positions, vf, vf_eta, ee, ee_eta):
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        tt = np.ascontiguousarray(times, dtype=np.float64)
+        pos = np.ascontiguousarray(positions, dtype=np.float64)
+        vf = np.ascontiguousarray(vf, dtype=np.int32).reshape(-1, 4)
+        ee = np.ascontiguousarray(ee, dtype=np.int32).reshape(-1, 4)
+        vfe = np.ascontiguousarray(np.broadcast_to(np.asarray(vf_eta, np.float64), (vf.shape[0],)))
+        eee = np.ascontiguousarray(np.broadcast_to(np.asarray(ee_eta, np.float64), (ee.shape[0],)))
+        vh = np.zeros(vf.shape[0], np.uint8)
+        eh = np.zeros(ee.shape[0], np.uint8)
+        self.lib.ref_separating_plane(off.size - 1, _ptr(off), _ptr(tt), _ptr(pos), vf.shape[0], _ptr(vf), _ptr(vfe),
+                                      ee.shape[0], _ptr(ee), _ptr(eee), _ptr(vh), _ptr(eh))
         return vh, eh
 
     def mesh_self_distance(self, verts, faces, fixed=None) -> float:

@@ -3,7 +3,8 @@
 // extern "C" wrapper over the reference library's own, unmodified sources
 // (src/CTCD.cpp, src/History.cpp, src/Mesh.cpp, src/KDOPBroadPhase.cpp,
 // src/AABBBroadPhase.cpp, src/TrivialBroadPhase.cpp, src/CTCDNarrowPhase.cpp,
-// src/Distance.cpp, src/PenaltyPotential.cpp, src/PenaltyGroup.cpp), compiled by
+// src/Distance.cpp, src/PenaltyPotential.cpp, src/PenaltyGroup.cpp,
+// src/SeparatingPlaneNarrowPhase.cpp), compiled by
 // oracle/Makefile against the project-written Eigen-API subset.  It exists so
 // that tests/golden/make_golden.py can pin the C restatement (ccd_oracle.c)
 // against the reference itself.  The reference tree is only present in the
@@ -18,6 +19,7 @@
 #include "Distance.h"
 #include "PenaltyGroup.h"
 #include "PenaltyPotential.h"
+#include "SeparatingPlaneNarrowPhase.h"
 #include "History.h"
 #include "KDOPBroadPhase.h"
 #include "Mesh.h"
@@ -251,6 +253,28 @@ void ref_narrowphase_history(int nverts, const int32_t *off, const double *times
   std::set<VertexFaceStencil> ovf;
   std::set<EdgeEdgeStencil> oee;
   CTCDNarrowPhase np;
+  np.findCollisions(*h, cvf, cee, ovf, oee);
+  delete h;
+  for (int64_t i = 0; i < n_vf; i++)
+    vf_hit[i] = (uint8_t)ovf.count(VertexFaceStencil(vf[4 * i], vf[4 * i + 1], vf[4 * i + 2], vf[4 * i + 3]));
+  for (int64_t i = 0; i < n_ee; i++)
+    ee_hit[i] = (uint8_t)oee.count(EdgeEdgeStencil(ee[4 * i], ee[4 * i + 1], ee[4 * i + 2], ee[4 * i + 3]));
+}
+
+// SeparatingPlaneNarrowPhase::findCollisions on a history built as above.
+void ref_separating_plane(int nverts, const int32_t *off, const double *times, const double *pos, int64_t n_vf,
+                          const int32_t *vf, const double *vf_eta, int64_t n_ee, const int32_t *ee,
+                          const double *ee_eta, uint8_t *vf_hit, uint8_t *ee_hit) {
+  History *h = make_history(nverts, off, times, pos);
+  std::set<std::pair<VertexFaceStencil, double> > cvf;
+  std::set<std::pair<EdgeEdgeStencil, double> > cee;
+  for (int64_t i = 0; i < n_vf; i++)
+    cvf.insert(std::make_pair(VertexFaceStencil(vf[4 * i], vf[4 * i + 1], vf[4 * i + 2], vf[4 * i + 3]), vf_eta[i]));
+  for (int64_t i = 0; i < n_ee; i++)
+    cee.insert(std::make_pair(EdgeEdgeStencil(ee[4 * i], ee[4 * i + 1], ee[4 * i + 2], ee[4 * i + 3]), ee_eta[i]));
+  std::set<VertexFaceStencil> ovf;
+  std::set<EdgeEdgeStencil> oee;
+  SeparatingPlaneNarrowPhase np;
   np.findCollisions(*h, cvf, cee, ovf, oee);
   delete h;
   for (int64_t i = 0; i < n_vf; i++)

@@ -30,7 +30,10 @@ the reference's example meshes, and writes:
 * ``history.npz`` / ``history.json`` -- multi-entry histories (built with
   History's constructor and addHistory) for the two spheres, a sheet on a
   sphere and two hand-built triangles: k-DOP and AABB candidate digests, free
-  and with fixed vertices, and CTCDNarrowPhase's colliding stencils.
+  and with fixed vertices, CTCDNarrowPhase's colliding stencils and
+  SeparatingPlaneNarrowPhase's hit flags (stencils on which its recursion
+  never ends, found by the oracle, are recorded instead of run: the
+  reference overflows its stack there).
 
 Only runs where the reference tree exists:
     python tests/golden/make_golden.py [--only distances|trivial|penalty|history]
@@ -370,6 +373,19 @@ def history_fixtures(ref) -> None:
         arrays[f"{name}_hit_vf"] = vf[vh.astype(bool)]
         arrays[f"{name}_hit_ee"] = ee[eh.astype(bool)]
         entry["narrow"] = {"n_vf_hit": int(vh.sum()), "n_ee_hit": int(eh.sum()), "digest": digest(vh, eh)}
+        # SeparatingPlaneNarrowPhase on the same candidates.  Its recursion
+        # never ends on some stencils (the reference overflows its stack);
+        # the oracle finds those first, and they are kept out of the
+        # reference's run and recorded as such.
+        o = O.Oracle()
+        _, _, vs, es = o.separating_plane(off, tt, pp, vf, eta, ee, eta)
+        svh, seh = ref.separating_plane(off, tt, pp, vf[vs == 0], eta, ee[es == 0], eta)
+        arrays[f"{name}_sp_vf_hit"] = svh
+        arrays[f"{name}_sp_ee_hit"] = seh
+        arrays[f"{name}_sp_vf_stalled"] = vs
+        arrays[f"{name}_sp_ee_stalled"] = es
+        entry["separating_plane"] = {"n_vf_hit": int(svh.sum()), "n_ee_hit": int(seh.sum()),
+                                     "n_stalled": int(vs.sum() + es.sum())}
         meta[name] = entry
     np.savez_compressed(os.path.join(HERE, "history.npz"), **arrays)
     with open(os.path.join(HERE, "history.json"), "w") as fh:

@@ -382,3 +382,40 @@ def test_history_rejects_bad_input(ctx):
         empty[0] = 0
         with pytest.raises(C.CcdError):
             m.set_history(empty, tt[: empty[-1]], pp[: empty[-1]])
+
+
+# ------------------------------------------------------------------ SeparatingPlaneNarrowPhase
+@pytest.mark.parametrize("scene", ["spheres", "cloth", "hand"])
+def test_separating_plane_matches_reference(ctx, golden_dir, scene):
+    meta = json.load(open(os.path.join(golden_dir, "history.json")))[scene]
+    g = np.load(os.path.join(golden_dir, "history.npz"))
+    off, tt, pp, f, eta = g[f"{scene}_offsets"], g[f"{scene}_times"], g[f"{scene}_positions"], g[f"{scene}_faces"], \
+        meta["eta"]
+    with C.Mesh(ctx, f, nverts=off.size - 1) as m:
+        m.set_history(off, tt, pp)
+        vf, ee = m.broadphase(C.BROADPHASE_KDOP13, eta)
+        out = m.narrowphase_separating_plane(vf, eta, ee, eta)
+    for k in ("vf", "ee"):
+        np.testing.assert_array_equal(out[f"{k}_status"], g[f"{scene}_sp_{k}_stalled"])
+        ok = out[f"{k}_status"] == 0
+        np.testing.assert_array_equal(out[f"{k}_hit"][ok], g[f"{scene}_sp_{k}_hit"])
+        assert not out[f"{k}_hit"][~ok].any()
+
+
+def test_separating_plane_on_a_step_matches_oracle(ctx, oracle):
+    """Without a history set, the two-entry step is the history (eps = 1/4)."""
+    qs, qe, f = W.two_spheres(seed=2)
+    nv = qs.size // 3
+    off = np.arange(0, 2 * nv + 1, 2, dtype=np.int32)
+    tt = np.tile([0.0, 1.0], nv)
+    pp = np.stack([qs.reshape(-1, 3), qe.reshape(-1, 3)], axis=1).reshape(-1, 3)
+    eta = 1e-3
+    with C.Mesh(ctx, f, qs, qe) as m:
+        vf, ee = m.broadphase(C.BROADPHASE_KDOP13, eta)
+        out = m.narrowphase_separating_plane(vf, eta, ee, eta)
+    vh, eh, vs, es = oracle.separating_plane(off, tt, pp, vf, eta, ee, eta)
+    np.testing.assert_array_equal(out["vf_hit"], vh)
+    np.testing.assert_array_equal(out["ee_hit"], eh)
+    np.testing.assert_array_equal(out["vf_status"], vs)
+    np.testing.assert_array_equal(out["ee_status"], es)
+    assert vh.sum() + eh.sum() > 0

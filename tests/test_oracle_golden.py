@@ -163,3 +163,18 @@ def test_multi_entry_history(oracle, golden_dir, scene):
     assert _digest(out["vf_hit"], out["ee_hit"]) == meta["narrow"]["digest"]
     np.testing.assert_array_equal(vf[out["vf_hit"] == 1], g[f"{scene}_hit_vf"])
     np.testing.assert_array_equal(ee[out["ee_hit"] == 1], g[f"{scene}_hit_ee"])
+
+
+@pytest.mark.parametrize("scene", ["spheres", "cloth", "hand"])
+def test_separating_plane_narrowphase(oracle, golden_dir, scene):
+    meta = json.load(open(os.path.join(golden_dir, "history.json")))[scene]
+    g = np.load(os.path.join(golden_dir, "history.npz"))
+    off, tt, pp, f, eta = g[f"{scene}_offsets"], g[f"{scene}_times"], g[f"{scene}_positions"], g[f"{scene}_faces"], \
+        meta["eta"]
+    vf, ee = oracle.broadphase_history(0, off, tt, pp, f, eta)
+    vh, eh, vs, es = oracle.separating_plane(off, tt, pp, vf, eta, ee, eta)
+    np.testing.assert_array_equal(vs, g[f"{scene}_sp_vf_stalled"])
+    np.testing.assert_array_equal(es, g[f"{scene}_sp_ee_stalled"])
+    np.testing.assert_array_equal(vh[vs == 0], g[f"{scene}_sp_vf_hit"])
+    np.testing.assert_array_equal(eh[es == 0], g[f"{scene}_sp_ee_hit"])
+    assert not vh[vs == 1].any() and not eh[es == 1].any()
