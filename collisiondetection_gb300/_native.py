@@ -43,6 +43,12 @@ class MeshStats(ctypes.Structure):
                 ("self_distance_eta", ctypes.c_double)]
 
 
+class VelocityFilterStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("layers", ctypes.c_int32), ("events", ctypes.c_int64),
+                ("collisions", ctypes.c_int64), ("history_entries", ctypes.c_int64),
+                ("start_distance", ctypes.c_double)]
+
+
 class BatchTimings(ctypes.Structure):
     _fields_ = [("cull_ms", ctypes.c_float), ("refine_ms", ctypes.c_float), ("launches", ctypes.c_int32)]
 
@@ -108,6 +114,10 @@ def load(path: str = LIB):
                                           ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _P,
                                           _P, _P, ctypes.POINTER(ctypes.c_int)]
     L.ccd_penalty_group_force_device.argtypes = L.ccd_penalty_group_force.argtypes
+    L.ccd_velocity_filter.argtypes = [_P, ctypes.c_int32, _P, _P, ctypes.c_int32, _P, _P, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                                      ctypes.POINTER(VelocityFilterStats)]
     _lib = L
     return L
 
@@ -266,6 +276,26 @@ class Context:
                                                             ee_fired_ptr, ctypes.byref(used)),
                     "ccd_penalty_group_force_device")
         return bool(used.value)
+
+    def velocity_filter(self, qstart, qend, faces, invmasses, outer_eta: float, inner_eta: float,
+                        base_stiffness: float = 1e-4, base_substep: float = 1e-4, cor: float = 0.1,
+                        max_rollbacks: int = 1000):
+        """VelocityFilter::velocityFilter (ccd_velocity_filter).  Returns
+        (result, qend_out, stats): result is the reference's return value;
+        qend_out the filtered end positions (qend unchanged when result < 0)."""
+        qs = np.ascontiguousarray(qstart, dtype=np.float64).ravel()
+        qe = np.ascontiguousarray(qend, dtype=np.float64).ravel().copy()
+        f = np.ascontiguousarray(faces, dtype=np.int32).reshape(-1, 3)
+        mi = np.ascontiguousarray(invmasses, dtype=np.float64).ravel()
+        if qe.size != qs.size or mi.size != qs.size:
+            raise ValueError("qstart, qend and invmasses must have the same size")
+        res = ctypes.c_int32(0)
+        st = VelocityFilterStats()
+        self._check(self.lib.ccd_velocity_filter(self.handle, qs.size // 3, _ptr(qs), _ptr(qe), f.shape[0], _ptr(f),
+                                                 _ptr(mi), outer_eta, inner_eta, base_stiffness, base_substep, cor,
+                                                 max_rollbacks, ctypes.byref(res), ctypes.byref(st)),
+                    "ccd_velocity_filter")
+        return res.value, qe, {k: getattr(st, k) for k, _ in VelocityFilterStats._fields_}
 
     def prim_batch_device(self, kind: int, n: int, rows_ptr: int, eta_ptr: int, eta_count: int, hit_ptr: int,
                           t_ptr: int, status_ptr: int | None = None, path: int = PATH_CULL_REFINE):

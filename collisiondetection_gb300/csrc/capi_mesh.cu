@@ -5,7 +5,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <functional>
+#include <map>
 #include <new>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -16,6 +19,8 @@
 #include "mesh.cuh"
 #include "radix_sort.cuh"
 #include "separating.cuh"
+#include "ccd_heap.h"
+#include "velocity.cuh"
 
 using namespace ccd_capi;
 
@@ -842,3 +847,462 @@ int ccd_mesh_last_stats(const ccd_mesh *m, ccd_mesh_stats *out) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ velocity filter
+namespace {
+
+// A canonical stencil as a map key, ordered like the reference's stencils
+// (lexicographic; src/Stencils.h).
+struct StencilKey {
+  int32_t a, b, c, d;
+  bool operator<(const StencilKey &o) const {
+    if (a != o.a) return a < o.a;
+    if (b != o.b) return b < o.b;
+    if (c != o.c) return c < o.c;
+    return d < o.d;
+  }
+};
+
+// PenaltyGroup (src/PenaltyGroup.h): its parameters, firing step and stencils.
+struct HostGroup {
+  double dt, eta, inner, k, cor;
+  int nextstep;
+  std::vector<StencilKey> vf, ee;  // insertion order
+  std::set<int32_t> verts;         // getGroupStencil
+};
+
+// ActiveLayers (src/ActiveLayers.cpp) without its time stepping, which runs
+// on the device: groups, the event queue, and the stencils' depths.
+struct Layers {
+  double outer, inner, base_dt, base_k, term, cor;
+  int deepest = 0;
+  std::vector<HostGroup> groups;
+  std::vector<int> heap;
+  int heap_size = 0;
+  std::map<StencilKey, int> vfdepth, eedepth;
+
+  bool later(int a, int b) const {
+    return (double)groups[b].nextstep * groups[b].dt < (double)groups[a].nextstep * groups[a].dt;
+  }
+  void push(std::vector<int> &h, int &size, int g) {
+    if ((int)h.size() < size + 1) h.resize(size + 1);
+    ccd::heap_push(h.data(), &size, g, [this](int a, int b) { return later(a, b); });
+  }
+  // ActiveLayers::layerDepth (:169-172)
+  double layer_depth(int layer) const { return inner + (outer - inner) / double(layer); }
+  // ActiveLayers::addGroups (:69-89)
+  void add_groups(int maxdepth) {
+    while (deepest < maxdepth) {
+      const int depth = deepest + 1;
+      const double fudge = 1e-4;
+      const double ki = base_k * depth * depth * depth;
+      const double etai = layer_depth(depth);
+      const double dti = base_dt / double(depth) / std::sqrt(double(depth) + fudge);
+      groups.push_back(HostGroup{dti, etai, inner, ki, cor, 1, {}, {}, {}});
+      push(heap, heap_size, (int)groups.size() - 1);
+      deepest++;
+    }
+  }
+  // ActiveLayers::addVFStencil / addEEStencil (:43-67)
+  void add(int kind, const StencilKey &st) {
+    std::map<StencilKey, int> &depth = kind == 0 ? vfdepth : eedepth;
+    const int olddepth = depth[st];
+    for (int i = 0; i < 5; i++) {
+      add_groups(olddepth + i + 1);
+      HostGroup &g = groups[(size_t)(olddepth + i)];
+      (kind == 0 ? g.vf : g.ee).push_back(st);
+      g.verts.insert(st.a);
+      g.verts.insert(st.b);
+      g.verts.insert(st.c);
+      g.verts.insert(st.d);
+      depth[st]++;
+    }
+  }
+  // ActiveLayers::VFStencilThickness / EEStencilThickness (:174-188)
+  double thickness(int kind, const StencilKey &st) const {
+    const std::map<StencilKey, int> &depth = kind == 0 ? vfdepth : eedepth;
+    auto it = depth.find(st);
+    return it != depth.end() ? layer_depth(it->second + 1) : layer_depth(1);
+  }
+  // ActiveLayers::rollback (:158-167): firing steps reset, then the queue
+  // re-built by popping the old one (whose keys just changed) into a new one.
+  void rollback() {
+    for (HostGroup &g : groups) g.nextstep = 1;
+    std::vector<int> fresh;
+    int fresh_size = 0;
+    while (heap_size > 0) {
+      push(fresh, fresh_size, heap[0]);
+      ccd::heap_pop(heap.data(), &heap_size, [this](int a, int b) { return later(a, b); });
+    }
+    heap = fresh;
+    heap_size = fresh_size;
+  }
+};
+
+// Device buffers of one velocity-filter call.
+struct FilterBuffers {
+  std::vector<void *> owned;
+  template <class T>
+  int alloc(ccd_context *ctx, T **p, size_t count) {
+    CCD_CUDA(cudaMalloc(p, std::max<size_t>(count, 1) * sizeof(T)));
+    owned.push_back(*p);
+    return CCD_OK;
+  }
+  ~FilterBuffers() {
+    for (void *p : owned) cudaFree(p);
+  }
+};
+
+// Makes device history arrays (off [nv+1], times, pos) the mesh's history.
+int adopt_history(ccd_mesh *m, const int32_t *off, const double *times, const double *pos, int64_t ne,
+                  double gap) {
+  ccd_context *ctx = m->ctx;
+  if (m->hist_cap < ne || !m->hist_off) {
+    CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+    cudaFree(m->hist_time);
+    cudaFree(m->hist_pos);
+    m->hist_time = m->hist_pos = nullptr;
+    m->hist_cap = 0;
+    CCD_CUDA(cudaMalloc(&m->hist_time, (size_t)ne * sizeof(double)));
+    CCD_CUDA(cudaMalloc(&m->hist_pos, (size_t)ne * 3 * sizeof(double)));
+    m->hist_cap = ne;
+    if (!m->hist_off) CCD_CUDA(cudaMalloc(&m->hist_off, ((size_t)m->nv + 1) * sizeof(int32_t)));
+  }
+  CCD_CUDA(cudaMemcpyAsync(m->hist_off, off, ((size_t)m->nv + 1) * sizeof(int32_t), cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+  CCD_CUDA(cudaMemcpyAsync(m->hist_time, times, (size_t)ne * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  CCD_CUDA(cudaMemcpyAsync(m->hist_pos, pos, (size_t)ne * 3 * sizeof(double), cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+  m->hist_min_gap = gap;
+  m->has_history = true;
+  m->have_cand = m->have_col = false;
+  return CCD_OK;
+}
+
+}  // namespace
+
+extern "C" int ccd_velocity_filter(ccd_context *ctx, int32_t nverts, const double *qstart, double *qend,
+                                   int32_t nfaces, const int32_t *faces, const double *invmasses, double outer_eta,
+                                   double inner_eta, double base_stiffness, double base_substep, double cor,
+                                   int32_t max_rollbacks, int32_t *result, ccd_velocity_filter_stats *stats) {
+  if (!ctx) return CCD_ERR_INVALID_ARGUMENT;
+  if (!result || nverts <= 0 || nfaces < 0 || !qstart || !qend || !invmasses || (nfaces && !faces))
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null buffer or empty mesh");
+  ccd_velocity_filter_stats st{};
+  // VelocityFilter.cpp:22-39: every vertex in some face
+  {
+    std::vector<uint8_t> used((size_t)nverts, 0);
+    for (int64_t i = 0; i < 3 * (int64_t)nfaces; i++) {
+      if (faces[i] < 0 || faces[i] >= nverts) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "face vertex out of range");
+      used[(size_t)faces[i]] = 1;
+    }
+    for (uint8_t u : used)
+      if (!u) {
+        *result = -1;  // DANGLING_VERTICES
+        if (stats) *stats = st;
+        return CCD_OK;
+      }
+  }
+  double maxmass = 0;
+  for (int64_t i = 0; i < 3 * (int64_t)nverts; i++) maxmass = ccd::smax(maxmass, invmasses[i]);
+  const double dt = base_substep;
+  const double k = base_stiffness / dt * std::sqrt(maxmass);
+  Layers al{outer_eta, inner_eta, dt, k, 1.0, cor};
+  ccd_mesh *m = nullptr;
+  int rc = ccd_mesh_create(ctx, nverts, nfaces, faces, &m);
+  if (rc) return rc;
+  struct MeshGuard {
+    ccd_mesh *m;
+    ~MeshGuard() { ccd_mesh_destroy(m); }
+  } guard{m};
+  std::vector<uint8_t> fixed((size_t)nverts, 0);
+  bool any_fixed = false;
+  for (int64_t i = 0; i < 3 * (int64_t)nverts; i++)
+    if (invmasses[i] == 0.0) fixed[(size_t)(i / 3)] = 1, any_fixed = true;
+  rc = ccd_mesh_set_fixed(m, any_fixed ? fixed.data() : nullptr);
+  if (rc) return rc;
+  // VelocityFilter.cpp:60-67
+  double closest = 0;
+  rc = ccd_mesh_self_distance(m, qstart, &closest, nullptr, nullptr);
+  if (rc) return rc;
+  st.start_distance = closest;
+  if (closest < inner_eta) {
+    *result = -2;  // STARTING_STATE_INTERSECTS
+    if (stats) *stats = st;
+    return CCD_OK;
+  }
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const int64_t n3 = 3 * (int64_t)nverts;
+  FilterBuffers fb;
+  double *d_q0 = nullptr, *d_q = nullptr, *d_v = nullptr, *d_lu = nullptr, *d_minv = nullptr, *d_newq = nullptr,
+         *d_newv = nullptr, *d_qend = nullptr;
+  rc = fb.alloc(ctx, &d_q0, n3);
+  if (!rc) rc = fb.alloc(ctx, &d_q, n3);
+  if (!rc) rc = fb.alloc(ctx, &d_v, n3);
+  if (!rc) rc = fb.alloc(ctx, &d_lu, n3);
+  if (!rc) rc = fb.alloc(ctx, &d_minv, n3);
+  if (!rc) rc = fb.alloc(ctx, &d_newq, n3);
+  if (!rc) rc = fb.alloc(ctx, &d_newv, n3);
+  if (!rc) rc = fb.alloc(ctx, &d_qend, n3);
+  int64_t *d_counts = nullptr;  // [0] log_n, [1] events
+  int *d_status = nullptr;
+  unsigned long long *d_gap = nullptr;
+  uint32_t *d_count = nullptr, *d_scan = nullptr;
+  int32_t *d_off = nullptr;
+  if (!rc) rc = fb.alloc(ctx, &d_counts, 2);
+  if (!rc) rc = fb.alloc(ctx, &d_status, 1);
+  if (!rc) rc = fb.alloc(ctx, &d_gap, 1);
+  if (!rc) rc = fb.alloc(ctx, &d_count, (size_t)nverts + 1);
+  if (!rc) rc = fb.alloc(ctx, &d_scan, (size_t)nverts + 1);
+  if (!rc) rc = fb.alloc(ctx, &d_off, (size_t)nverts + 1);
+  if (rc) return rc;
+  CCD_CUDA(cudaMemcpyAsync(d_q0, qstart, n3 * 8, cudaMemcpyHostToDevice, s));
+  CCD_CUDA(cudaMemcpyAsync(d_qend, qend, n3 * 8, cudaMemcpyHostToDevice, s));
+  CCD_CUDA(cudaMemcpyAsync(d_minv, invmasses, n3 * 8, cudaMemcpyHostToDevice, s));
+  std::vector<double> hv((size_t)n3);
+  for (int64_t i = 0; i < n3; i++) hv[(size_t)i] = qend[i] - qstart[i];  // s.v = qend - qstart
+  // growable per-iteration buffers
+  int64_t log_cap = 0, grp_cap[4] = {0, 0, 0, 0};
+  int32_t *log_v = nullptr;
+  double *log_t = nullptr, *log_p = nullptr;
+  double *h_times = nullptr, *h_pos = nullptr;
+  uint64_t *keys = nullptr, *keys_alt = nullptr;
+  void *temp = nullptr;
+  size_t temp_bytes = 0;
+  std::vector<void *> grow_owned;
+  auto release_growable = [&]() {
+    for (void *p : grow_owned) cudaFree(p);
+    grow_owned.clear();
+  };
+  struct Release {
+    std::function<void()> f;
+    ~Release() { f(); }
+  } release{release_growable};
+  auto dev = [&](auto **p, size_t count) -> int {
+    CCD_CUDA(cudaMalloc(p, std::max<size_t>(count, 1) * sizeof(**p)));
+    grow_owned.push_back(*p);
+    return CCD_OK;
+  };
+  (void)grp_cap;
+  for (int iter = 0; iter < max_rollbacks; iter++) {
+    // ---- the groups of this iteration, flattened
+    const int G = (int)al.groups.size();
+    std::vector<double> g_dt, g_eta, g_inner, g_k, g_cor;
+    std::vector<int> g_next;
+    std::vector<int64_t> st_off(1, 0), gv_off(1, 0), co_off(1, 0);
+    std::vector<int32_t> n_vf, stv, gvv, cov;
+    int64_t max_st = 1;
+    for (const HostGroup &g : al.groups) {
+      g_dt.push_back(g.dt), g_eta.push_back(g.eta), g_inner.push_back(g.inner), g_k.push_back(g.k);
+      g_cor.push_back(g.cor), g_next.push_back(g.nextstep);
+      n_vf.push_back((int32_t)g.vf.size());
+      std::vector<const StencilKey *> all;
+      for (const StencilKey &x : g.vf) all.push_back(&x);
+      for (const StencilKey &x : g.ee) all.push_back(&x);
+      for (const StencilKey *x : all) stv.insert(stv.end(), {x->a, x->b, x->c, x->d});
+      st_off.push_back(st_off.back() + (int64_t)all.size());
+      max_st = std::max<int64_t>(max_st, (int64_t)all.size());
+      std::vector<int32_t> verts(g.verts.begin(), g.verts.end());
+      std::vector<std::vector<int32_t>> lists(verts.size());
+      for (size_t i = 0; i < all.size(); i++) {
+        const int32_t vs[4] = {all[i]->a, all[i]->b, all[i]->c, all[i]->d};
+        for (int slot = 0; slot < 4; slot++) {
+          const size_t at = (size_t)(std::lower_bound(verts.begin(), verts.end(), vs[slot]) - verts.begin());
+          lists[at].push_back((int32_t)((i << 2) | (size_t)slot));
+        }
+      }
+      for (size_t j = 0; j < verts.size(); j++) {
+        gvv.push_back(verts[j]);
+        cov.insert(cov.end(), lists[j].begin(), lists[j].end());
+        co_off.push_back((int64_t)cov.size());
+      }
+      gv_off.push_back((int64_t)gvv.size());
+    }
+    release_growable();
+    double *d_gdt = nullptr, *d_geta = nullptr, *d_ginner = nullptr, *d_gk = nullptr, *d_gcor = nullptr,
+           *d_contrib = nullptr;
+    int *d_next = nullptr, *d_heap = nullptr, *d_heap_size = nullptr;
+    int64_t *d_st_off = nullptr, *d_gv_off = nullptr, *d_co_off = nullptr;
+    int32_t *d_nvf = nullptr, *d_st = nullptr, *d_gv = nullptr, *d_co = nullptr;
+    uint8_t *d_fired = nullptr;
+    rc = dev(&d_gdt, G);
+    if (!rc) rc = dev(&d_geta, G);
+    if (!rc) rc = dev(&d_ginner, G);
+    if (!rc) rc = dev(&d_gk, G);
+    if (!rc) rc = dev(&d_gcor, G);
+    if (!rc) rc = dev(&d_next, G);
+    if (!rc) rc = dev(&d_heap, G + 1);
+    if (!rc) rc = dev(&d_heap_size, 1);
+    if (!rc) rc = dev(&d_st_off, st_off.size());
+    if (!rc) rc = dev(&d_gv_off, gv_off.size());
+    if (!rc) rc = dev(&d_co_off, co_off.size());
+    if (!rc) rc = dev(&d_nvf, G);
+    if (!rc) rc = dev(&d_st, stv.size());
+    if (!rc) rc = dev(&d_gv, gvv.size());
+    if (!rc) rc = dev(&d_co, cov.size());
+    if (!rc) rc = dev(&d_contrib, 12 * (size_t)max_st);
+    if (!rc) rc = dev(&d_fired, (size_t)max_st);
+    if (!rc && log_cap == 0) log_cap = std::max<int64_t>(1 << 20, 4 * (int64_t)nverts);
+    if (!rc) rc = dev(&log_v, (size_t)log_cap);
+    if (!rc) rc = dev(&log_t, (size_t)log_cap);
+    if (!rc) rc = dev(&log_p, 3 * (size_t)log_cap);
+    if (rc) return rc;
+    auto up = [&](void *d, const void *h, size_t bytes) -> int {
+      if (bytes) CCD_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, s));
+      return CCD_OK;
+    };
+    rc = up(d_gdt, g_dt.data(), G * 8);
+    if (!rc) rc = up(d_geta, g_eta.data(), G * 8);
+    if (!rc) rc = up(d_ginner, g_inner.data(), G * 8);
+    if (!rc) rc = up(d_gk, g_k.data(), G * 8);
+    if (!rc) rc = up(d_gcor, g_cor.data(), G * 8);
+    if (!rc) rc = up(d_next, g_next.data(), G * 4);
+    if (!rc) rc = up(d_heap, al.heap.data(), (size_t)al.heap_size * 4);
+    if (!rc) rc = up(d_heap_size, &al.heap_size, 4);
+    if (!rc) rc = up(d_st_off, st_off.data(), st_off.size() * 8);
+    if (!rc) rc = up(d_gv_off, gv_off.data(), gv_off.size() * 8);
+    if (!rc) rc = up(d_co_off, co_off.data(), co_off.size() * 8);
+    if (!rc) rc = up(d_nvf, n_vf.data(), n_vf.size() * 4);
+    if (!rc) rc = up(d_st, stv.data(), stv.size() * 4);
+    if (!rc) rc = up(d_gv, gvv.data(), gvv.size() * 4);
+    if (!rc) rc = up(d_co, cov.data(), cov.size() * 4);
+    if (rc) return rc;
+    // ---- the state (VelocityFilter.cpp:75-80) and the event loop (ActiveLayers::step)
+    CCD_CUDA(cudaMemcpyAsync(d_q, d_q0, n3 * 8, cudaMemcpyDeviceToDevice, s));
+    CCD_CUDA(cudaMemcpyAsync(d_v, hv.data(), n3 * 8, cudaMemcpyHostToDevice, s));
+    CCD_CUDA(cudaMemsetAsync(d_lu, 0, n3 * 8, s));
+    CCD_CUDA(cudaMemsetAsync(d_counts, 0, 16, s));
+    ccd::LayerGroups lg{G, d_gdt, d_geta, d_ginner, d_gk, d_gcor, d_next, d_st_off, d_nvf, d_st,
+                        d_gv_off, d_gv, d_co_off, d_co, d_heap, d_heap_size};
+    for (;;) {
+      ccd::LayerState ls{nverts, d_q, d_v, d_lu, d_minv, d_newq, d_newv, d_contrib, d_fired,
+                         log_v, log_t, log_p, log_cap, d_counts, 1.0, d_status, d_counts + 1};
+      CCD_CUDA(ccd::launch_layer_events(lg, ls, (int64_t)1 << 20, s));
+      int status = 0;
+      int64_t counts[2] = {0, 0};
+      CCD_CUDA(cudaMemcpyAsync(&status, d_status, 4, cudaMemcpyDeviceToHost, s));
+      CCD_CUDA(cudaMemcpyAsync(counts, d_counts, 16, cudaMemcpyDeviceToHost, s));
+      CCD_CUDA(cudaStreamSynchronize(s));
+      if (status == 1) {
+        st.events += counts[1];
+        break;
+      }
+      if (counts[0] + (gv_off.back() + 1) > log_cap) {
+        // the log is full: double it, keeping what it holds
+        const int64_t ncap = 2 * log_cap;
+        int32_t *nv_ = nullptr;
+        double *nt = nullptr, *np = nullptr;
+        rc = dev(&nv_, (size_t)ncap);
+        if (!rc) rc = dev(&nt, (size_t)ncap);
+        if (!rc) rc = dev(&np, 3 * (size_t)ncap);
+        if (rc) return rc;
+        CCD_CUDA(cudaMemcpyAsync(nv_, log_v, (size_t)counts[0] * 4, cudaMemcpyDeviceToDevice, s));
+        CCD_CUDA(cudaMemcpyAsync(nt, log_t, (size_t)counts[0] * 8, cudaMemcpyDeviceToDevice, s));
+        CCD_CUDA(cudaMemcpyAsync(np, log_p, (size_t)counts[0] * 24, cudaMemcpyDeviceToDevice, s));
+        log_v = nv_, log_t = nt, log_p = np, log_cap = ncap;
+      }
+    }
+    ccd::LayerState ls{nverts, d_q, d_v, d_lu, d_minv, d_newq, d_newv, d_contrib, d_fired,
+                       log_v, log_t, log_p, log_cap, d_counts, 1.0, d_status, d_counts + 1};
+    CCD_CUDA(ccd::launch_layer_finish(ls, s));
+    int64_t nlog = 0;
+    CCD_CUDA(cudaMemcpyAsync(&nlog, d_counts, 8, cudaMemcpyDeviceToHost, s));
+    CCD_CUDA(cudaStreamSynchronize(s));
+    // the nextstep values advanced on the device: the host's groups follow
+    {
+      std::vector<int> nx((size_t)G);
+      std::vector<int> hp((size_t)G + 1);
+      int hs = 0;
+      if (G) CCD_CUDA(cudaMemcpyAsync(nx.data(), d_next, (size_t)G * 4, cudaMemcpyDeviceToHost, s));
+      CCD_CUDA(cudaMemcpyAsync(&hs, d_heap_size, 4, cudaMemcpyDeviceToHost, s));
+      CCD_CUDA(cudaStreamSynchronize(s));
+      if (hs) CCD_CUDA(cudaMemcpyAsync(hp.data(), d_heap, (size_t)hs * 4, cudaMemcpyDeviceToHost, s));
+      CCD_CUDA(cudaStreamSynchronize(s));
+      for (int g = 0; g < G; g++) al.groups[(size_t)g].nextstep = nx[(size_t)g];
+      al.heap.assign(hp.begin(), hp.begin() + hs);
+      al.heap_size = hs;
+    }
+    // ---- the iteration's History
+    const int64_t ne = 2 * (int64_t)nverts + nlog;
+    rc = dev(&h_times, (size_t)ne);
+    if (!rc) rc = dev(&h_pos, 3 * (size_t)ne);
+    if (!rc) rc = dev(&keys, (size_t)std::max<int64_t>(nlog, 1));
+    if (!rc) rc = dev(&keys_alt, (size_t)std::max<int64_t>(nlog, 1));
+    if (rc) return rc;
+    temp_bytes = std::max(ccd::radix_sort_temp_bytes(std::max<int64_t>(nlog, 1)), ccd::scan_temp_bytes(nverts));
+    rc = dev((char **)&temp, temp_bytes);
+    if (rc) return rc;
+    const unsigned long long one = 0x3ff0000000000000ull;
+    CCD_CUDA(cudaMemcpyAsync(d_gap, &one, 8, cudaMemcpyHostToDevice, s));
+    CCD_CUDA(ccd::build_layer_history(nverts, d_q0, d_q, log_v, log_t, log_p, nlog, keys, keys_alt, temp, temp_bytes,
+                                      d_count, d_scan, d_off, h_times, h_pos, d_gap, s));
+    unsigned long long gap_bits = one;
+    CCD_CUDA(cudaMemcpyAsync(&gap_bits, d_gap, 8, cudaMemcpyDeviceToHost, s));
+    CCD_CUDA(cudaStreamSynchronize(s));
+    double gap = 1.0;
+    memcpy(&gap, &gap_bits, 8);
+    st.history_entries = ne;
+    rc = adopt_history(m, d_off, h_times, h_pos, ne, gap);
+    if (rc) return rc;
+    // ---- ActiveLayers::collisionDetection (:190-226)
+    rc = run_broadphase(m, CCD_BROADPHASE_KDOP13, outer_eta);
+    if (rc) return rc;
+    const int64_t nc[2] = {m->n_cand[0], m->n_cand[1]};
+    std::vector<int32_t> cand[2];
+    std::vector<uint8_t> hit[2], stat[2];
+    for (int kind = 0; kind < 2; kind++) {
+      const int64_t n = nc[kind];
+      cand[kind].resize(4 * (size_t)n);
+      hit[kind].assign((size_t)n, 0);
+      stat[kind].assign((size_t)n, 0);
+      if (!n) continue;
+      CCD_CUDA(cudaMemcpyAsync(cand[kind].data(), m->cand[kind], (size_t)n * 16, cudaMemcpyDeviceToHost, s));
+      CCD_CUDA(cudaStreamSynchronize(s));
+      std::vector<double> eta((size_t)n);
+      for (int64_t i = 0; i < n; i++) {
+        const int32_t *c = cand[kind].data() + 4 * i;
+        eta[(size_t)i] = al.thickness(kind, StencilKey{c[0], c[1], c[2], c[3]});
+      }
+      Lane &L = m->lane[0];
+      rc = grow(ctx, &m->in_eta, &m->in_eta_cap, n);
+      if (!rc) rc = grow(ctx, &L.hit, &L.hit_cap, 2 * n);
+      if (rc) return rc;
+      CCD_CUDA(cudaMemcpyAsync(m->in_eta, eta.data(), (size_t)n * 8, cudaMemcpyHostToDevice, s));
+      const ccd::HistoryView hv2{m->hist_off, m->hist_time, m->hist_pos};
+      CCD_CUDA(ccd::launch_separating_plane(kind, hv2, m->cand[kind], n, m->in_eta, 1, gap / 4.0, L.hit, L.hit + n,
+                                            s));
+      CCD_CUDA(cudaMemcpyAsync(hit[kind].data(), L.hit, (size_t)n, cudaMemcpyDeviceToHost, s));
+      CCD_CUDA(cudaMemcpyAsync(stat[kind].data(), L.hit + n, (size_t)n, cudaMemcpyDeviceToHost, s));
+      CCD_CUDA(cudaStreamSynchronize(s));
+      for (uint8_t x : stat[kind])
+        if (x)
+          return mesh_fail(m, CCD_ERR_INVALID_ARGUMENT,
+                           "separating-plane search stalled (the reference's recursion does not end on this input)");
+    }
+    std::vector<StencilKey> found[2];
+    for (int kind = 0; kind < 2; kind++)
+      for (int64_t i = 0; i < nc[kind]; i++)
+        if (hit[kind][(size_t)i]) {
+          const int32_t *c = cand[kind].data() + 4 * i;
+          found[kind].push_back(StencilKey{c[0], c[1], c[2], c[3]});
+        }
+    st.iterations = iter + 1;
+    st.collisions += (int64_t)(found[0].size() + found[1].size());
+    // ActiveLayers::runOneIteration (:244-255)
+    al.rollback();
+    for (int kind = 0; kind < 2; kind++)
+      for (const StencilKey &x : found[kind]) al.add(kind, x);
+    st.layers = al.deepest;
+    if (found[0].empty() && found[1].empty()) {
+      CCD_CUDA(cudaMemcpyAsync(qend, d_q, n3 * 8, cudaMemcpyDeviceToHost, s));
+      CCD_CUDA(cudaStreamSynchronize(s));
+      *result = iter;
+      if (stats) *stats = st;
+      return CCD_OK;
+    }
+  }
+  *result = -3;  // MAXROLLBACKS_EXCEEDED
+  if (stats) *stats = st;
+  return CCD_OK;
+}

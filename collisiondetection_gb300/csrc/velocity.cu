@@ -1,0 +1,273 @@
+// The active layers' event loop on the device (velocity.cuh).
+//
+// ActiveLayers::step (src/ActiveLayers.cpp:91-156) fires one penalty group at
+// a time, in the order of a priority queue keyed by the groups' next firing
+// times; each firing moves the group's vertices to the firing time, applies
+// the group's penalty impulses and logs the touched vertices' positions.
+// Firings depend on one another through shared vertices, so they run in
+// sequence -- here inside one persistent block, so that no firing costs a
+// kernel launch: thread 0 keeps the queue (ccd_heap.h, the library heap's
+// exact order), and the block's threads share each firing's vertices and
+// stencils, with a barrier between the phases of a firing.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "ccd_heap.h"
+#include "penalty.cuh"
+#include "radix_sort.cuh"
+#include "velocity.cuh"
+
+namespace ccd {
+
+namespace {
+
+constexpr int kLoopThreads = 512;
+
+struct FireLater {
+  const int *nextstep;
+  const double *dt;
+  // PenaltyGroupComparator (src/ActiveLayers.cpp:18-21): a ranks below b when
+  // b fires first; PenaltyGroup::nextFireTime is nextstep * dt.
+  __device__ bool operator()(int a, int b) const {
+    return (double)nextstep[b] * dt[b] < (double)nextstep[a] * dt[a];
+  }
+};
+
+__global__ void __launch_bounds__(kLoopThreads) layer_events(LayerGroups g, LayerState s, int64_t max_events) {
+  __shared__ int sh_group, sh_action;
+  __shared__ double sh_time;
+  __shared__ int64_t sh_base;
+  __shared__ int sh_scan[kLoopThreads];
+  const int tid = threadIdx.x;
+  const FireLater later{g.nextstep, g.dt};
+  int action = 0;
+  for (int64_t ev = 0;; ev++) {
+    if (tid == 0) {
+      int a = 0, grp = -1;
+      double t = 0.0;
+      if (*g.heap_size == 0) {
+        a = 1;
+      } else {
+        grp = g.heap[0];
+        t = (double)g.nextstep[grp] * g.dt[grp];
+        if (!(t < s.term)) {
+          a = 1;
+        } else if (ev >= max_events || *s.log_n + (g.gv_off[grp + 1] - g.gv_off[grp]) > s.log_cap) {
+          a = 2;
+        } else {
+          heap_pop(g.heap, g.heap_size, later);
+        }
+      }
+      sh_action = a;
+      sh_group = grp;
+      sh_time = t;
+      sh_base = *s.log_n;
+    }
+    __syncthreads();
+    action = sh_action;
+    if (action) break;
+    const int grp = sh_group;
+    const double t = sh_time;
+    const int64_t v0 = g.gv_off[grp], v1 = g.gv_off[grp + 1];
+    const int64_t s0 = g.st_off[grp], s1 = g.st_off[grp + 1];
+    const int nvf = g.n_vf[grp];
+    // (1) the group's vertices at the firing time (src/ActiveLayers.cpp:105-114)
+    for (int64_t j = v0 + tid; j < v1; j += blockDim.x) {
+      const int vert = g.gv[j];
+      for (int c = 0; c < 3; c++) {
+        const int64_t i = 3 * (int64_t)vert + c;
+        const double dt = t - s.lu[i];
+        const double nq = s.q[i] + (t - s.lu[i]) * s.v[i];
+        s.newq[i] = nq;
+        s.newv[i] = (nq - s.q[i]) / dt;
+      }
+    }
+    __syncthreads();
+    // (2) each stencil's potential (PenaltyGroup::addForce, src/PenaltyGroup.cpp:34-52)
+    const PenaltyParams pp{g.eta[grp], g.inner[grp], g.stiffness[grp], g.cor[grp]};
+    for (int64_t k = s0 + tid; k < s1; k += blockDim.x) {
+      const int64_t local = k - s0;
+      const int v4[4] = {g.st[4 * k], g.st[4 * k + 1], g.st[4 * k + 2], g.st[4 * k + 3]};
+      v3d c[4];
+      const bool f = local < nvf ? stencil_force<0>(s.newq, s.newv, v4, pp, c)
+                                 : stencil_force<1>(s.newq, s.newv, v4, pp, c);
+      s.fired[local] = f ? 1 : 0;
+      if (f) {
+        double *out = s.contrib + 12 * local;
+        for (int q = 0; q < 4; q++) {
+          out[3 * q] = c[q].x;
+          out[3 * q + 1] = c[q].y;
+          out[3 * q + 2] = c[q].z;
+        }
+      }
+    }
+    __syncthreads();
+    // (3) per vertex: the group force summed in the reference's order, F =
+    // 0 + group * dt, the impulse on touched vertices, and their history
+    // entries in ascending vertex order (src/ActiveLayers.cpp:116-139)
+    const double gdt = g.dt[grp];
+    for (int64_t tile = v0; tile < v1; tile += blockDim.x) {
+      const int64_t j = tile + tid;
+      int touched = 0, vert = 0;
+      if (j < v1) {
+        vert = g.gv[j];
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int64_t e = g.co_off[j]; e < g.co_off[j + 1]; e++) {
+          const int code = g.co[e];
+          const int local = code >> 2, slot = code & 3;
+          if (!s.fired[local]) continue;
+          const double *cv = s.contrib + 12 * (int64_t)local + 3 * slot;
+          const bool minus = local < nvf ? slot == 0 : slot <= 1;
+          for (int c = 0; c < 3; c++) acc[c] = minus ? acc[c] - cv[c] : acc[c] + cv[c];
+        }
+        double F[3];
+        for (int c = 0; c < 3; c++) F[c] = 0.0 + acc[c] * gdt;
+        touched = (F[0] != 0.0 || F[1] != 0.0 || F[2] != 0.0) ? 1 : 0;
+        if (touched) {
+          for (int c = 0; c < 3; c++) {
+            const int64_t i = 3 * (int64_t)vert + c;
+            s.v[i] = s.v[i] + s.minv[i] * F[c];
+            s.q[i] = s.newq[i];
+            s.lu[i] = t;
+          }
+        }
+      }
+      // exclusive block scan of the touched flags (Hillis-Steele)
+      sh_scan[tid] = touched;
+      __syncthreads();
+      for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        const int add = tid >= o ? sh_scan[tid - o] : 0;
+        __syncthreads();
+        sh_scan[tid] += add;
+        __syncthreads();
+      }
+      const int incl = sh_scan[tid];
+      const int total = sh_scan[blockDim.x - 1];
+      if (touched) {
+        const int64_t at = sh_base + incl - 1;
+        s.log_v[at] = vert;
+        s.log_t[at] = t;
+        for (int c = 0; c < 3; c++) s.log_p[3 * at + c] = s.q[3 * (int64_t)vert + c];
+      }
+      __syncthreads();
+      if (tid == 0) sh_base += total;
+      __syncthreads();
+    }
+    if (tid == 0) {
+      *s.log_n = sh_base;
+      *s.events += 1;
+      g.nextstep[grp] += 1;  // PenaltyGroup::incrementTimeStep
+      heap_push(g.heap, g.heap_size, grp, later);
+    }
+    __syncthreads();
+  }
+  if (tid == 0) *s.status = action;
+}
+
+__global__ void __launch_bounds__(256) layer_finish(int64_t n3, double *q, const double *v, double *lu, double term) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  q[i] += (term - lu[i]) * v[i];
+  lu[i] = term;
+}
+
+__global__ void __launch_bounds__(256) count_log(const int32_t *log_v, int64_t n, uint32_t *count, uint64_t *keys) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  atomicAdd(&count[log_v[i]], 1u);
+  keys[i] = ((uint64_t)(uint32_t)log_v[i] << 32) | (uint64_t)i;
+}
+
+// Vertex v's entries: History's first (time 0, q0), its logged entries in
+// log order, finishHistory's (time 1.0, qend).  scan = exclusive prefix of the
+// logged counts, so off[v] = 2 v + scan[v].
+__global__ void __launch_bounds__(256) place_ends(int nv, const uint32_t *scan, const double *q0, const double *qend,
+                                                  int32_t *off, double *times, double *pos) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v > nv) return;
+  const int64_t first = 2 * (int64_t)v + scan[v];
+  off[v] = (int32_t)first;
+  if (v == nv) return;
+  const int64_t last = 2 * (int64_t)(v + 1) + scan[v + 1] - 1;
+  times[first] = 0.0;
+  times[last] = 1.0;
+  for (int c = 0; c < 3; c++) {
+    pos[3 * first + c] = q0[3 * (int64_t)v + c];
+    pos[3 * last + c] = qend[3 * (int64_t)v + c];
+  }
+}
+
+// Sorted position i of a logged entry of vertex v lands at 2 v + 1 + i.
+__global__ void __launch_bounds__(256) place_log(const uint64_t *keys, int64_t n, const double *log_t,
+                                                 const double *log_p, double *times, double *pos) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t k = keys[i];
+  const int64_t v = (int64_t)(k >> 32), e = (int64_t)(k & 0xffffffffull);
+  const int64_t at = 2 * v + 1 + i;
+  times[at] = log_t[e];
+  for (int c = 0; c < 3; c++) pos[3 * at + c] = log_p[3 * e + c];
+}
+
+// History::computeMinimumGap (src/History.cpp:82-96): the least gap between
+// consecutive entries of a vertex, at most 1.0 (times are non-decreasing, so
+// the gaps are non-negative and their bits order like the doubles).
+__global__ void __launch_bounds__(256) min_gap(int nv, const int32_t *off, const double *times,
+                                               unsigned long long *best) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= off[nv]) return;
+  // the vertex of entry e: the last v with off[v] <= e
+  int lo = 0, hi = nv - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (off[mid] <= e)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  if (e == off[lo]) return;
+  const double gap = times[e] - times[e - 1];
+  atomicMin(best, (unsigned long long)__double_as_longlong(gap));
+}
+
+unsigned grid_of(int64_t n, int threads) { return (unsigned)std::max<int64_t>(1, (n + threads - 1) / threads); }
+
+}  // namespace
+
+cudaError_t launch_layer_events(const LayerGroups &g, const LayerState &s, int64_t max_events, cudaStream_t st) {
+  layer_events<<<1, kLoopThreads, 0, st>>>(g, s, max_events);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_layer_finish(const LayerState &s, cudaStream_t st) {
+  const int64_t n3 = 3 * (int64_t)s.nverts;
+  layer_finish<<<grid_of(n3, 256), 256, 0, st>>>(n3, s.q, s.v, s.lu, s.term);
+  return cudaGetLastError();
+}
+
+cudaError_t build_layer_history(int nverts, const double *q0, const double *qend, const int32_t *log_v,
+                                const double *log_t, const double *log_p, int64_t n_log, uint64_t *keys,
+                                uint64_t *keys_alt, void *temp, size_t temp_bytes, uint32_t *count, uint32_t *scan,
+                                int32_t *off, double *times, double *pos, unsigned long long *best, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(count, 0, ((size_t)nverts + 1) * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  if (n_log > 0) {
+    count_log<<<grid_of(n_log, 256), 256, 0, st>>>(log_v, n_log, count, keys);
+    int vbits = 1;
+    while (vbits < 31 && ((int64_t)1 << vbits) < nverts) vbits++;
+    e = radix_sort_u64(keys, keys_alt, nullptr, nullptr, n_log, 0, 32 + vbits, temp, temp_bytes, st);
+    if (e != cudaSuccess) return e;
+  }
+  e = exclusive_scan_u32(count, scan, nverts, scan + nverts, temp, temp_bytes, st);
+  if (e != cudaSuccess) return e;
+  place_ends<<<grid_of((int64_t)nverts + 1, 256), 256, 0, st>>>(nverts, scan, q0, qend, off, times, pos);
+  if (n_log > 0) place_log<<<grid_of(n_log, 256), 256, 0, st>>>(keys, n_log, log_t, log_p, times, pos);
+  const int64_t entries = 2 * (int64_t)nverts + n_log;
+  min_gap<<<grid_of(entries, 256), 256, 0, st>>>(nverts, off, times, best);
+  return cudaGetLastError();
+}
+
+}  // namespace ccd

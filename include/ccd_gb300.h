@@ -359,6 +359,38 @@ int ccd_penalty_group_force_device(ccd_context *ctx, int32_t nverts, const doubl
                                    double cor, double dt, double *F, uint8_t *vf_fired, uint8_t *ee_fired,
                                    int *newused);
 
+/* ------------------------------------------------------------------ velocity filter
+ * VelocityFilter::velocityFilter (include/VelocityFilter.h:45-46,
+ * src/VelocityFilter.cpp:15-87) with the active layers it runs
+ * (src/ActiveLayers.cpp): penalty groups fired in the order of their event
+ * queue, the k-DOP broad phase over each iteration's history and the
+ * separating-plane narrow phase, until no collision is left.  The event loop
+ * of an iteration runs on the device in one persistent block; results are
+ * the reference's bit for bit.
+ *   qstart, qend  [nverts][3]; qend is overwritten with the filtered end
+ *                 positions when *result >= 0 (as the reference does)
+ *   faces         [nfaces][3]; invmasses [nverts][3] inverse mass per DOF
+ * *result receives the reference's return value: the number of outer
+ * iterations (>= 0), or -1 (a vertex in no face), -2 (the start is closer
+ * than inner_eta), -3 (max_rollbacks iterations were not enough).  A search
+ * of the separating-plane phase that the reference cannot finish (see
+ * ccd_narrowphase_separating_plane) fails the call with
+ * CCD_ERR_INVALID_ARGUMENT.  The reference's defaults: base_stiffness 1e-4,
+ * base_substep 1e-4, cor 0.1, max_rollbacks 1000. */
+typedef struct {
+  int32_t iterations;      /* outer iterations run */
+  int32_t layers;          /* penalty layers at the end */
+  int64_t events;          /* group firings, all iterations */
+  int64_t collisions;      /* colliding stencils found, all iterations */
+  int64_t history_entries; /* entries of the last iteration's history */
+  double start_distance;   /* Distance::meshSelfDistance of the start */
+} ccd_velocity_filter_stats;
+
+int ccd_velocity_filter(ccd_context *ctx, int32_t nverts, const double *qstart, double *qend, int32_t nfaces,
+                        const int32_t *faces, const double *invmasses, double outer_eta, double inner_eta,
+                        double base_stiffness, double base_substep, double cor, int32_t max_rollbacks,
+                        int32_t *result, ccd_velocity_filter_stats *stats);
+
 /* ------------------------------------------------------------------ serving
  * No counterpart in the reference (its detection runs in the caller's
  * thread).  A server runs collision queries for many callers at once on one

@@ -262,6 +262,9 @@ class Reference(_Lib):
                                              ctypes.c_double, _P, _P, _P]
         L.ref_narrowphase_history.argtypes = [ctypes.c_int, _P, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P]
         L.ref_separating_plane.argtypes = [ctypes.c_int, _P, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P]
+        L.ref_velocity_filter.argtypes = [ctypes.c_int, _P, _P, ctypes.c_int, _P, _P] + [ctypes.c_double] * 5 + \
+            [ctypes.c_int]
+        L.ref_velocity_filter.restype = ctypes.c_int
         self._distance_setup()
 
     def broadphase_history(self, kind: int, offsets, times, positions, faces, eta: float, fixed=None):
@@ -305,6 +308,17 @@ class Reference(_Lib):
         self.lib.ref_separating_plane(off.size - 1, _ptr(off), _ptr(tt), _ptr(pos), vf.shape[0], _ptr(vf), _ptr(vfe),
                                       ee.shape[0], _ptr(ee), _ptr(eee), _ptr(vh), _ptr(eh))
         return vh, eh
+
+    def velocity_filter(self, qstart, qend, faces, invmasses, outer_eta, inner_eta, base_stiffness=1e-4,
+                        base_substep=1e-4, cor=0.1, max_rollbacks=1000):
+        """VelocityFilter::velocityFilter: (return value, filtered qend)."""
+        qs = np.ascontiguousarray(qstart, dtype=np.float64).ravel()
+        qe = np.ascontiguousarray(qend, dtype=np.float64).ravel().copy()
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        mi = np.ascontiguousarray(invmasses, dtype=np.float64).ravel()
+        r = self.lib.ref_velocity_filter(qs.size // 3, _ptr(qs), _ptr(qe), faces.shape[0], _ptr(faces), _ptr(mi),
+                                         outer_eta, inner_eta, base_stiffness, base_substep, cor, max_rollbacks)
+        return int(r), qe
 
     def mesh_self_distance(self, verts, faces, fixed=None) -> float:
         verts = np.ascontiguousarray(verts, dtype=np.float64).ravel()

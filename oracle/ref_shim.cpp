@@ -4,7 +4,8 @@
 // (src/CTCD.cpp, src/History.cpp, src/Mesh.cpp, src/KDOPBroadPhase.cpp,
 // src/AABBBroadPhase.cpp, src/TrivialBroadPhase.cpp, src/CTCDNarrowPhase.cpp,
 // src/Distance.cpp, src/PenaltyPotential.cpp, src/PenaltyGroup.cpp,
-// src/SeparatingPlaneNarrowPhase.cpp), compiled by
+// src/SeparatingPlaneNarrowPhase.cpp, src/ActiveLayers.cpp,
+// src/VelocityFilter.cpp), compiled by
 // oracle/Makefile against the project-written Eigen-API subset.  It exists so
 // that tests/golden/make_golden.py can pin the C restatement (ccd_oracle.c)
 // against the reference itself.  The reference tree is only present in the
@@ -20,6 +21,7 @@
 #include "PenaltyGroup.h"
 #include "PenaltyPotential.h"
 #include "SeparatingPlaneNarrowPhase.h"
+#include "VelocityFilter.h"
 #include "History.h"
 #include "KDOPBroadPhase.h"
 #include "Mesh.h"
@@ -281,6 +283,21 @@ void ref_separating_plane(int nverts, const int32_t *off, const double *times, c
     vf_hit[i] = (uint8_t)ovf.count(VertexFaceStencil(vf[4 * i], vf[4 * i + 1], vf[4 * i + 2], vf[4 * i + 3]));
   for (int64_t i = 0; i < n_ee; i++)
     ee_hit[i] = (uint8_t)oee.count(EdgeEdgeStencil(ee[4 * i], ee[4 * i + 1], ee[4 * i + 2], ee[4 * i + 3]));
+}
+
+// ---------------------------------------------------------------- velocity filter
+// VelocityFilter::velocityFilter (src/VelocityFilter.cpp:15-87); qend is
+// overwritten, the return value is the reference's.
+int ref_velocity_filter(int nverts, const double *qstart, double *qend, int nfaces, const int32_t *faces,
+                        const double *invmasses, double outer_eta, double inner_eta, double base_stiffness,
+                        double base_substep, double cor, int max_rollbacks) {
+  Mesh m;
+  build_mesh(nverts, qstart, nfaces, faces, m);
+  Eigen::VectorXd q1 = vecx(nverts, qstart), q2 = vecx(nverts, qend), minv = vecx(nverts, invmasses);
+  const int r = VelocityFilter::velocityFilter(q1, q2, m.faces, minv, outer_eta, inner_eta, base_stiffness,
+                                               base_substep, cor, max_rollbacks);
+  for (int i = 0; i < 3 * nverts; i++) qend[i] = q2[i];
+  return r;
 }
 
 // ---------------------------------------------------------------- penalty forces

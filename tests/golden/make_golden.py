@@ -34,9 +34,13 @@ the reference's example meshes, and writes:
   SeparatingPlaneNarrowPhase's hit flags (stencils on which its recursion
   never ends, found by the oracle, are recorded instead of run: the
   reference overflows its stack there).
+* ``velocity_filter.npz`` / ``velocity_filter.json`` --
+  VelocityFilter::velocityFilter on small scenes (a triangle and a sheet
+  falling onto fixed ones, two spheres thrown together) and on its two early
+  exits: the return value and the filtered end positions.
 
 Only runs where the reference tree exists:
-    python tests/golden/make_golden.py [--only distances|trivial|penalty|history]
+    python tests/golden/make_golden.py [--only distances|trivial|penalty|history|velocity_filter]
 """
 from __future__ import annotations
 
@@ -392,6 +396,53 @@ def history_fixtures(ref) -> None:
         json.dump(meta, fh, indent=1, sort_keys=True)
 
 
+def velocity_filter_scenes():
+    """Scenes for VelocityFilter::velocityFilter: (qstart, qend, faces,
+    invmasses, outer_eta, inner_eta)."""
+    scenes = {}
+    # a triangle falling through a fixed one
+    q0 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.2, 0.2, 0.1], [1.2, 0.2, 0.1], [0.2, 1.2, 0.1]], float)
+    q1 = q0.copy()
+    q1[3:, 2] = -0.1
+    mi = np.ones(18)
+    mi[:9] = 0
+    scenes["triangles"] = (q0, q1, np.array([[0, 1, 2], [3, 4, 5]], np.int32), mi, 0.01, 0.005)
+    # a 6x6 sheet falling onto a fixed one
+    v, f = W.grid_sheet(6, 6)
+    v = np.asarray(v).reshape(-1, 3)
+    n = v.shape[0]
+    upper = v.copy()
+    upper[:, 2] += 0.05
+    q0 = np.concatenate([v, upper])
+    q1 = q0.copy()
+    q1[n:, 2] -= 0.1
+    mi = np.ones(q0.size)
+    mi[: 3 * n] = 0
+    scenes["sheets"] = (q0, q1, np.concatenate([f, f + n]).astype(np.int32), mi, 0.01, 0.005)
+    # two small spheres thrown into each other, all masses finite
+    qs, qe, f = W.two_spheres(seed=3, level=1, radius=0.5, gap=1.2, approach=0.25)
+    scenes["spheres"] = (qs.reshape(-1, 3), qe.reshape(-1, 3), f, np.ones(qs.size), 0.02, 0.01)
+    # the start already closer than inner_eta, and a vertex in no face
+    q0 = scenes["triangles"][0].copy()
+    q0[3:, 2] = 0.001
+    scenes["intersecting_start"] = (q0, q0, scenes["triangles"][2], scenes["triangles"][3], 0.01, 0.005)
+    q0 = np.concatenate([scenes["triangles"][0], [[5.0, 5.0, 5.0]]])
+    scenes["dangling"] = (q0, q0, scenes["triangles"][2], np.ones(q0.size), 0.01, 0.005)
+    return scenes
+
+
+def velocity_filter_fixtures(ref) -> None:
+    arrays, meta = {}, {}
+    for name, (q0, q1, f, mi, oe, ie) in velocity_filter_scenes().items():
+        ret, qe = ref.velocity_filter(q0, q1, f, mi, oe, ie)
+        for key, val in (("qstart", q0), ("qend", q1), ("faces", f), ("invmasses", mi), ("result", qe)):
+            arrays[f"{name}_{key}"] = np.ascontiguousarray(val)
+        meta[name] = {"outer_eta": oe, "inner_eta": ie, "return": int(ret)}
+    np.savez_compressed(os.path.join(HERE, "velocity_filter.npz"), **arrays)
+    with open(os.path.join(HERE, "velocity_filter.json"), "w") as fh:
+        json.dump(meta, fh, indent=1, sort_keys=True)
+
+
 def main() -> None:
     if not os.path.isdir(REF_TREE):
         sys.exit(f"reference tree not found at {REF_TREE}")
@@ -409,6 +460,9 @@ def main() -> None:
         return
     if only == "history":
         history_fixtures(ref)
+        return
+    if only == "velocity_filter":
+        velocity_filter_fixtures(ref)
         return
 
     kat = []
@@ -471,6 +525,7 @@ def main() -> None:
     trivial_fixtures(ref)
     penalty_fixtures(ref)
     history_fixtures(ref)
+    velocity_filter_fixtures(ref)
     print("wrote", sorted(os.listdir(HERE)))
 
 

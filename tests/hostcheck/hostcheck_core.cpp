@@ -35,3 +35,44 @@ extern "C" void hc_cull(int kind, int64_t n, const double *x, const double *eta,
     rej[i] = kind == 0 ? ccd::vf_rejects(xi, e) : (kind == 1 ? ccd::ee_rejects(xi, e) : ccd::ve_rejects(xi, e));
   }
 }
+
+#include <queue>
+#include <vector>
+
+#include "../../collisiondetection_gb300/csrc/ccd_heap.h"
+
+// The device event queue's heap (csrc/ccd_heap.h) against std::priority_queue
+// with the active layers' comparator on the same operations: op[i] >= 0
+// pushes element op[i] (its key key[op[i]], which may change between
+// operations as the firing times do: newkey[i] replaces key[op_key[i]] first
+// when op_key[i] >= 0), op[i] < 0 pops.  The top seen before every pop is
+// written to ours[] / theirs[] (-1 when empty).
+extern "C" void hc_heap_replay(int n, const int *op, const int *op_key, const double *newkey, double *key,
+                               int nkeys, int *ours, int *theirs) {
+  std::vector<double> k1(key, key + nkeys), k2(key, key + nkeys);
+  struct Cmp {
+    const std::vector<double> *k;
+    bool operator()(int a, int b) const { return (*k)[b] < (*k)[a]; }
+  };
+  std::priority_queue<int, std::vector<int>, Cmp> pq(Cmp{&k2});
+  std::vector<int> heap(n + 1);
+  int size = 0;
+  auto lower = [&](int a, int b) { return k1[b] < k1[a]; };
+  int npop = 0;
+  for (int i = 0; i < n; i++) {
+    if (op_key[i] >= 0) {
+      k1[op_key[i]] = newkey[i];
+      k2[op_key[i]] = newkey[i];
+    }
+    if (op[i] >= 0) {
+      ccd::heap_push(heap.data(), &size, op[i], lower);
+      pq.push(op[i]);
+    } else {
+      ours[npop] = size ? heap[0] : -1;
+      theirs[npop] = pq.empty() ? -1 : pq.top();
+      npop++;
+      if (size) ccd::heap_pop(heap.data(), &size, lower);
+      if (!pq.empty()) pq.pop();
+    }
+  }
+}

@@ -156,3 +156,26 @@ def test_fast_exp_log_equal_slow_exact_paths():
     xe = np.concatenate([rng.uniform(-745, 709.7, 200000), rng.normal(0, 1e-8, 20000),
                          [0.0, -0.0, 699.99, -699.99, 700.1, -700.1, 709.78, -745.1]])
     np.testing.assert_array_equal(_run(lib, "hc_exp", xe).view(np.uint64), _run(lib, "hc_exp_slow", xe).view(np.uint64))
+
+
+def test_event_heap_matches_priority_queue():
+    """The event queue's heap (csrc/ccd_heap.h) pops in std::priority_queue's
+    order on the same operations, ties and keys changed under a built heap
+    included (the active layers' rollback re-queues groups whose firing times
+    were reset)."""
+    lib = core_lib()
+    rng = np.random.default_rng(12)
+    for trial in range(40):
+        nkeys = int(rng.integers(1, 60))
+        key = rng.integers(0, 6, nkeys).astype(np.float64) * 0.25  # many ties
+        n = int(rng.integers(1, 400))
+        op = np.where(rng.random(n) < 0.55, rng.integers(0, nkeys, n), -1).astype(np.int32)
+        op_key = np.where(rng.random(n) < 0.2, rng.integers(0, nkeys, n), -1).astype(np.int32)
+        newkey = rng.integers(0, 6, n).astype(np.float64) * 0.25
+        ours = np.full(n, -2, np.int32)
+        theirs = np.full(n, -3, np.int32)
+        lib.hc_heap_replay(ctypes.c_int(n), op.ctypes.data_as(P), op_key.ctypes.data_as(P), newkey.ctypes.data_as(P),
+                           key.ctypes.data_as(P), ctypes.c_int(nkeys), ours.ctypes.data_as(P),
+                           theirs.ctypes.data_as(P))
+        npop = int((op < 0).sum())
+        np.testing.assert_array_equal(ours[:npop], theirs[:npop])
