@@ -48,6 +48,8 @@ def parse():
                     help="instances of the uneven-batch sample (0: skip; the configuration has 512)")
     ap.add_argument("--distance", type=int, default=1,
                     help="also time meshSelfDistance, the closest-point batches and the penalty forces (1) or not (0)")
+    ap.add_argument("--velocity", type=int, default=1, help="also time the velocity filter (1) or not (0)")
+    ap.add_argument("--vf-grid", type=int, default=16, help="sheet resolution of the velocity-filter scene")
     ap.add_argument("--serve", type=int, default=1, help="also run the serving loop (1) or not (0)")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0])
@@ -450,6 +452,61 @@ def penalty_section(ctx, rank, args):
     return out
 
 
+def velocity_filter_section(ctx, rank, args):
+    """VelocityFilter::velocityFilter (src/VelocityFilter.cpp:15-87) through
+    ccd_velocity_filter, wall time of the whole call (host memory in and out),
+    with the oracle's sequential restatement timed beside it on one core:
+      sheets: a 16x16 sheet (512 vertices with the fixed lower one) dropped
+        onto a fixed sheet, layers of 0.2 / 0.1 of the sheet spacing; one
+        rollback iteration, 282,050 group firings over groups spanning the
+        contact (thousands of stencils each);
+      triangles: a triangle falling through a fixed one (2 stencils per
+        group, 1.7 M firings): the latency-bound extreme."""
+    import collisiondetection_gb300 as C
+    from collisiondetection_gb300 import workloads as W
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    orc = O.Oracle()
+    scenes = {}
+    g = args.vf_grid
+    v, f = W.grid_sheet(g, g)
+    v = np.asarray(v).reshape(-1, 3)
+    n = v.shape[0]
+    upper = v.copy()
+    upper[:, 2] += 0.02
+    q0 = np.concatenate([v, upper])
+    q1 = q0.copy()
+    q1[n:, 2] -= 0.04
+    mi = np.ones(q0.size)
+    mi[: 3 * n] = 0
+    sp = 1.0 / (g - 1)
+    scenes["sheets"] = (q0, q1, np.concatenate([f, f + n]).astype(np.int32), mi, 0.2 * sp, 0.1 * sp)
+    t0 = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0.2, 0.2, 0.1], [1.2, 0.2, 0.1], [0.2, 1.2, 0.1]], float)
+    t1 = t0.copy()
+    t1[3:, 2] = -0.1
+    tm = np.ones(18)
+    tm[:9] = 0
+    scenes["triangles"] = (t0, t1, np.array([[0, 1, 2], [3, 4, 5]], np.int32), tm, 0.01, 0.005)
+    out = {}
+    for name, (a, b, ff, m, oe, ie) in scenes.items():
+        t = time.perf_counter()
+        res, qe, st = ctx.velocity_filter(a, b, ff, m, oe, ie)
+        gpu_s = time.perf_counter() - t
+        entry = {"vertices": int(a.size // 3), "faces": int(ff.shape[0]), "result": res,
+                 "iterations": st["iterations"], "layers": st["layers"], "firings": st["events"],
+                 "gpu_s": gpu_s, "firings_per_s": st["events"] / gpu_s if gpu_s > 0 else None}
+        if rank == 0:
+            t = time.perf_counter()
+            r2, q2, ev = orc.velocity_filter(a, b, ff, m, oe, ie)
+            entry["cpu_oracle"] = {"s": time.perf_counter() - t, "cores": 1, "sample": "whole call",
+                                   "same_result": bool(r2 == res and np.array_equal(q2.view(np.uint64),
+                                                                                    qe.view(np.uint64)))}
+        out[name] = entry
+    return out
+
+
 def serving_section(args):
     """Serving loop: Poisson arrivals of collision queries (mesh + 10 steps of
     seeded rigid + jitter motion, triangle counts log-uniform in [1e3, 5e5])
@@ -725,6 +782,7 @@ def run_ours(args, rank, world, local, pg):
     mesh = mesh_section(ctx, stream, rank, args) if args.mesh and full else None
     distance = distance_section(ctx, stream, rank, args) if args.distance and full else None
     penalty = penalty_section(ctx, rank, args) if args.distance and full else None
+    velocity = velocity_filter_section(ctx, rank, args) if args.velocity and full and world == 1 else None
     serving = serving_section(args) if args.serve and full and world == 1 else None
     uneven = uneven_section(args) if args.uneven_instances and full and world == 1 else None
 
@@ -749,6 +807,7 @@ def run_ours(args, rank, world, local, pg):
             "mesh": mesh,
             "distance": distance,
             "penalty": penalty,
+            "velocity_filter": velocity,
             "serving": serving,
             "uneven_batch": uneven,
         }

@@ -300,6 +300,9 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
   } else if (key == "wave_min_rows") {
     if (value < 0) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "wave_min_rows must be >= 0");
     ctx->opt_wave_min_rows = value;
+  } else if (key == "layer_grid_min") {
+    if (value < 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "layer_grid_min must be >= 1");
+    ctx->opt_layer_grid_min = value;
   } else {
     return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown option " + key);
   }

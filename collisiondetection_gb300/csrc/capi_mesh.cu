@@ -1046,11 +1046,13 @@ extern "C" int ccd_velocity_filter(ccd_context *ctx, int32_t nverts, const doubl
   if (!rc) rc = fb.alloc(ctx, &d_newv, n3);
   if (!rc) rc = fb.alloc(ctx, &d_qend, n3);
   int64_t *d_counts = nullptr;  // [0] log_n, [1] events
+  ccd::GridStep *d_step = nullptr;
   int *d_status = nullptr;
   unsigned long long *d_gap = nullptr;
   uint32_t *d_count = nullptr, *d_scan = nullptr;
   int32_t *d_off = nullptr;
   if (!rc) rc = fb.alloc(ctx, &d_counts, 2);
+  if (!rc) rc = fb.alloc(ctx, &d_step, 1);
   if (!rc) rc = fb.alloc(ctx, &d_status, 1);
   if (!rc) rc = fb.alloc(ctx, &d_gap, 1);
   if (!rc) rc = fb.alloc(ctx, &d_count, (size_t)nverts + 1);
@@ -1092,8 +1094,9 @@ extern "C" int ccd_velocity_filter(ccd_context *ctx, int32_t nverts, const doubl
     std::vector<int> g_next;
     std::vector<int64_t> st_off(1, 0), gv_off(1, 0), co_off(1, 0);
     std::vector<int32_t> n_vf, stv, gvv, cov;
-    int64_t max_st = 1;
+    int64_t max_st = 1, max_gv = 1;
     for (const HostGroup &g : al.groups) {
+      max_gv = std::max<int64_t>(max_gv, (int64_t)g.verts.size());
       g_dt.push_back(g.dt), g_eta.push_back(g.eta), g_inner.push_back(g.inner), g_k.push_back(g.k);
       g_cor.push_back(g.cor), g_next.push_back(g.nextstep);
       n_vf.push_back((int32_t)g.vf.size());
@@ -1177,8 +1180,9 @@ extern "C" int ccd_velocity_filter(ccd_context *ctx, int32_t nverts, const doubl
                         d_gv_off, d_gv, d_co_off, d_co, d_heap, d_heap_size};
     for (;;) {
       ccd::LayerState ls{nverts, d_q, d_v, d_lu, d_minv, d_newq, d_newv, d_contrib, d_fired,
-                         log_v, log_t, log_p, log_cap, d_counts, 1.0, d_status, d_counts + 1};
-      CCD_CUDA(ccd::launch_layer_events(lg, ls, (int64_t)1 << 20, s));
+                         log_v, log_t, log_p, log_cap, d_counts, 1.0, d_status, d_counts + 1, d_step};
+      CCD_CUDA(ccd::launch_layer_events(lg, ls, (int64_t)1 << 20, std::max<int64_t>(max_st, max_gv),
+                                        ctx->opt_layer_grid_min, s));
       int status = 0;
       int64_t counts[2] = {0, 0};
       CCD_CUDA(cudaMemcpyAsync(&status, d_status, 4, cudaMemcpyDeviceToHost, s));
@@ -1204,7 +1208,7 @@ extern "C" int ccd_velocity_filter(ccd_context *ctx, int32_t nverts, const doubl
       }
     }
     ccd::LayerState ls{nverts, d_q, d_v, d_lu, d_minv, d_newq, d_newv, d_contrib, d_fired,
-                       log_v, log_t, log_p, log_cap, d_counts, 1.0, d_status, d_counts + 1};
+                       log_v, log_t, log_p, log_cap, d_counts, 1.0, d_status, d_counts + 1, d_step};
     CCD_CUDA(ccd::launch_layer_finish(ls, s));
     int64_t nlog = 0;
     CCD_CUDA(cudaMemcpyAsync(&nlog, d_counts, 8, cudaMemcpyDeviceToHost, s));

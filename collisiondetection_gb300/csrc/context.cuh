@@ -84,6 +84,7 @@ struct ccd_context {
   int64_t opt_wave_min_rows = ccd::kWaveMinRows;
   int opt_pool_budget = ccd::kPoolBudget;
   int opt_count_tests = 0;
+  int64_t opt_layer_grid_min = 1024;  // velocity filter: groups this large fire over the whole GPU
   std::string err;
 };
 

@@ -40,9 +40,21 @@ struct PenaltyParams {
 // vector the reference adds to (slot with sign +) or subtracts from (sign -)
 // the group force of vertex v[slot]: vertex-face p -, q0 q1 q2 +; edge-edge
 // p0 p1 -, q0 q1 +.
-template <int KIND>
+// Position / velocity loads: plain, or through L2 only (data that other SMs
+// rewrite between a kernel's grid-wide barriers).
+struct PlainLoad {
+  __device__ v3d operator()(const double *x, int v) const { return ldv(x, v); }
+};
+struct L2Load {
+  __device__ v3d operator()(const double *x, int v) const {
+    const double *p = x + 3 * (int64_t)v;
+    return v3d{__ldcg(p), __ldcg(p + 1), __ldcg(p + 2)};
+  }
+};
+
+template <int KIND, class Load = PlainLoad>
 __device__ __forceinline__ bool stencil_force(const double *q, const double *vel, const int *v, PenaltyParams pp,
-                                              v3d (&c)[4]) {
+                                              v3d (&c)[4], Load ldv = Load()) {
   const v3d x0 = ldv(q, v[0]), x1 = ldv(q, v[1]), x2 = ldv(q, v[2]), x3 = ldv(q, v[3]);
   double stiffness = pp.stiffness;
   if constexpr (KIND == 0) {

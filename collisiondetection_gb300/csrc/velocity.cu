@@ -15,6 +15,8 @@
 
 #include <algorithm>
 
+#include <cooperative_groups.h>
+
 #include "ccd_heap.h"
 #include "penalty.cuh"
 #include "radix_sort.cuh"
@@ -24,7 +26,10 @@ namespace ccd {
 
 namespace {
 
-constexpr int kLoopThreads = 512;
+// Groups whose queue state (heap, firing steps, time steps) fits in shared
+// memory keep it there: every firing reads it several times on the loop's
+// critical path.
+constexpr int kSharedGroups = 4096;
 
 struct FireLater {
   const int *nextstep;
@@ -36,35 +41,56 @@ struct FireLater {
   }
 };
 
-__global__ void __launch_bounds__(kLoopThreads) layer_events(LayerGroups g, LayerState s, int64_t max_events) {
-  __shared__ int sh_group, sh_action;
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) layer_events(LayerGroups g, LayerState s, int64_t max_events) {
+  constexpr int kWarps = THREADS / 32;
+  extern __shared__ double smem[];
+  __shared__ int sh_group, sh_action, sh_heap_size;
   __shared__ double sh_time;
   __shared__ int64_t sh_base;
-  __shared__ int sh_scan[kLoopThreads];
-  const int tid = threadIdx.x;
-  const FireLater later{g.nextstep, g.dt};
+  __shared__ int sh_warp[kWarps + 1];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool in_shared = g.ngroups <= kSharedGroups;
+  double *dt_q = in_shared ? smem : nullptr;
+  int *next_q = in_shared ? reinterpret_cast<int *>(smem + g.ngroups) : g.nextstep;
+  int *heap = in_shared ? next_q + g.ngroups : g.heap;
+  if (in_shared) {
+    for (int i = tid; i < g.ngroups; i += THREADS) {
+      dt_q[i] = g.dt[i];
+      next_q[i] = g.nextstep[i];
+    }
+    for (int i = tid; i < *g.heap_size; i += THREADS) heap[i] = g.heap[i];
+  } else {
+    dt_q = const_cast<double *>(g.dt);
+  }
+  if (tid == 0) {
+    sh_heap_size = *g.heap_size;
+    sh_base = *s.log_n;
+  }
+  __syncthreads();
+  const FireLater later{next_q, dt_q};
   int action = 0;
+  int64_t done = 0;
   for (int64_t ev = 0;; ev++) {
     if (tid == 0) {
       int a = 0, grp = -1;
       double t = 0.0;
-      if (*g.heap_size == 0) {
+      if (sh_heap_size == 0) {
         a = 1;
       } else {
-        grp = g.heap[0];
-        t = (double)g.nextstep[grp] * g.dt[grp];
+        grp = heap[0];
+        t = (double)next_q[grp] * dt_q[grp];
         if (!(t < s.term)) {
           a = 1;
-        } else if (ev >= max_events || *s.log_n + (g.gv_off[grp + 1] - g.gv_off[grp]) > s.log_cap) {
+        } else if (ev >= max_events || sh_base + (g.gv_off[grp + 1] - g.gv_off[grp]) > s.log_cap) {
           a = 2;
         } else {
-          heap_pop(g.heap, g.heap_size, later);
+          heap_pop(heap, &sh_heap_size, later);
         }
       }
       sh_action = a;
       sh_group = grp;
       sh_time = t;
-      sh_base = *s.log_n;
     }
     __syncthreads();
     action = sh_action;
@@ -75,7 +101,7 @@ __global__ void __launch_bounds__(kLoopThreads) layer_events(LayerGroups g, Laye
     const int64_t s0 = g.st_off[grp], s1 = g.st_off[grp + 1];
     const int nvf = g.n_vf[grp];
     // (1) the group's vertices at the firing time (src/ActiveLayers.cpp:105-114)
-    for (int64_t j = v0 + tid; j < v1; j += blockDim.x) {
+    for (int64_t j = v0 + tid; j < v1; j += THREADS) {
       const int vert = g.gv[j];
       for (int c = 0; c < 3; c++) {
         const int64_t i = 3 * (int64_t)vert + c;
@@ -88,7 +114,7 @@ __global__ void __launch_bounds__(kLoopThreads) layer_events(LayerGroups g, Laye
     __syncthreads();
     // (2) each stencil's potential (PenaltyGroup::addForce, src/PenaltyGroup.cpp:34-52)
     const PenaltyParams pp{g.eta[grp], g.inner[grp], g.stiffness[grp], g.cor[grp]};
-    for (int64_t k = s0 + tid; k < s1; k += blockDim.x) {
+    for (int64_t k = s0 + tid; k < s1; k += THREADS) {
       const int64_t local = k - s0;
       const int v4[4] = {g.st[4 * k], g.st[4 * k + 1], g.st[4 * k + 2], g.st[4 * k + 3]};
       v3d c[4];
@@ -108,10 +134,11 @@ __global__ void __launch_bounds__(kLoopThreads) layer_events(LayerGroups g, Laye
     // (3) per vertex: the group force summed in the reference's order, F =
     // 0 + group * dt, the impulse on touched vertices, and their history
     // entries in ascending vertex order (src/ActiveLayers.cpp:116-139)
-    const double gdt = g.dt[grp];
-    for (int64_t tile = v0; tile < v1; tile += blockDim.x) {
+    const double gdt = dt_q[grp];
+    for (int64_t tile = v0; tile < v1; tile += THREADS) {
       const int64_t j = tile + tid;
-      int touched = 0, vert = 0;
+      bool touched = false;
+      int vert = 0;
       if (j < v1) {
         vert = g.gv[j];
         double acc[3] = {0.0, 0.0, 0.0};
@@ -125,7 +152,7 @@ __global__ void __launch_bounds__(kLoopThreads) layer_events(LayerGroups g, Laye
         }
         double F[3];
         for (int c = 0; c < 3; c++) F[c] = 0.0 + acc[c] * gdt;
-        touched = (F[0] != 0.0 || F[1] != 0.0 || F[2] != 0.0) ? 1 : 0;
+        touched = F[0] != 0.0 || F[1] != 0.0 || F[2] != 0.0;
         if (touched) {
           for (int c = 0; c < 3; c++) {
             const int64_t i = 3 * (int64_t)vert + c;
@@ -135,36 +162,243 @@ __global__ void __launch_bounds__(kLoopThreads) layer_events(LayerGroups g, Laye
           }
         }
       }
-      // exclusive block scan of the touched flags (Hillis-Steele)
-      sh_scan[tid] = touched;
+      // exclusive block scan of the touched flags: ballots within warps,
+      // then the warps' counts
+      const unsigned ballot = __ballot_sync(0xffffffffu, touched);
+      if (lane == 0) sh_warp[warp] = __popc(ballot);
       __syncthreads();
-      for (int o = 1; o < (int)blockDim.x; o <<= 1) {
-        const int add = tid >= o ? sh_scan[tid - o] : 0;
-        __syncthreads();
-        sh_scan[tid] += add;
-        __syncthreads();
+      if (tid == 0) {
+        int acc = 0;
+        for (int w = 0; w < kWarps; w++) {
+          const int c = sh_warp[w];
+          sh_warp[w] = acc;
+          acc += c;
+        }
+        sh_warp[kWarps] = acc;
       }
-      const int incl = sh_scan[tid];
-      const int total = sh_scan[blockDim.x - 1];
+      __syncthreads();
       if (touched) {
-        const int64_t at = sh_base + incl - 1;
+        const int64_t at = sh_base + sh_warp[warp] + __popc(ballot & ((1u << lane) - 1));
         s.log_v[at] = vert;
         s.log_t[at] = t;
         for (int c = 0; c < 3; c++) s.log_p[3 * at + c] = s.q[3 * (int64_t)vert + c];
       }
       __syncthreads();
-      if (tid == 0) sh_base += total;
-      __syncthreads();
+      if (tid == 0) sh_base += sh_warp[kWarps];
     }
     if (tid == 0) {
-      *s.log_n = sh_base;
-      *s.events += 1;
-      g.nextstep[grp] += 1;  // PenaltyGroup::incrementTimeStep
-      heap_push(g.heap, g.heap_size, grp, later);
+      next_q[grp] += 1;  // PenaltyGroup::incrementTimeStep
+      heap_push(heap, &sh_heap_size, grp, later);
     }
+    done++;
     __syncthreads();
   }
-  if (tid == 0) *s.status = action;
+  // the queue's state back to global memory for the next launch and the host
+  if (in_shared) {
+    for (int i = tid; i < g.ngroups; i += THREADS) g.nextstep[i] = next_q[i];
+    for (int i = tid; i < sh_heap_size; i += THREADS) g.heap[i] = heap[i];
+  }
+  if (tid == 0) {
+    *g.heap_size = sh_heap_size;
+    *s.log_n = sh_base;
+    *s.events += done;
+    *s.status = action;
+  }
+}
+
+// Large groups: one firing spread over the whole GPU.  The block version
+// above is bound by a single SM's FP64 rate (1/64 of its FP32 rate on this
+// part) once a group holds thousands of stencils; here every SM takes a share
+// of each phase, with a grid-wide barrier between phases (a cooperative
+// launch, every block resident).  Block 0 keeps the queue.  Data that other
+// SMs rewrite between barriers is read through L2 (__ldcg).  History entries
+// are appended through an atomic counter: within one firing a vertex appears
+// at most once, so each vertex's entries stay in firing order, which is all
+// the history needs.
+constexpr int kGridThreads = 256;
+
+__device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
+
+// The group force of one vertex slot j, its contributions accumulated in
+// order; the loads of eight contributions are issued before their additions.
+__device__ __forceinline__ void ordered_sum(const LayerGroups &g, const LayerState &s, int64_t j, int nvf,
+                                            double (&acc)[3]) {
+  const int64_t e0 = g.co_off[j], e1 = g.co_off[j + 1];
+  for (int64_t e = e0; e < e1; e += 8) {
+    int code[8];
+    uint8_t fired[8];
+    double cv[8][3];
+#pragma unroll
+    for (int u = 0; u < 8; u++) code[u] = e + u < e1 ? g.co[e + u] : 0;
+#pragma unroll
+    for (int u = 0; u < 8; u++) fired[u] = e + u < e1 ? __ldcg(s.fired + (code[u] >> 2)) : 0;
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const double *p = s.contrib + 12 * (int64_t)(code[u] >> 2) + 3 * (code[u] & 3);
+      for (int c = 0; c < 3; c++) cv[u][c] = fired[u] ? __ldcg(p + c) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      if (!fired[u]) continue;
+      const int local = code[u] >> 2, slot = code[u] & 3;
+      const bool minus = local < nvf ? slot == 0 : slot <= 1;
+      for (int c = 0; c < 3; c++) acc[c] = minus ? acc[c] - cv[u][c] : acc[c] + cv[u][c];
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kGridThreads) layer_events_grid(LayerGroups g, LayerState s, int64_t max_events,
+                                                                 GridStep *step) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  extern __shared__ double smem[];
+  __shared__ int sh_heap_size;
+  const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  const int64_t gtid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t gsize = (int64_t)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const bool in_shared = g.ngroups <= kSharedGroups;
+  double *dt_q = in_shared ? smem : const_cast<double *>(g.dt);
+  int *next_q = in_shared ? reinterpret_cast<int *>(smem + g.ngroups) : g.nextstep;
+  int *heap = in_shared ? next_q + g.ngroups : g.heap;
+  if (blockIdx.x == 0) {
+    if (in_shared) {
+      for (int i = threadIdx.x; i < g.ngroups; i += blockDim.x) {
+        dt_q[i] = g.dt[i];
+        next_q[i] = g.nextstep[i];
+      }
+      for (int i = threadIdx.x; i < *g.heap_size; i += blockDim.x) heap[i] = g.heap[i];
+    }
+    if (threadIdx.x == 0) sh_heap_size = *g.heap_size;
+    __syncthreads();
+  }
+  const FireLater later{next_q, dt_q};
+  // The leader decides the next firing: pops it from the queue, or stops
+  // (1: the next firing time reaches the end; 2: the event budget or the
+  // log's room, counting `pending` entries not yet appended, is used up).
+  auto decide = [&](int64_t ev, int64_t pending) {
+    int a = 0, grp = -1;
+    double t = 0.0;
+    if (sh_heap_size == 0) {
+      a = 1;
+    } else {
+      grp = heap[0];
+      t = (double)next_q[grp] * dt_q[grp];
+      if (!(t < s.term)) {
+        a = 1;
+      } else if (ev >= max_events || (int64_t)__ldcg((const long long *)s.log_n) + pending +
+                                             (g.gv_off[grp + 1] - g.gv_off[grp]) > s.log_cap) {
+        a = 2;
+      } else {
+        heap_pop(heap, &sh_heap_size, later);
+      }
+    }
+    step->action = a;
+    step->group = grp;
+    step->time = t;
+  };
+  if (leader) decide(0, 0);
+  grid.sync();
+  int64_t done = 0;
+  int action = 0;
+  for (int64_t ev = 0;; ev++) {
+    action = __ldcg(&step->action);
+    if (action) break;
+    const int grp = __ldcg(&step->group);
+    const double t = __ldcg(&step->time);
+    const int64_t v0 = g.gv_off[grp], v1 = g.gv_off[grp + 1];
+    const int64_t s0 = g.st_off[grp], s1 = g.st_off[grp + 1];
+    const int nvf = g.n_vf[grp];
+    // (1) the group's vertices at the firing time
+    for (int64_t j = v0 + gtid; j < v1; j += gsize) {
+      const int vert = g.gv[j];
+      for (int c = 0; c < 3; c++) {
+        const int64_t i = 3 * (int64_t)vert + c;
+        const double q = ldcg(s.q + i), lu = ldcg(s.lu + i);
+        const double dt = t - lu;
+        const double nq = q + (t - lu) * ldcg(s.v + i);
+        s.newq[i] = nq;
+        s.newv[i] = (nq - q) / dt;
+      }
+    }
+    grid.sync();
+    // (2) each stencil's potential
+    const PenaltyParams pp{g.eta[grp], g.inner[grp], g.stiffness[grp], g.cor[grp]};
+    for (int64_t k = s0 + gtid; k < s1; k += gsize) {
+      const int64_t local = k - s0;
+      const int v4[4] = {g.st[4 * k], g.st[4 * k + 1], g.st[4 * k + 2], g.st[4 * k + 3]};
+      v3d c[4];
+      const bool f = local < nvf ? stencil_force<0>(s.newq, s.newv, v4, pp, c, L2Load())
+                                 : stencil_force<1>(s.newq, s.newv, v4, pp, c, L2Load());
+      s.fired[local] = f ? 1 : 0;
+      if (f) {
+        double *out = s.contrib + 12 * local;
+        for (int q = 0; q < 4; q++) {
+          out[3 * q] = c[q].x;
+          out[3 * q + 1] = c[q].y;
+          out[3 * q + 2] = c[q].z;
+        }
+      }
+    }
+    grid.sync();
+    // the queue moves on while the vertices are summed: this group's next
+    // firing goes back in, the next firing comes out (the queue holds only
+    // firing times, which phase (3) does not touch)
+    if (leader) {
+      next_q[grp] += 1;  // PenaltyGroup::incrementTimeStep
+      heap_push(heap, &sh_heap_size, grp, later);
+      decide(ev + 1, v1 - v0);
+    }
+    // (3) per vertex: the ordered group force, the impulse, the history entry
+    const double gdt = g.dt[grp];  // every block: only block 0's shared memory holds the queue's copy
+    for (int64_t base = v0; base < v1; base += gsize) {
+      const int64_t j = base + gtid;
+      bool touched = false;
+      int vert = 0;
+      if (j < v1) {
+        vert = g.gv[j];
+        double acc[3] = {0.0, 0.0, 0.0};
+        ordered_sum(g, s, j, nvf, acc);
+        double F[3];
+        for (int c = 0; c < 3; c++) F[c] = 0.0 + acc[c] * gdt;
+        touched = F[0] != 0.0 || F[1] != 0.0 || F[2] != 0.0;
+        if (touched) {
+          for (int c = 0; c < 3; c++) {
+            const int64_t i = 3 * (int64_t)vert + c;
+            s.v[i] = ldcg(s.v + i) + s.minv[i] * F[c];
+            s.q[i] = ldcg(s.newq + i);
+            s.lu[i] = t;
+          }
+        }
+      }
+      const unsigned ballot = __ballot_sync(0xffffffffu, touched);
+      unsigned long long first = 0;
+      if (ballot) {
+        const int lead = __ffs(ballot) - 1;
+        if (lane == lead) first = atomicAdd((unsigned long long *)s.log_n, (unsigned long long)__popc(ballot));
+        first = __shfl_sync(0xffffffffu, first, lead);
+      }
+      if (touched) {
+        const int64_t at = (int64_t)first + __popc(ballot & ((1u << lane) - 1));
+        s.log_v[at] = vert;
+        s.log_t[at] = t;
+        for (int c = 0; c < 3; c++) s.log_p[3 * at + c] = s.q[3 * (int64_t)vert + c];
+      }
+    }
+    done++;
+    grid.sync();
+  }
+  if (blockIdx.x == 0) {
+    if (in_shared) {
+      for (int i = threadIdx.x; i < g.ngroups; i += blockDim.x) g.nextstep[i] = next_q[i];
+      for (int i = threadIdx.x; i < sh_heap_size; i += blockDim.x) g.heap[i] = heap[i];
+    }
+    if (threadIdx.x == 0) {
+      *g.heap_size = sh_heap_size;
+      *s.events += done;
+      *s.status = action;
+    }
+  }
 }
 
 __global__ void __launch_bounds__(256) layer_finish(int64_t n3, double *q, const double *v, double *lu, double term) {
@@ -237,8 +471,37 @@ unsigned grid_of(int64_t n, int threads) { return (unsigned)std::max<int64_t>(1,
 
 }  // namespace
 
-cudaError_t launch_layer_events(const LayerGroups &g, const LayerState &s, int64_t max_events, cudaStream_t st) {
-  layer_events<<<1, kLoopThreads, 0, st>>>(g, s, max_events);
+cudaError_t launch_layer_events(const LayerGroups &g, const LayerState &s, int64_t max_events, int64_t max_group,
+                                int64_t grid_min, cudaStream_t st) {
+  const size_t shared = g.ngroups <= kSharedGroups ? (size_t)g.ngroups * (sizeof(double) + 2 * sizeof(int)) + 16 : 0;
+  if (max_group >= grid_min) {
+    // every block must be resident at once: size the grid by occupancy
+    if (shared > 48 * 1024)
+      cudaFuncSetAttribute(layer_events_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, layer_events_grid, kGridThreads,
+                                                                            shared);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int64_t want = (max_group + kGridThreads - 1) / kGridThreads;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * per_sm));
+    GridStep *step = s.grid_step;
+    LayerGroups gg = g;
+    LayerState ss = s;
+    void *args[] = {&gg, &ss, &max_events, &step};
+    return cudaLaunchCooperativeKernel((void *)layer_events_grid, blocks, kGridThreads, args, shared, st);
+  }
+  if (shared > 48 * 1024) {
+    cudaFuncSetAttribute(layer_events<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared);
+    cudaFuncSetAttribute(layer_events<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared);
+  }
+  // small groups: a small block, whose barriers are cheap
+  if (max_group <= 256)
+    layer_events<128><<<1, 128, shared, st>>>(g, s, max_events);
+  else
+    layer_events<512><<<1, 512, shared, st>>>(g, s, max_events);
   return cudaGetLastError();
 }
 

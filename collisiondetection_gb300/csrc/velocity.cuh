@@ -29,6 +29,12 @@ struct LayerGroups {
   int *heap_size;
 };
 
+// Where the grid-wide loop's leader publishes each firing (global memory).
+struct GridStep {
+  int action, group;
+  double time;
+};
+
 // The simulation state and the history log.  The loop appends one entry
 // (vertex, time, position) per touched vertex per event, in event order and
 // ascending vertex order within an event (ActiveLayers::step's
@@ -47,12 +53,18 @@ struct LayerState {
   double term;         // termination time (1.0)
   int *status;         // out: 1 finished, 2 paused (log full or event budget used)
   int64_t *events;     // events processed, accumulated
+  GridStep *grid_step; // scratch of the grid-wide loop
 };
 
 // Runs events until the queue's next firing time reaches the termination
 // time (status 1) or max_events events or the log's capacity stop it
-// (status 2; call again to continue).
-cudaError_t launch_layer_events(const LayerGroups &g, const LayerState &s, int64_t max_events, cudaStream_t st);
+// (status 2; call again to continue).  When the largest group holds
+// grid_min or more stencils or vertices, the firings run over the whole GPU
+// (a cooperative launch sized so that every block is resident); otherwise in
+// one block.
+// max_group: the largest group's stencil or vertex count.
+cudaError_t launch_layer_events(const LayerGroups &g, const LayerState &s, int64_t max_events, int64_t max_group,
+                                int64_t grid_min, cudaStream_t st);
 
 // The final step (src/ActiveLayers.cpp:145-152): every coordinate advances to
 // the termination time.

@@ -99,6 +99,9 @@ int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
  *   "pool_budget"    further steps the unfinished polynomials get, many per
  *                    warp, before the last ones are finished one per warp
  *                    (0: no limit); default 0
+ *   "layer_grid_min" ccd_velocity_filter: when a penalty group holds this
+ *                    many stencils or vertices, each firing runs over the
+ *                    whole GPU instead of one block; default 1024
  * Unknown names and out-of-range values return CCD_ERR_INVALID_ARGUMENT. */
 int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value);
 /* Library version as MAJOR*10000 + MINOR*100 + PATCH. */

@@ -181,6 +181,30 @@ inline double meshSelfDistance(const Eigen::VectorXd &verts, const Eigen::Matrix
   return d;
 }
 
+// ------------------------------------------------------------------ velocity filter
+// VelocityFilter::velocityFilter (include/VelocityFilter.h:45-46) with the
+// same signature and return values; qend is overwritten as the reference
+// does.  The active layers, broad phase and narrow phase run on the device.
+inline int velocityFilter(const Eigen::VectorXd &qstart, Eigen::VectorXd &qend, const Eigen::Matrix3Xi &faces,
+                          const Eigen::VectorXd &masses, double outerEta, double innerEta,
+                          double baseStiffness = .0001, double baseSubstepSize = 0.0001, double CoR = 0.1,
+                          int maxRollbacks = 1000) {
+  const int nv = (int)(qstart.size() / 3), nf = (int)faces.cols();
+  std::vector<double> qs(qstart.data(), qstart.data() + 3 * nv), qe(qend.data(), qend.data() + 3 * nv),
+      mi(masses.data(), masses.data() + 3 * nv);
+  std::vector<int32_t> f((size_t)3 * nf);
+  for (int c = 0; c < nf; c++)
+    for (int j = 0; j < 3; j++) f[(size_t)3 * c + j] = faces.coeff(j, c);
+  int32_t result = 0;
+  check(default_context(),
+        ccd_velocity_filter(default_context(), nv, qs.data(), qe.data(), nf, f.data(), mi.data(), outerEta, innerEta,
+                            baseStiffness, baseSubstepSize, CoR, maxRollbacks, &result, nullptr),
+        "ccd_velocity_filter");
+  if (result >= 0)
+    for (int i = 0; i < 3 * nv; i++) qend[i] = qe[(size_t)i];
+  return result;
+}
+
 // ------------------------------------------------------------------ penalty groups
 // PenaltyGroup (src/PenaltyGroup.h) with the same interface; addForce runs on
 // the device (ccd_penalty_group_force) with bit-identical forces.

@@ -1986,3 +1986,328 @@ int64_t oracle_separating_plane(int nverts, const int32_t *offsets, const double
   }
   return capped_total;
 }
+
+/* ------------------------------------------------------------ velocity filter
+ * VelocityFilter::velocityFilter (src/VelocityFilter.cpp:15-87) and the
+ * ActiveLayers it runs (src/ActiveLayers.cpp), on the restated pieces above. */
+typedef struct { int32_t v[4]; } vf_st4;
+
+static int st4_cmp(const vf_st4 *x, const vf_st4 *y) {
+  for (int i = 0; i < 4; i++) {
+    if (x->v[i] < y->v[i]) return -1;
+    if (x->v[i] > y->v[i]) return 1;
+  }
+  return 0;
+}
+
+/* std::map<Stencil, int> as a sorted array (insertions keep it sorted). */
+typedef struct { vf_st4 *key; int *val; int n, cap; } depth_map;
+
+static int *depth_ref(depth_map *m, vf_st4 k) { /* operator[]: inserts 0 when absent */
+  int lo = 0, hi = m->n;
+  while (lo < hi) {
+    int mid = (lo + hi) / 2;
+    if (st4_cmp(&m->key[mid], &k) < 0) lo = mid + 1; else hi = mid;
+  }
+  if (lo < m->n && st4_cmp(&m->key[lo], &k) == 0) return &m->val[lo];
+  if (m->n == m->cap) {
+    m->cap = m->cap ? 2 * m->cap : 64;
+    m->key = (vf_st4 *)realloc(m->key, (size_t)m->cap * sizeof(vf_st4));
+    m->val = (int *)realloc(m->val, (size_t)m->cap * sizeof(int));
+  }
+  memmove(m->key + lo + 1, m->key + lo, (size_t)(m->n - lo) * sizeof(vf_st4));
+  memmove(m->val + lo + 1, m->val + lo, (size_t)(m->n - lo) * sizeof(int));
+  m->key[lo] = k;
+  m->val[lo] = 0;
+  m->n++;
+  return &m->val[lo];
+}
+
+static const int *depth_find(const depth_map *m, vf_st4 k) {
+  int lo = 0, hi = m->n;
+  while (lo < hi) {
+    int mid = (lo + hi) / 2;
+    if (st4_cmp(&m->key[mid], &k) < 0) lo = mid + 1; else hi = mid;
+  }
+  return (lo < m->n && st4_cmp(&m->key[lo], &k) == 0) ? &m->val[lo] : NULL;
+}
+
+typedef struct {
+  double dt, eta, inner, k, cor;
+  int nextstep;
+  vf_st4 *st; /* vertex-face stencils first (nvf), then edge-edge (nee); kept apart until a firing */
+  int nvf, nee, cvf, cee;
+  vf_st4 *ee;
+  int *verts; /* ascending, unique */
+  int nverts, cverts;
+} pgroup;
+
+typedef struct {
+  double outer, inner, base_dt, base_k, term, cor;
+  int deepest;
+  pgroup *g;
+  int ng, cg;
+  int *heap;
+  int heap_size, heap_cap;
+  depth_map vfdepth, eedepth;
+} layers_t;
+
+static int fires_later(const layers_t *L, int a, int b) {
+  return (double)L->g[b].nextstep * L->g[b].dt < (double)L->g[a].nextstep * L->g[a].dt;
+}
+
+/* The standard library's binary heap (priority_queue over a vector). */
+static void lheap_up(const layers_t *L, int *h, int hole, int value) {
+  int parent = (hole - 1) / 2;
+  while (hole > 0 && fires_later(L, h[parent], value)) {
+    h[hole] = h[parent];
+    hole = parent;
+    parent = (hole - 1) / 2;
+  }
+  h[hole] = value;
+}
+static void lheap_push(layers_t *L, int **h, int *size, int *cap, int value) {
+  if (*size == *cap) {
+    *cap = *cap ? 2 * *cap : 16;
+    *h = (int *)realloc(*h, (size_t)*cap * sizeof(int));
+  }
+  lheap_up(L, *h, (*size)++, value);
+}
+static void lheap_pop(const layers_t *L, int *h, int *size) {
+  int len = *size - 1;
+  if (len > 0) {
+    int value = h[len], hole = 0, child = 0;
+    h[len] = h[0];
+    while (child < (len - 1) / 2) {
+      child = 2 * (child + 1);
+      if (fires_later(L, h[child], h[child - 1])) child--;
+      h[hole] = h[child];
+      hole = child;
+    }
+    if ((len & 1) == 0 && child == (len - 2) / 2) {
+      child = 2 * (child + 1);
+      h[hole] = h[child - 1];
+      hole = child - 1;
+    }
+    lheap_up(L, h, hole, value);
+  }
+  *size = len;
+}
+
+static double layer_depth(const layers_t *L, int layer) { return L->inner + (L->outer - L->inner) / (double)layer; }
+
+static void add_groups(layers_t *L, int maxdepth) {
+  while (L->deepest < maxdepth) {
+    int depth = L->deepest + 1;
+    double fudge = 1e-4;
+    double ki = L->base_k * depth * depth * depth;
+    double etai = layer_depth(L, depth);
+    double dti = L->base_dt / (double)depth / sqrt((double)depth + fudge);
+    if (L->ng == L->cg) {
+      L->cg = L->cg ? 2 * L->cg : 16;
+      L->g = (pgroup *)realloc(L->g, (size_t)L->cg * sizeof(pgroup));
+    }
+    pgroup z;
+    memset(&z, 0, sizeof z);
+    z.dt = dti; z.eta = etai; z.inner = L->inner; z.k = ki; z.cor = L->cor; z.nextstep = 1;
+    L->g[L->ng++] = z;
+    lheap_push(L, &L->heap, &L->heap_size, &L->heap_cap, L->ng - 1);
+    L->deepest++;
+  }
+}
+
+static void group_add(pgroup *g, int kind, vf_st4 s) {
+  if (kind == 0) {
+    if (g->nvf == g->cvf) { g->cvf = g->cvf ? 2 * g->cvf : 8; g->st = (vf_st4 *)realloc(g->st, (size_t)g->cvf * sizeof(vf_st4)); }
+    g->st[g->nvf++] = s;
+  } else {
+    if (g->nee == g->cee) { g->cee = g->cee ? 2 * g->cee : 8; g->ee = (vf_st4 *)realloc(g->ee, (size_t)g->cee * sizeof(vf_st4)); }
+    g->ee[g->nee++] = s;
+  }
+  for (int i = 0; i < 4; i++) { /* groupStencil_.insert */
+    int v = s.v[i], lo = 0, hi = g->nverts;
+    while (lo < hi) { int mid = (lo + hi) / 2; if (g->verts[mid] < v) lo = mid + 1; else hi = mid; }
+    if (lo < g->nverts && g->verts[lo] == v) continue;
+    if (g->nverts == g->cverts) { g->cverts = g->cverts ? 2 * g->cverts : 16; g->verts = (int *)realloc(g->verts, (size_t)g->cverts * sizeof(int)); }
+    memmove(g->verts + lo + 1, g->verts + lo, (size_t)(g->nverts - lo) * sizeof(int));
+    g->verts[lo] = v;
+    g->nverts++;
+  }
+}
+
+/* ActiveLayers::addVFStencil / addEEStencil (:43-67). */
+static void layers_add(layers_t *L, int kind, vf_st4 s) {
+  depth_map *dm = kind == 0 ? &L->vfdepth : &L->eedepth;
+  int olddepth = *depth_ref(dm, s);
+  for (int i = 0; i < 5; i++) {
+    add_groups(L, olddepth + i + 1);
+    group_add(&L->g[olddepth + i], kind, s);
+    (*depth_ref(dm, s))++;
+  }
+}
+
+/* ActiveLayers::rollback (:158-167). */
+static void layers_rollback(layers_t *L) {
+  for (int i = 0; i < L->ng; i++) L->g[i].nextstep = 1;
+  int *fresh = NULL, fs = 0, fc = 0;
+  while (L->heap_size > 0) {
+    lheap_push(L, &fresh, &fs, &fc, L->heap[0]);
+    lheap_pop(L, L->heap, &L->heap_size);
+  }
+  free(L->heap);
+  L->heap = fresh; L->heap_size = fs; L->heap_cap = fc;
+}
+
+typedef struct { int n, cap; double *t, *p; } vhist;
+static void vhist_add(vhist *h, double t, const double *p) {
+  if (h->n == h->cap) {
+    h->cap = h->cap ? 2 * h->cap : 4;
+    h->t = (double *)realloc(h->t, (size_t)h->cap * sizeof(double));
+    h->p = (double *)realloc(h->p, (size_t)h->cap * 3 * sizeof(double));
+  }
+  h->t[h->n] = t;
+  memcpy(h->p + 3 * (size_t)h->n, p, 3 * sizeof(double));
+  h->n++;
+}
+
+int oracle_velocity_filter(int nverts, const double *qstart, double *qend, int nfaces, const int32_t *faces,
+                           const double *invmasses, double outer_eta, double inner_eta, double base_stiffness,
+                           double base_substep, double cor, int max_rollbacks, int64_t *events_out) {
+  if (nverts < 0 || nfaces < 0) return -1;
+  if (nverts == 0) return 0; /* nothing to move; the first iteration finds nothing */
+  const int64_t n3 = 3 * (int64_t)nverts;
+  /* :22-39 dangling vertices */
+  uint8_t *used = (uint8_t *)calloc((size_t)nverts + 1, 1);
+  for (int64_t i = 0; i < 3 * (int64_t)nfaces; i++) used[faces[i]] = 1;
+  for (int v = 0; v < nverts; v++)
+    if (!used[v]) { free(used); return -1; }
+  free(used);
+  double maxmass = 0;
+  for (int64_t i = 0; i < n3; i++) maxmass = smax(maxmass, invmasses[i]);
+  double dt = base_substep;
+  double k = base_stiffness / dt * sqrt(maxmass);
+  layers_t L;
+  memset(&L, 0, sizeof L);
+  L.outer = outer_eta; L.inner = inner_eta; L.base_dt = dt; L.base_k = k; L.term = 1.0; L.cor = cor;
+  uint8_t *fixed = (uint8_t *)calloc((size_t)nverts, 1);
+  int any_fixed = 0;
+  for (int64_t i = 0; i < n3; i++)
+    if (invmasses[i] == 0.0) fixed[i / 3] = 1, any_fixed = 1;
+  double closest = oracle_mesh_self_distance(nverts, qstart, nfaces, faces, any_fixed ? fixed : NULL, NULL, NULL);
+  int result = -3;
+  int64_t events = 0;
+  double *q = (double *)malloc((size_t)n3 * 8), *v = (double *)malloc((size_t)n3 * 8), *lu = (double *)malloc((size_t)n3 * 8);
+  double *newq = (double *)malloc((size_t)n3 * 8), *newv = (double *)malloc((size_t)n3 * 8), *G = (double *)calloc((size_t)n3, 8);
+  vhist *hist = (vhist *)calloc((size_t)nverts, sizeof(vhist));
+  if (closest < inner_eta) { result = -2; goto done; }
+  for (int iter = 0; iter < max_rollbacks; iter++) {
+    memcpy(q, qstart, (size_t)n3 * 8);
+    for (int64_t i = 0; i < n3; i++) v[i] = qend[i] - qstart[i];
+    memset(lu, 0, (size_t)n3 * 8);
+    for (int vv = 0; vv < nverts; vv++) { hist[vv].n = 0; vhist_add(&hist[vv], 0.0, q + 3 * (size_t)vv); }
+    /* ActiveLayers::step (:91-156) until the end of the step */
+    for (;;) {
+      if (L.heap_size > 0) {
+        int gi = L.heap[0];
+        pgroup *g = &L.g[gi];
+        double newtime = (double)g->nextstep * g->dt;
+        if (newtime < L.term) {
+          lheap_pop(&L, L.heap, &L.heap_size);
+          for (int j = 0; j < g->nverts; j++) {
+            int vert = g->verts[j];
+            for (int c = 0; c < 3; c++) {
+              int64_t i = 3 * (int64_t)vert + c;
+              double dtt = newtime - lu[i];
+              newq[i] = q[i] + (newtime - lu[i]) * v[i];
+              newv[i] = (newq[i] - q[i]) / dtt;
+            }
+          }
+          /* PenaltyGroup::addForce into G (zero on the group's vertices) */
+          for (int j = 0; j < g->nverts; j++)
+            for (int c = 0; c < 3; c++) G[3 * (int64_t)g->verts[j] + c] = 0.0;
+          for (int s = 0; s < g->nvf; s++) vf_penalty(newq, newv, G, g->st[s].v, g->eta, g->inner, g->k, g->cor);
+          for (int s = 0; s < g->nee; s++) ee_penalty(newq, newv, G, g->ee[s].v, g->eta, g->inner, g->k, g->cor);
+          for (int j = 0; j < g->nverts; j++) {
+            int vert = g->verts[j];
+            double F[3];
+            int touched = 0;
+            for (int c = 0; c < 3; c++) {
+              F[c] = 0.0 + G[3 * (int64_t)vert + c] * g->dt;
+              if (F[c] != 0.0) touched = 1;
+            }
+            if (touched) {
+              for (int c = 0; c < 3; c++) {
+                int64_t i = 3 * (int64_t)vert + c;
+                v[i] += invmasses[i] * F[c];
+                q[i] = newq[i];
+                lu[i] = newtime;
+              }
+              vhist_add(&hist[vert], newtime, q + 3 * (size_t)vert);
+            }
+          }
+          g->nextstep++;
+          lheap_push(&L, &L.heap, &L.heap_size, &L.heap_cap, gi);
+          events++;
+          continue;
+        }
+      }
+      for (int64_t i = 0; i < n3; i++) {
+        q[i] += (L.term - lu[i]) * v[i];
+        lu[i] = L.term;
+      }
+      for (int vv = 0; vv < nverts; vv++) vhist_add(&hist[vv], 1.0, q + 3 * (size_t)vv);
+      break;
+    }
+    /* the history as arrays */
+    int32_t *off = (int32_t *)malloc(((size_t)nverts + 1) * sizeof(int32_t));
+    off[0] = 0;
+    for (int vv = 0; vv < nverts; vv++) off[vv + 1] = off[vv] + hist[vv].n;
+    double *ht = (double *)malloc((size_t)off[nverts] * 8), *hp = (double *)malloc((size_t)off[nverts] * 24);
+    for (int vv = 0; vv < nverts; vv++) {
+      memcpy(ht + off[vv], hist[vv].t, (size_t)hist[vv].n * 8);
+      memcpy(hp + 3 * (size_t)off[vv], hist[vv].p, (size_t)hist[vv].n * 24);
+    }
+    /* ActiveLayers::collisionDetection (:190-226) */
+    int64_t nvf = 0, nee = 0;
+    oracle_broadphase_history(0, nverts, off, hp, nfaces, faces, outer_eta, any_fixed ? fixed : NULL, &nvf, &nee);
+    int32_t *cvf = (int32_t *)malloc((size_t)(4 * nvf + 4) * sizeof(int32_t));
+    int32_t *cee = (int32_t *)malloc((size_t)(4 * nee + 4) * sizeof(int32_t));
+    oracle_broadphase_get(cvf, cee);
+    double *evf = (double *)malloc((size_t)(nvf + 1) * 8), *eee = (double *)malloc((size_t)(nee + 1) * 8);
+    for (int64_t i = 0; i < nvf; i++) {
+      vf_st4 s; memcpy(s.v, cvf + 4 * i, 16);
+      const int *d = depth_find(&L.vfdepth, s);
+      evf[i] = d ? layer_depth(&L, *d + 1) : layer_depth(&L, 1);
+    }
+    for (int64_t i = 0; i < nee; i++) {
+      vf_st4 s; memcpy(s.v, cee + 4 * i, 16);
+      const int *d = depth_find(&L.eedepth, s);
+      eee[i] = d ? layer_depth(&L, *d + 1) : layer_depth(&L, 1);
+    }
+    uint8_t *hvf = (uint8_t *)calloc((size_t)nvf + 1, 1), *hee = (uint8_t *)calloc((size_t)nee + 1, 1);
+    uint8_t *svf = (uint8_t *)calloc((size_t)nvf + 1, 1), *see = (uint8_t *)calloc((size_t)nee + 1, 1);
+    int64_t stalled = oracle_separating_plane(nverts, off, ht, hp, nvf, cvf, evf, nee, cee, eee, hvf, hee, svf, see);
+    /* ActiveLayers::runOneIteration (:244-255) */
+    layers_rollback(&L);
+    int64_t found = 0;
+    for (int64_t i = 0; i < nvf; i++)
+      if (hvf[i]) { vf_st4 s; memcpy(s.v, cvf + 4 * i, 16); layers_add(&L, 0, s); found++; }
+    for (int64_t i = 0; i < nee; i++)
+      if (hee[i]) { vf_st4 s; memcpy(s.v, cee + 4 * i, 16); layers_add(&L, 1, s); found++; }
+    free(off); free(ht); free(hp); free(cvf); free(cee); free(evf); free(eee); free(hvf); free(hee); free(svf); free(see);
+    if (stalled) { result = -4; break; } /* the reference overflows its stack here */
+    if (found == 0) {
+      memcpy(qend, q, (size_t)n3 * 8);
+      result = iter;
+      break;
+    }
+  }
+done:
+  for (int vv = 0; vv < nverts; vv++) { free(hist[vv].t); free(hist[vv].p); }
+  free(hist); free(q); free(v); free(lu); free(newq); free(newv); free(G); free(fixed);
+  for (int i = 0; i < L.ng; i++) { free(L.g[i].st); free(L.g[i].ee); free(L.g[i].verts); }
+  free(L.g); free(L.heap);
+  free(L.vfdepth.key); free(L.vfdepth.val); free(L.eedepth.key); free(L.eedepth.val);
+  if (events_out) *events_out = events;
+  return result;
+}

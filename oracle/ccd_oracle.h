@@ -106,6 +106,15 @@ int64_t oracle_separating_plane(int nverts, const int32_t *offsets, const double
                                 const int32_t *ee, const double *ee_eta, uint8_t *vf_hit, uint8_t *ee_hit,
                                 uint8_t *vf_status, uint8_t *ee_status);
 
+/* VelocityFilter::velocityFilter (src/VelocityFilter.cpp:15-87) with the
+ * ActiveLayers it runs (src/ActiveLayers.cpp): returns the reference's value
+ * (iterations >= 0, -1, -2, -3), or -4 when a separating-plane search stalls
+ * (the reference overflows its stack there); qend is overwritten on success.
+ * *events (may be NULL) receives the number of group firings. */
+int oracle_velocity_filter(int nverts, const double *qstart, double *qend, int nfaces, const int32_t *faces,
+                           const double *invmasses, double outer_eta, double inner_eta, double base_stiffness,
+                           double base_substep, double cor, int max_rollbacks, int64_t *events);
+
 /* Stencil canonical forms (src/Stencils.h): writes the canonical 4-tuple. */
 void oracle_vf_canon(int p, int q0, int q1, int q2, int32_t *out);
 void oracle_ee_canon(int p0, int p1, int q0, int q1, int32_t *out);

@@ -123,6 +123,9 @@ class Oracle(_Lib):
         L.oracle_narrowphase_history.restype = ctypes.c_int
         L.oracle_separating_plane.argtypes = [ctypes.c_int, _P, _P, _P, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P]
         L.oracle_separating_plane.restype = ctypes.c_int64
+        L.oracle_velocity_filter.argtypes = [ctypes.c_int, _P, _P, ctypes.c_int, _P, _P] + [ctypes.c_double] * 5 + \
+            [ctypes.c_int, _P]
+        L.oracle_velocity_filter.restype = ctypes.c_int
         self._distance_setup()
 
     def broadphase_history(self, kind: int, offsets, times, positions, faces, eta: float, fixed=None):
@@ -179,6 +182,19 @@ class Oracle(_Lib):
                                          _ptr(vfe), ee.shape[0], _ptr(ee), _ptr(eee), _ptr(vh), _ptr(eh), _ptr(vs),
                                          _ptr(es))
         return vh, eh, vs, es
+
+    def velocity_filter(self, qstart, qend, faces, invmasses, outer_eta, inner_eta, base_stiffness=1e-4,
+                        base_substep=1e-4, cor=0.1, max_rollbacks=1000):
+        """VelocityFilter::velocityFilter: (return value, filtered qend, events)."""
+        qs = np.ascontiguousarray(qstart, dtype=np.float64).ravel()
+        qe = np.ascontiguousarray(qend, dtype=np.float64).ravel().copy()
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        mi = np.ascontiguousarray(invmasses, dtype=np.float64).ravel()
+        ev = ctypes.c_int64(0)
+        r = self.lib.oracle_velocity_filter(qs.size // 3, _ptr(qs), _ptr(qe), faces.shape[0], _ptr(faces), _ptr(mi),
+                                            outer_eta, inner_eta, base_stiffness, base_substep, cor, max_rollbacks,
+                                            ctypes.byref(ev))
+        return int(r), qe, int(ev.value)
 
     def vertex_scan(self, verts, faces, i0: int, i1: int) -> float:
         """meshSelfDistance's O(V F) vertex scan over vertices [i0, i1)."""

@@ -16,6 +16,7 @@ CHECK = r'''
 #include "ccd_gb300_reference.hpp"
 #include "Distance.h"
 #include "PenaltyGroup.h"
+#include "VelocityFilter.h"
 #include <type_traits>
 static_assert(std::is_base_of<BroadPhase, ccd_gb300::GpuKDOPBroadPhase>::value, "k-DOP adapter");
 static_assert(std::is_base_of<BroadPhase, ccd_gb300::GpuAABBBroadPhase>::value, "AABB adapter");
@@ -34,6 +35,8 @@ static_assert(std::is_same<decltype(&Distance::vertexPlaneDistanceLessThan),
 static_assert(std::is_same<decltype(&Distance::lineLineDistanceLessThan),
                            decltype(&ccd_gb300::lineLineDistanceLessThan)>::value, "lll");
 static_assert(std::is_same<decltype(&Distance::meshSelfDistance), decltype(&ccd_gb300::meshSelfDistance)>::value, "msd");
+static_assert(std::is_same<decltype(&VelocityFilter::velocityFilter), decltype(&ccd_gb300::velocityFilter)>::value,
+              "velocity filter");
 // GpuPenaltyGroup keeps PenaltyGroup's interface (src/PenaltyGroup.h).
 static bool (ccd_gb300::GpuPenaltyGroup::*add_force)(const Eigen::VectorXd &, const Eigen::VectorXd &,
                                                        Eigen::VectorXd &) = &ccd_gb300::GpuPenaltyGroup::addForce;
