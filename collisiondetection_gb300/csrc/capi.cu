@@ -300,6 +300,10 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
   } else if (key == "wave_min_rows") {
     if (value < 0) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "wave_min_rows must be >= 0");
     ctx->opt_wave_min_rows = value;
+  } else if (key == "chunk_rows") {
+    if (value < 1024 || value > ((int64_t)1 << 26))
+      return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "chunk_rows must be in [1024, 2^26]");
+    ctx->opt_chunk_rows = value;
   } else if (key == "layer_grid_min") {
     if (value < 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "layer_grid_min must be >= 1");
     ctx->opt_layer_grid_min = value;
@@ -367,7 +371,8 @@ int ccd_prim_batch(ccd_context *ctx, int kind, int path, int64_t n, const double
   if (n == 0) return CCD_OK;
   CCD_CUDA(cudaSetDevice(ctx->device));
   const int W = ccd::row_width(kind);
-  const int64_t chunk = std::min<int64_t>(n, kChunkRows);
+  const int64_t pieces = (n + ctx->opt_chunk_rows - 1) / ctx->opt_chunk_rows;
+  const int64_t chunk = (n + pieces - 1) / pieces;  // equal chunks, none small
   for (auto &s : ctx->slot) {
     rc = ensure_slot(ctx, s, chunk);
     if (rc) return rc;

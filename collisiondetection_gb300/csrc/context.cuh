@@ -13,8 +13,14 @@
 
 namespace ccd_capi {
 
-// Rows per chunk of the host-memory batch pipeline (two chunks in flight).
-constexpr int64_t kChunkRows = 1 << 20;
+// Largest chunk of the host-memory batch pipeline (two chunks in flight); a
+// batch is cut into equal chunks no larger than this.  Large chunks keep the
+// refinement's survivors above the wavefront solver's threshold (smaller
+// ones fall back to the slower per-warp solver) and pay its latency-bound
+// tail once per chunk: on the 20M-row raw batch, 8M-row chunks run 1.54x
+// faster end to end than 1M-row ones.  ccd_context_set_option "chunk_rows"
+// changes it per context.
+constexpr int64_t kChunkRows = 1 << 23;
 // Survivor rows per tile of the staged refinement.  Each tile ends in a
 // latency-bound tail (the slowest root solves), so tiles are large: the
 // scratch is about 5 KB per survivor row (about 20 GB at this size; a batch
@@ -85,6 +91,7 @@ struct ccd_context {
   int opt_pool_budget = ccd::kPoolBudget;
   int opt_count_tests = 0;
   int64_t opt_layer_grid_min = 1024;  // velocity filter: groups this large fire over the whole GPU
+  int64_t opt_chunk_rows = ccd_capi::kChunkRows;  // host-memory batches: rows per chunk
   std::string err;
 };
 

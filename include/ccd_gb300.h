@@ -99,6 +99,9 @@ int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
  *   "pool_budget"    further steps the unfinished polynomials get, many per
  *                    warp, before the last ones are finished one per warp
  *                    (0: no limit); default 0
+ *   "chunk_rows"     ccd_prim_batch: largest chunk (rows) streamed through
+ *                    the device, two in flight; a batch is cut into equal
+ *                    chunks; in [1024, 2^26], default 2^23
  *   "layer_grid_min" ccd_velocity_filter: when a penalty group holds this
  *                    many stencils or vertices, each firing runs over the
  *                    whole GPU instead of one block; default 1024
