@@ -53,6 +53,9 @@ def parse():
                     help="also time meshSelfDistance, the closest-point batches and the penalty forces (1) or not (0)")
     ap.add_argument("--velocity", type=int, default=1, help="also time the velocity filter (1) or not (0)")
     ap.add_argument("--vf-grid", type=int, default=16, help="sheet resolution of the velocity-filter scene")
+    ap.add_argument("--vf-events-per-launch", type=int, default=0,
+                    help="velocity filter: firings per event-loop launch (0: the library's default); short launches "
+                         "for profilers")
     ap.add_argument("--serve", type=int, default=1, help="also run the serving loop (1) or not (0)")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0])
@@ -493,6 +496,8 @@ def velocity_filter_section(ctx, rank, args):
     tm[:9] = 0
     scenes["triangles"] = (t0, t1, np.array([[0, 1, 2], [3, 4, 5]], np.int32), tm, 0.01, 0.005)
     out = {}
+    if args.vf_events_per_launch:
+        ctx.set_option("layer_events_per_launch", args.vf_events_per_launch)
     for name, (a, b, ff, m, oe, ie) in scenes.items():
         t = time.perf_counter()
         res, qe, st = ctx.velocity_filter(a, b, ff, m, oe, ie)

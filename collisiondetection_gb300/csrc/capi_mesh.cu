@@ -1181,7 +1181,7 @@ extern "C" int ccd_velocity_filter(ccd_context *ctx, int32_t nverts, const doubl
     for (;;) {
       ccd::LayerState ls{nverts, d_q, d_v, d_lu, d_minv, d_newq, d_newv, d_contrib, d_fired,
                          log_v, log_t, log_p, log_cap, d_counts, 1.0, d_status, d_counts + 1, d_step};
-      CCD_CUDA(ccd::launch_layer_events(lg, ls, (int64_t)1 << 20, std::max<int64_t>(max_st, max_gv),
+      CCD_CUDA(ccd::launch_layer_events(lg, ls, ctx->opt_layer_events, std::max<int64_t>(max_st, max_gv),
                                         ctx->opt_layer_grid_min, s));
       int status = 0;
       int64_t counts[2] = {0, 0};

@@ -92,6 +92,7 @@ struct ccd_context {
   int opt_count_tests = 0;
   int64_t opt_layer_grid_min = 1024;  // velocity filter: groups this large fire over the whole GPU
   int64_t opt_chunk_rows = ccd_capi::kChunkRows;  // host-memory batches: rows per chunk
+  int64_t opt_layer_events = (int64_t)1 << 20;      // velocity filter: firings per event-loop launch
   std::string err;
 };
 

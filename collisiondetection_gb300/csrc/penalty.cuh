@@ -52,21 +52,21 @@ struct L2Load {
   }
 };
 
-template <int KIND, class Load = PlainLoad>
-__device__ __forceinline__ bool stencil_force(const double *q, const double *vel, const int *v, PenaltyParams pp,
-                                              v3d (&c)[4], Load ldv = Load()) {
-  const v3d x0 = ldv(q, v[0]), x1 = ldv(q, v[1]), x2 = ldv(q, v[2]), x3 = ldv(q, v[3]);
+// The potential from the stencil's four positions x; vel(k) gives vertex k's
+// velocity and is called only when the potential fires, in the reference's
+// order of the relative-velocity sum.
+template <int KIND, class Vel>
+__device__ __forceinline__ bool stencil_force_at(const v3d (&x)[4], Vel vel, PenaltyParams pp, v3d (&c)[4]) {
   double stiffness = pp.stiffness;
   if constexpr (KIND == 0) {
     // VertexFacePenaltyPotential::addForce (src/PenaltyPotential.cpp:7-34)
-    if (!vertex_plane_distance_less_than(x0, x1, x2, x3, pp.outer_eta)) return false;
+    if (!vertex_plane_distance_less_than(x[0], x[1], x[2], x[3], pp.outer_eta)) return false;
     double b[3];
-    const v3d cv = vertex_face_closest(x0, x1, x2, x3, b);
+    const v3d cv = vertex_face_closest(x[0], x[1], x[2], x[3], b);
     const double dist = norm(cv);
     if (dist >= pp.outer_eta || dist < pp.inner_eta) return false;
-    const v3d vp = ldv(vel, v[0]);
-    const v3d relvel = (((v3d{-vp.x, -vp.y, -vp.z}) + b[0] * ldv(vel, v[1])) + b[1] * ldv(vel, v[2])) +
-                       b[2] * ldv(vel, v[3]);
+    const v3d vp = vel(0);
+    const v3d relvel = (((v3d{-vp.x, -vp.y, -vp.z}) + b[0] * vel(1)) + b[1] * vel(2)) + b[2] * vel(3);
     if (dot(relvel, cv) > 0) stiffness *= pp.cor;
     const double s = stiffness * (pp.outer_eta - dist) / (pp.outer_eta - pp.inner_eta);
     const v3d sc = s * cv;
@@ -77,13 +77,12 @@ __device__ __forceinline__ bool stencil_force(const double *q, const double *vel
     c[3] = b[2] * lf;
   } else {
     // EdgeEdgePenaltyPotential::addForce (src/PenaltyPotential.cpp:36-64)
-    if (!line_line_distance_less_than(x0, x1, x2, x3, pp.outer_eta)) return false;
+    if (!line_line_distance_less_than(x[0], x[1], x[2], x[3], pp.outer_eta)) return false;
     double b[4];
-    const v3d cv = edge_edge_closest(x0, x1, x2, x3, b);
+    const v3d cv = edge_edge_closest(x[0], x[1], x[2], x[3], b);
     const double dist = norm(cv);
     if (dist >= pp.outer_eta || dist < pp.inner_eta) return false;
-    const v3d relvel =
-        (((-b[0]) * ldv(vel, v[0]) - b[1] * ldv(vel, v[1])) + b[2] * ldv(vel, v[2])) + b[3] * ldv(vel, v[3]);
+    const v3d relvel = (((-b[0]) * vel(0) - b[1] * vel(1)) + b[2] * vel(2)) + b[3] * vel(3);
     if (dot(relvel, cv) > 0) stiffness *= pp.cor;
     const double s = stiffness * (pp.outer_eta - dist) / (pp.outer_eta - pp.inner_eta);
     const v3d sc = s * cv;
@@ -94,6 +93,14 @@ __device__ __forceinline__ bool stencil_force(const double *q, const double *vel
     c[3] = b[3] * lf;
   }
   return true;
+}
+
+// The same from position and velocity arrays indexed by vertex.
+template <int KIND, class Load = PlainLoad>
+__device__ __forceinline__ bool stencil_force(const double *q, const double *vel, const int *v, PenaltyParams pp,
+                                              v3d (&c)[4], Load ldv = Load()) {
+  const v3d x[4] = {ldv(q, v[0]), ldv(q, v[1]), ldv(q, v[2]), ldv(q, v[3])};
+  return stencil_force_at<KIND>(x, [&](int k) { return ldv(vel, v[k]); }, pp, c);
 }
 
 }  // namespace ccd

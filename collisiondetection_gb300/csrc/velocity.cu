@@ -219,6 +219,33 @@ constexpr int kGridThreads = 256;
 
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
 
+// A vertex coordinate at the firing time t (src/ActiveLayers.cpp:109-112):
+// newq = q + (t - lu) * v, newv = (newq - q) / (t - lu).  Every use below
+// recomputes it from the same three loads, so the values are the same
+// wherever they are needed.
+struct Advance {
+  const double *q, *v, *lu;
+  double t;
+  __device__ __forceinline__ double pos(int64_t i) const {
+    const double lu_i = __ldcg(lu + i);
+    return __ldcg(q + i) + (t - lu_i) * __ldcg(v + i);
+  }
+  __device__ __forceinline__ double vel(int64_t i) const {
+    const double q_i = __ldcg(q + i), lu_i = __ldcg(lu + i);
+    const double dt = t - lu_i;
+    const double nq = q_i + (t - lu_i) * __ldcg(v + i);
+    return (nq - q_i) / dt;
+  }
+  __device__ __forceinline__ v3d pos3(int vert) const {
+    const int64_t i = 3 * (int64_t)vert;
+    return v3d{pos(i), pos(i + 1), pos(i + 2)};
+  }
+  __device__ __forceinline__ v3d vel3(int vert) const {
+    const int64_t i = 3 * (int64_t)vert;
+    return v3d{vel(i), vel(i + 1), vel(i + 2)};
+  }
+};
+
 // The group force of one vertex slot j, its contributions accumulated in
 // order; the loads of eight contributions are issued before their additions.
 __device__ __forceinline__ void ordered_sum(const LayerGroups &g, const LayerState &s, int64_t j, int nvf,
@@ -309,27 +336,17 @@ __global__ void __launch_bounds__(kGridThreads) layer_events_grid(LayerGroups g,
     const int64_t v0 = g.gv_off[grp], v1 = g.gv_off[grp + 1];
     const int64_t s0 = g.st_off[grp], s1 = g.st_off[grp + 1];
     const int nvf = g.n_vf[grp];
-    // (1) the group's vertices at the firing time
-    for (int64_t j = v0 + gtid; j < v1; j += gsize) {
-      const int vert = g.gv[j];
-      for (int c = 0; c < 3; c++) {
-        const int64_t i = 3 * (int64_t)vert + c;
-        const double q = ldcg(s.q + i), lu = ldcg(s.lu + i);
-        const double dt = t - lu;
-        const double nq = q + (t - lu) * ldcg(s.v + i);
-        s.newq[i] = nq;
-        s.newv[i] = (nq - q) / dt;
-      }
-    }
-    grid.sync();
-    // (2) each stencil's potential
+    // (1, 2) each stencil's potential, its vertices advanced to the firing
+    // time on the fly (no barrier between moving the vertices and using them)
+    const Advance adv{s.q, s.v, s.lu, t};
     const PenaltyParams pp{g.eta[grp], g.inner[grp], g.stiffness[grp], g.cor[grp]};
     for (int64_t k = s0 + gtid; k < s1; k += gsize) {
       const int64_t local = k - s0;
       const int v4[4] = {g.st[4 * k], g.st[4 * k + 1], g.st[4 * k + 2], g.st[4 * k + 3]};
+      const v3d x[4] = {adv.pos3(v4[0]), adv.pos3(v4[1]), adv.pos3(v4[2]), adv.pos3(v4[3])};
+      const auto vel = [&](int kk) { return adv.vel3(v4[kk]); };
       v3d c[4];
-      const bool f = local < nvf ? stencil_force<0>(s.newq, s.newv, v4, pp, c, L2Load())
-                                 : stencil_force<1>(s.newq, s.newv, v4, pp, c, L2Load());
+      const bool f = local < nvf ? stencil_force_at<0>(x, vel, pp, c) : stencil_force_at<1>(x, vel, pp, c);
       s.fired[local] = f ? 1 : 0;
       if (f) {
         double *out = s.contrib + 12 * local;
@@ -365,8 +382,9 @@ __global__ void __launch_bounds__(kGridThreads) layer_events_grid(LayerGroups g,
         if (touched) {
           for (int c = 0; c < 3; c++) {
             const int64_t i = 3 * (int64_t)vert + c;
+            const double nq = adv.pos(i);
             s.v[i] = ldcg(s.v + i) + s.minv[i] * F[c];
-            s.q[i] = ldcg(s.newq + i);
+            s.q[i] = nq;
             s.lu[i] = t;
           }
         }
