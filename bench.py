@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0])
     ap.add_argument("--serve-fp64-requests", type=int, default=6)
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="choose each context's refinement work split with ccd_autotune_prim_batch first (1) or not (0)")
     ap.add_argument("--only", default="all", choices=["all", "device"],
                     help="device: only the resident cull + refine steps (a short run for profilers)")
     ap.add_argument("--cloth-grid", type=int, default=256)
@@ -680,6 +682,17 @@ def run_ours(args, rank, world, local, pg):
     d_eta = torch.full((1,), ETA, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
 
+    # the work split of each kind's refinement, chosen by the autotuner on the
+    # batch itself (outside the timed regions; results never change)
+    tune = None
+    if args.autotune:
+        tune = {}
+        for kind, name in ((C.VERTEX_FACE, "vf"), (C.EDGE_EDGE, "ee")):
+            b = d[name]
+            tune[name] = kind_ctx[name].autotune_prim_batch(kind, b["rows"].shape[0], b["rows"].data_ptr(),
+                                                            d_eta.data_ptr(), 1, reps=2)
+        torch.cuda.synchronize()
+
     def step(path):
         for kind, name in ((C.VERTEX_FACE, "vf"), (C.EDGE_EDGE, "ee")):
             b = d[name]
@@ -854,6 +867,7 @@ def run_ours(args, rank, world, local, pg):
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": int(tm["launches"]),
+            "autotune": tune,
             "mesh": mesh,
             "distance": distance,
             "penalty": penalty,

@@ -53,6 +53,12 @@ class BatchTimings(ctypes.Structure):
     _fields_ = [("cull_ms", ctypes.c_float), ("refine_ms", ctypes.c_float), ("launches", ctypes.c_int32)]
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [("wave_steps", ctypes.c_int32), ("pool_budget", ctypes.c_int32), ("wave_min_rows", ctypes.c_int64),
+                ("candidates", ctypes.c_int32), ("mismatches", ctypes.c_int32), ("chosen", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("default_ms", ctypes.c_double), ("best_ms", ctypes.c_double)]
+
+
 _lib = None
 
 
@@ -89,6 +95,8 @@ def load(path: str = LIB):
         fn.argtypes = [_P, _P, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
     L.ccd_prim_batch.argtypes = [_P, ctypes.c_int, ctypes.c_int, _I64, _P, _P, _I64, _P, _P]
     L.ccd_prim_batch_device.argtypes = [_P, ctypes.c_int, ctypes.c_int, _I64, _P, _P, _I64, _P, _P, _P]
+    L.ccd_autotune_prim_batch.argtypes = [_P, ctypes.c_int, _I64, _P, _P, _I64, ctypes.c_int,
+                                          ctypes.POINTER(TuneResult)]
     L.ccd_mesh_create.argtypes = [_P, ctypes.c_int32, ctypes.c_int32, _P, ctypes.POINTER(_P)]
     L.ccd_mesh_destroy.argtypes = [_P]
     L.ccd_mesh_create_instances.argtypes = [_P, ctypes.c_int32, _P, _P, _P, ctypes.POINTER(_P)]
@@ -171,7 +179,8 @@ class Context:
         return {f: getattr(st, f) for f, _ in BatchStats._fields_}
 
     def set_option(self, name: str, value: int):
-        """Tuning option (ccd_context_set_option): "wave_steps", "wave_min_rows"."""
+        """Tuning option (ccd_context_set_option): "wave_steps", "wave_min_rows",
+        "pool_budget", "chunk_rows", ... (include/ccd_gb300.h lists them)."""
         self._check(self.lib.ccd_context_set_option(self.handle, name.encode(), int(value)), "ccd_context_set_option")
 
     def set_profiling(self, on: bool):
@@ -303,6 +312,17 @@ class Context:
         addresses (e.g. torch tensor data_ptr()).  Asynchronous."""
         self._check(self.lib.ccd_prim_batch_device(self.handle, kind, path, n, rows_ptr, eta_ptr, eta_count,
                                                    hit_ptr, t_ptr, status_ptr), "ccd_prim_batch_device")
+
+
+    def autotune_prim_batch(self, kind: int, n: int, rows_ptr: int, eta_ptr: int, eta_count: int = 1,
+                            reps: int = 3) -> dict:
+        """Work-split autotuner (ccd_autotune_prim_batch) on a device batch of
+        vertex-face or edge-edge rows; sets the fastest split as this
+        context's options and returns what it measured."""
+        res = TuneResult()
+        self._check(self.lib.ccd_autotune_prim_batch(self.handle, kind, n, rows_ptr, eta_ptr, eta_count, reps,
+                                                     ctypes.byref(res)), "ccd_autotune_prim_batch")
+        return {f: getattr(res, f) for f, _ in TuneResult._fields_ if f != "reserved"}
 
 
 def _stencils(a) -> np.ndarray:

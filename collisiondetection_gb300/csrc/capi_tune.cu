@@ -1,0 +1,192 @@
+// Work-split autotuner of the staged refinement (C ABI: ccd_autotune_prim_batch).
+//
+// The refinement of a large vertex-face or edge-edge batch splits its root
+// solves between a lock-step wavefront (wave_steps launches over every queued
+// polynomial), a pool kernel that packs the unfinished solves many per warp
+// (pool_budget steps each), and a one-per-warp finish of the last ones; batches
+// below wave_min_rows skip the wavefront.  Which split is fastest depends on
+// the batch (how many rows survive the cull, how many solves run long) and on
+// the GPU, so the tuner times each candidate split on the caller's own rows
+// and keeps the fastest.  A split changes only the schedule of the solves,
+// never their arithmetic: every candidate's hits and contact times are
+// compared bit for bit with the first run's, and a candidate that differs is
+// counted and never chosen.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "context.cuh"
+
+namespace {
+
+// Counts the rows whose hit flag differs, or whose contact time differs bit
+// for bit where both hit.
+__global__ void count_mismatches(const uint8_t *h0, const double *t0, const uint8_t *h1, const double *t1,
+                                 int64_t n, unsigned long long *out) {
+  unsigned bad = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const bool h = h0[i] != 0;
+    bad += (h != (h1[i] != 0)) ||
+           (h && __double_as_longlong(t0[i]) != __double_as_longlong(t1[i]));
+  }
+  bad = __reduce_add_sync(0xffffffffu, bad);
+  if ((threadIdx.x & 31) == 0 && bad) atomicAdd(out, (unsigned long long)bad);
+}
+
+struct Split {
+  int wave_steps;
+  int pool_budget;
+};
+
+struct TuneBuffers {
+  uint8_t *hit[2] = {nullptr, nullptr};
+  double *t[2] = {nullptr, nullptr};
+  unsigned long long *bad = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  ~TuneBuffers() {
+    for (int k = 0; k < 2; k++) {
+      cudaFree(hit[k]);
+      cudaFree(t[k]);
+      if (ev[k]) cudaEventDestroy(ev[k]);
+    }
+    cudaFree(bad);
+  }
+};
+
+}  // namespace
+
+using namespace ccd_capi;
+
+extern "C" {
+
+int ccd_autotune_prim_batch(ccd_context *ctx, int kind, int64_t n, const double *rows, const double *eta,
+                            int64_t eta_count, int reps, ccd_tune_result *out) {
+  if (!ctx) return CCD_ERR_INVALID_ARGUMENT;
+  if (!out) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null result");
+  if (kind != CCD_VERTEX_FACE && kind != CCD_EDGE_EDGE)
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "only vertex-face and edge-edge batches have a staged refinement");
+  if (n <= 0 || n > INT32_MAX) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "n must be in [1, 2^31)");
+  if (!rows || !eta) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null buffer");
+  if (eta_count != 1 && eta_count != n) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "eta_count must be 1 or n");
+  if (reps < 1 || reps > 64) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "reps must be in [1, 64]");
+  *out = ccd_tune_result{};
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+
+  TuneBuffers tb;
+  for (int k = 0; k < 2; k++) {
+    CCD_CUDA(cudaMalloc(&tb.hit[k], (size_t)n));
+    CCD_CUDA(cudaMalloc(&tb.t[k], (size_t)n * sizeof(double)));
+    CCD_CUDA(cudaEventCreate(&tb.ev[k]));
+  }
+  CCD_CUDA(cudaMalloc(&tb.bad, sizeof(unsigned long long)));
+
+  // Restores the context's options on every early return; the chosen split
+  // is committed at the end.
+  struct Saved {
+    ccd_context *ctx;
+    int steps, budget;
+    int64_t min_rows;
+    bool profiling, committed = false;
+    ~Saved() {
+      ctx->profiling = profiling;
+      if (committed) return;
+      ctx->opt_wave_steps = steps;
+      ctx->opt_pool_budget = budget;
+      ctx->opt_wave_min_rows = min_rows;
+    }
+  } saved{ctx, ctx->opt_wave_steps, ctx->opt_pool_budget, ctx->opt_wave_min_rows, ctx->profiling};
+  const int saved_steps = saved.steps, saved_budget = saved.budget;
+  const int64_t saved_min_rows = saved.min_rows;
+  ctx->profiling = false;
+
+  // The context's own settings come first: their output is the one every
+  // other candidate must reproduce.  Then the pool kernel alone, then the
+  // wavefront at each step count with each pool budget.
+  std::vector<Split> cands;
+  cands.push_back({n >= saved_min_rows ? saved_steps : 0, saved_budget});
+  cands.push_back({0, 0});
+  for (int steps : {16, 32, 48, 64, 96, 128})
+    for (int budget : {0, 256, 4096}) cands.push_back({steps, budget});
+
+  // One run of the batch under the current options into output set k, with
+  // the contact times starting as NaN (t is written only where hit).
+  auto run = [&](int k, float *ms) -> int {
+    CCD_CUDA(cudaMemsetAsync(tb.t[k], 0xff, (size_t)n * sizeof(double), ctx->stream));
+    CCD_CUDA(cudaEventRecord(tb.ev[0], ctx->stream));
+    int rc = ccd_prim_batch_device(ctx, kind, CCD_PATH_CULL_REFINE, n, rows, eta, eta_count, tb.hit[k], tb.t[k],
+                                   nullptr);
+    if (rc) return rc;
+    CCD_CUDA(cudaEventRecord(tb.ev[1], ctx->stream));
+    CCD_CUDA(cudaEventSynchronize(tb.ev[1]));
+    if (ms) CCD_CUDA(cudaEventElapsedTime(ms, tb.ev[0], tb.ev[1]));
+    return CCD_OK;
+  };
+
+  double best_ms = 0.0;
+  Split best{};
+  int best_i = -1;
+  for (size_t i = 0; i < cands.size(); i++) {
+    const Split c = cands[i];
+    // The wavefront runs only for batches of at least wave_min_rows rows.
+    ctx->opt_wave_steps = c.wave_steps;
+    ctx->opt_pool_budget = c.pool_budget;
+    ctx->opt_wave_min_rows = std::min<int64_t>(saved_min_rows, n);
+    const int k = i == 0 ? 0 : 1;
+    int rc = run(k, nullptr);  // warm-up (and scratch growth outside the timing)
+    std::vector<float> times;
+    for (int r = 0; !rc && r < reps; r++) {
+      float ms = 0.f;
+      rc = run(k, &ms);
+      times.push_back(ms);
+    }
+    if (rc) return rc;
+    std::sort(times.begin(), times.end());
+    const double med = times[times.size() / 2];
+    out->candidates++;
+    if (i == 0) {
+      out->default_ms = med;
+    } else {
+      CCD_CUDA(cudaMemsetAsync(tb.bad, 0, sizeof(unsigned long long), ctx->stream));
+      count_mismatches<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(tb.hit[0], tb.t[0], tb.hit[1], tb.t[1], n,
+                                                                  tb.bad);
+      CCD_CUDA(cudaGetLastError());
+      unsigned long long bad = 0;
+      CCD_CUDA(cudaMemcpyAsync(&bad, tb.bad, sizeof(bad), cudaMemcpyDeviceToHost, ctx->stream));
+      CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (bad) {
+        out->mismatches++;
+        continue;
+      }
+    }
+    if (best_i < 0 || med < best_ms) {
+      best_ms = med;
+      best = c;
+      best_i = (int)i;
+    }
+  }
+
+  out->best_ms = best_ms;
+  saved.committed = true;
+  if (best.wave_steps > 0) {
+    // Batches as large as this one take the wavefront with the chosen split.
+    ctx->opt_wave_steps = best.wave_steps;
+    ctx->opt_pool_budget = best.pool_budget;
+    ctx->opt_wave_min_rows = std::min<int64_t>(saved_min_rows, n);
+  } else {
+    // The pool kernel alone won: batches up to this size skip the wavefront;
+    // larger ones keep the context's split.
+    ctx->opt_wave_steps = saved_steps;
+    ctx->opt_pool_budget = saved_budget;
+    ctx->opt_wave_min_rows = std::max<int64_t>(saved_min_rows, n + 1);
+  }
+  out->wave_steps = ctx->opt_wave_steps;
+  out->pool_budget = ctx->opt_pool_budget;
+  out->wave_min_rows = ctx->opt_wave_min_rows;
+  out->chosen = best_i;
+  return CCD_OK;
+}
+
+}  // extern "C"

@@ -141,6 +141,34 @@ int ccd_prim_batch(ccd_context *ctx, int kind, int path, int64_t n, const double
 int ccd_prim_batch_device(ccd_context *ctx, int kind, int path, int64_t n, const double *rows, const double *eta,
                           int64_t eta_count, uint8_t *hit, double *t, uint8_t *status);
 
+/* ---------------------------------------------------------- autotuner
+ * No counterpart in the reference (its narrow phase is one scalar call per
+ * stencil).  Chooses the work split of the FP64 refinement for batches like
+ * the given one: how many lock-step wavefront steps every queued root solve
+ * takes ("wave_steps"), how many further steps the pool kernel gives each
+ * unfinished solve ("pool_budget"), and the batch size from which the
+ * wavefront runs at all ("wave_min_rows").  It runs `rows` (device memory, a
+ * vertex-face or edge-edge batch of n rows, CCD_PATH_CULL_REFINE) once to
+ * warm up and `reps` timed times under the context's own split, the pool
+ * kernel alone and each of 18 wavefront splits, checks that every split's
+ * hits and contact times equal the first split's bit for bit, and sets the
+ * fastest matching split as the context's options.  Blocks until done;
+ * allocates its own output buffers.  Results of later batches never change,
+ * only their speed. */
+typedef struct {
+  int32_t wave_steps;    /* the context's options after the call */
+  int32_t pool_budget;
+  int64_t wave_min_rows;
+  int32_t candidates;    /* splits timed */
+  int32_t mismatches;    /* splits whose output differed (never chosen; 0 expected) */
+  int32_t chosen;        /* index of the chosen split in the order timed (0: the context's own) */
+  int32_t reserved;
+  double default_ms;     /* median time of the context's own split */
+  double best_ms;        /* median time of the chosen split */
+} ccd_tune_result;
+int ccd_autotune_prim_batch(ccd_context *ctx, int kind, int64_t n, const double *rows, const double *eta,
+                            int64_t eta_count, int reps, ccd_tune_result *out);
+
 /* ---------------------------------------------------------- allocation-free batch
  * No counterpart in the reference.  The same results as
  * ccd_prim_batch_device with CCD_PATH_CULL_REFINE (no per-row status), for
