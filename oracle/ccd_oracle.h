@@ -8,7 +8,7 @@
  * (start, end) history.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
- * this library, and only as the checker.  It is pinned against the reference's
+ * this library, and only to check results.  It is pinned against the reference's
  * own sources (oracle/_ref, built from the reference tree by oracle/Makefile)
  * through the fixtures in tests/golden/.
  */

@@ -3,7 +3,7 @@
 ctypes loader for the C restatement (oracle/_build/libccd_oracle.so) and, where
 it was built, the reference compiled from its own sources
 (oracle/_ref/libccd_ref.so).  Only tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline leg import this module, and only as the checker.
+bench.py's CPU-baseline leg import this module, and only to check results.
 """
 from __future__ import annotations
 
