@@ -125,17 +125,15 @@ int ccd_autotune_prim_batch(ccd_context *ctx, int kind, int64_t n, const double 
     return CCD_OK;
   };
 
-  double best_ms = 0.0;
-  Split best{};
-  int best_i = -1;
-  for (size_t i = 0; i < cands.size(); i++) {
-    const Split c = cands[i];
+  // Median time of one split (after a warm-up run, which also grows the
+  // scratch outside the timing) into output set k; for k = 1, *bad receives
+  // the rows that differ from set 0.
+  auto time_split = [&](const Split &c, int k, double *med, unsigned long long *bad) -> int {
     // The wavefront runs only for batches of at least wave_min_rows rows.
     ctx->opt_wave_steps = c.wave_steps;
     ctx->opt_pool_budget = c.pool_budget;
     ctx->opt_wave_min_rows = std::min<int64_t>(saved_min_rows, n);
-    const int k = i == 0 ? 0 : 1;
-    int rc = run(k, nullptr);  // warm-up (and scratch growth outside the timing)
+    int rc = run(k, nullptr);
     std::vector<float> times;
     for (int r = 0; !rc && r < reps; r++) {
       float ms = 0.f;
@@ -144,27 +142,59 @@ int ccd_autotune_prim_batch(ccd_context *ctx, int kind, int64_t n, const double 
     }
     if (rc) return rc;
     std::sort(times.begin(), times.end());
-    const double med = times[times.size() / 2];
-    out->candidates++;
-    if (i == 0) {
-      out->default_ms = med;
-    } else {
+    *med = times[times.size() / 2];
+    *bad = 0;
+    if (k == 1) {
       CCD_CUDA(cudaMemsetAsync(tb.bad, 0, sizeof(unsigned long long), ctx->stream));
       count_mismatches<<<ctx->num_sms * 4, 256, 0, ctx->stream>>>(tb.hit[0], tb.t[0], tb.hit[1], tb.t[1], n,
                                                                   tb.bad);
       CCD_CUDA(cudaGetLastError());
-      unsigned long long bad = 0;
-      CCD_CUDA(cudaMemcpyAsync(&bad, tb.bad, sizeof(bad), cudaMemcpyDeviceToHost, ctx->stream));
+      CCD_CUDA(cudaMemcpyAsync(bad, tb.bad, sizeof(*bad), cudaMemcpyDeviceToHost, ctx->stream));
       CCD_CUDA(cudaStreamSynchronize(ctx->stream));
-      if (bad) {
-        out->mismatches++;
-        continue;
-      }
+    }
+    return CCD_OK;
+  };
+
+  double best_ms = 0.0;
+  Split best{};
+  int best_i = -1;
+  for (size_t i = 0; i < cands.size(); i++) {
+    double med = 0.0;
+    unsigned long long bad = 0;
+    int rc = time_split(cands[i], i == 0 ? 0 : 1, &med, &bad);
+    if (rc) return rc;
+    out->candidates++;
+    if (i == 0) out->default_ms = med;
+    if (bad) {
+      out->mismatches++;
+      continue;
     }
     if (best_i < 0 || med < best_ms) {
       best_ms = med;
-      best = c;
+      best = cands[i];
       best_i = (int)i;
+    }
+  }
+  // The first split is timed first, before the GPU has run this batch for
+  // long; on GB300 its edge-edge median came out about 5% slower than the
+  // same split timed later in the sweep.  Time it once more at the end and
+  // keep its faster median.
+  {
+    double med = 0.0;
+    unsigned long long bad = 0;
+    int rc = time_split(cands[0], 1, &med, &bad);
+    if (rc) return rc;
+    if (bad) {
+      out->mismatches++;
+    } else {
+      out->default_ms = std::min(out->default_ms, med);
+      if (best_i != 0 && med <= best_ms) {
+        best_ms = med;
+        best = cands[0];
+        best_i = 0;
+      } else if (best_i == 0) {
+        best_ms = out->default_ms;
+      }
     }
   }
 

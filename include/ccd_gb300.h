@@ -150,9 +150,10 @@ int ccd_prim_batch_device(ccd_context *ctx, int kind, int path, int64_t n, const
  * wavefront runs at all ("wave_min_rows").  It runs `rows` (device memory, a
  * vertex-face or edge-edge batch of n rows, CCD_PATH_CULL_REFINE) once to
  * warm up and `reps` timed times under the context's own split, the pool
- * kernel alone and each of 18 wavefront splits, checks that every split's
- * hits and contact times equal the first split's bit for bit, and sets the
- * fastest matching split as the context's options.  Blocks until done;
+ * kernel alone, each of 18 wavefront splits and the context's own split once
+ * more, checks that every split's hits and contact times equal the first
+ * split's bit for bit, and sets the fastest matching split as the context's
+ * options.  Blocks until done;
  * allocates its own output buffers.  Results of later batches never change,
  * only their speed. */
 typedef struct {
