@@ -327,13 +327,18 @@ def motion_request(tris: int, seed: int, steps: int = 10):
     return np.ascontiguousarray(f, dtype=np.int32), frames
 
 
+def uneven_sizes(n_instances: int = 512, lo: float = 200.0, hi: float = 2e5, seed: int = 0) -> np.ndarray:
+    """Requested triangle counts of an uneven batch: log-uniform in [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), n_instances)).astype(int)
+
+
 def uneven_batch(n_instances: int = 512, lo: float = 200.0, hi: float = 2e5, seed: int = 0, steps: int = 1):
     """Uneven batch of independent collision queries: `n_instances` motion
     requests (motion_request) with triangle counts log-uniform in [lo, hi],
     concatenated.  Returns (faces (F, 3) int32 with global vertex indices,
     frames (steps + 1, 3V), vertex_offsets, face_offsets)."""
-    rng = np.random.default_rng(seed)
-    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), n_instances)).astype(int)
+    sizes = uneven_sizes(n_instances, lo, hi, seed)
     faces, frames, vo, fo = [], [], [0], [0]
     for i, t in enumerate(sizes):
         f, fr = motion_request(int(t), 100000 + seed * 10000 + i, steps=steps)
