@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0])
     ap.add_argument("--serve-fp64-requests", type=int, default=6)
+    ap.add_argument("--graph-rows", type=int, default=4096,
+                    help="rows per kind of the small-batch CUDA-graph comparison (0: skip it)")
+    ap.add_argument("--graph-iters", type=int, default=50)
     ap.add_argument("--autotune", type=int, default=1,
                     help="choose each context's refinement work split with ccd_autotune_prim_batch first (1) or not (0)")
     ap.add_argument("--only", default="all", choices=["all", "device"],
@@ -612,6 +615,73 @@ def uneven_section(args):
     return out
 
 
+def graph_section(ctx, stream, args):
+    """Small device batches issued directly and replayed from a CUDA graph.
+
+    One step is `graph_rows` vertex-face rows and as many edge-edge rows
+    through ccd_prim_batch_device on one context and stream: the size of a
+    serving step's narrow phase, where launch costs are a visible share.  The
+    step is captured once (after a direct call that sizes the context's
+    scratch) and replayed; replays must reproduce the direct call's hits and
+    contact times bit for bit.  Errors are reported, not raised, so that
+    this section cannot stop the bench line."""
+    import torch
+
+    import collisiondetection_gb300 as C
+
+    try:
+        n = args.graph_rows
+        ctx.set_profiling(False)
+        bufs = {}
+        with torch.cuda.stream(stream):
+            for kind in (C.VERTEX_FACE, C.EDGE_EDGE):
+                rows = C.workloads.primitive_batch(kind, n, seed=90 + kind)
+                bufs[kind] = (torch.from_numpy(rows).cuda(), torch.zeros(n, dtype=torch.uint8, device="cuda"),
+                              torch.full((n,), float("nan"), dtype=torch.float64, device="cuda"))
+            d_eta = torch.full((1,), ETA, dtype=torch.float64, device="cuda")
+        stream.synchronize()
+
+        def step():
+            for kind, (r, h, t) in bufs.items():
+                ctx.prim_batch_device(kind, n, r.data_ptr(), d_eta.data_ptr(), 1, h.data_ptr(), t.data_ptr())
+
+        step()
+        ctx.synchronize()
+        ref = {k: (h.cpu().numpy(), t.cpu().numpy()) for k, (_, h, t) in bufs.items()}
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            step()
+
+        def timeit(fn, iters):
+            for _ in range(3):
+                fn()
+            stream.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0 = time.perf_counter()
+            e0.record(stream)
+            for _ in range(iters):
+                fn()
+            e1.record(stream)
+            stream.synchronize()
+            wall = time.perf_counter() - t0
+            return e0.elapsed_time(e1) * 1e3 / iters, wall * 1e6 / iters
+
+        with torch.cuda.stream(stream):  # replay() launches on the current stream
+            dev_direct, wall_direct = timeit(step, args.graph_iters)
+            dev_graph, wall_graph = timeit(g.replay, args.graph_iters)
+        same = all(np.array_equal(ref[k][0], h.cpu().numpy()) and
+                   np.array_equal(ref[k][1].view(np.uint64), t.cpu().numpy().view(np.uint64))
+                   for k, (_, h, t) in bufs.items())
+        del g
+        return {"rows_per_kind": n, "iters": args.graph_iters,
+                "direct": {"device_us_per_step": dev_direct, "wall_us_per_step": wall_direct},
+                "graph": {"device_us_per_step": dev_graph, "wall_us_per_step": wall_graph},
+                "tests_per_s": {"direct": 2 * n / (dev_direct / 1e6), "graph": 2 * n / (dev_graph / 1e6)},
+                "replays_match_direct_call": bool(same)}
+    except Exception as exc:  # noqa: BLE001 - reported in the bench line instead
+        return {"error": f"{type(exc).__name__}: {exc}"}
+
+
 def run_reference(args, rank, world, pg):
     if rank != 0:
         return
@@ -847,6 +917,7 @@ def run_ours(args, rank, world, local, pg):
     velocity = velocity_filter_section(ctx, rank, args) if args.velocity and full and world == 1 else None
     serving = serving_section(args) if args.serve and full and world == 1 else None
     uneven = uneven_section(args) if args.uneven_instances and full and world == 1 else None
+    graph = graph_section(ctx, stream, args) if args.graph_rows and full else None
 
     if rank == 0:
         line = {
@@ -874,6 +945,7 @@ def run_ours(args, rank, world, local, pg):
             "velocity_filter": velocity,
             "serving": serving,
             "uneven_batch": uneven,
+            "graph_small_batches": graph,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -135,7 +135,15 @@ int ccd_vertex_vertex_ctcd(ccd_context *ctx, const double *points, double eta, i
  * streamed through the device in chunks with copies overlapped with compute.
  * ccd_prim_batch_device: all pointers are device memory; enqueued on the
  * context's stream and returns without waiting.  status (optional, n bytes)
- * receives per-row status bits (0 = ok). */
+ * receives per-row status bits (0 = ok).
+ * Stream capture: once the context has run a device batch of at least n rows
+ * (which sizes its scratch) and with profiling off, ccd_prim_batch_device
+ * enqueues only kernels, memsets and copies, so a caller may capture it on
+ * the context's stream into a CUDA graph and replay it.  The graph keeps the
+ * pointers and sizes it was captured with, and the context's scratch: replays
+ * on one context must not overlap other work of that context.  A call that
+ * would grow the scratch during capture fails with CCD_ERR_CUDA (and the
+ * capture is invalidated). */
 int ccd_prim_batch(ccd_context *ctx, int kind, int path, int64_t n, const double *rows, const double *eta,
                    int64_t eta_count, uint8_t *hit, double *t);
 int ccd_prim_batch_device(ccd_context *ctx, int kind, int path, int64_t n, const double *rows, const double *eta,
