@@ -167,8 +167,25 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(vf, ee, max_rows=None):
-    """The oracle restatement of the reference's CPU path on all host cores."""
+def compare_results(h_ref, t_ref, h, t):
+    """Hit sets and contact times of (h, t) against a reference result of the
+    same rows: rows the reference hits and (h, t) misses (false negatives),
+    the converse, and the largest relative contact-time error over common
+    hits (t is only defined where hit)."""
+    ref = np.asarray(h_ref).astype(bool)
+    got = np.asarray(h).astype(bool)
+    both = ref & got
+    tr, tg = np.asarray(t_ref)[both], np.asarray(t)[both]
+    rel = np.abs(tg - tr) / np.maximum(np.abs(tr), 1e-300)
+    return {"hits": int(ref.sum()), "false_negatives": int((ref & ~got).sum()),
+            "false_positives": int((~ref & got).sum()), "max_rel_t_err": float(rel.max()) if rel.size else 0.0,
+            "t_bit_identical": bool(np.array_equal(tr.view(np.uint64), tg.view(np.uint64)))}
+
+
+def cpu_baseline(vf, ee, max_rows=None, results=None):
+    """The oracle restatement of the reference's CPU path on all host cores.
+    With `results` (a dict), the oracle's (hit, t) per kind go into it too:
+    the bench checks the GPU's results against them."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
@@ -178,9 +195,11 @@ def cpu_baseline(vf, ee, max_rows=None):
     if max_rows:
         vf, ee = vf[:max_rows], ee[:max_rows]
     t0 = time.perf_counter()
-    orc.batch(0, vf, ETA, nthreads=threads)
-    orc.batch(1, ee, ETA, nthreads=threads)
+    out_vf = orc.batch(0, vf, ETA, nthreads=threads)
+    out_ee = orc.batch(1, ee, ETA, nthreads=threads)
     dt = time.perf_counter() - t0
+    if results is not None:
+        results["vf"], results["ee"] = out_vf, out_ee
     rows = vf.shape[0] + ee.shape[0]
     return {"value": rows / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{vf.shape[0]} VF + {ee.shape[0]} EE rows of the same workload, {dt:.2f} s wall"}
@@ -809,6 +828,8 @@ def run_ours(args, rank, world, local, pg):
     if full:
         ms64, _ = timed(C.PATH_FP64, max(1, min(args.steps, 3)), 1)
         fp64_tps = rows_per_step * max(1, min(args.steps, 3)) / (ms64 / 1e3)
+        # the plain FP64 path's results, to check the cull path against
+        fp64_out = {name: (d[name]["hit"].cpu().numpy(), d[name]["t"].cpu().numpy()) for name in ("vf", "ee")}
 
     # headline: FP32 cull + FP64 refine, rows resident in HBM; clocks sampled meanwhile
     with ClockSampler(local) as clk:
@@ -825,6 +846,7 @@ def run_ours(args, rank, world, local, pg):
                             b["hit"].data_ptr(), b["t"].data_ptr(), None, path=C.PATH_CULL_REFINE)
         c.synchronize()
         counts[name] = c.stats()
+    gpu_out = {name: (d[name]["hit"].cpu().numpy(), d[name]["t"].cpu().numpy()) for name in ("vf", "ee")}
 
     # end to end through the host-memory entry point (copies inside the timed
     # region), from pinned host buffers
@@ -910,7 +932,15 @@ def run_ours(args, rank, world, local, pg):
                 "cull_ms_per_launch": cull_ms_launch, "refine_ms_per_launch": refine_ms_launch,
                 "share": {"cull": tm["cull_ms"] / (tm["cull_ms"] + tm["refine_ms"]),
                           "refine": tm["refine_ms"] / (tm["cull_ms"] + tm["refine_ms"])}}
-    cpu = cpu_baseline(vf, ee) if rank == 0 and full else None
+    oracle_out = {}
+    cpu = cpu_baseline(vf, ee, results=oracle_out) if rank == 0 and full else None
+    # the FP32 cull's false negatives and the contact-time error of the
+    # headline path, against the plain FP64 GPU path and the oracle
+    parity = None
+    if full:
+        parity = {"cull_refine_vs_fp64_path": {k: compare_results(*fp64_out[k], *gpu_out[k]) for k in gpu_out}}
+        if oracle_out:
+            parity["cull_refine_vs_oracle"] = {k: compare_results(*oracle_out[k], *gpu_out[k]) for k in gpu_out}
     mesh = mesh_section(ctx, stream, rank, args) if args.mesh and full else None
     distance = distance_section(ctx, stream, rank, args) if args.distance and full else None
     penalty = penalty_section(ctx, rank, args) if args.distance and full else None
@@ -936,6 +966,7 @@ def run_ours(args, rank, world, local, pg):
             "e2e": e2e,
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "parity": parity,
             "clocks": clk.summary(),
             "gpu_launches": int(tm["launches"]),
             "autotune": tune,
