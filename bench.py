@@ -778,8 +778,11 @@ def run_ours(args, rank, world, local, pg):
         tune = {}
         for kind, name in ((C.VERTEX_FACE, "vf"), (C.EDGE_EDGE, "ee")):
             b = d[name]
-            tune[name] = kind_ctx[name].autotune_prim_batch(kind, b["rows"].shape[0], b["rows"].data_ptr(),
-                                                            d_eta.data_ptr(), 1, reps=2)
+            try:
+                tune[name] = kind_ctx[name].autotune_prim_batch(kind, b["rows"].shape[0], b["rows"].data_ptr(),
+                                                                d_eta.data_ptr(), 1, reps=2)
+            except C.CcdError as exc:  # the context keeps its own split; reported in the line
+                tune[name] = {"error": str(exc)}
         torch.cuda.synchronize()
 
     def step(path):
