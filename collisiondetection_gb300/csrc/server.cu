@@ -117,14 +117,14 @@ void worker_loop(ccd_server *s, int slot) {
     std::shared_ptr<Job> job;
     {
       std::unique_lock<std::mutex> lock(s->mu);
+      // Queued requests are admitted under the memory budget, also while the
+      // server shuts down (it finishes them before its workers exit).
       s->cv.wait(lock, [&] {
-        if (s->stop) return true;
-        if (s->queue.empty()) return false;
+        if (s->queue.empty()) return s->stop;
         const int64_t need = s->queue.front()->bytes;
         return s->running == 0 || s->in_use + need <= s->budget;
       });
-      if (s->stop && s->queue.empty()) return;
-      if (s->queue.empty()) continue;
+      if (s->queue.empty()) return;  // woken by the shutdown with nothing left to run
       job = s->queue.front();
       s->queue.pop_front();
       s->in_use += job->bytes;
