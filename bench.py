@@ -45,9 +45,10 @@ def parse():
     ap.add_argument("--n-vf", type=int, default=10_000_000)
     ap.add_argument("--n-ee", type=int, default=10_000_000)
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--ref-sample", type=int, default=2_000_000, help="rows per kind per reference step")
+    ap.add_argument("--ref-sample", type=int, default=0,
+                    help="reference arm: rows per kind per step (0: every row, the same config as this arm)")
     ap.add_argument("--mesh", type=int, default=1, help="also time the mesh configurations (1) or not (0)")
-    ap.add_argument("--uneven-instances", type=int, default=8,
+    ap.add_argument("--uneven-instances", type=int, default=32,
                     help="instances of the uneven-batch sample (0: skip; the configuration has 512)")
     ap.add_argument("--distance", type=int, default=1,
                     help="also time meshSelfDistance, the closest-point batches and the penalty forces (1) or not (0)")
@@ -70,6 +71,8 @@ def parse():
     ap.add_argument("--cloth-grid", type=int, default=256)
     ap.add_argument("--cloth-level", type=int, default=6)
     ap.add_argument("--cloth-steps", type=int, default=50)
+    ap.add_argument("--detail-out", default=os.path.join(ROOT, "gpurun_out", "bench_detail.json"),
+                    help="where the full results go (the printed line is their summary)")
     return ap.parse_args()
 
 
@@ -182,6 +185,93 @@ def compare_results(h_ref, t_ref, h, t):
             "t_bit_identical": bool(np.array_equal(tr.view(np.uint64), tg.view(np.uint64)))}
 
 
+def workload_config(args) -> dict:
+    """The workload both arms run (identical in the reference arm's line)."""
+    return {"workload": f"raw narrow-phase batch, {args.n_vf:,} VF + {args.n_ee:,} EE swept quadruples, eta=1e-6, "
+                        "20% near-degenerate",
+            "rows_per_step": args.n_vf + args.n_ee, "bytes_per_step": 192 * (args.n_vf + args.n_ee),
+            "l2": "inputs larger than L2 (129 MB); no flush"}
+
+
+def compact(d, keys):
+    return None if d is None else {k: d[k] for k in keys if k in d}
+
+
+def round_floats(x, digits=5):
+    """Shortens the floats of the bench line (the line must stay a few KB)."""
+    if isinstance(x, float):
+        return float(f"{x:.{digits}g}")
+    if isinstance(x, dict):
+        return {k: round_floats(v, digits) for k, v in x.items()}
+    if isinstance(x, list):
+        return [round_floats(v, digits) for v in x]
+    return x
+
+
+def parity_summary(parity):
+    """False negatives / positives and contact-time error of the headline
+    path over every row, against the oracle (else the plain FP64 GPU path)."""
+    if not parity:
+        return None
+    ref = parity.get("cull_refine_vs_oracle") or parity["cull_refine_vs_fp64_path"]
+    out = {"vs": "oracle" if "cull_refine_vs_oracle" in parity else "fp64_path",
+           "rows": "all rows of both kinds"}
+    for key in ("false_negatives", "false_positives"):
+        out[key] = sum(ref[k][key] for k in ref)
+    out["hits"] = sum(ref[k]["hits"] for k in ref)
+    out["max_rel_t_err"] = max(ref[k]["max_rel_t_err"] for k in ref)
+    out["t_bit_identical"] = all(ref[k]["t_bit_identical"] for k in ref)
+    st = parity.get("refine_all_vs_fp64_path")
+    if st:
+        out["staged_fp64_identical"] = all(st[k]["false_negatives"] == 0 and st[k]["false_positives"] == 0 and
+                                           st[k]["t_bit_identical"] for k in st)
+    return out
+
+
+def mesh_summary(mesh, uneven):
+    """Mesh configurations in a few numbers: step time, parity against the
+    oracle (identical candidate and colliding sets) and the traversal's
+    roofline."""
+    if not mesh and not uneven:
+        return None
+    out = {}
+    if mesh:
+        c1 = mesh.get("two_spheres_kdop", {})
+        out["two_spheres"] = {"ms_per_step": c1.get("ms_per_step"),
+                              "identical": _identical(c1.get("parity"))}
+        c3 = mesh.get("cloth_on_sphere_kdop", {})
+        tr = c3.get("traversal", {})
+        out["cloth_on_sphere"] = {"faces": c3.get("faces"), "ms_per_step": c3.get("ms_per_step"),
+                                  "identical": _identical(c3.get("parity")),
+                                  "checked_steps": (c3.get("parity") or {}).get("steps"),
+                                  "traversal": {"frac": tr.get("frac"), "achieved_gbs": tr.get("achieved_gbs"),
+                                                "ms": tr.get("traversal_ms")}}
+    if uneven:
+        out["uneven_batch"] = {"instances": uneven.get("instances"), "faces": uneven.get("faces"),
+                               "ms": uneven["one_call"]["ms"], "value": uneven["one_call"]["value"],
+                               "per_instance_ms": uneven.get("per_instance_calls", {}).get("ms"),
+                               "identical": _identical(uneven.get("parity"))}
+    return out
+
+
+def _identical(par):
+    if not par:
+        return None
+    return bool(par["identical_candidates"] and par["identical_collisions"] and par["max_rel_t_err"] <= 1e-12)
+
+
+def write_detail(args, detail) -> str:
+    """Writes the bench's full results beside the one-line summary."""
+    path = args.detail_out
+    try:
+        os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+        with open(path, "w") as fh:
+            json.dump(detail, fh, indent=1, default=str)
+    except OSError as exc:
+        return f"not written: {exc}"
+    return os.path.relpath(path, ROOT) if os.path.abspath(path).startswith(ROOT) else path
+
+
 def cpu_baseline(vf, ee, max_rows=None, results=None):
     """The oracle restatement of the reference's CPU path on all host cores.
     With `results` (a dict), the oracle's (hit, t) per kind go into it too:
@@ -242,17 +332,24 @@ def mesh_section(ctx, stream, rank, args):
 
         torch.cuda.synchronize()
 
-    def oracle_steps(frames, faces, eta, idx):
+    def oracle_steps(m, frames, faces, eta, idx):
+        """The oracle's broad and narrow phase on steps idx, timed, and each
+        step's candidate and colliding sets checked against the GPU's."""
         t_bp = t_np = 0.0
+        checks = []
         for k in idx:
+            m.set_positions(frames[k], frames[k + 1])
+            col = m.detect(C.BROADPHASE_KDOP13, eta, eta, path=C.PATH_CULL_REFINE)
+            cand = m.candidates()
             t0 = time.perf_counter()
             vf, ee = orc.broadphase(0, frames[k], frames[k + 1], faces, eta)
             t1 = time.perf_counter()
-            orc.narrowphase(frames[k], frames[k + 1], vf, eta, ee, eta, nthreads=threads)
+            out = orc.narrowphase(frames[k], frames[k + 1], vf, eta, ee, eta, nthreads=threads)
             t2 = time.perf_counter()
             t_bp += t1 - t0
             t_np += t2 - t1
-        return 1e3 * t_bp / len(idx), 1e3 * t_np / len(idx)
+            checks.append(O.compare_step_results(vf, ee, out, cand, col))
+        return 1e3 * t_bp / len(idx), 1e3 * t_np / len(idx), O.merge_checks(checks, idx)
 
     # Two level-3 icospheres (2 x 642 v / 1,280 f), 0.8 approach + N(0, 0.01) jitter.
     qs, qe, f = W.two_spheres(seed=1)
@@ -265,10 +362,11 @@ def mesh_section(ctx, stream, rank, args):
             out[f"two_spheres_{label}"] = {
                 "ms_per_step": ms, "stencil_tests_per_step": tests // 20, "collisions_per_step": hits // 20,
                 "value": (tests // 20) / (ms / 1e3), "unit": "stencil tests/s"}
-    if rank == 0:
-        bp, nph = oracle_steps(frames, f, 1e-6, [0])
-        out["two_spheres_kdop"]["cpu_oracle"] = {"broadphase_ms": bp, "narrowphase_ms": nph,
-                                                 "cores": {"broadphase": 1, "narrowphase": threads}}
+        if rank == 0:
+            bp, nph, par = oracle_steps(m, frames, f, 1e-6, [0])
+            out["two_spheres_kdop"]["cpu_oracle"] = {"broadphase_ms": bp, "narrowphase_ms": nph,
+                                                     "cores": {"broadphase": 1, "narrowphase": threads}}
+            out["two_spheres_kdop"]["parity"] = par
     # Cloth on sphere: sheet + level-6 icosphere, one step per frame pair.
     faces, frames = W.cloth_frames(grid=args.cloth_grid, level=args.cloth_level, seed=0, steps=args.cloth_steps)
     with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3) as m:
@@ -304,11 +402,13 @@ def mesh_section(ctx, stream, rank, args):
             "broadphase_ms": statistics.median(bpms), "algorithmic_bytes": algo,
             "achieved_gbs": algo / (tms / 1e3) / 1e9, "peak_gbs": peak, "frac": algo / (tms / 1e3) / 1e9 / peak,
             "note": "the tree (about 300 B per face: two 128 B slab records and the links) fits in L2, so DRAM is not what bounds this traversal"}
-    if rank == 0:
-        idx = [len(frames) - 2, len(frames) // 2]
-        bp, nph = oracle_steps(frames, faces, 1e-6, idx)
-        out["cloth_on_sphere_kdop"]["cpu_oracle"] = {"broadphase_ms": bp, "narrowphase_ms": nph, "sample_steps": idx,
-                                                    "cores": {"broadphase": 1, "narrowphase": threads}}
+        if rank == 0:
+            idx = [len(frames) - 2, len(frames) // 2, 0]
+            bp, nph, par = oracle_steps(m, frames, faces, 1e-6, idx)
+            out["cloth_on_sphere_kdop"]["cpu_oracle"] = {"broadphase_ms": bp, "narrowphase_ms": nph,
+                                                        "sample_steps": idx,
+                                                        "cores": {"broadphase": 1, "narrowphase": threads}}
+            out["cloth_on_sphere_kdop"]["parity"] = par
     return out
 
 
@@ -594,7 +694,7 @@ def serving_section(args):
     return out
 
 
-def uneven_section(args):
+def uneven_section(args, rank):
     """Uneven batch: independent mesh instances (icospheres and grid-sheet
     pairs, triangle counts log-uniform in [200, 2e5], rigid + jitter motion)
     detected in one call on a mesh of instances, against the same instances
@@ -612,12 +712,36 @@ def uneven_section(args):
         m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6, fetch=False)  # warm-up
         t0 = time.perf_counter()
         m.set_positions(frames[0], frames[1])
-        m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6)
+        col = m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6)
         dt = time.perf_counter() - t0
         st = m.stats()
+        cand = m.candidates()
     tests = st["n_vf"] + st["n_ee"]
     out["one_call"] = {"ms": 1e3 * dt, "stencil_tests": tests, "collisions": st["vf_hits"] + st["ee_hits"],
                        "value": tests / dt, "unit": "stencil tests/s"}
+    if rank == 0:
+        # every instance through the oracle alone (instances are never paired)
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        orc = O.Oracle()
+        parts = {"vf_c": [], "ee_c": [], "vf_hit": [], "ee_hit": [], "vf_t": [], "ee_t": []}
+        t0 = time.perf_counter()
+        for i in range(n):
+            a, b = 3 * vo[i], 3 * vo[i + 1]
+            qs, qe = frames[0][a:b], frames[1][a:b]
+            fi = faces[fo[i]:fo[i + 1]] - vo[i]
+            vf_c, ee_c = orc.broadphase(0, qs, qe, fi, 1e-6)
+            r = orc.narrowphase(qs, qe, vf_c, 1e-6, ee_c, 1e-6, nthreads=os.cpu_count() or 1)
+            parts["vf_c"].append(vf_c + vo[i])
+            parts["ee_c"].append(ee_c + vo[i])
+            for k in ("vf_hit", "ee_hit", "vf_t", "ee_t"):
+                parts[k].append(r[k])
+        cat = {k: np.concatenate(v) for k, v in parts.items()}
+        par = O.compare_step_results(cat["vf_c"], cat["ee_c"], cat, cand, col)
+        par["instances"] = n
+        par["oracle_s"] = time.perf_counter() - t0
+        out["parity"] = par
     # One mesh at a time (created and freed outside the timed steps).
     hits, dt1 = 0, 0.0
     for i in range(n):
@@ -702,10 +826,14 @@ def graph_section(ctx, stream, args):
 
 
 def run_reference(args, rank, world, pg):
+    """The reference's CPU path (the oracle restatement, all host threads) on
+    the same workload and config as this arm's line: every row of both kinds
+    per step unless --ref-sample bounds it."""
     if rank != 0:
         return
     vf, ee = workload(args.n_vf, args.n_ee)
-    m = min(args.ref_sample, vf.shape[0], ee.shape[0])
+    m_vf = min(args.ref_sample, vf.shape[0]) if args.ref_sample else vf.shape[0]
+    m_ee = min(args.ref_sample, ee.shape[0]) if args.ref_sample else ee.shape[0]
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
@@ -714,23 +842,24 @@ def run_reference(args, rank, world, pg):
     threads = os.cpu_count() or 1
     times = []
     for step in range(args.warmup + args.steps):
-        off = (step * m) % max(1, vf.shape[0] - m + 1)
+        o_vf = (step * m_vf) % max(1, vf.shape[0] - m_vf + 1)
+        o_ee = (step * m_ee) % max(1, ee.shape[0] - m_ee + 1)
         t0 = time.perf_counter()
-        orc.batch(0, vf[off:off + m], ETA, nthreads=threads)
-        orc.batch(1, ee[off:off + m], ETA, nthreads=threads)
+        orc.batch(0, vf[o_vf:o_vf + m_vf], ETA, nthreads=threads)
+        orc.batch(1, ee[o_ee:o_ee + m_ee], ETA, nthreads=threads)
         dt = time.perf_counter() - t0
         if step >= args.warmup:
             times.append(dt)
     total = sum(times)
-    value = 2 * m * len(times) / total
+    value = (m_vf + m_ee) * len(times) / total
+    sample = (f"{m_vf} VF + {m_ee} EE rows per step ({'all rows' if m_vf + m_ee == vf.shape[0] + ee.shape[0] else 'a sample'}), "
+              f"{args.steps} steps")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "raw narrow-phase batch, 10M VF + 10M EE swept quadruples, eta=1e-6",
-                   "step_sample": f"{m} VF + {m} EE rows per step"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{m} VF + {m} EE rows per step, {args.steps} steps"},
+        "config": workload_config(args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -821,18 +950,26 @@ def run_ours(args, rank, world, local, pg):
         if profile:
             t_vf, t_ee = ctx.timings(), ctx_ee.timings()
             tm = {k: t_vf[k] + t_ee[k] for k in t_vf}
+            tm["per_kind"] = {"vf": t_vf, "ee": t_ee}
             ctx.set_profiling(False)
             ctx_ee.set_profiling(False)
         return ms, tm
 
-    # plain all-FP64 GPU path on the same rows (the comparison point of the metric)
+    # The all-FP64 GPU paths on the same rows (the comparison points of the
+    # metric): the plain kernel (one thread per row, the whole test inline)
+    # and the staged refinement of every row with no FP32 stage.
     full = args.only == "all"
-    fp64_tps = None
+    fp64_tps = staged_tps = None
     if full:
         ms64, _ = timed(C.PATH_FP64, max(1, min(args.steps, 3)), 1)
         fp64_tps = rows_per_step * max(1, min(args.steps, 3)) / (ms64 / 1e3)
         # the plain FP64 path's results, to check the cull path against
         fp64_out = {name: (d[name]["hit"].cpu().numpy(), d[name]["t"].cpu().numpy()) for name in ("vf", "ee")}
+        ms_st, _ = timed(C.PATH_REFINE_ALL, 1, 1)
+        staged_tps = rows_per_step / (ms_st / 1e3)
+        staged_out = {name: (d[name]["hit"].cpu().numpy(), d[name]["t"].cpu().numpy()) for name in ("vf", "ee")}
+    # FP64 add / multiply rate of this GPU: the refinement's roofline peak
+    peak64 = ctx.fp64_peak(reps=3)
 
     # headline: FP32 cull + FP64 refine, rows resident in HBM; clocks sampled meanwhile
     with ClockSampler(local) as clk:
@@ -913,35 +1050,54 @@ def run_ours(args, rank, world, local, pg):
                "entry_point": "ccd_prim_batch (pinned host buffers; the two kinds from two host threads, one "
                               "context each)", "matches_device_path": same}
 
-    # roofline of the dominant kernel (algorithmic bytes per launch / event time)
-    peak, peak_src = measured_peaks()
-    launches_per_kind = args.steps  # one cull + one refine launch per kind per step
-    surv = counts["vf"]["survivors"] + counts["ee"]["survivors"]
-    cull_bytes = rows_per_step * 192 + surv * 4 + (rows_per_step - surv) * 1
-    refine_bytes = surv * (4 + 192 + 1 + 8)
-    cull_ms_launch = tm["cull_ms"] / (2 * launches_per_kind)
-    refine_ms_launch = tm["refine_ms"] / (2 * launches_per_kind)
-    if tm["cull_ms"] >= tm["refine_ms"]:
-        kname, bytes_launch, ms_launch = "prims_cull_kernel", cull_bytes / 2, cull_ms_launch
-    else:
-        kname, bytes_launch, ms_launch = ("staged FP64 refine of the cull survivors (stage_build, wavefront root "
-                                          "solver wave_step, stage_roots, wave_finish, stage_combine)",
-                                          refine_bytes / 2, refine_ms_launch)
-    achieved = bytes_launch / (ms_launch / 1e3) / 1e9
-    roofline = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": f"{peak_src} hbm_gbs", "traffic": None,
-                "note": "the refine is bound by FP64 issue (GB300 FP64 is 1/64 of FP32), not by HBM; its FP64 "
-                        "pipe utilisation is in the committed ncu summaries",
-                "cull_ms_per_launch": cull_ms_launch, "refine_ms_per_launch": refine_ms_launch,
-                "share": {"cull": tm["cull_ms"] / (tm["cull_ms"] + tm["refine_ms"]),
-                          "refine": tm["refine_ms"] / (tm["cull_ms"] + tm["refine_ms"])}}
+    # The refinement's roofline: the reference's FP64 operations on the rows
+    # the FP32 stage passes on (counted by the oracle over a counting
+    # scalar), per second of the refinement's launches (CUDA events on each
+    # kind's stream), against this GPU's FP64 add / multiply rate.
     oracle_out = {}
     cpu = cpu_baseline(vf, ee, results=oracle_out) if rank == 0 and full else None
+    flops = {}
+    if rank == 0 and full:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        fc = O.FlopCounter()
+        threads = os.cpu_count() or 1
+        for kind, name, arr in ((C.VERTEX_FACE, "vf", vf), (C.EDGE_EDGE, "ee", ee)):
+            n = arr.shape[0]
+            surv = torch.empty(n, dtype=torch.int32, device="cuda")
+            htmp = torch.empty(n, dtype=torch.uint8, device="cuda")
+            ns = kind_ctx[name].prim_cull_device(kind, n, d[name]["rows"].data_ptr(), d_eta.data_ptr(), 1,
+                                                 htmp.data_ptr(), surv.data_ptr())
+            idx = surv[:ns].cpu().numpy()
+            _, _, fl, tot = fc.batch(kind, arr, ETA, nthreads=threads)
+            flops[name] = {"survivors": int(ns), "flops_all_rows": int(fl.astype(np.int64).sum()),
+                           "flops_survivors": int(fl[idx].astype(np.int64).sum()), "ops": tot}
+            del surv, htmp
+    pk = tm["per_kind"]
+    refine_ms_launch = {k: pk[k]["refine_ms"] / args.steps for k in ("vf", "ee")}
+    cull_ms_launch = {k: pk[k]["cull_ms"] / args.steps for k in ("vf", "ee")}
+    roofline = None
+    if flops:
+        f_step = flops["vf"]["flops_survivors"] + flops["ee"]["flops_survivors"]
+        ms_launches = refine_ms_launch["vf"] + refine_ms_launch["ee"]
+        achieved = f_step / (ms_launches / 1e3) / 1e9
+        peak = peak64["ops_per_s"] / 1e9
+        roofline = {"kernel": "staged FP64 refine of the FP32 survivors (stage_build, wave_step, stage_roots, "
+                              "wave_finish, stage_combine)",
+                    "bound": "fp64", "achieved": achieved, "peak": peak, "unit": "GFLOP/s", "frac": achieved / peak,
+                    "peak_source": "measured: ccd_fp64_peak (own DADD/DMUL kernel, CUDA events)",
+                    "traffic": None,
+                    "flops_per_survivor": {k: flops[k]["flops_survivors"] / max(1, flops[k]["survivors"])
+                                           for k in ("vf", "ee")},
+                    "refine_ms_per_launch": refine_ms_launch, "cull_ms_per_launch": cull_ms_launch,
+                    "share_refine": (tm["refine_ms"] / (tm["cull_ms"] + tm["refine_ms"]))}
     # the FP32 cull's false negatives and the contact-time error of the
-    # headline path, against the plain FP64 GPU path and the oracle
+    # headline path, against the oracle (all rows) and the all-FP64 GPU paths
     parity = None
     if full:
-        parity = {"cull_refine_vs_fp64_path": {k: compare_results(*fp64_out[k], *gpu_out[k]) for k in gpu_out}}
+        parity = {"cull_refine_vs_fp64_path": {k: compare_results(*fp64_out[k], *gpu_out[k]) for k in gpu_out},
+                  "refine_all_vs_fp64_path": {k: compare_results(*fp64_out[k], *staged_out[k]) for k in gpu_out}}
         if oracle_out:
             parity["cull_refine_vs_oracle"] = {k: compare_results(*oracle_out[k], *gpu_out[k]) for k in gpu_out}
     mesh = mesh_section(ctx, stream, rank, args) if args.mesh and full else None
@@ -949,39 +1105,37 @@ def run_ours(args, rank, world, local, pg):
     penalty = penalty_section(ctx, rank, args) if args.distance and full else None
     velocity = velocity_filter_section(ctx, rank, args) if args.velocity and full and world == 1 else None
     serving = serving_section(args) if args.serve and full and world == 1 else None
-    uneven = uneven_section(args) if args.uneven_instances and full and world == 1 else None
+    uneven = uneven_section(args, rank) if args.uneven_instances and full and world == 1 else None
     graph = graph_section(ctx, stream, args) if args.graph_rows and full else None
 
     if rank == 0:
+        detail = {
+            "fp64_peak": peak64, "flops": flops, "survivors": {"vf": counts["vf"]["survivors"] / n_vf,
+                                                                "ee": counts["ee"]["survivors"] / n_ee},
+            "hits": {"vf": counts["vf"]["hits"], "ee": counts["ee"]["hits"]},
+            "status_flags": counts["vf"]["status_flags"] + counts["ee"]["status_flags"], "timings": tm,
+            "roofline": roofline, "parity": parity, "autotune": tune, "mesh": mesh, "distance": distance,
+            "penalty": penalty, "velocity_filter": velocity, "serving": serving, "uneven_batch": uneven,
+            "graph_small_batches": graph, "e2e": e2e}
+        detail_path = write_detail(args, detail)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "raw narrow-phase batch, 10M VF + 10M EE swept quadruples, eta=1e-6, 20% "
-                                   "near-degenerate", "rows_per_step": rows_per_step, "bytes_per_step": int(vf.nbytes + ee.nbytes),
-                       "l2": "inputs (3.84 GB) larger than L2; no flush", "path": "FP32 cull + FP64 refine",
-                       "streams": "vertex-face and edge-edge batches on two contexts / streams",
-                       "replicas": world},
-            "fp64_path": {"value": fp64_tps, "unit": UNIT, "speedup_of_value": value / (world * fp64_tps)} if fp64_tps else None,
-            "survivors": {"vf": counts["vf"]["survivors"] / n_vf, "ee": counts["ee"]["survivors"] / n_ee},
-            "hits": {"vf": counts["vf"]["hits"], "ee": counts["ee"]["hits"]},
-            "status_flags": counts["vf"]["status_flags"] + counts["ee"]["status_flags"],
-            "e2e": e2e,
-            "roofline": roofline,
-            "cpu_baseline": cpu,
-            "parity": parity,
-            "clocks": clk.summary(),
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args),
+            "path": "FP32 cull + FP64 refine; the two kinds on two contexts / streams",
             "gpu_launches": int(tm["launches"]),
-            "autotune": tune,
-            "mesh": mesh,
-            "distance": distance,
-            "penalty": penalty,
-            "velocity_filter": velocity,
-            "serving": serving,
-            "uneven_batch": uneven,
-            "graph_small_batches": graph,
+            "e2e": compact(e2e, ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step", "matches_device_path")),
+            "roofline": compact(roofline, ("kernel", "bound", "achieved", "peak", "unit", "frac", "peak_source",
+                                           "traffic", "flops_per_survivor")),
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "fp64_path": ({"plain": fp64_tps, "staged": staged_tps, "speedup_vs_plain": value / (world * fp64_tps),
+                           "speedup_vs_staged": value / (world * staged_tps)} if fp64_tps else None),
+            "parity": parity_summary(parity),
+            "mesh": mesh_summary(mesh, uneven),
+            "detail": detail_path,
         }
-        print(json.dumps(line), flush=True)
+        print(json.dumps(round_floats(line)), flush=True)
     ctx.close()
     ctx_ee.close()
 

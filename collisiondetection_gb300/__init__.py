@@ -11,6 +11,7 @@ and the synthetic workload generators.
 from . import workloads  # noqa: F401
 from ._native import (BROADPHASE_AABB, BROADPHASE_KDOP13, BROADPHASE_TRIVIAL, DISTANCE_EDGE_EDGE, DISTANCE_LINE_LINE,  # noqa: F401
                       DISTANCE_VERTEX_FACE, DISTANCE_VERTEX_PLANE, EDGE_EDGE, PATH_CULL_REFINE, PATH_FP64,
+                      PATH_REFINE_ALL,
                       ROW_WIDTH, VERTEX_EDGE, VERTEX_FACE, VERTEX_VERTEX, CcdError, Context, Mesh, Server,
                       header_functions, load)
 

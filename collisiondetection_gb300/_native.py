@@ -17,7 +17,7 @@ HEADER = os.path.join(ROOT, "include", "ccd_gb300.h")
 
 CCD_OK = 0
 VERTEX_FACE, EDGE_EDGE, VERTEX_EDGE, VERTEX_VERTEX = 0, 1, 2, 3
-PATH_FP64, PATH_CULL_REFINE = 0, 1
+PATH_FP64, PATH_CULL_REFINE, PATH_REFINE_ALL = 0, 1, 2
 BROADPHASE_KDOP13, BROADPHASE_AABB, BROADPHASE_TRIVIAL = 0, 1, 2
 DISTANCE_VERTEX_FACE, DISTANCE_EDGE_EDGE = 0, 1    # ccd_distance_batch
 DISTANCE_VERTEX_PLANE, DISTANCE_LINE_LINE = 0, 1   # ccd_distance_less_than_batch
@@ -59,6 +59,11 @@ class TuneResult(ctypes.Structure):
                 ("reserved", ctypes.c_int32), ("default_ms", ctypes.c_double), ("best_ms", ctypes.c_double)]
 
 
+class Fp64Peak(ctypes.Structure):
+    _fields_ = [("ops_per_s", ctypes.c_double), ("fma_flops_per_s", ctypes.c_double), ("ms", ctypes.c_double),
+                ("ops", ctypes.c_int64)]
+
+
 _lib = None
 
 
@@ -97,6 +102,8 @@ def load(path: str = LIB):
     L.ccd_prim_batch_device.argtypes = [_P, ctypes.c_int, ctypes.c_int, _I64, _P, _P, _I64, _P, _P, _P]
     L.ccd_autotune_prim_batch.argtypes = [_P, ctypes.c_int, _I64, _P, _P, _I64, ctypes.c_int,
                                           ctypes.POINTER(TuneResult)]
+    L.ccd_prim_cull_device.argtypes = [_P, ctypes.c_int, _I64, _P, _P, _I64, _P, _P, ctypes.POINTER(_I64)]
+    L.ccd_fp64_peak.argtypes = [_P, ctypes.c_int, ctypes.POINTER(Fp64Peak)]
     L.ccd_mesh_create.argtypes = [_P, ctypes.c_int32, ctypes.c_int32, _P, ctypes.POINTER(_P)]
     L.ccd_mesh_destroy.argtypes = [_P]
     L.ccd_mesh_create_instances.argtypes = [_P, ctypes.c_int32, _P, _P, _P, ctypes.POINTER(_P)]
@@ -313,6 +320,22 @@ class Context:
         self._check(self.lib.ccd_prim_batch_device(self.handle, kind, path, n, rows_ptr, eta_ptr, eta_count,
                                                    hit_ptr, t_ptr, status_ptr), "ccd_prim_batch_device")
 
+
+    def prim_cull_device(self, kind: int, n: int, rows_ptr: int, eta_ptr: int, eta_count: int, hit_ptr: int,
+                         survivors_ptr: int) -> int:
+        """The FP32 stage alone (ccd_prim_cull_device): rejected rows get
+        hit = 0, the others' indices go to survivors; returns their count."""
+        cnt = _I64(0)
+        self._check(self.lib.ccd_prim_cull_device(self.handle, kind, n, rows_ptr, eta_ptr, eta_count, hit_ptr,
+                                                  survivors_ptr, ctypes.byref(cnt)), "ccd_prim_cull_device")
+        return int(cnt.value)
+
+    def fp64_peak(self, reps: int = 3) -> dict:
+        """This device's FP64 add / multiply and fused multiply-add rates
+        (ccd_fp64_peak)."""
+        res = Fp64Peak()
+        self._check(self.lib.ccd_fp64_peak(self.handle, reps, ctypes.byref(res)), "ccd_fp64_peak")
+        return {f: getattr(res, f) for f, _ in Fp64Peak._fields_}
 
     def autotune_prim_batch(self, kind: int, n: int, rows_ptr: int, eta_ptr: int, eta_count: int = 1,
                             reps: int = 3) -> dict:

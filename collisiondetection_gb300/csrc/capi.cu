@@ -80,8 +80,7 @@ int check_batch_args(ccd_context *ctx, int kind, int path, int64_t n, const void
                      int64_t eta_count, const void *hit, const void *t) {
   if (!ctx) return CCD_ERR_INVALID_ARGUMENT;
   if (kind < CCD_VERTEX_FACE || kind > CCD_VERTEX_VERTEX) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown kind");
-  if (path != CCD_PATH_FP64 && path != CCD_PATH_CULL_REFINE)
-    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown path");
+  if (!valid_path(path)) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown path");
   if (n < 0 || n > INT32_MAX) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "n must be in [0, 2^31)");
   if (n == 0) return CCD_OK;
   if (!rows || !eta || !hit || !t) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null buffer");
@@ -124,10 +123,26 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
   }
   // The FP32 stage covers vertex-face, edge-edge and vertex-edge rows;
   // vertex-vertex rows (one quadratic) always take the FP64 kernel.
-  bool culled = !(path == CCD_PATH_FP64 || b.kind == CCD_VERTEX_VERTEX);
+  // CCD_PATH_REFINE_ALL runs the staged refinement of vertex-face and
+  // edge-edge rows on a list of every row instead of the cull's survivors.
+  const bool all = path == CCD_PATH_REFINE_ALL && (b.kind == CCD_VERTEX_FACE || b.kind == CCD_EDGE_EDGE);
+  bool culled = !(path == CCD_PATH_FP64 || b.kind == CCD_VERTEX_VERTEX) && (path != CCD_PATH_REFINE_ALL || all);
   if (!culled) {
     CCD_CUDA(ccd::launch_prims_fp64(b, ctx->num_sms, s));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[1], s));
+  } else if (all) {
+    int rc = ensure_stage(ctx, stage, b.n, s);
+    if (rc) return rc;
+    CCD_CUDA(ccd::launch_all_rows(b, surv, s));
+    if (pe) CCD_CUDA(cudaEventRecord(pe->ev[1], s));
+    int launches = 0;
+    ccd::StageScratch view = stage.view;
+    view.wave_steps = view.wd ? ctx->opt_wave_steps : 0;
+    view.wave_min_rows = ctx->opt_wave_min_rows;
+    view.pool_budget = ctx->opt_pool_budget;
+    CCD_CUDA(ccd::launch_stages(b, surv, view, ctx->num_sms, s, &launches));
+    if (pe) CCD_CUDA(cudaEventRecord(pe->ev[2], s));
+    if (pe) pe->stage_launches = launches;
   } else if (b.kind == CCD_VERTEX_EDGE) {
     CCD_CUDA(ccd::launch_prims_cull(b, surv, ctx->num_sms, s));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[1], s));
@@ -338,7 +353,7 @@ int ccd_prim_batch_device(ccd_context *ctx, int kind, int path, int64_t n, const
   ctx->last.rows = n;
   if (n == 0) return CCD_OK;
   CCD_CUDA(cudaSetDevice(ctx->device));
-  if (path == CCD_PATH_CULL_REFINE && ctx->surv_cap < n) {
+  if (path != CCD_PATH_FP64 && ctx->surv_cap < n) {
     CCD_CUDA(cudaStreamSynchronize(ctx->stream));
     cudaFree(ctx->d_surv);
     ctx->d_surv = nullptr;
@@ -362,6 +377,32 @@ int ccd_prim_batch_device(ccd_context *ctx, int kind, int path, int64_t n, const
   CCD_CUDA(cudaMemcpyAsync(ctx->h_counters, ctx->d_counters, sizeof(ccd::BatchCounters), cudaMemcpyDeviceToHost,
                            ctx->stream));
   ctx->pending_stats = true;
+  return CCD_OK;
+}
+
+int ccd_prim_cull_device(ccd_context *ctx, int kind, int64_t n, const double *rows, const double *eta,
+                         int64_t eta_count, uint8_t *hit, int32_t *survivors, int64_t *n_survivors) {
+  if (!ctx) return CCD_ERR_INVALID_ARGUMENT;
+  if (!n_survivors) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null survivor count");
+  *n_survivors = 0;
+  if (kind != CCD_VERTEX_FACE && kind != CCD_EDGE_EDGE && kind != CCD_VERTEX_EDGE)
+    return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "the FP32 stage takes vertex-face, edge-edge and vertex-edge rows");
+  if (n < 0 || n > INT32_MAX) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "n must be in [0, 2^31)");
+  if (n == 0) return CCD_OK;
+  if (!rows || !eta || !hit || !survivors) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null buffer");
+  if (eta_count != 1 && eta_count != n) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "eta_count must be 1 or n");
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  ccd::PrimBatch b{kind, n, rows, eta, eta_count == n && n != 1, hit, nullptr, nullptr, ctx->d_counters};
+  CCD_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(ccd::BatchCounters), ctx->stream));
+  CCD_CUDA(ccd::launch_prims_cull(b, survivors, ctx->num_sms, ctx->stream));
+  CCD_CUDA(cudaMemcpyAsync(ctx->h_counters, ctx->d_counters, sizeof(ccd::BatchCounters), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->pending_stats = false;
+  ctx->last = ccd_batch_stats{};
+  ctx->last.rows = n;
+  ctx->last.survivors = (int64_t)ctx->h_counters->survivors;
+  *n_survivors = ctx->last.survivors;
   return CCD_OK;
 }
 

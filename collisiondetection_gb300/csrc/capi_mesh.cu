@@ -582,7 +582,7 @@ int ccd_narrowphase(ccd_mesh *m, int path, int64_t n_vf, const int32_t *vf, cons
                     int8_t *ee_which) {
   if (!m) return CCD_ERR_INVALID_ARGUMENT;
   ccd_context *ctx = m->ctx;
-  if (path != CCD_PATH_FP64 && path != CCD_PATH_CULL_REFINE)
+  if (!valid_path(path))
     return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown path");
   if (n_vf < 0 || n_ee < 0 || n_vf > INT32_MAX / 4 || n_ee > INT32_MAX / 4)
     return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "stencil counts must be in [0, 2^29)");
@@ -707,7 +707,7 @@ int ccd_mesh_detect(ccd_mesh *m, int broadphase_kind, double outer_eta, double e
   if (broadphase_kind != CCD_BROADPHASE_KDOP13 && broadphase_kind != CCD_BROADPHASE_AABB &&
       broadphase_kind != CCD_BROADPHASE_TRIVIAL)
     return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown broadphase kind");
-  if (path != CCD_PATH_FP64 && path != CCD_PATH_CULL_REFINE)
+  if (!valid_path(path))
     return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "unknown path");
   CCD_CUDA(cudaSetDevice(ctx->device));
   int rc = run_broadphase(m, broadphase_kind, outer_eta);

@@ -47,14 +47,7 @@ constexpr size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign;
 constexpr size_t kCountersOff = 0;
 constexpr size_t kSurvOff = align_up(sizeof(ccd::BatchCounters));
 constexpr size_t kStageOff = kSurvOff + align_up((size_t)CCD_NOALLOC_MAX_ROWS * sizeof(int32_t));
-// stage_scratch_bytes(kTileRows), restated as a constant expression: three
-// [5][7][tile] double arrays, one [5][6][tile] double array, a [5][tile]
-// int32 array, two [5][tile] byte arrays, 6 queue words and a [tile] word
-// array, each rounded up to 256 bytes.  Checked against the function at setup.
-constexpr size_t kStageBytes = align_up(5 * 7 * kTileRows * sizeof(double)) * 3 +
-                               align_up(5 * 6 * kTileRows * sizeof(double)) + align_up(5 * kTileRows * sizeof(int32_t)) +
-                               align_up(5 * kTileRows) * 2 + align_up(6 * sizeof(unsigned)) +
-                               align_up(kTileRows * sizeof(uint32_t));
+constexpr size_t kStageBytes = ccd::stage_scratch_bytes(kTileRows);
 constexpr size_t kScratchBytes = kStageOff + kStageBytes;  // about 9.4 MB
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -78,7 +71,6 @@ int setup_current_device(DeviceSetup *out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   DeviceSetup &d = g_setup[dev];
   if (!d.ready) {
-    if (ccd::stage_scratch_bytes(kTileRows) != kStageBytes) return CCD_ERR_INVALID_ARGUMENT;  // layout drifted
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return CCD_ERR_CUDA;
     int sms = 0;
@@ -110,11 +102,16 @@ extern "C" int ccd_prim_batch_device_noalloc(int kind, int64_t n, const double *
   const ccd::StageScratch stage = ccd::stage_scratch_view(d.scratch + kStageOff, kTileRows);
   const ccd::PrimBatch b{kind, n, rows, eta, eta_count == n && n != 1, hit, t, nullptr, counters};
   if (cudaMemsetAsync(counters, 0, sizeof(ccd::BatchCounters), s) != cudaSuccess) return CCD_ERR_CUDA;
+  // The kernels of the batch entry points' cull + refine path: vertex-vertex
+  // rows (one quadratic) in FP64 directly, vertex-edge survivors by one FP64
+  // pass over the survivor list, vertex-face and edge-edge survivors by the
+  // staged refinement in tiles of kTileRows.
   cudaError_t e;
-  if (kind >= CCD_VERTEX_EDGE) {
-    // The two degenerate kinds have no FP32 stage (as in the batch entry
-    // points) and need only the counters.
+  if (kind == CCD_VERTEX_VERTEX) {
     e = ccd::launch_prims_fp64(b, d.num_sms, s);
+  } else if (kind == CCD_VERTEX_EDGE) {
+    e = ccd::launch_prims_cull(b, surv, d.num_sms, s);
+    if (e == cudaSuccess) e = ccd::launch_prims_fp64_list(b, surv, d.num_sms, s);
   } else {
     e = ccd::launch_prims_cull(b, surv, d.num_sms, s);
     int launches = 0;

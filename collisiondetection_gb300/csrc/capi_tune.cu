@@ -55,6 +55,36 @@ struct TuneBuffers {
   }
 };
 
+// FP64 throughput probe: every thread runs kChains independent chains of
+// x = x * a + b, as a DMUL and a DADD (the library is built without FMA
+// contraction) or as one DFMA.  a is just below 1 and b small, so the chains
+// stay finite and normal.  The sum is stored only if it equals an impossible
+// value, which keeps the chains live without a store per thread.
+constexpr int kPeakThreads = 256;
+constexpr int kChains = 8;
+
+template <bool FMA>
+__global__ void __launch_bounds__(kPeakThreads) fp64_chains(int iters, double a, double b, double *sink) {
+  double x[kChains];
+#pragma unroll
+  for (int k = 0; k < kChains; k++) x[k] = 1.0 + 1e-3 * (double)(threadIdx.x + k);
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < kChains; k++) {
+      if (FMA) {
+        x[k] = __fma_rn(x[k], a, b);
+      } else {
+        x[k] = x[k] * a;
+        x[k] = x[k] + b;
+      }
+    }
+  }
+  double sum = 0.0;
+#pragma unroll
+  for (int k = 0; k < kChains; k++) sum += x[k];
+  if (sum == -1.0) sink[0] = sum;
+}
+
 }  // namespace
 
 using namespace ccd_capi;
@@ -216,6 +246,54 @@ int ccd_autotune_prim_batch(ccd_context *ctx, int kind, int64_t n, const double 
   out->pool_budget = ctx->opt_pool_budget;
   out->wave_min_rows = ctx->opt_wave_min_rows;
   out->chosen = best_i;
+  return CCD_OK;
+}
+
+int ccd_fp64_peak(ccd_context *ctx, int reps, ccd_fp64_peak_result *out) {
+  if (!ctx) return CCD_ERR_INVALID_ARGUMENT;
+  if (!out) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "null result");
+  if (reps < 1 || reps > 64) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "reps must be in [1, 64]");
+  *out = ccd_fp64_peak_result{};
+  CCD_CUDA(cudaSetDevice(ctx->device));
+  int per_sm = 0;
+  CCD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fp64_chains<false>, kPeakThreads, 0));
+  const int grid = ctx->num_sms * std::max(1, per_sm);
+  const int iters = 4096;
+  double *sink = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  struct Cleanup {
+    double *&sink;
+    cudaEvent_t *ev;
+    ~Cleanup() {
+      cudaFree(sink);
+      for (int k = 0; k < 2; k++)
+        if (ev[k]) cudaEventDestroy(ev[k]);
+    }
+  } cleanup{sink, ev};
+  CCD_CUDA(cudaMalloc(&sink, sizeof(double)));
+  for (int k = 0; k < 2; k++) CCD_CUDA(cudaEventCreate(&ev[k]));
+  const double a = 0.9999999, b = 1e-7;
+  float best[2] = {0.f, 0.f};
+  for (int fma = 0; fma < 2; fma++) {
+    for (int r = 0; r <= reps; r++) {  // the first run warms up
+      CCD_CUDA(cudaEventRecord(ev[0], ctx->stream));
+      if (fma)
+        fp64_chains<true><<<grid, kPeakThreads, 0, ctx->stream>>>(iters, a, b, sink);
+      else
+        fp64_chains<false><<<grid, kPeakThreads, 0, ctx->stream>>>(iters, a, b, sink);
+      CCD_CUDA(cudaGetLastError());
+      CCD_CUDA(cudaEventRecord(ev[1], ctx->stream));
+      CCD_CUDA(cudaEventSynchronize(ev[1]));
+      float ms = 0.f;
+      CCD_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+      if (r > 0 && (best[fma] == 0.f || ms < best[fma])) best[fma] = ms;
+    }
+  }
+  const double lanes = (double)grid * kPeakThreads * kChains * iters;
+  out->ops = (int64_t)(2.0 * lanes);
+  out->ms = best[0];
+  out->ops_per_s = 2.0 * lanes / (best[0] * 1e-3);
+  out->fma_flops_per_s = 2.0 * lanes / (best[1] * 1e-3);
   return CCD_OK;
 }
 

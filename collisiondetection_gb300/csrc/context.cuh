@@ -99,6 +99,9 @@ struct ccd_context {
 
 namespace ccd_capi {
 
+inline bool valid_path(int path) {
+  return path == CCD_PATH_FP64 || path == CCD_PATH_CULL_REFINE || path == CCD_PATH_REFINE_ALL;
+}
 int fail(ccd_context *ctx, int code, const std::string &msg);
 int cuda_fail(ccd_context *ctx, cudaError_t e, const char *what);
 // Grows a staged-refinement scratch to cover min(rows, tile) survivor rows.

@@ -150,7 +150,8 @@ int check_request(const ccd_request *r) {
   if (r->broadphase_kind != CCD_BROADPHASE_KDOP13 && r->broadphase_kind != CCD_BROADPHASE_AABB &&
       r->broadphase_kind != CCD_BROADPHASE_TRIVIAL)
     return CCD_ERR_INVALID_ARGUMENT;
-  if (r->path != CCD_PATH_FP64 && r->path != CCD_PATH_CULL_REFINE) return CCD_ERR_INVALID_ARGUMENT;
+  if (r->path != CCD_PATH_FP64 && r->path != CCD_PATH_CULL_REFINE && r->path != CCD_PATH_REFINE_ALL)
+    return CCD_ERR_INVALID_ARGUMENT;
   return CCD_OK;
 }
 

@@ -5,16 +5,8 @@
 namespace ccd {
 
 namespace {
-constexpr size_t kAlign = 256;
-size_t up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+size_t up(size_t x) { return scratch_up(x); }
 }  // namespace
-
-size_t stage_scratch_bytes(int64_t cap) {
-  const size_t c = (size_t)cap;
-  return up(kMaxSlots * 7 * c * sizeof(double)) * 3 + up(kMaxSlots * 6 * c * sizeof(double)) +
-         up(kMaxSlots * c * sizeof(int32_t)) +
-         up(kMaxSlots * c) * 2 + up((kMaxSlots + 1) * sizeof(unsigned)) + up(c * sizeof(uint32_t));
-}
 
 StageScratch stage_scratch_view(void *base, int64_t cap) {
   const size_t c = (size_t)cap;
@@ -73,6 +65,20 @@ void attach_wave(StageScratch &sc, void *base) {
   sc.wave_steps = kWaveSteps;
   sc.wave_min_rows = kWaveMinRows;
   sc.pool_budget = kPoolBudget;
+}
+
+namespace {
+__global__ void all_rows(int64_t n, int32_t *list, BatchCounters *c) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) list[i] = (int32_t)i;
+  if (i == 0) c->survivors = (unsigned long long)n;
+}
+}  // namespace
+
+cudaError_t launch_all_rows(const PrimBatch &b, int32_t *list, cudaStream_t s) {
+  if (b.n <= 0) return cudaSuccess;
+  all_rows<<<(unsigned)((b.n + 255) / 256), 256, 0, s>>>(b.n, list, b.counters);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_stages(const PrimBatch &b, const int32_t *list, const StageScratch &sc, int num_sms,

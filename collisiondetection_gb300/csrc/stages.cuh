@@ -83,7 +83,18 @@ struct StageScratch {
   int pool_budget;      // steps the pool kernel gives a resumed job before handing it on
 };
 
-size_t stage_scratch_bytes(int64_t cap);
+// Bytes of the scratch for a tile of `cap` rows: three [slot][7][cap]
+// double arrays (coefficients, span bounds), one [slot][6][cap] double array
+// (roots), a [slot][cap] int32 array, two [slot][cap] byte arrays, the queue
+// words and a [cap] status array, each rounded up to 256 bytes.
+constexpr size_t kScratchAlign = 256;
+constexpr size_t scratch_up(size_t x) { return (x + kScratchAlign - 1) / kScratchAlign * kScratchAlign; }
+constexpr size_t stage_scratch_bytes(int64_t cap) {
+  return scratch_up(kMaxSlots * 7 * (size_t)cap * sizeof(double)) * 3 +
+         scratch_up(kMaxSlots * 6 * (size_t)cap * sizeof(double)) + scratch_up(kMaxSlots * (size_t)cap * sizeof(int32_t)) +
+         scratch_up(kMaxSlots * (size_t)cap) * 2 + scratch_up((kMaxSlots + 1) * sizeof(unsigned)) +
+         scratch_up((size_t)cap * sizeof(uint32_t));
+}
 // Carves the scratch arrays out of one allocation of stage_scratch_bytes(cap)
 // (no wavefront solver attached).
 StageScratch stage_scratch_view(void *base, int64_t cap);
@@ -91,6 +102,10 @@ StageScratch stage_scratch_view(void *base, int64_t cap);
 // attachment to a view.
 size_t wave_scratch_bytes(int64_t cap);
 void attach_wave(StageScratch &sc, void *base);
+
+// The list of every row (0 .. n-1) with counters->survivors = n: the input
+// of the staged refinement when no FP32 stage runs (CCD_PATH_REFINE_ALL).
+cudaError_t launch_all_rows(const PrimBatch &b, int32_t *list, cudaStream_t s);
 
 // Enqueues build/roots/combine over every tile of the survivor list.
 // Returns the number of kernels launched through *launches.
@@ -566,19 +581,17 @@ inline int stage_grid(int64_t work, int num_sms) {
 template <class Polys>
 cudaError_t run(const PrimBatch &b, const int32_t *list, const StageScratch &sc, int num_sms, cudaStream_t s,
                 int *launches) {
-  static bool smem_set = false;
-  if (!smem_set) {
-    cudaError_t e = cudaFuncSetAttribute(stage_roots<Polys>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kPoolSmem);
-    if (e != cudaSuccess) return e;
-    smem_set = true;
-  }
+  // The pool kernel's dynamic shared memory stays under the 48 KB that any
+  // launch may use without an opt-in attribute (set once per device and
+  // function), so launches from any host thread or device need no setup.
+  static_assert(kPoolSmem + 1024 <= 48 * 1024, "stage_roots needs an opt-in shared-memory attribute");
+  cudaError_t e;
   const int64_t tiles = (b.n + sc.cap - 1) / sc.cap;
   const int grid = stage_grid(sc.cap, num_sms);
   const int pool_grid = num_sms * 5;  // five 40 KB warp pools fit one SM's shared memory
   const int wave_grid = num_sms * 8;
   for (int64_t tile = 0; tile < tiles; tile++) {
-    cudaError_t e = cudaMemsetAsync(sc.queue, 0, (kMaxSlots + 1) * sizeof(unsigned), s);
+    e = cudaMemsetAsync(sc.queue, 0, (kMaxSlots + 1) * sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     stage_build<Polys><<<grid, kStageThreads, 0, s>>>(b, list, tile * sc.cap, sc);
     if (sc.wd && sc.wave_steps > 0 && b.n >= sc.wave_min_rows) {

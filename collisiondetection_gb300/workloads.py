@@ -333,15 +333,18 @@ def uneven_sizes(n_instances: int = 512, lo: float = 200.0, hi: float = 2e5, see
     return np.exp(rng.uniform(np.log(lo), np.log(hi), n_instances)).astype(int)
 
 
-def uneven_batch(n_instances: int = 512, lo: float = 200.0, hi: float = 2e5, seed: int = 0, steps: int = 1):
+def uneven_batch(n_instances: int = 512, lo: float = 200.0, hi: float = 2e5, seed: int = 0, steps: int = 1,
+                 select=None):
     """Uneven batch of independent collision queries: `n_instances` motion
     requests (motion_request) with triangle counts log-uniform in [lo, hi],
-    concatenated.  Returns (faces (F, 3) int32 with global vertex indices,
-    frames (steps + 1, 3V), vertex_offsets, face_offsets)."""
+    concatenated.  `select` (optional) keeps only the instances with those
+    indices, each exactly as in the whole batch.  Returns (faces (F, 3) int32
+    with global vertex indices, frames (steps + 1, 3V), vertex_offsets,
+    face_offsets)."""
     sizes = uneven_sizes(n_instances, lo, hi, seed)
     faces, frames, vo, fo = [], [], [0], [0]
-    for i, t in enumerate(sizes):
-        f, fr = motion_request(int(t), 100000 + seed * 10000 + i, steps=steps)
+    for i in (range(n_instances) if select is None else select):
+        f, fr = motion_request(int(sizes[i]), 100000 + seed * 10000 + i, steps=steps)
         faces.append(f + vo[-1])
         frames.append(fr.reshape(steps + 1, -1, 3))
         vo.append(vo[-1] + fr.shape[1] // 3)

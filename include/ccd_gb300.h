@@ -49,7 +49,12 @@ typedef enum {
    * hit", then the FP64 evaluation of the surviving rows only.  Same results
    * as CCD_PATH_FP64 (the FP32 stage never rejects a row that hits).
    * Vertex-vertex rows (one quadratic) are always evaluated in FP64. */
-  CCD_PATH_CULL_REFINE = 1
+  CCD_PATH_CULL_REFINE = 1,
+  /* No FP32 stage: every row through the FP64 refinement that
+   * CCD_PATH_CULL_REFINE applies to its survivors (batched root solvers for
+   * vertex-face and edge-edge rows).  Same results; the all-FP64 baseline
+   * that isolates what the FP32 stage saves. */
+  CCD_PATH_REFINE_ALL = 2
 } ccd_path;
 
 /* Counters of the most recent batch call on a context. */
@@ -148,6 +153,33 @@ int ccd_prim_batch(ccd_context *ctx, int kind, int path, int64_t n, const double
                    int64_t eta_count, uint8_t *hit, double *t);
 int ccd_prim_batch_device(ccd_context *ctx, int kind, int path, int64_t n, const double *rows, const double *eta,
                           int64_t eta_count, uint8_t *hit, double *t, uint8_t *status);
+
+/* ---------------------------------------------------------- FP32 stage alone
+ * No counterpart in the reference.  The FP32 conservative rejection of
+ * CCD_PATH_CULL_REFINE without the refinement: rows (device memory, n rows of
+ * a vertex-face, edge-edge or vertex-edge kind) that provably do not hit get
+ * hit[i] = 0; the indices of the others go to survivors[] (device, room for n,
+ * in no particular order) and their count to *n_survivors (host).  Blocks
+ * until the count is known.  For callers that schedule the FP64 work
+ * themselves, and for measuring what the FP32 stage passes on. */
+int ccd_prim_cull_device(ccd_context *ctx, int kind, int64_t n, const double *rows, const double *eta,
+                         int64_t eta_count, uint8_t *hit, int32_t *survivors, int64_t *n_survivors);
+
+/* ---------------------------------------------------------- FP64 peak
+ * No counterpart in the reference.  Measures the context device's FP64
+ * arithmetic throughput with a kernel of independent add / multiply chains
+ * and one of fused multiply-adds over every SM, timed with CUDA events on
+ * the context's stream (best of `reps`).  ops_per_s counts one operation per
+ * DADD or DMUL (the library is built without FMA contraction, so each of its
+ * FP64 additions and multiplications is one such instruction); fma_flops_per_s
+ * counts two per DFMA.  Blocks until done. */
+typedef struct {
+  double ops_per_s;        /* FP64 add + multiply instructions per second (lanes) */
+  double fma_flops_per_s;  /* 2 x FP64 fused multiply-adds per second (lanes) */
+  double ms;               /* duration of the best add / multiply run */
+  int64_t ops;             /* operations of one add / multiply run */
+} ccd_fp64_peak_result;
+int ccd_fp64_peak(ccd_context *ctx, int reps, ccd_fp64_peak_result *out);
 
 /* ---------------------------------------------------------- autotuner
  * No counterpart in the reference (its narrow phase is one scalar call per

@@ -16,6 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libccd_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libccd_ref.so")
+FLOPS_SO = os.path.join(HERE, "_build", "libccd_flops.so")
 
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -261,6 +262,35 @@ class Oracle(_Lib):
         return out
 
 
+class FlopCounter:
+    """The oracle's primitive tests over a counting scalar (oracle/flops.cpp):
+    per row, the floating-point operations the reference's op sequence
+    performs for that test (src/CTCD.cpp, src/rpoly.h)."""
+
+    CATEGORIES = ("add", "mul", "div", "sqrt", "cmp", "transcendental")
+
+    def __init__(self, path: str = FLOPS_SO):
+        self.lib = ctypes.CDLL(path)
+        self.lib.oracle_flops_batch.argtypes = [ctypes.c_int, _I64, _P, _P, ctypes.c_int, _P, _P, _P, _P,
+                                                ctypes.c_int]
+        self.lib.oracle_flops_batch.restype = None
+
+    def batch(self, kind: int, x, eta, nthreads: int = 1):
+        """Returns (hit uint8[n], t float64[n] (NaN where no hit), flops
+        uint32[n] (add + mul + div + sqrt per row), totals dict)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        n = x.shape[0]
+        eta_a = np.ascontiguousarray(np.atleast_1d(np.asarray(eta, dtype=np.float64)))
+        per = 1 if eta_a.size == n and n != 1 else 0
+        hit = np.zeros(n, np.uint8)
+        t = np.full(n, np.nan)
+        flops = np.zeros(n, np.uint32)
+        totals = np.zeros(6, np.uint64)
+        self.lib.oracle_flops_batch(kind, n, _ptr(x), _ptr(eta_a), per, _ptr(hit), _ptr(t), _ptr(flops),
+                                    _ptr(totals), nthreads)
+        return hit, t, flops, {k: int(v) for k, v in zip(self.CATEGORIES, totals)}
+
+
 class Reference(_Lib):
     """The reference's own compiled sources (development container only)."""
 
@@ -382,3 +412,44 @@ class Reference(_Lib):
         self.lib.ref_narrowphase(qstart.size // 3, _ptr(qstart), _ptr(qend), vf.shape[0], _ptr(vf), _ptr(vfe),
                                  ee.shape[0], _ptr(ee), _ptr(eee), _ptr(vh), _ptr(eh))
         return vh, eh
+
+
+def compare_mesh_step(orc: Oracle, qs, qe, faces, eta: float, candidates, collisions, nthreads: int = 1,
+                      kind: int = 0) -> dict:
+    """The oracle's broad phase (kind 0 k-DOP, 1 AABB) and CTCD narrow phase
+    on one step (qs -> qe), against a GPU step's candidate stencils
+    (vf, ee) and colliding stencils (vf, vf_t, ee, ee_t)."""
+    vf_c, ee_c = orc.broadphase(kind, qs, qe, faces, eta)
+    out = orc.narrowphase(qs, qe, vf_c, eta, ee_c, eta, nthreads=nthreads)
+    return compare_step_results(vf_c, ee_c, out, candidates, collisions)
+
+
+def compare_step_results(vf_c, ee_c, out, candidates, collisions) -> dict:
+    """The oracle's candidates (vf_c, ee_c) and narrow-phase results `out`
+    against a GPU step's candidate stencils (vf, ee) and colliding stencils
+    (vf, vf_t, ee, ee_t).  Candidate and colliding sets must be identical
+    (same stencils, same order); contact times are compared relative to the
+    oracle's."""
+    g_vf_c, g_ee_c = candidates
+    g_vf, g_vft, g_ee, g_eet = collisions
+    vh, eh = out["vf_hit"] == 1, out["ee_hit"] == 1
+    same_cand = bool(np.array_equal(vf_c, g_vf_c) and np.array_equal(ee_c, g_ee_c))
+    same_col = bool(np.array_equal(vf_c[vh], g_vf) and np.array_equal(ee_c[eh], g_ee))
+    err = 0.0
+    if same_col:
+        for ref, got in ((out["vf_t"][vh], g_vft), (out["ee_t"][eh], g_eet)):
+            if ref.size:
+                err = max(err, float(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300))))
+    return {"candidates": int(vf_c.shape[0] + ee_c.shape[0]), "collisions": int(vh.sum() + eh.sum()),
+            "identical_candidates": same_cand, "identical_collisions": same_col, "max_rel_t_err": err}
+
+
+def merge_checks(checks, steps=None) -> dict:
+    """One summary of several compare_step_results."""
+    d = {"candidates": sum(c["candidates"] for c in checks), "collisions": sum(c["collisions"] for c in checks),
+         "identical_candidates": all(c["identical_candidates"] for c in checks),
+         "identical_collisions": all(c["identical_collisions"] for c in checks),
+         "max_rel_t_err": max([c["max_rel_t_err"] for c in checks] + [0.0])}
+    if steps is not None:
+        d["steps"] = list(steps)
+    return d

@@ -124,6 +124,62 @@ def test_larger_scene_matches_oracle(ctx, oracle, label):
         assert out["vf_hit"].any() and out["ee_hit"].any()
 
 
+@pytest.fixture(scope="module")
+def cloth():
+    # The cloth-on-sphere configuration at full size: a 256 x 256 sheet
+    # (65,536 vertices, 130,050 faces) over a level-6 icosphere (40,962
+    # vertices, 81,920 faces), 50 seeded steps.
+    return W.cloth_frames(grid=256, level=6, seed=0, steps=50)
+
+
+@pytest.mark.parametrize("step", [0, 25, 49])
+def test_full_size_cloth_step_matches_oracle(ctx, oracle, cloth, step):
+    import oracle as O
+
+    faces, frames = cloth
+    assert faces.shape[0] == 211_970 and frames.shape[1] == 3 * 106_498
+    eta = 1e-6
+    with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3) as m:
+        m.set_positions(frames[step], frames[step + 1])
+        col = m.detect(C.BROADPHASE_KDOP13, eta, eta)
+        cand = m.candidates()
+    r = O.compare_mesh_step(oracle, frames[step], frames[step + 1], faces, eta, cand, col,
+                            nthreads=os.cpu_count() or 4)
+    assert r["identical_candidates"] and r["identical_collisions"], r
+    assert r["max_rel_t_err"] <= TOL and r["candidates"] > 100_000
+
+
+def test_uneven_instances_match_oracle(ctx, oracle):
+    # 32 instances of the 512-instance uneven batch (icospheres and sheet
+    # pairs; the first 32 with at most 30,000 requested triangles, so that
+    # the oracle finishes in seconds) in one instance mesh, against the
+    # oracle run on each instance alone.
+    import oracle as O
+
+    sizes = W.uneven_sizes(512, seed=0)
+    pick = [int(i) for i in np.nonzero(sizes <= 30_000)[0][:32]]
+    faces, frames, vo, fo = W.uneven_batch(512, seed=0, select=pick)
+    eta = 1e-6
+    with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3, instances=(vo, fo)) as m:
+        m.set_positions(frames[0], frames[1])
+        col = m.detect(C.BROADPHASE_KDOP13, eta, eta)
+        cand = m.candidates()
+    parts = {k: [] for k in ("vf_c", "ee_c", "vf_hit", "ee_hit", "vf_t", "ee_t")}
+    for i in range(32):
+        a, b = 3 * vo[i], 3 * vo[i + 1]
+        fi = faces[fo[i]:fo[i + 1]] - vo[i]
+        vf_c, ee_c = oracle.broadphase(0, frames[0][a:b], frames[1][a:b], fi, eta)
+        r = oracle.narrowphase(frames[0][a:b], frames[1][a:b], vf_c, eta, ee_c, eta, nthreads=os.cpu_count() or 4)
+        parts["vf_c"].append(vf_c + vo[i])
+        parts["ee_c"].append(ee_c + vo[i])
+        for k in ("vf_hit", "ee_hit", "vf_t", "ee_t"):
+            parts[k].append(r[k])
+    cat = {k: np.concatenate(v) for k, v in parts.items()}
+    r = O.compare_step_results(cat["vf_c"], cat["ee_c"], cat, cand, col)
+    assert r["identical_candidates"] and r["identical_collisions"], r
+    assert r["max_rel_t_err"] <= TOL and r["collisions"] > 0
+
+
 def test_per_stencil_eta_and_order_independence(ctx, oracle, golden):
     qs, qe, f, _, meta = _scene(golden, "spheres")
     with C.Mesh(ctx, f, qs, qe) as m:

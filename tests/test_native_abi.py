@@ -32,6 +32,9 @@ def test_null_arguments_are_rejected(lib):
     assert lib.ccd_context_destroy(None) == 0
     assert lib.ccd_prim_batch(None, 0, 0, 1, None, None, 1, None, None) == 1
     assert lib.ccd_autotune_prim_batch(None, 0, 1, None, None, 1, 3, None) == 1
+    assert lib.ccd_prim_cull_device(None, 0, 1, None, None, 1, None, None, None) == 1
+    assert lib.ccd_fp64_peak(None, 3, None) == 1
+    assert lib.ccd_prim_batch_device(None, 0, 2, 1, None, None, 1, None, None, None) == 1
     assert lib.ccd_server_create(0, 0, 1, None) == 1
     assert lib.ccd_server_destroy(None) == 0
 

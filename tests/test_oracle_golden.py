@@ -38,6 +38,41 @@ def test_primitives_bit_exact(oracle, golden_dir, kind):
     assert hit.sum() > 0 and (hit == 0).sum() > 0
 
 
+@pytest.mark.parametrize("kind", [0, 1, 2, 3])
+def test_flop_counter_runs_the_oracle(golden_dir, kind):
+    # The counting build of the primitive tests computes exactly the
+    # reference's results (same operations, same rounding), so its counts are
+    # those of the reference's op sequence on these rows.
+    import oracle as O
+
+    O.build()
+    fc = O.FlopCounter()
+    g = np.load(os.path.join(golden_dir, "prims.npz"))
+    x, eta, hit, t = g[f"x{kind}"], g[f"eta{kind}"], g[f"hit{kind}"], g[f"t{kind}"]
+    h2, t2, flops, tot = fc.batch(kind, x, eta, nthreads=4)
+    np.testing.assert_array_equal(h2, hit)
+    same = (t2.view(np.uint64) == t.view(np.uint64)) | (np.isnan(t) & np.isnan(t2))
+    assert same.all()
+    assert flops.min() > 0  # every test forms at least its first polynomial
+    assert int(flops.astype(np.int64).sum()) == tot["add"] + tot["mul"] + tot["div"] + tot["sqrt"]
+    _, _, f1, tot1 = fc.batch(kind, x, eta, nthreads=1)
+    np.testing.assert_array_equal(f1, flops)
+    assert tot1 == tot
+
+
+def test_flop_counts_of_simple_cases():
+    # Vertex-vertex rows that meet the quadratic branch with two roots: the
+    # count is the reference's fixed sequence (src/CTCD.cpp:604-692) and does
+    # not depend on the coordinates.
+    import oracle as O
+
+    fc = O.FlopCounter()
+    rows = np.array([[0, 0, 0, 1, 0, 0, 0.5, 0, 0, 0.6, 0, 0],
+                     [0, 0, 0, 2, 0, 0, 0.7, 0, 0, 1.0, 0, 0]], float)
+    h, t, flops, tot = fc.batch(3, rows, 1e-3)
+    assert flops[0] == flops[1] > 20 and tot["transcendental"] == 0 and tot["sqrt"] == 2
+
+
 def test_threaded_batch_matches_serial(oracle, golden_dir):
     g = np.load(os.path.join(golden_dir, "prims.npz"))
     for kind in range(4):

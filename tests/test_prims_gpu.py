@@ -15,7 +15,7 @@ import collisiondetection_gb300 as C
 pytestmark = pytest.mark.gpu
 
 KINDS = [C.VERTEX_FACE, C.EDGE_EDGE, C.VERTEX_EDGE, C.VERTEX_VERTEX]
-PATHS = [C.PATH_FP64, C.PATH_CULL_REFINE]
+PATHS = [C.PATH_FP64, C.PATH_CULL_REFINE, C.PATH_REFINE_ALL]
 TOL = 1e-12
 
 
@@ -92,6 +92,54 @@ def test_wavefront_batch_matches_oracle(ctx, oracle, kind):
     ctx.set_profiling(False)
     _assert_same(h, t, h_ref, t_ref, f"kind {kind} wavefront")
     assert tm["launches"] > 10  # cull, build, wavefront steps, tail, combine
+
+
+@pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE])
+def test_refine_all_equals_fp64_at_wavefront_size(ctx, kind):
+    # Every row through the staged refinement (no FP32 stage): the wavefront
+    # solver runs (more than 2^18 rows) and every result is the plain
+    # kernel's, bit for bit.
+    rows = C.workloads.primitive_batch(kind, 600_000, seed=77)
+    h64, t64 = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_FP64)
+    ha, ta = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_REFINE_ALL)
+    st = ctx.stats()
+    np.testing.assert_array_equal(ha, h64)
+    np.testing.assert_array_equal(ta[h64 == 1].view(np.uint64), t64[h64 == 1].view(np.uint64))
+    assert st["survivors"] == rows.shape[0] and st["hits"] == int(h64.sum())
+
+
+@pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE, C.VERTEX_EDGE])
+def test_cull_alone_keeps_every_hit(ctx, oracle, kind):
+    torch = pytest.importorskip("torch")
+    rows = C.workloads.primitive_batch(kind, 100_000, seed=31)
+    h_ref, _ = oracle.batch(kind, rows, 1e-6, nthreads=os.cpu_count() or 4)
+    n = rows.shape[0]
+    d_rows = torch.from_numpy(rows).cuda()
+    d_eta = torch.full((1,), 1e-6, dtype=torch.float64, device="cuda")
+    d_hit = torch.full((n,), 7, dtype=torch.uint8, device="cuda")
+    d_surv = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    ns = ctx.prim_cull_device(kind, n, d_rows.data_ptr(), d_eta.data_ptr(), 1, d_hit.data_ptr(), d_surv.data_ptr())
+    surv = np.sort(d_surv.cpu().numpy()[:ns])
+    hit = d_hit.cpu().numpy()
+    assert 0 < ns < n and np.unique(surv).size == ns and surv[0] >= 0 and surv[-1] < n
+    kept = np.zeros(n, bool)
+    kept[surv] = True
+    assert np.all(hit[~kept] == 0) and np.all(hit[kept] == 7)  # rejected rows only are written
+    assert not np.any((h_ref == 1) & ~kept)  # no hit is rejected
+    # the same survivors as the cull + refine path counts
+    ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_CULL_REFINE)
+    assert ctx.stats()["survivors"] == ns
+    with pytest.raises(C.CcdError):
+        ctx.prim_cull_device(C.VERTEX_VERTEX, n, d_rows.data_ptr(), d_eta.data_ptr(), 1, d_hit.data_ptr(),
+                             d_surv.data_ptr())
+
+
+def test_fp64_peak_is_plausible(ctx):
+    p = ctx.fp64_peak(reps=2)
+    # GB300: about 1.2 TFLOP/s of FP64 FMA; DADD / DMUL issue at the same rate
+    assert 1e11 < p["ops_per_s"] < 1e13 and 1e11 < p["fma_flops_per_s"] < 1e13
+    assert p["ms"] > 0 and p["ops"] > 0
 
 
 def test_t_untouched_on_miss_and_eta_per_row(ctx):

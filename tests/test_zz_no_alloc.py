@@ -1,11 +1,14 @@
 """The allocation-free batch entry point (ccd_prim_batch_device_noalloc)
 against the context batch entry point (ccd_prim_batch_device, cull + refine)
-on the same device inputs, two calls in a row.  Collected last on purpose:
-it must pass after the other GPU tests as well as alone in a fresh process.
+and the oracle on the same device inputs: two full-size calls in a row, then
+smaller calls over the scratch the last one left, with the device's free
+memory unchanged across them.  Collected last on purpose: it must pass after
+the other GPU tests as well as alone in a fresh process.
 
 Tolerance: identical hit flags; contact times within 1e-12 relative (the two
 entry points run the same kernels, so they agree exactly in practice)."""
 import ctypes
+import os
 import re
 
 import numpy as np
@@ -44,7 +47,7 @@ def setup():
 
 @pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE, C.VERTEX_EDGE, C.VERTEX_VERTEX])
 @pytest.mark.parametrize("per_row_eta", [False, True])
-def test_noalloc_matches_batch_entry_point(setup, kind, per_row_eta):
+def test_noalloc_matches_batch_entry_point(setup, oracle, kind, per_row_eta):
     torch, ctx, fn, stream = setup
     n = _max_rows()
     rows = W.primitive_batch(kind, n, seed=11 + kind)
@@ -62,20 +65,34 @@ def test_noalloc_matches_batch_entry_point(setup, kind, per_row_eta):
     ctx.synchronize()
     h_ref, t_ref = ref_hit.cpu().numpy(), ref_t.cpu().numpy()
     assert h_ref.any()
-    for _ in range(2):
+    # the oracle agrees with the context entry point on these rows
+    h_orc, t_orc = oracle.batch(kind, rows, eta if per_row_eta else eta[0], nthreads=os.cpu_count() or 4)
+    np.testing.assert_array_equal(h_ref, h_orc)
+
+    def call(m):
+        """The first m rows through the allocation-free entry point, with hit
+        starting at a sentinel so that a row it never writes shows."""
         with torch.cuda.stream(stream):
-            hit.zero_()
+            hit.fill_(7)
             t.fill_(float("nan"))
-        rc = fn(kind, n, d_rows.data_ptr(), d_eta.data_ptr(), eta.size, hit.data_ptr(), t.data_ptr(),
-                stream.cuda_stream)
+        e = eta.size if eta.size == 1 else m
+        rc = fn(kind, m, d_rows.data_ptr(), d_eta.data_ptr(), e, hit.data_ptr(), t.data_ptr(), stream.cuda_stream)
         assert rc == 0, f"status {rc}"
         stream.synchronize()
         h, tt = hit.cpu().numpy(), t.cpu().numpy()
-        np.testing.assert_array_equal(h, h_ref)
-        m = h_ref == 1
-        rel = np.abs(tt[m] - t_ref[m]) / np.maximum(np.abs(t_ref[m]), 1e-300)
-        assert rel.max() <= TOL
-        assert np.isnan(tt[~m]).all()  # t is written only where hit
+        assert np.isin(h[:m], (0, 1)).all() and (h[m:] == 7).all()
+        np.testing.assert_array_equal(h[:m], h_ref[:m])
+        mk = h_ref[:m] == 1
+        for ref in (t_ref, t_orc):
+            rel = np.abs(tt[:m][mk] - ref[:m][mk]) / np.maximum(np.abs(ref[:m][mk]), 1e-300)
+            assert not mk.any() or rel.max() <= TOL
+        assert np.isnan(tt[:m][~mk]).all()  # t is written only where hit
+
+    call(n)  # the first call on the device may do the setup
+    free0 = torch.cuda.mem_get_info()[0]
+    for m in (n, n, 1, 5000):  # two full calls in a row, then smaller ones over the last call's scratch
+        call(m)
+    assert torch.cuda.mem_get_info()[0] == free0  # nothing was allocated
 
 
 def test_noalloc_rejects_oversized_and_bad_arguments(setup):
