@@ -403,7 +403,7 @@ def mesh_section(ctx, stream, rank, args):
             "achieved_gbs": algo / (tms / 1e3) / 1e9, "peak_gbs": peak, "frac": algo / (tms / 1e3) / 1e9 / peak,
             "note": "the tree (about 300 B per face: two 128 B slab records and the links) fits in L2, so DRAM is not what bounds this traversal"}
         if rank == 0:
-            idx = [len(frames) - 2, len(frames) // 2, 0]
+            idx = [len(frames) - 2, len(frames) // 2, (4 * len(frames)) // 5]
             bp, nph, par = oracle_steps(m, frames, faces, 1e-6, idx)
             out["cloth_on_sphere_kdop"]["cpu_oracle"] = {"broadphase_ms": bp, "narrowphase_ms": nph,
                                                         "sample_steps": idx,

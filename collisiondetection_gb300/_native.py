@@ -40,7 +40,8 @@ class MeshStats(ctypes.Structure):
     _fields_ = [("face_pairs", ctypes.c_int64), ("n_vf", ctypes.c_int64), ("n_ee", ctypes.c_int64),
                 ("vf_hits", ctypes.c_int64), ("ee_hits", ctypes.c_int64), ("slab_tests", ctypes.c_int64),
                 ("broadphase_ms", ctypes.c_float), ("traversal_ms", ctypes.c_float),
-                ("self_distance_eta", ctypes.c_double)]
+                ("self_distance_eta", ctypes.c_double), ("tree_built", ctypes.c_int32),
+                ("tree_refits", ctypes.c_int32)]
 
 
 class VelocityFilterStats(ctypes.Structure):

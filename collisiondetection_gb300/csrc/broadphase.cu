@@ -278,24 +278,34 @@ __global__ void __launch_bounds__(kThreads) build_lbvh(int n, const uint64_t *ke
   if (i == 0) parent[0] = -1;
 }
 
-// Bottom-up FP32 slab unions; the second child to arrive at a node builds it.
+// The surface of a box over its first three slabs (the x, y, z axes of both
+// layouts): the tree-quality measure behind the rebuild decision of
+// refit-only calls.
 template <int K>
-__global__ void __launch_bounds__(kThreads) refit(int n, const int32_t *child, const int32_t *parent, uint32_t *arrive,
-                                                  const float *leaf_box, float *node_box,
-                                                  unsigned long long *counters) {
+__device__ __forceinline__ float box_surface(const float (&lo)[K], const float (&hi)[K]) {
+  const float x = fmaxf(hi[0] - lo[0], 0.0f), y = fmaxf(hi[1] - lo[1], 0.0f), z = fmaxf(hi[2] - lo[2], 0.0f);
+  const float a = x * y + y * z + z * x;
+  return isfinite(a) ? a : 0.0f;
+}
+
+// Bottom-up walk from leaf s: the second child to arrive at a node builds its
+// FP32 slab union.  Returns the surface of the nodes this walk built.
+template <int K>
+__device__ __forceinline__ float refit_walk(int s, int n, const int32_t *child, const int32_t *parent,
+                                            uint32_t *arrive, const float *leaf_box, float *node_box,
+                                            unsigned long long *counters) {
   typedef BoxLayout<K> L;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
+  float area = 0.0f;
   int node = parent[(n - 1) + s];
   // Unique 64-bit keys bound the depth by 65; a longer walk means a broken
   // tree and is reported instead of followed.
   for (int level = 0; node >= 0; level++) {
     if (level > 70) {
       atomicOr(&counters[3], 2ull);
-      return;
+      return area;
     }
     __threadfence();
-    if (atomicAdd(&arrive[node], 1u) == 0) return;
+    if (atomicAdd(&arrive[node], 1u) == 0) return area;
     __threadfence();
     const int c0 = child[2 * node], c1 = child[2 * node + 1];
     float lo0[K], hi0[K], lo1[K], hi1[K];
@@ -313,8 +323,23 @@ __global__ void __launch_bounds__(kThreads) refit(int n, const int32_t *child, c
       hi0[k] = fmaxf(hi0[k], hi1[k]);
     }
     store_box_cg<K>(node_box + (int64_t)node * L::S, lo0, hi0);
+    area += box_surface<K>(lo0, hi0);
     node = parent[node];
   }
+  return area;
+}
+
+// Node slabs of the whole tree; the summed node surface goes to counters[5]
+// (a float), one atomic per warp.
+template <int K>
+__global__ void __launch_bounds__(kThreads) refit(int n, const int32_t *child, const int32_t *parent, uint32_t *arrive,
+                                                  const float *leaf_box, float *node_box,
+                                                  unsigned long long *counters) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  float area = 0.0f;
+  if (s < n) area = refit_walk<K>(s, n, child, parent, arrive, leaf_box, node_box, counters);
+  for (int o = 16; o > 0; o >>= 1) area += __shfl_xor_sync(0xffffffffu, area, o);
+  if ((threadIdx.x & 31) == 0 && area != 0.0f) atomicAdd(reinterpret_cast<float *>(&counters[5]), area);
 }
 
 // ------------------------------------------------------------------ traversal
@@ -401,6 +426,155 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
     }
   }
   if (COUNT && tests) atomicAdd(&counters[4], tests);
+}
+
+// Warp-cooperative (packet) traversal.  A warp takes 32 consecutive leaves in
+// Morton order -- spatially close queries -- and walks the tree once for all
+// of them: each stack entry holds a node and the mask of lanes whose query
+// overlapped it (a lane whose query misses a node misses its whole subtree,
+// since a parent's slab contains its children's).  At each node every lane in
+// the mask tests its own query against the two child records, which all lanes
+// load from the same addresses (one memory request per 16-byte piece for the
+// warp instead of one per lane); the lanes that pass make up the child's
+// mask.  Each lane therefore performs exactly the slab tests of its own
+// per-leaf traversal, and the stack and the record loads are shared.  Pairs
+// that pass the exact test are appended with one atomic per warp (ballot +
+// prefix of the lanes that emit).
+constexpr int kPacketWarps = 4;
+constexpr int kPacketStack = 128;
+
+__device__ __forceinline__ void emit_pairs(bool emit, int fa, int fb, uint32_t *pairs, uint64_t cap,
+                                           unsigned long long *counters) {
+  const unsigned m = __ballot_sync(0xffffffffu, emit);
+  if (!m) return;
+  const unsigned lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  const int leader = __ffs(m) - 1;
+  if ((int)lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(m));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (emit) {
+    const unsigned long long idx = base + __popc(m & ((1u << lane) - 1u));
+    if (idx < cap) {
+      pairs[2 * (int64_t)idx] = (uint32_t)fa;
+      pairs[2 * (int64_t)idx + 1] = (uint32_t)fb;
+    }
+  }
+}
+
+template <int K, bool COUNT>
+__global__ void __launch_bounds__(kPacketWarps * 32)
+    find_pairs_packet(MeshTopology topo, int n, const uint64_t *keys, uint64_t fmask, int ishift, bool multi,
+                      const int32_t *child, const int32_t *range, const float *leaf_box, const float *node_box,
+                      const double *lo64, const double *hi64, uint32_t *pairs, uint64_t cap,
+                      unsigned long long *counters) {
+  typedef BoxLayout<K> L;
+  __shared__ int st_node[kPacketWarps][kPacketStack];
+  __shared__ unsigned st_mask[kPacketWarps][kPacketStack];
+  const unsigned lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int64_t first = ((int64_t)blockIdx.x * kPacketWarps + w) * 32;
+  if (first >= n || n < 2) return;  // whole warps leave together
+  const int s = (int)(first + lane);
+  const bool valid = s < n;
+  float qlo[K], qhi[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    qlo[k] = INFINITY;  // an empty box for lanes past the last leaf
+    qhi[k] = -INFINITY;
+  }
+  int a0 = -1, a1 = -1, a2 = -1, fa = 0;
+  uint64_t my_inst = 0;
+  if (valid) {
+    load_box<K>(leaf_box + (int64_t)s * L::S, qlo, qhi);
+    fa = (int)(keys[s] & fmask);
+    a0 = topo.faces[3 * fa];
+    a1 = topo.faces[3 * fa + 1];
+    a2 = topo.faces[3 * fa + 2];
+    my_inst = keys[s] >> ishift;
+  }
+  int sp = 0;
+  if (lane == 0) {
+    st_node[w][0] = 0;
+    st_mask[w][0] = __ballot_sync(0xffffffffu, valid);
+  } else {
+    __ballot_sync(0xffffffffu, valid);
+  }
+  sp = 1;
+  __syncwarp();
+  unsigned long long tests = 0;
+  // A valid tree is visited at most once per node (n - 1 internal nodes).
+  for (int visits = 0; sp > 0; visits++) {
+    if (visits >= n) {
+      if (lane == 0) atomicOr(&counters[3], 2ull);
+      return;
+    }
+    sp--;
+    const int node = st_node[w][sp];
+    const unsigned mask = st_mask[w][sp];
+    __syncwarp();
+    const bool me = (mask >> lane) & 1u;
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const int ch = child[2 * node + c];
+      if (ch < 0) {
+        const int j = ~ch;
+        const bool test = me && j > s && (!multi || (keys[j] >> ishift) == my_inst);
+        if (COUNT && test) tests++;
+        bool emit = false;
+        int fb = 0;
+        if (__any_sync(0xffffffffu, test)) {
+          float blo[K], bhi[K];
+          load_box<K>(leaf_box + (int64_t)j * L::S, blo, bhi);
+          bool sep = !test;
+#pragma unroll
+          for (int k = 0; k < K; k++) sep |= (qhi[k] < blo[k]) || (bhi[k] < qlo[k]);
+          fb = (int)(keys[j] & fmask);
+          if (!sep) {
+            // Mesh::neighboringFaces (src/Mesh.cpp:13-20) before the FP64
+            // test: most overlapping leaf pairs are adjacent faces.
+            const int b0 = topo.faces[3 * fb], b1 = topo.faces[3 * fb + 1], b2 = topo.faces[3 * fb + 2];
+            sep = a0 == b0 || a0 == b1 || a0 == b2 || a1 == b0 || a1 == b1 || a1 == b2 || a2 == b0 || a2 == b1 ||
+                  a2 == b2;
+            // The reference's exact FP64 test (KDOPBroadPhase.cpp:132-137).
+            for (int k = 0; k < K && !sep; k++)
+              sep = (hi64[(int64_t)k * topo.nf + fa] < lo64[(int64_t)k * topo.nf + fb]) ||
+                    (hi64[(int64_t)k * topo.nf + fb] < lo64[(int64_t)k * topo.nf + fa]);
+            emit = !sep;
+          }
+        }
+        emit_pairs(emit, fa, fb, pairs, cap, counters);
+      } else {
+        const bool test = me && range[2 * ch + 1] > s && (!multi || (keys[range[2 * ch]] >> ishift) <= my_inst);
+        if (COUNT && test) tests++;
+        bool hit = false;
+        if (__any_sync(0xffffffffu, test)) {
+          float blo[K], bhi[K];
+          load_box<K>(node_box + (int64_t)ch * L::S, blo, bhi);
+          bool sep = !test;
+#pragma unroll
+          for (int k = 0; k < K; k++) sep |= (qhi[k] < blo[k]) || (bhi[k] < qlo[k]);
+          hit = !sep;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (m) {
+          if (sp >= kPacketStack) {  // deeper than any valid tree: reported as an error
+            if (lane == 0) atomicOr(&counters[3], 1ull);
+            return;
+          }
+          if (lane == 0) {
+            st_node[w][sp] = ch;
+            st_mask[w][sp] = m;
+          }
+          sp++;
+          __syncwarp();
+        }
+      }
+    }
+  }
+  if (COUNT) {
+    tests = __reduce_add_sync(0xffffffffu, (unsigned)tests);
+    if (lane == 0 && tests) atomicAdd(&counters[4], tests);
+  }
 }
 
 // ------------------------------------------------------------------ stencils
@@ -766,7 +940,8 @@ void broadphase_free(BroadphaseBuffers &b) {
 // candidate face pairs exceed 2^27.
 int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, BroadphaseBuffers &b, int32_t **vf_out,
                    int64_t *vf_cap, int32_t **ee_out, int64_t *ee_cap, int64_t *n_vf, int64_t *n_ee,
-                   int64_t *n_pairs, int64_t *slab_tests, int num_sms, cudaStream_t s, cudaError_t *err) {
+                   int64_t *n_pairs, int64_t *slab_tests, int num_sms, cudaStream_t s, cudaError_t *err,
+                   bool *rebuilt) {
   (void)num_sms;
   *n_vf = *n_ee = *n_pairs = 0;
   const int nf = topo.nf;
@@ -832,16 +1007,34 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
     leaf_slabs<3><<<grid_of(nf), kThreads, 0, s>>>(topo, p, ax, b.lo64, b.hi64, flo, fhi, b.bounds);
   BP_CUDA(cudaGetLastError());
   const KeyBits kb = key_bits(topo);
-  morton_keys<<<grid_of(nf), kThreads, 0, s>>>(nf, flo, fhi, b.bounds, topo.ninst > 1 ? topo.face_inst : nullptr, kb,
-                                                b.keys);
-  BP_CUDA(cudaGetLastError());
-  BP_CUDA(radix_sort_u64(b.keys, (uint64_t *)b.vals, nullptr, nullptr, nf, 0, kb.ishift + kb.ibits, b.temp,
-                         b.temp_bytes, s));
+  // Refit only: the kept tree's leaf order and links stay, its node slabs are
+  // rebuilt from the new leaf slabs.  Otherwise a new tree: Morton keys of
+  // the slab centres, radix sort, Karras hierarchy.
+  const bool reuse = p.refit && b.tree_kind == p.kind && b.tree_nf == nf && b.tree_ninst == topo.ninst &&
+                     !b.rebuild_next && b.refits < p.max_refits;
+  if (rebuilt) *rebuilt = !reuse;
+  if (!reuse) {
+    morton_keys<<<grid_of(nf), kThreads, 0, s>>>(nf, flo, fhi, b.bounds, topo.ninst > 1 ? topo.face_inst : nullptr,
+                                                  kb, b.keys);
+    BP_CUDA(cudaGetLastError());
+    BP_CUDA(radix_sort_u64(b.keys, (uint64_t *)b.vals, nullptr, nullptr, nf, 0, kb.ishift + kb.ibits, b.temp,
+                           b.temp_bytes, s));
+  }
   if (kdop)
     gather_leaves<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, flo, fhi, b.leaf_box);
   else
     gather_leaves<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, flo, fhi, b.leaf_box);
-  build_lbvh<<<grid_of(nf - 1), kThreads, 0, s>>>(nf, b.keys, b.node_child, b.node_range, b.parent);
+  if (!reuse) {
+    build_lbvh<<<grid_of(nf - 1), kThreads, 0, s>>>(nf, b.keys, b.node_child, b.node_range, b.parent);
+    b.tree_kind = p.kind;
+    b.tree_nf = nf;
+    b.tree_ninst = topo.ninst;
+    b.refits = 0;
+    b.build_area = -1.0f;
+  } else {
+    b.refits++;
+  }
+  b.rebuild_next = false;
   BP_CUDA(cudaMemsetAsync(b.arrive, 0, (size_t)nf * sizeof(uint32_t), s));
   BP_CUDA(cudaMemsetAsync(b.counters, 0, 8 * sizeof(unsigned long long), s));
   if (kdop)
@@ -855,6 +1048,20 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[1], s));
   auto traverse = [&]() {
     const bool multi = topo.ninst > 1;
+    if (p.traversal == kTraversalPacket) {
+      const unsigned grid = (unsigned)((nf + 32 * kPacketWarps - 1) / (32 * kPacketWarps));
+#define BP_FIND(KK, CC)                                                                                         \
+  find_pairs_packet<KK, CC><<<grid, kPacketWarps * 32, 0, s>>>(topo, nf, b.keys, kb.fmask, kb.ishift, multi,   \
+                                                               b.node_child, b.node_range, b.leaf_box,         \
+                                                               b.node_box, b.lo64, b.hi64, b.pairs,            \
+                                                               (uint64_t)b.cap_pairs, b.counters)
+      if (kdop && p.count_tests) BP_FIND(13, true);
+      else if (kdop) BP_FIND(13, false);
+      else if (p.count_tests) BP_FIND(3, true);
+      else BP_FIND(3, false);
+#undef BP_FIND
+      return;
+    }
 #define BP_FIND(KK, CC)                                                                                           \
   find_pairs<KK, CC><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, kb.fmask, kb.ishift, multi, b.node_child, \
                                                       b.node_range, b.leaf_box, b.node_box,                     \
@@ -872,10 +1079,24 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
     traverse();
     BP_CUDA(cudaGetLastError());
     if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[2], s));
-    unsigned long long hc[5];
+    unsigned long long hc[6];
     BP_CUDA(cudaMemcpyAsync(hc, b.counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
     BP_CUDA(cudaStreamSynchronize(s));
-    if (hc[3]) return 3;
+    if (hc[3]) {
+      b.tree_kind = -1;  // never refit a tree that failed
+      return 3;
+    }
+    {
+      // Tree quality: the summed node surface against its value after the
+      // build; a kept tree whose nodes have grown too much is rebuilt next.
+      float area;
+      const uint32_t bits = (uint32_t)hc[5];
+      memcpy(&area, &bits, sizeof(area));
+      if (b.build_area < 0.0f)
+        b.build_area = area;
+      else if (!(area <= p.rebuild_ratio * b.build_area))
+        b.rebuild_next = true;
+    }
     *n_pairs = hc[0];
     if (slab_tests) *slab_tests = (int64_t)hc[4];
     if ((int64_t)hc[0] <= b.cap_pairs) break;

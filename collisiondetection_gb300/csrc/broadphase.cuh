@@ -64,7 +64,17 @@ struct BroadphaseBuffers {
   uint32_t *flags = nullptr, *scan = nullptr;
   void *temp = nullptr;
   size_t temp_bytes = 0;
+  // The tree kept from the last call (leaf order, links) for refit-only
+  // calls: valid for this kind, face count and instance count.
+  int tree_kind = -1, tree_nf = 0, tree_ninst = 0;
+  int refits = 0;            // refit-only calls since the last build
+  float build_area = -1.0f;  // summed node surface after the last build (-1: not yet measured)
+  bool rebuild_next = false;
 };
+
+// Traversal kernels: one thread per query leaf with a private stack, or one
+// warp per 32 consecutive query leaves with a shared stack (the default).
+enum TraversalKind : int { kTraversalThread = 0, kTraversalPacket = 1 };
 
 struct BroadphaseParams {
   int kind;
@@ -74,15 +84,27 @@ struct BroadphaseParams {
   const double *hpos;     // [entries][3]
   const uint8_t *fixed;   // [nv] or null
   bool count_tests;       // count the traversal's slab tests (a slower, counting variant)
+  int traversal;          // TraversalKind
+  // Keep the last call's tree and only refit its node slabs when the mesh
+  // and kind are unchanged, until the summed surface of its nodes grows by
+  // more than rebuild_ratio over its value after the build (or max_refits
+  // calls in a row).  The candidate set depends on the leaf slabs alone, so
+  // this changes speed only.
+  bool refit;
+  float rebuild_ratio;
+  int max_refits;
   cudaEvent_t ev[4];      // optional (all null or all set): start, before / after the traversal, end
 };
 
 // Runs the candidate search; on return (stream synchronised) n_vf / n_ee
 // hold the counts and vf_out / ee_out (device, [n][4] int32) the stencils in
 // the reference's order.  The output arrays are grown as needed.
+// *rebuilt (optional) tells whether this call built its tree (or refitted
+// the kept one).
 int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, BroadphaseBuffers &buf, int32_t **vf_out,
                    int64_t *vf_cap, int32_t **ee_out, int64_t *ee_cap, int64_t *n_vf, int64_t *n_ee,
-                   int64_t *n_pairs, int64_t *slab_tests, int num_sms, cudaStream_t s, cudaError_t *err);
+                   int64_t *n_pairs, int64_t *slab_tests, int num_sms, cudaStream_t s, cudaError_t *err,
+                   bool *rebuilt = nullptr);
 
 void broadphase_free(BroadphaseBuffers &buf);
 

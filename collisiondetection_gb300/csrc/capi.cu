@@ -312,6 +312,18 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
   } else if (key == "count_slab_tests") {
     if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "count_slab_tests must be 0 or 1");
     ctx->opt_count_tests = (int)value;
+  } else if (key == "tree_refit") {
+    if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "tree_refit must be 0 or 1");
+    ctx->opt_tree_refit = (int)value;
+  } else if (key == "tree_rebuild_pct") {
+    if (value < 100 || value > 100000) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "tree_rebuild_pct must be in [100, 100000]");
+    ctx->opt_tree_rebuild_pct = (int)value;
+  } else if (key == "tree_max_refits") {
+    if (value < 0 || value > (1 << 20)) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "tree_max_refits must be in [0, 2^20]");
+    ctx->opt_tree_max_refits = (int)value;
+  } else if (key == "traversal") {
+    if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "traversal must be 0 or 1");
+    ctx->opt_traversal = (int)value;
   } else if (key == "wave_min_rows") {
     if (value < 0) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "wave_min_rows must be >= 0");
     ctx->opt_wave_min_rows = value;

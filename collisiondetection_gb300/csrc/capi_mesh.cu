@@ -280,6 +280,10 @@ int run_broadphase(ccd_mesh *m, int kind, double outer_eta, bool whole = false) 
                           m->has_history ? m->hist_pos : nullptr,
                           m->has_fixed ? m->fixed : nullptr,
                           ctx->opt_count_tests != 0,
+                          (int)ctx->opt_traversal,
+                          ctx->opt_tree_refit != 0,
+                          (float)ctx->opt_tree_rebuild_pct / 100.0f,
+                          ctx->opt_tree_max_refits,
                           {nullptr, nullptr, nullptr, nullptr}};
   const bool timed = ctx->profiling && m->nf >= 2;
   if (timed) {
@@ -302,8 +306,12 @@ int run_broadphase(ccd_mesh *m, int kind, double outer_eta, bool whole = false) 
     m->have_cand = true;
     return CCD_OK;
   }
+  bool built = true;
   const int rc = ccd::broadphase_run(topo, p, m->bp, &m->cand[0], &m->cand_cap[0], &m->cand[1], &m->cand_cap[1],
-                                     &m->n_cand[0], &m->n_cand[1], &npairs, &tests, ctx->num_sms, ctx->stream, &err);
+                                     &m->n_cand[0], &m->n_cand[1], &npairs, &tests, ctx->num_sms, ctx->stream, &err,
+                                     &built);
+  m->stats.tree_built = built ? 1 : 0;
+  m->stats.tree_refits = m->bp.refits;
   if (rc == 2) return cuda_fail(ctx, err, "broadphase");
   if (rc == 3) return mesh_fail(m, CCD_ERR_CUDA, "broadphase: malformed tree (traversal beyond its size)");
   if (rc == 4) return mesh_fail(m, CCD_ERR_OUT_OF_MEMORY, "broadphase: more than 2^27 overlapping face pairs");

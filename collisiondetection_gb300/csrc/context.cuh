@@ -90,6 +90,10 @@ struct ccd_context {
   int64_t opt_wave_min_rows = ccd::kWaveMinRows;
   int opt_pool_budget = ccd::kPoolBudget;
   int opt_count_tests = 0;
+  int opt_traversal = 1;  // broad-phase traversal: 0 thread per leaf, 1 warp per 32 leaves
+  int opt_tree_refit = 1;         // keep a mesh's tree and refit it while its quality holds
+  int opt_tree_rebuild_pct = 130;  // rebuild once the node surface exceeds this percentage of its built value
+  int opt_tree_max_refits = 64;    // ... or after this many refits in a row
   int64_t opt_layer_grid_min = 1024;  // velocity filter: groups this large fire over the whole GPU
   int64_t opt_chunk_rows = ccd_capi::kChunkRows;  // host-memory batches: rows per chunk
   int64_t opt_layer_events = (int64_t)1 << 20;      // velocity filter: firings per event-loop launch

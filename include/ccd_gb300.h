@@ -101,6 +101,17 @@ int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
  *                    default 262144
  *   "count_slab_tests" 1: the broad phase counts its traversal's slab tests
  *                    (ccd_mesh_stats.slab_tests; a slower variant); default 0
+ *   "tree_refit"     1: a mesh keeps its broad-phase tree between calls and,
+ *                    while its kind and faces are unchanged, only refits the
+ *                    node slabs to the new positions, rebuilding it when the
+ *                    summed surface of its nodes has grown past
+ *                    "tree_rebuild_pct" percent of its value after the build
+ *                    or after "tree_max_refits" refits in a row; 0: every
+ *                    call builds a new tree; defaults 1, 130, 64
+ *   "traversal"      broad-phase tree traversal: 0 one thread per query face
+ *                    with its own stack, 1 one warp per 32 query faces
+ *                    adjacent in Morton order sharing one stack and each
+ *                    node's loads; default 1
  *   "pool_budget"    further steps the unfinished polynomials get, many per
  *                    warp, before the last ones are finished one per warp
  *                    (0: no limit); default 0
@@ -268,6 +279,8 @@ typedef struct {
   float traversal_ms;  /* traversal (both 0 unless the context's profiling is on) */
   double self_distance_eta; /* ccd_mesh_self_distance: its broad phase's padding, the least
                                qualifying vertex distance (+inf if none); 0 otherwise */
+  int32_t tree_built;       /* 1: the broad phase built its tree; 0: it refitted the kept one */
+  int32_t tree_refits;      /* refit-only broad phases since the tree was last built */
 } ccd_mesh_stats;
 
 /* faces: nfaces x 3 vertex indices in [0, nverts).  Topology is fixed for the

