@@ -58,8 +58,8 @@ def parse():
                     help="velocity filter: firings per event-loop launch (0: the library's default); short launches "
                          "for profilers")
     ap.add_argument("--serve", type=int, default=1, help="also run the serving loop (1) or not (0)")
-    ap.add_argument("--serve-requests", type=int, default=24)
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0])
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 200.0, 500.0, 1000.0, 2000.0, 5000.0])
     ap.add_argument("--serve-fp64-requests", type=int, default=6)
     ap.add_argument("--graph-rows", type=int, default=4096,
                     help="rows per kind of the small-batch CUDA-graph comparison (0: skip it)")
@@ -252,6 +252,18 @@ def mesh_summary(mesh, uneven):
                                "per_instance_ms": uneven.get("per_instance_calls", {}).get("ms"),
                                "identical": _identical(uneven.get("parity"))}
     return out
+
+
+def serving_summary(serving):
+    """Per arrival rate: throughput and per-step latency percentiles."""
+    if not serving or "rates" not in serving:
+        return None
+    r = serving["rates"]
+    return {"requests": serving.get("requests"), "rates": [x["arrival_rate"] for x in r],
+            "req_s": [x["throughput_req_s"] for x in r], "step_ms_p50": [x["step_ms_p50"] for x in r],
+            "step_ms_p95": [x["step_ms_p95"] for x in r], "step_ms_p99": [x["step_ms_p99"] for x in r],
+            "collisions": [x["collisions"] for x in r],
+            "fp64_one_at_a_time_req_s": serving.get("fp64_one_at_a_time", {}).get("throughput_req_s")}
 
 
 def _identical(par):
@@ -640,8 +652,9 @@ def velocity_filter_section(ctx, rank, args):
 
 
 def serving_section(args):
-    """Serving loop: Poisson arrivals of collision queries (mesh + 10 steps of
-    seeded rigid + jitter motion, triangle counts log-uniform in [1e3, 5e5])
+    """Serving loop: Poisson arrivals of collision queries (a mesh pair that
+    closes in and touches halfway through 10 steps of seeded rigid + jitter
+    motion, triangle counts log-uniform in [1e3, 5e5])
     through the serving engine (ccd_server_*, 4 slots, 60 GB admission
     budget).  Reports throughput and per-step latency percentiles at each
     arrival rate, beside the same queries one at a time on the plain FP64
@@ -652,7 +665,7 @@ def serving_section(args):
     rng = np.random.default_rng(7)
     n_req = args.serve_requests
     sizes = np.exp(rng.uniform(np.log(1e3), np.log(5e5), n_req)).astype(int)
-    reqs = [W.motion_request(int(t), 1000 + i, steps=10) for i, t in enumerate(sizes)]
+    reqs = [W.pair_request(int(t), 1000 + i, steps=10) for i, t in enumerate(sizes)]
     out = {"requests": n_req, "steps_per_request": 10, "faces_mean": float(np.mean([f.shape[0] for f, _ in reqs])),
            "slots": 4, "memory_budget_gb": 60, "rates": []}
 
@@ -1133,6 +1146,7 @@ def run_ours(args, rank, world, local, pg):
                            "speedup_vs_staged": value / (world * staged_tps)} if fp64_tps else None),
             "parity": parity_summary(parity),
             "mesh": mesh_summary(mesh, uneven),
+            "serving": serving_summary(serving),
             "detail": detail_path,
         }
         print(json.dumps(round_floats(line)), flush=True)

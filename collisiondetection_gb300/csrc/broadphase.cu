@@ -343,28 +343,89 @@ __global__ void __launch_bounds__(kThreads) refit(int n, const int32_t *child, c
 }
 
 // ------------------------------------------------------------------ traversal
-// COUNT: also count the slab tests (leaf and node), for the traversal's
-// algorithmic bytes; a separate variant so that timed runs carry no counter.
-template <int K, bool COUNT>
-__global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n, const uint64_t *keys, uint64_t fmask,
-                                                       int ishift, bool multi,
-                                                       const int32_t *child, const int32_t *range, const float *leaf_box,
-                                                       const float *node_box, const double *lo64, const double *hi64,
-                                                       uint32_t *pairs,
+// The links a traversal needs, in 16-byte records beside the slab records so
+// that visiting a node costs one memory round trip: a stack entry holds the
+// two child references of a node whose slab the query overlapped, and a pop
+// loads both children's slab records and link records at once.
+//   node_links[i] = (child 0, child 1, first leaf, last leaf)   (child < 0: leaf ~child)
+//   leaf_links[j] = (face, its three vertices)
+//   leaf_end[j]   = first sorted leaf of a later instance (instance meshes)
+__global__ void __launch_bounds__(kThreads) link_tree(int n, const uint64_t *keys, uint64_t fmask, int ishift,
+                                                      bool multi, const int32_t *faces, const int32_t *child,
+                                                      const int32_t *range, int4 *node_links, int4 *leaf_links,
+                                                      int32_t *leaf_end) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (i < n - 1) node_links[i] = make_int4(child[2 * i], child[2 * i + 1], range[2 * i], range[2 * i + 1]);
+  const int f = (int)(keys[i] & fmask);
+  leaf_links[i] = make_int4(f, faces[3 * f], faces[3 * f + 1], faces[3 * f + 2]);
+  if (multi) {
+    // keys are sorted by instance first: binary search for the first leaf of
+    // a later instance
+    const uint64_t inst = keys[i] >> ishift;
+    int lo = i + 1, hi = n;
+    while (lo < hi) {
+      const int mid = lo + ((hi - lo) >> 1);
+      if ((keys[mid] >> ishift) > inst)
+        hi = mid;
+      else
+        lo = mid + 1;
+    }
+    leaf_end[i] = lo;
+  }
+}
+
+// The part of a face-pair test after the conservative FP32 slab test:
+// Mesh::neighboringFaces (src/Mesh.cpp:13-20) first -- most overlapping leaf
+// pairs are adjacent faces, and this integer test spares them the FP64 one
+// (FP64 compares run at 1/64 of the FP32 rate) -- then the reference's exact
+// FP64 slab test (KDOPBroadPhase.cpp:132-137, strict '<').
+template <int K>
+__device__ __forceinline__ bool exact_pair(const MeshTopology &topo, int fa, int a0, int a1, int a2, const int4 &b,
+                                           const double *lo64, const double *hi64) {
+  if (a0 == b.y || a0 == b.z || a0 == b.w || a1 == b.y || a1 == b.z || a1 == b.w || a2 == b.y || a2 == b.z ||
+      a2 == b.w)
+    return false;
+  const int fb = b.x;
+  for (int k = 0; k < K; k++)
+    if ((hi64[(int64_t)k * topo.nf + fa] < lo64[(int64_t)k * topo.nf + fb]) ||
+        (hi64[(int64_t)k * topo.nf + fb] < lo64[(int64_t)k * topo.nf + fa]))
+      return false;
+  return true;
+}
+
+template <int K>
+__device__ __forceinline__ bool slabs_overlap(const float (&qlo)[K], const float (&qhi)[K], const float (&blo)[K],
+                                              const float (&bhi)[K]) {
+  bool sep = false;
+#pragma unroll
+  for (int k = 0; k < K; k++) sep |= (qhi[k] < blo[k]) || (bhi[k] < qlo[k]);
+  return !sep;
+}
+
+// One thread per query leaf s, over the leaves after s in sorted order (each
+// pair once) and of the same instance.  COUNT: also count the slab tests
+// (leaf and node), for the traversal's algorithmic bytes; a separate variant
+// so that timed runs carry no counter.
+template <int K, bool COUNT, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) find_pairs(MeshTopology topo, int n, const int4 *node_links,
+                                                       const int4 *leaf_links, const int32_t *leaf_end,
+                                                       const float *leaf_box, const float *node_box,
+                                                       const double *lo64, const double *hi64, uint32_t *pairs,
                                                        uint64_t cap, unsigned long long *counters) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n || n < 2) return;
   typedef BoxLayout<K> L;
   float qlo[K], qhi[K];
   load_box<K>(leaf_box + (int64_t)s * L::S, qlo, qhi);
-  const int fa = (int)(keys[s] & fmask);
-  const int a0 = topo.faces[3 * fa], a1 = topo.faces[3 * fa + 1], a2 = topo.faces[3 * fa + 2];
-  // Keys are ordered by instance first: a subtree whose first leaf belongs to
-  // a later instance holds no partner of this face.
-  const uint64_t my_inst = keys[s] >> ishift;
-  int stack[kStack];
+  const int4 me = __ldg(leaf_links + s);
+  const int my_end = leaf_end ? leaf_end[s] : n;
+  int2 stack[kStack];
   int sp = 0;
-  stack[sp++] = 0;
+  {
+    const int4 root = __ldg(node_links);
+    stack[sp++] = make_int2(root.x, root.y);
+  }
   unsigned long long tests = 0;
   // A valid tree is visited at most once per node (n - 1 internal nodes).
   for (int visits = 0; sp > 0; visits++) {
@@ -372,54 +433,42 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
       atomicOr(&counters[3], 2ull);
       return;
     }
-    const int node = stack[--sp];
+    const int2 e = stack[--sp];
+    // both children's records at once
+    int4 lk[2];
+    float blo[2][K], bhi[2][K];
+#pragma unroll
     for (int c = 0; c < 2; c++) {
-      const int ch = child[2 * node + c];
+      const int ch = c ? e.y : e.x;
+      if (ch < 0) {
+        lk[c] = __ldg(leaf_links + ~ch);
+        load_box<K>(leaf_box + (int64_t)(~ch) * L::S, blo[c], bhi[c]);
+      } else {
+        lk[c] = __ldg(node_links + ch);
+        load_box<K>(node_box + (int64_t)ch * L::S, blo[c], bhi[c]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const int ch = c ? e.y : e.x;
       if (ch < 0) {
         const int j = ~ch;
-        if (j <= s) continue;
-        if (multi && (keys[j] >> ishift) != my_inst) continue;
+        if (j <= s || j >= my_end) continue;
         if (COUNT) tests++;
-        bool sep = false;
-        {
-          float blo[K], bhi[K];
-          load_box<K>(leaf_box + (int64_t)j * L::S, blo, bhi);
-#pragma unroll
-          for (int k = 0; k < K; k++) sep |= (qhi[k] < blo[k]) || (bhi[k] < qlo[k]);
-        }
-        if (sep) continue;
-        // Mesh::neighboringFaces (src/Mesh.cpp:13-20) first: most leaf pairs
-        // whose slabs overlap are adjacent faces, and this integer test spares
-        // them the FP64 one (FP64 compares run at 1/64 of the FP32 rate).
-        const int fb = (int)(keys[j] & fmask);
-        const int b0 = topo.faces[3 * fb], b1 = topo.faces[3 * fb + 1], b2 = topo.faces[3 * fb + 2];
-        if (a0 == b0 || a0 == b1 || a0 == b2 || a1 == b0 || a1 == b1 || a1 == b2 || a2 == b0 || a2 == b1 ||
-            a2 == b2)
-          continue;
-        // The reference's exact FP64 test (KDOPBroadPhase.cpp:132-137).
-        for (int k = 0; k < K && !sep; k++)
-          sep = (hi64[(int64_t)k * topo.nf + fa] < lo64[(int64_t)k * topo.nf + fb]) ||
-                (hi64[(int64_t)k * topo.nf + fb] < lo64[(int64_t)k * topo.nf + fa]);
-        if (sep) continue;
+        if (!slabs_overlap<K>(qlo, qhi, blo[c], bhi[c])) continue;
+        if (!exact_pair<K>(topo, me.x, me.y, me.z, me.w, lk[c], lo64, hi64)) continue;
         const unsigned long long idx = atomicAdd(&counters[0], 1ull);
         if (idx < cap) {
-          pairs[2 * (int64_t)idx] = (uint32_t)fa;
-          pairs[2 * (int64_t)idx + 1] = (uint32_t)fb;
+          pairs[2 * (int64_t)idx] = (uint32_t)me.x;
+          pairs[2 * (int64_t)idx + 1] = (uint32_t)lk[c].x;
         }
       } else {
-        if (range[2 * ch + 1] <= s) continue;
-        if (multi && (keys[range[2 * ch]] >> ishift) > my_inst) continue;
+        // later leaves only, and no subtree that starts in a later instance
+        if (lk[c].w <= s || lk[c].z >= my_end) continue;
         if (COUNT) tests++;
-        bool sep = false;
-        {
-          float blo[K], bhi[K];
-          load_box<K>(node_box + (int64_t)ch * L::S, blo, bhi);
-#pragma unroll
-          for (int k = 0; k < K; k++) sep |= (qhi[k] < blo[k]) || (bhi[k] < qlo[k]);
-        }
-        if (sep) continue;
+        if (!slabs_overlap<K>(qlo, qhi, blo[c], bhi[c])) continue;
         if (sp < kStack)
-          stack[sp++] = ch;
+          stack[sp++] = make_int2(lk[c].x, lk[c].y);
         else
           atomicOr(&counters[3], 1ull);  // stack overflow: reported as an error
       }
@@ -430,16 +479,17 @@ __global__ void __launch_bounds__(kThreads) find_pairs(MeshTopology topo, int n,
 
 // Warp-cooperative (packet) traversal.  A warp takes 32 consecutive leaves in
 // Morton order -- spatially close queries -- and walks the tree once for all
-// of them: each stack entry holds a node and the mask of lanes whose query
-// overlapped it (a lane whose query misses a node misses its whole subtree,
-// since a parent's slab contains its children's).  At each node every lane in
-// the mask tests its own query against the two child records, which all lanes
-// load from the same addresses (one memory request per 16-byte piece for the
-// warp instead of one per lane); the lanes that pass make up the child's
-// mask.  Each lane therefore performs exactly the slab tests of its own
-// per-leaf traversal, and the stack and the record loads are shared.  Pairs
-// that pass the exact test are appended with one atomic per warp (ballot +
-// prefix of the lanes that emit).
+// of them: each stack entry holds a node's two child references and the mask
+// of lanes whose query overlapped the node (a lane whose query misses a node
+// misses its whole subtree, since a parent's slab contains its children's).
+// At each pop every lane in the mask tests its own query against the two
+// child records, which all lanes load from the same addresses (one memory
+// request per 16-byte piece for the warp instead of one per lane); the lanes
+// that pass make up the child's mask.  Each lane therefore performs exactly
+// the slab tests of its own per-leaf traversal; the stack and the loads are
+// shared, and the chain of visits is the union of the lanes' traversals.
+// Pairs that pass the exact test are appended with one atomic per warp
+// (ballot + prefix of the lanes that emit).
 constexpr int kPacketWarps = 4;
 constexpr int kPacketStack = 128;
 
@@ -462,13 +512,12 @@ __device__ __forceinline__ void emit_pairs(bool emit, int fa, int fb, uint32_t *
 }
 
 template <int K, bool COUNT>
-__global__ void __launch_bounds__(kPacketWarps * 32)
-    find_pairs_packet(MeshTopology topo, int n, const uint64_t *keys, uint64_t fmask, int ishift, bool multi,
-                      const int32_t *child, const int32_t *range, const float *leaf_box, const float *node_box,
-                      const double *lo64, const double *hi64, uint32_t *pairs, uint64_t cap,
-                      unsigned long long *counters) {
+__global__ void __launch_bounds__(kPacketWarps * 32, 4)
+    find_pairs_packet(MeshTopology topo, int n, const int4 *node_links, const int4 *leaf_links,
+                      const int32_t *leaf_end, const float *leaf_box, const float *node_box, const double *lo64,
+                      const double *hi64, uint32_t *pairs, uint64_t cap, unsigned long long *counters) {
   typedef BoxLayout<K> L;
-  __shared__ int st_node[kPacketWarps][kPacketStack];
+  __shared__ int2 st_node[kPacketWarps][kPacketStack];
   __shared__ unsigned st_mask[kPacketWarps][kPacketStack];
   const unsigned lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
@@ -482,87 +531,66 @@ __global__ void __launch_bounds__(kPacketWarps * 32)
     qlo[k] = INFINITY;  // an empty box for lanes past the last leaf
     qhi[k] = -INFINITY;
   }
-  int a0 = -1, a1 = -1, a2 = -1, fa = 0;
-  uint64_t my_inst = 0;
+  int4 me = make_int4(0, -1, -1, -1);
+  int my_end = n;
   if (valid) {
     load_box<K>(leaf_box + (int64_t)s * L::S, qlo, qhi);
-    fa = (int)(keys[s] & fmask);
-    a0 = topo.faces[3 * fa];
-    a1 = topo.faces[3 * fa + 1];
-    a2 = topo.faces[3 * fa + 2];
-    my_inst = keys[s] >> ishift;
+    me = __ldg(leaf_links + s);
+    if (leaf_end) my_end = leaf_end[s];
   }
-  int sp = 0;
+  const unsigned all = __ballot_sync(0xffffffffu, valid);
   if (lane == 0) {
-    st_node[w][0] = 0;
-    st_mask[w][0] = __ballot_sync(0xffffffffu, valid);
-  } else {
-    __ballot_sync(0xffffffffu, valid);
+    const int4 root = __ldg(node_links);
+    st_node[w][0] = make_int2(root.x, root.y);
+    st_mask[w][0] = all;
   }
-  sp = 1;
+  int sp = 1;
   __syncwarp();
   unsigned long long tests = 0;
-  // A valid tree is visited at most once per node (n - 1 internal nodes).
   for (int visits = 0; sp > 0; visits++) {
     if (visits >= n) {
       if (lane == 0) atomicOr(&counters[3], 2ull);
       return;
     }
     sp--;
-    const int node = st_node[w][sp];
+    const int2 e = st_node[w][sp];
     const unsigned mask = st_mask[w][sp];
     __syncwarp();
-    const bool me = (mask >> lane) & 1u;
+    const bool mine = (mask >> lane) & 1u;
+    int4 lk[2];
+    float blo[2][K], bhi[2][K];
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      const int ch = child[2 * node + c];
+      const int ch = c ? e.y : e.x;
+      if (ch < 0) {
+        lk[c] = __ldg(leaf_links + ~ch);
+        load_box<K>(leaf_box + (int64_t)(~ch) * L::S, blo[c], bhi[c]);
+      } else {
+        lk[c] = __ldg(node_links + ch);
+        load_box<K>(node_box + (int64_t)ch * L::S, blo[c], bhi[c]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const int ch = c ? e.y : e.x;
       if (ch < 0) {
         const int j = ~ch;
-        const bool test = me && j > s && (!multi || (keys[j] >> ishift) == my_inst);
+        const bool test = mine && j > s && j < my_end;
         if (COUNT && test) tests++;
-        bool emit = false;
-        int fb = 0;
-        if (__any_sync(0xffffffffu, test)) {
-          float blo[K], bhi[K];
-          load_box<K>(leaf_box + (int64_t)j * L::S, blo, bhi);
-          bool sep = !test;
-#pragma unroll
-          for (int k = 0; k < K; k++) sep |= (qhi[k] < blo[k]) || (bhi[k] < qlo[k]);
-          fb = (int)(keys[j] & fmask);
-          if (!sep) {
-            // Mesh::neighboringFaces (src/Mesh.cpp:13-20) before the FP64
-            // test: most overlapping leaf pairs are adjacent faces.
-            const int b0 = topo.faces[3 * fb], b1 = topo.faces[3 * fb + 1], b2 = topo.faces[3 * fb + 2];
-            sep = a0 == b0 || a0 == b1 || a0 == b2 || a1 == b0 || a1 == b1 || a1 == b2 || a2 == b0 || a2 == b1 ||
-                  a2 == b2;
-            // The reference's exact FP64 test (KDOPBroadPhase.cpp:132-137).
-            for (int k = 0; k < K && !sep; k++)
-              sep = (hi64[(int64_t)k * topo.nf + fa] < lo64[(int64_t)k * topo.nf + fb]) ||
-                    (hi64[(int64_t)k * topo.nf + fb] < lo64[(int64_t)k * topo.nf + fa]);
-            emit = !sep;
-          }
-        }
-        emit_pairs(emit, fa, fb, pairs, cap, counters);
+        const bool emit = test && slabs_overlap<K>(qlo, qhi, blo[c], bhi[c]) &&
+                          exact_pair<K>(topo, me.x, me.y, me.z, me.w, lk[c], lo64, hi64);
+        emit_pairs(emit, me.x, lk[c].x, pairs, cap, counters);
       } else {
-        const bool test = me && range[2 * ch + 1] > s && (!multi || (keys[range[2 * ch]] >> ishift) <= my_inst);
+        const bool test = mine && lk[c].w > s && lk[c].z < my_end;
         if (COUNT && test) tests++;
-        bool hit = false;
-        if (__any_sync(0xffffffffu, test)) {
-          float blo[K], bhi[K];
-          load_box<K>(node_box + (int64_t)ch * L::S, blo, bhi);
-          bool sep = !test;
-#pragma unroll
-          for (int k = 0; k < K; k++) sep |= (qhi[k] < blo[k]) || (bhi[k] < qlo[k]);
-          hit = !sep;
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        const unsigned m = __ballot_sync(0xffffffffu, test && slabs_overlap<K>(qlo, qhi, blo[c], bhi[c]));
         if (m) {
           if (sp >= kPacketStack) {  // deeper than any valid tree: reported as an error
             if (lane == 0) atomicOr(&counters[3], 1ull);
             return;
           }
           if (lane == 0) {
-            st_node[w][sp] = ch;
+            st_node[w][sp] = make_int2(lk[c].x, lk[c].y);
             st_mask[w][sp] = m;
           }
           sp++;
@@ -919,7 +947,8 @@ __global__ void __launch_bounds__(kThreads) pair_search(int n, const uint64_t *k
 }  // namespace
 
 void broadphase_free(BroadphaseBuffers &b) {
-  void *ptrs[] = {b.lo64, b.hi64, b.face_lo, b.face_hi, b.leaf_box, b.node_box, b.node_child, b.node_range, b.parent,
+  void *ptrs[] = {b.lo64, b.hi64, b.face_lo, b.face_hi, b.leaf_box, b.node_box, b.node_child, b.node_range,
+                  b.node_links, b.leaf_links, b.leaf_end, b.parent,
                   b.arrive, b.keys, b.keys_alt, b.vals, b.vals_alt, b.bounds, b.counters, b.pairs, b.vf_keys,
                   b.ee_keys, b.flags, b.scan, b.temp};
   for (void *p : ptrs) cudaFree(p);
@@ -959,6 +988,9 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
     BP_CUDA(cudaMalloc(&b.node_box, 32 * F * sizeof(float)));  // [node][record]
     BP_CUDA(cudaMalloc(&b.node_child, 2 * F * sizeof(int32_t)));
     BP_CUDA(cudaMalloc(&b.node_range, 2 * F * sizeof(int32_t)));
+    BP_CUDA(cudaMalloc(&b.node_links, F * sizeof(int4)));
+    BP_CUDA(cudaMalloc(&b.leaf_links, F * sizeof(int4)));
+    BP_CUDA(cudaMalloc(&b.leaf_end, F * sizeof(int32_t)));
     BP_CUDA(cudaMalloc(&b.parent, 2 * F * sizeof(int32_t)));
     BP_CUDA(cudaMalloc(&b.arrive, F * sizeof(uint32_t)));
     BP_CUDA(cudaMalloc(&b.keys, F * sizeof(uint64_t)));
@@ -1026,6 +1058,8 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
     gather_leaves<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, flo, fhi, b.leaf_box);
   if (!reuse) {
     build_lbvh<<<grid_of(nf - 1), kThreads, 0, s>>>(nf, b.keys, b.node_child, b.node_range, b.parent);
+    link_tree<<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, kb.ishift, topo.ninst > 1, topo.faces,
+                                               b.node_child, b.node_range, b.node_links, b.leaf_links, b.leaf_end);
     b.tree_kind = p.kind;
     b.tree_nf = nf;
     b.tree_ninst = topo.ninst;
@@ -1047,14 +1081,13 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
 
   if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[1], s));
   auto traverse = [&]() {
-    const bool multi = topo.ninst > 1;
+    const int32_t *lend = topo.ninst > 1 ? b.leaf_end : nullptr;
     if (p.traversal == kTraversalPacket) {
       const unsigned grid = (unsigned)((nf + 32 * kPacketWarps - 1) / (32 * kPacketWarps));
 #define BP_FIND(KK, CC)                                                                                         \
-  find_pairs_packet<KK, CC><<<grid, kPacketWarps * 32, 0, s>>>(topo, nf, b.keys, kb.fmask, kb.ishift, multi,   \
-                                                               b.node_child, b.node_range, b.leaf_box,         \
-                                                               b.node_box, b.lo64, b.hi64, b.pairs,            \
-                                                               (uint64_t)b.cap_pairs, b.counters)
+  find_pairs_packet<KK, CC><<<grid, kPacketWarps * 32, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend,     \
+                                                               b.leaf_box, b.node_box, b.lo64, b.hi64,         \
+                                                               b.pairs, (uint64_t)b.cap_pairs, b.counters)
       if (kdop && p.count_tests) BP_FIND(13, true);
       else if (kdop) BP_FIND(13, false);
       else if (p.count_tests) BP_FIND(3, true);
@@ -1062,14 +1095,21 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
 #undef BP_FIND
       return;
     }
-#define BP_FIND(KK, CC)                                                                                           \
-  find_pairs<KK, CC><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.keys, kb.fmask, kb.ishift, multi, b.node_child, \
-                                                      b.node_range, b.leaf_box, b.node_box,                     \
-                                                      b.lo64, b.hi64, b.pairs, (uint64_t)b.cap_pairs, b.counters)
-    if (kdop && p.count_tests) BP_FIND(13, true);
-    else if (kdop) BP_FIND(13, false);
-    else if (p.count_tests) BP_FIND(3, true);
-    else BP_FIND(3, false);
+#define BP_FIND(KK, CC, MB)                                                                                       \
+  find_pairs<KK, CC, MB><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend, b.leaf_box, \
+                                                          b.node_box, b.lo64, b.hi64, b.pairs,                  \
+                                                          (uint64_t)b.cap_pairs, b.counters)
+    if (p.traversal == kTraversalThreadDense) {
+      if (kdop && p.count_tests) BP_FIND(13, true, 3);
+      else if (kdop) BP_FIND(13, false, 3);
+      else if (p.count_tests) BP_FIND(3, true, 3);
+      else BP_FIND(3, false, 3);
+    } else {
+      if (kdop && p.count_tests) BP_FIND(13, true, 2);
+      else if (kdop) BP_FIND(13, false, 2);
+      else if (p.count_tests) BP_FIND(3, true, 2);
+      else BP_FIND(3, false, 2);
+    }
 #undef BP_FIND
   };
   for (;;) {

@@ -54,6 +54,9 @@ struct BroadphaseBuffers {
   int32_t *node_child = nullptr;                  // [nf-1][2]  >= 0 internal, < 0 leaf ~s
   int32_t *node_range = nullptr;                  // [nf-1][2]  first, last sorted leaf
   int32_t *parent = nullptr;                      // [2 nf]     internal then leaves
+  int4 *node_links = nullptr;                     // [nf-1]     children, first and last leaf of each node
+  int4 *leaf_links = nullptr;                     // [nf]       face and its vertices of each sorted leaf
+  int32_t *leaf_end = nullptr;                    // [nf]       first sorted leaf of a later instance
   uint32_t *arrive = nullptr;                     // [nf]
   uint64_t *keys = nullptr, *keys_alt = nullptr;  // [max(nf, 9 pairs)]
   uint32_t *vals = nullptr, *vals_alt = nullptr;  // [2 nf]: second Morton key buffer
@@ -72,9 +75,10 @@ struct BroadphaseBuffers {
   bool rebuild_next = false;
 };
 
-// Traversal kernels: one thread per query leaf with a private stack, or one
-// warp per 32 consecutive query leaves with a shared stack (the default).
-enum TraversalKind : int { kTraversalThread = 0, kTraversalPacket = 1 };
+// Traversal kernels: one thread per query leaf with a private stack (two
+// register budgets: up to 112 registers, or 80 with three blocks per SM), or
+// one warp per 32 consecutive query leaves with a shared stack.
+enum TraversalKind : int { kTraversalThread = 0, kTraversalPacket = 1, kTraversalThreadDense = 2 };
 
 struct BroadphaseParams {
   int kind;

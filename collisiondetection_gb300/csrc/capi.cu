@@ -140,6 +140,7 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     view.wave_steps = view.wd ? ctx->opt_wave_steps : 0;
     view.wave_min_rows = ctx->opt_wave_min_rows;
     view.pool_budget = ctx->opt_pool_budget;
+    view.warp_finish = ctx->opt_warp_finish;
     CCD_CUDA(ccd::launch_stages(b, surv, view, ctx->num_sms, s, &launches));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[2], s));
     if (pe) pe->stage_launches = launches;
@@ -159,6 +160,7 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     view.wave_steps = view.wd ? ctx->opt_wave_steps : 0;
     view.wave_min_rows = ctx->opt_wave_min_rows;
     view.pool_budget = ctx->opt_pool_budget;
+    view.warp_finish = ctx->opt_warp_finish;
     CCD_CUDA(ccd::launch_stages(b, surv, view, ctx->num_sms, s, &launches));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[2], s));
     if (pe) pe->stage_launches = launches;
@@ -312,6 +314,9 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
   } else if (key == "count_slab_tests") {
     if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "count_slab_tests must be 0 or 1");
     ctx->opt_count_tests = (int)value;
+  } else if (key == "warp_finish") {
+    if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "warp_finish must be 0 or 1");
+    ctx->opt_warp_finish = (int)value;
   } else if (key == "tree_refit") {
     if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "tree_refit must be 0 or 1");
     ctx->opt_tree_refit = (int)value;
@@ -322,7 +327,7 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
     if (value < 0 || value > (1 << 20)) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "tree_max_refits must be in [0, 2^20]");
     ctx->opt_tree_max_refits = (int)value;
   } else if (key == "traversal") {
-    if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "traversal must be 0 or 1");
+    if (value < 0 || value > 2) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "traversal must be 0, 1 or 2");
     ctx->opt_traversal = (int)value;
   } else if (key == "wave_min_rows") {
     if (value < 0) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "wave_min_rows must be >= 0");

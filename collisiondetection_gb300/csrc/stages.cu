@@ -39,6 +39,7 @@ StageScratch stage_scratch_view(void *base, int64_t cap) {
   sc.wave_steps = 0;
   sc.wave_min_rows = 0;
   sc.pool_budget = 0;
+  sc.warp_finish = 1;
   return sc;
 }
 

@@ -34,6 +34,7 @@
 #pragma once
 
 #include "ccd_ctcd64.h"
+#include "ccd_jt_warp.h"
 #include "narrow.cuh"
 
 namespace ccd {
@@ -81,6 +82,7 @@ struct StageScratch {
   int wave_steps;       // wavefront steps (0: pool kernel only)
   int64_t wave_min_rows;
   int pool_budget;      // steps the pool kernel gives a resumed job before handing it on
+  int warp_finish;      // 1: the last solves run on all 32 lanes of their warp (ccd_jt_warp.h); 0: on one lane
 };
 
 // Bytes of the scratch for a tile of `cap` rows: three [slot][7][cap]
@@ -303,20 +305,47 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
     }
     __syncwarp();
     // The most populated working phase.
-    int best = 0, bestc = 0;
+    int best = 0, bestc = 0, working = 0;
     bool pending = false;
     for (int m = jt::kInit; m <= jt::kDone; m++) {
       const int c = __popc(__ballot_sync(0xffffffffu, mode[lane] == m)) +
                     __popc(__ballot_sync(0xffffffffu, mode[lane + 32] == m));
       if (m == jt::kDone) {
         pending = c > 0;
-      } else if (c > bestc) {
-        best = m;
-        bestc = c;
+      } else {
+        working += c;
+        if (c > bestc) {
+          best = m;
+          bestc = c;
+        }
       }
     }
     if (bestc == 0) {
       if (exhausted && !pending) break;
+      continue;
+    }
+    if (exhausted && working == 1 && sc.warp_finish) {
+      // The warp's last unfinished solve, with no job left to take: all 32
+      // lanes copy its state and advance it together to the end
+      // (jt::warp::step), then lane 0 writes it out.
+      const unsigned w0 = __ballot_sync(0xffffffffu, mode[lane] == best);
+      const unsigned w1 = __ballot_sync(0xffffffffu, mode[lane + 32] == best);
+      const int k = w0 ? __ffs(w0) - 1 : 32 + __ffs(w1) - 1;
+      const jt::PoolState<kWarpPool> ps = state(k);
+      jt::LocalStorage st;
+      for (int f = 0; f < jt::kDoubles; f++) st.d[f] = ps.D(f);
+      for (int f = 0; f < jt::kInts; f++) st.i[f] = ps.I(f);
+      for (int z = 0; z < 6; z++) st.zr[z] = ps.Z(z);
+      __syncwarp();
+      const jt::LocalState ls{&st};
+      while (ls.I(jt::MODE) != jt::kDone) jt::warp::step(ls);
+      if (lane == 0) {
+        const int64_t g = job_of[k];
+        const int q = job_queue(qbase, Polys::kSlots, g);
+        finish_job<Polys>(sc, ls, q, g - qbase[q]);
+        mode[k] = jt::kEmpty;
+      }
+      __syncwarp();
       continue;
     }
     // Up to 32 slots of that phase, one per lane.
@@ -503,16 +532,20 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gather_tail(StageScratch sc
     sc.tail[r] = (uint32_t)list_entry(in, off, sc.jcap, r);
 }
 
-// The jobs the wavefront steps left unfinished, one per warp: lane 0 copies
-// the job's state into thread-private storage and runs it to the end (the
-// solver's own iteration limits bound the loop).  Few jobs remain by then and
-// each is a long sequential chain, so latency, not lane use, matters here.
+// The jobs the wavefront steps left unfinished, one per warp, each run to
+// its end from a copy of its state (the solver's own iteration limits bound
+// the loop).  Few jobs remain by then and each is a long sequential chain, so
+// latency, not lane use, matters here.  With sc.warp_finish every lane copies
+// the state and the warp advances the solve together (jt::warp::step: the
+// independent divisions and K-polynomial terms of a step spread over the
+// lanes); otherwise lane 0 runs it alone.
 template <class Polys>
 __global__ void __launch_bounds__(32) wave_finish(StageScratch sc, const uint32_t *tail, const unsigned *tcount) {
   __shared__ int qbase[kMaxSlots + 1];
   if (threadIdx.x == 0) queue_bases(sc, Polys::kSlots, qbase);
   __syncwarp();
-  if (threadIdx.x != 0) return;
+  const bool whole = sc.warp_finish != 0;
+  if (!whole && threadIdx.x != 0) return;
   const int64_t count = *tcount;
   for (int64_t r = blockIdx.x; r < count; r += gridDim.x) {
     const int64_t g = tail[r];
@@ -522,8 +555,13 @@ __global__ void __launch_bounds__(32) wave_finish(StageScratch sc, const uint32_
     jt::LocalStorage st;
     load_state(fs, st);
     const jt::LocalState s{&st};
-    while (s.I(jt::MODE) != jt::kDone) jt::step(s);
-    finish_job<Polys>(sc, s, q, j);
+    if (whole) {
+      while (s.I(jt::MODE) != jt::kDone) jt::warp::step(s);
+      if (threadIdx.x == 0) finish_job<Polys>(sc, s, q, j);
+    } else {
+      while (s.I(jt::MODE) != jt::kDone) jt::step(s);
+      finish_job<Polys>(sc, s, q, j);
+    }
   }
 }
 

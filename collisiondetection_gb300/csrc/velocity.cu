@@ -512,11 +512,15 @@ cudaError_t launch_layer_events(const LayerGroups &g, const LayerState &s, int64
     return cudaLaunchCooperativeKernel((void *)layer_events_grid, blocks, kGridThreads, args, shared, st);
   }
   if (shared > 48 * 1024) {
+    cudaFuncSetAttribute(layer_events<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared);
     cudaFuncSetAttribute(layer_events<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared);
     cudaFuncSetAttribute(layer_events<512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shared);
   }
-  // small groups: a small block, whose barriers are cheap
-  if (max_group <= 256)
+  // small groups: a small block, whose barriers are cheap (one warp for
+  // groups of at most 32 stencils and vertices)
+  if (max_group <= 32)
+    layer_events<32><<<1, 32, shared, st>>>(g, s, max_events);
+  else if (max_group <= 256)
     layer_events<128><<<1, 128, shared, st>>>(g, s, max_events);
   else
     layer_events<512><<<1, 512, shared, st>>>(g, s, max_events);

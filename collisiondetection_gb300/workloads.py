@@ -327,6 +327,46 @@ def motion_request(tris: int, seed: int, steps: int = 10):
     return np.ascontiguousarray(f, dtype=np.int32), frames
 
 
+def pair_request(tris: int, seed: int, steps: int = 10, contact_step: float = 0.5):
+    """One collision query of the serving workload: a mesh pair -- two
+    icospheres side by side, or two grid sheets one above the other -- of
+    about `tris` triangles together, a gap of three mean edge lengths apart.
+    Each step moves the pair by a rigid translation of 0.5-2 mean edge lengths
+    in a random direction, closes the gap by a constant amount so that the
+    two meshes first touch about `contact_step` of the way through the
+    sequence (and then pass into each other), and adds N(0, 0.1 edge)
+    per-vertex jitter.  Returns (faces (F, 3) int32, frames (steps + 1, 3V))."""
+    rng = np.random.default_rng(seed)
+    if rng.random() < 0.5:
+        level = int(np.clip(np.rint(np.log(max(tris / 2, 20) / 20.0) / np.log(4.0)), 1, 7))
+        a, fa = _icosphere_cached(level)
+        edge = _mean_edge(a, fa)
+        gap = 3.0 * edge
+        axis = np.array([1.0, 0.0, 0.0])
+        b = a + (2.0 + gap) * axis
+    else:
+        n = int(max(3, np.rint(np.sqrt(max(tris / 2, 8) / 2.0) + 1)))
+        a, fa = grid_sheet(n, n)
+        edge = 1.0 / (n - 1)
+        gap = 3.0 * edge
+        axis = np.array([0.0, 0.0, 1.0])
+        b = a + np.array([0.3 * edge, 0.3 * edge, gap])
+    v = np.concatenate([a, b])
+    f = np.concatenate([fa, fa + a.shape[0]]).astype(np.int32)
+    close = gap / max(contact_step * steps, 1e-9)  # gap closed per step
+    frames = np.empty((steps + 1, v.size))
+    pos = v.copy()
+    frames[0] = pos.ravel()
+    nb = b.shape[0]
+    for k in range(steps):
+        d = rng.normal(size=3)
+        d *= rng.uniform(0.5, 2.0) * edge / np.linalg.norm(d)
+        pos = pos + d
+        pos[-nb:] -= close * axis
+        frames[k + 1] = (pos + rng.normal(0.0, 0.1 * edge, pos.shape)).ravel()
+    return np.ascontiguousarray(f, dtype=np.int32), frames
+
+
 def uneven_sizes(n_instances: int = 512, lo: float = 200.0, hi: float = 2e5, seed: int = 0) -> np.ndarray:
     """Requested triangle counts of an uneven batch: log-uniform in [lo, hi]."""
     rng = np.random.default_rng(seed)

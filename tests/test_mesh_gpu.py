@@ -181,12 +181,12 @@ def test_refitted_tree_gives_the_built_trees_results(ctx, cloth):
 @pytest.mark.parametrize("label", ["kdop", "aabb"])
 def test_traversal_kernels_agree(ctx, cloth, label):
     # The warp-per-32-faces traversal performs exactly the slab tests of the
-    # thread-per-face one (each lane tests only the nodes its own query
-    # reaches) and finds the same candidates.
+    # thread-per-face ones (each lane tests only the nodes its own query
+    # reaches), and all find the same candidates.
     faces, frames = cloth
     k = 40
     out = {}
-    for trav in (0, 1):
+    for trav in (0, 1, 2):
         ctx.set_option("traversal", trav)
         ctx.set_option("count_slab_tests", 1)
         try:
@@ -196,10 +196,11 @@ def test_traversal_kernels_agree(ctx, cloth, label):
                 out[trav] = (vf, ee, m.stats()["slab_tests"], m.stats()["face_pairs"])
         finally:
             ctx.set_option("count_slab_tests", 0)
-            ctx.set_option("traversal", 1)
-    np.testing.assert_array_equal(out[0][0], out[1][0])
-    np.testing.assert_array_equal(out[0][1], out[1][1])
-    assert out[0][2] == out[1][2] > 0 and out[0][3] == out[1][3]
+            ctx.set_option("traversal", 0)
+    for trav in (1, 2):
+        np.testing.assert_array_equal(out[0][0], out[trav][0])
+        np.testing.assert_array_equal(out[0][1], out[trav][1])
+        assert out[0][2] == out[trav][2] > 0 and out[0][3] == out[trav][3]
 
 
 def test_uneven_instances_match_oracle(ctx, oracle):

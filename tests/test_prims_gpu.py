@@ -108,6 +108,28 @@ def test_refine_all_equals_fp64_at_wavefront_size(ctx, kind):
     assert st["survivors"] == rows.shape[0] and st["hits"] == int(h64.sum())
 
 
+@pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE])
+@pytest.mark.parametrize("n", [4096, 600_000])
+def test_warp_finish_is_bit_identical(ctx, kind, n):
+    # The slowest solves advanced by all 32 lanes of a warp (independent
+    # divisions and K terms spread over lanes) against one lane alone: the
+    # same operations on the same operands, so the same bits.  4,096 rows
+    # take the pool kernel alone (its last solve per warp), 600,000 the
+    # wavefront and the one-solve-per-warp finish.
+    rows = C.workloads.primitive_batch(kind, n, seed=505)
+    out = {}
+    for mode in (0, 1):
+        ctx.set_option("warp_finish", mode)
+        try:
+            out[mode] = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_CULL_REFINE)
+        finally:
+            ctx.set_option("warp_finish", 1)
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    m = out[0][0] == 1
+    np.testing.assert_array_equal(out[0][1][m].view(np.uint64), out[1][1][m].view(np.uint64))
+    assert m.any()
+
+
 @pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE, C.VERTEX_EDGE])
 def test_cull_alone_keeps_every_hit(ctx, oracle, kind):
     torch = pytest.importorskip("torch")

@@ -111,6 +111,21 @@ def test_motion_request_moves_rigidly_by_half_to_two_edges():
             assert 0.45 * edge < step < 2.1 * edge
 
 
+def test_pair_request_meshes_meet_halfway():
+    for seed in range(6):
+        f, frames = W.pair_request(4000, seed=seed, steps=10)
+        v = frames.reshape(11, -1, 3)
+        nf = f.shape[0]
+        assert 1500 <= nf <= 20000 and f.min() >= 0 and f.max() < v.shape[1]
+        half = v.shape[1] // 2
+        # the second mesh closes in on the first at a constant rate
+        d0 = (v[0, half:] - v[0, :half]).mean(0)
+        d0 /= np.linalg.norm(d0)
+        gaps = [float((v[k, half:] - v[k, :half]).mean(0) @ d0) for k in range(11)]
+        steps = np.diff(gaps)
+        assert np.all(steps < 0) and np.ptp(steps) < 0.2 * abs(steps.mean())
+
+
 def test_uneven_batch_offsets_and_sizes():
     faces, frames, vo, fo = W.uneven_batch(n_instances=12, lo=200, hi=5000, seed=2, steps=1)
     assert vo[0] == 0 and fo[0] == 0 and np.all(np.diff(vo) > 0) and np.all(np.diff(fo) > 0)
