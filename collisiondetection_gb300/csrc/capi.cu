@@ -336,6 +336,10 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
     if (value < 1024 || value > ((int64_t)1 << 26))
       return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "chunk_rows must be in [1024, 2^26]");
     ctx->opt_chunk_rows = value;
+  } else if (key == "narrow_chunk") {
+    if (value < 1024 || value > ((int64_t)1 << 24))
+      return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "narrow_chunk must be in [1024, 2^24]");
+    ctx->opt_narrow_chunk = value;
   } else if (key == "layer_events_per_launch") {
     if (value < 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "layer_events_per_launch must be >= 1");
     ctx->opt_layer_events = value;

@@ -26,8 +26,9 @@ using namespace ccd_capi;
 
 namespace {
 
-// Stencils per chunk of the narrow phase (bounds its row scratch to about
-// 1.2 GB).
+// Segments per chunk of the narrow phase over a multi-entry history (bounds
+// its row scratch to about 1.3 GB); two-entry steps take chunks of the
+// context's "narrow_chunk" stencils.
 constexpr int64_t kNarrowChunk = 1 << 20;
 
 // Per-chunk rows and results of the narrow-phase chain.
@@ -246,7 +247,7 @@ int narrow_device(ccd_mesh *m, Lane &L, int kind, int path, int64_t n, const int
   ccd_context *ctx = m->ctx;
   if (n == 0) return CCD_OK;
   if (m->has_history) return narrow_device_history(m, L, kind, path, n, st, eta, eta_per_row, hit, t, which);
-  const int64_t chunk = std::min<int64_t>(n, kNarrowChunk);
+  const int64_t chunk = std::min<int64_t>(n, ctx->opt_narrow_chunk);
   int rc = ensure_narrow(m, L, chunk);
   if (rc) return rc;
   NarrowScratch &ns = L.ns;

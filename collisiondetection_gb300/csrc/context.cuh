@@ -97,6 +97,10 @@ struct ccd_context {
   int opt_tree_max_refits = 64;    // ... or after this many refits in a row
   int64_t opt_layer_grid_min = 1024;  // velocity filter: groups this large fire over the whole GPU
   int64_t opt_chunk_rows = ccd_capi::kChunkRows;  // host-memory batches: rows per chunk
+  // Mesh narrow phase: stencils per chunk.  Each chunk's refinement ends in
+  // the latency-bound tail of its slowest root solves, so chunks are large
+  // (about 1.3 KB of rows and results per stencil).
+  int64_t opt_narrow_chunk = (int64_t)1 << 22;
   int64_t opt_layer_events = (int64_t)1 << 20;      // velocity filter: firings per event-loop launch
   std::string err;
 };

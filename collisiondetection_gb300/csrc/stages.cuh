@@ -193,19 +193,38 @@ constexpr int kWarpPool = 64;
 constexpr size_t kPoolSmem = (size_t)kWarpPool * (jt::kDoubles * sizeof(double) + jt::kInts * sizeof(int));
 
 // Spans of a finished solve, written to the polynomial's row slot.
+// Spans of a solve that found `roots` zeros tr[0 .. deg-1] (sorted in place).
+template <class Polys>
+__device__ __forceinline__ void finish_roots(const StageScratch &sc, int slot, int64_t j, double *tr, int roots,
+                                             int status) {
+  const int deg = sc.job_deg[slot * sc.cap + j];
+  double op[7];
+  for (int k = 0; k <= deg; k++) op[k] = sc.coef[(slot * 7 + k) * sc.cap + j];
+  SpanList sl;
+  sl.clear();
+  root_spans(op, deg, tr, roots, sl, Polys::want_pos(slot));
+  const int64_t row = sc.job_row[slot * sc.cap + j];
+  store_spans(sc, slot, row, sl);
+  if (status) atomicOr(&sc.row_status[row], (uint32_t)status);
+}
+
 template <class Polys, class S>
 __device__ __forceinline__ void finish_job(const StageScratch &sc, const S &st, int slot, int64_t j) {
   const int deg = sc.job_deg[slot * sc.cap + j];
-  double op[7], tr[6];
-  for (int k = 0; k <= deg; k++) op[k] = sc.coef[(slot * 7 + k) * sc.cap + j];
+  double tr[6];
   for (int k = 0; k < deg; k++) tr[k] = st.Z(k);
-  SpanList sl;
-  sl.clear();
-  root_spans(op, deg, tr, st.I(jt::ROOTS), sl, Polys::want_pos(slot));
-  const int64_t row = sc.job_row[slot * sc.cap + j];
-  store_spans(sc, slot, row, sl);
-  const int status = st.I(jt::STATUS);
-  if (status) atomicOr(&sc.row_status[row], (uint32_t)status);
+  finish_roots<Polys>(sc, slot, j, tr, st.I(jt::ROOTS), st.I(jt::STATUS));
+}
+
+// The solve of state st run to its end by the whole (converged) warp
+// (ccd_jt_warp.h); lane 0 writes its spans.
+template <class Polys, class S>
+__device__ __forceinline__ void warp_solve(const StageScratch &sc, const S &st, int slot, int64_t j) {
+  jt::warp::Solve ws;
+  ws.load(st);
+  double tr[6];
+  ws.run(tr);
+  if ((threadIdx.x & 31) == 0) finish_roots<Polys>(sc, slot, j, tr, ws.roots, ws.status);
 }
 
 __device__ __forceinline__ int job_queue(const int *qbase, int nslots, int64_t g) {
@@ -331,20 +350,11 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
       const unsigned w0 = __ballot_sync(0xffffffffu, mode[lane] == best);
       const unsigned w1 = __ballot_sync(0xffffffffu, mode[lane + 32] == best);
       const int k = w0 ? __ffs(w0) - 1 : 32 + __ffs(w1) - 1;
-      const jt::PoolState<kWarpPool> ps = state(k);
-      jt::LocalStorage st;
-      for (int f = 0; f < jt::kDoubles; f++) st.d[f] = ps.D(f);
-      for (int f = 0; f < jt::kInts; f++) st.i[f] = ps.I(f);
-      for (int z = 0; z < 6; z++) st.zr[z] = ps.Z(z);
+      const int64_t g = job_of[k];
+      const int q = job_queue(qbase, Polys::kSlots, g);
+      warp_solve<Polys>(sc, state(k), q, g - qbase[q]);
       __syncwarp();
-      const jt::LocalState ls{&st};
-      while (ls.I(jt::MODE) != jt::kDone) jt::warp::step(ls);
-      if (lane == 0) {
-        const int64_t g = job_of[k];
-        const int q = job_queue(qbase, Polys::kSlots, g);
-        finish_job<Polys>(sc, ls, q, g - qbase[q]);
-        mode[k] = jt::kEmpty;
-      }
+      if (lane == 0) mode[k] = jt::kEmpty;
       __syncwarp();
       continue;
     }
@@ -533,12 +543,12 @@ __global__ void __launch_bounds__(kWaveThreads) wave_gather_tail(StageScratch sc
 }
 
 // The jobs the wavefront steps left unfinished, one per warp, each run to
-// its end from a copy of its state (the solver's own iteration limits bound
-// the loop).  Few jobs remain by then and each is a long sequential chain, so
-// latency, not lane use, matters here.  With sc.warp_finish every lane copies
-// the state and the warp advances the solve together (jt::warp::step: the
-// independent divisions and K-polynomial terms of a step spread over the
-// lanes); otherwise lane 0 runs it alone.
+// its end (the solver's own iteration limits bound the loop).  Few jobs
+// remain by then and each is a long sequential chain, so latency, not lane
+// use, matters here.  With sc.warp_finish the warp holds the state in
+// registers spread over its lanes and advances the solve together
+// (jt::warp::Solve: element-wise updates and independent divisions on
+// different lanes); otherwise lane 0 runs it alone from a private copy.
 template <class Polys>
 __global__ void __launch_bounds__(32) wave_finish(StageScratch sc, const uint32_t *tail, const unsigned *tcount) {
   __shared__ int qbase[kMaxSlots + 1];
@@ -552,13 +562,12 @@ __global__ void __launch_bounds__(32) wave_finish(StageScratch sc, const uint32_
     int q;
     int64_t j;
     const jt::FieldState fs = wave_state<Polys>(sc, qbase, g, q, j);
-    jt::LocalStorage st;
-    load_state(fs, st);
-    const jt::LocalState s{&st};
     if (whole) {
-      while (s.I(jt::MODE) != jt::kDone) jt::warp::step(s);
-      if (threadIdx.x == 0) finish_job<Polys>(sc, s, q, j);
+      warp_solve<Polys>(sc, fs, q, j);
     } else {
+      jt::LocalStorage st;
+      load_state(fs, st);
+      const jt::LocalState s{&st};
       while (s.I(jt::MODE) != jt::kDone) jt::step(s);
       finish_job<Polys>(sc, s, q, j);
     }
