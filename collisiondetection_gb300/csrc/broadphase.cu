@@ -477,6 +477,108 @@ __global__ void __launch_bounds__(kThreads, MINB) find_pairs(MeshTopology topo, 
   if (COUNT && tests) atomicAdd(&counters[4], tests);
 }
 
+// Four lanes per query face (13-DOP records only).  Lane q of a quad loads
+// the q-th 16-byte piece of the lower-bound half and of the upper-bound half
+// of every record it visits and tests the query's slabs 4q .. 4q+3 (the pad
+// slots past slab 12 hold zero in both the query and the node, so they never
+// separate); two shuffles within the quad combine the four answers.  A
+// record's four pieces are thus read by four neighbouring lanes -- one
+// 128-byte line per quad per load instruction instead of one line per lane
+// -- and each lane needs a quarter of the registers, so more warps stay
+// resident.  The quad follows one traversal, so it never diverges; lane 0 of
+// the quad keeps the stack and hands each popped entry to the others.  Each
+// quad performs exactly the per-face traversal's slab tests.
+template <bool COUNT>
+__global__ void __launch_bounds__(kThreads) find_pairs_quad(MeshTopology topo, int n, const int4 *node_links,
+                                                            const int4 *leaf_links, const int32_t *leaf_end,
+                                                            const float *leaf_box, const float *node_box,
+                                                            const double *lo64, const double *hi64, uint32_t *pairs,
+                                                            uint64_t cap, unsigned long long *counters) {
+  typedef BoxLayout<13> L;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = (int)(t >> 2), q = (int)(t & 3);
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned qmask = 0xfu << (lane & ~3u);
+  if (s >= n || n < 2) return;  // whole quads leave together
+  const float4 *qrec = reinterpret_cast<const float4 *>(leaf_box + (int64_t)s * L::S);
+  const float4 qlo = __ldg(qrec + q), qhi = __ldg(qrec + L::V + q);
+  const int4 me = __ldg(leaf_links + s);
+  const int my_end = leaf_end ? leaf_end[s] : n;
+  int2 stack[kStack];
+  int sp = 0;
+  if (q == 0) {
+    const int4 root = __ldg(node_links);
+    stack[sp++] = make_int2(root.x, root.y);
+  }
+  sp = __shfl_sync(qmask, sp, 0, 4);
+  unsigned long long tests = 0;
+  for (int visits = 0; sp > 0; visits++) {
+    if (visits >= n) {
+      if (q == 0) atomicOr(&counters[3], 2ull);
+      return;
+    }
+    int2 e = make_int2(0, 0);
+    if (q == 0) e = stack[sp - 1];
+    sp--;
+    e.x = __shfl_sync(qmask, e.x, 0, 4);
+    e.y = __shfl_sync(qmask, e.y, 0, 4);
+    int4 lk[2];
+    float4 blo[2], bhi[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const int ch = c ? e.y : e.x;
+      const float4 *rec = reinterpret_cast<const float4 *>(ch < 0 ? leaf_box + (int64_t)(~ch) * L::S
+                                                                   : node_box + (int64_t)ch * L::S);
+      lk[c] = __ldg(ch < 0 ? leaf_links + ~ch : node_links + ch);
+      blo[c] = __ldg(rec + q);
+      bhi[c] = __ldg(rec + L::V + q);
+    }
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const int ch = c ? e.y : e.x;
+      const bool leaf = ch < 0;
+      const bool want = leaf ? ((~ch) > s && (~ch) < my_end) : (lk[c].w > s && lk[c].z < my_end);
+      if (!want) continue;  // uniform within the quad
+      if (COUNT && q == 0) tests++;
+      bool sep = (qhi.x < blo[c].x) || (bhi[c].x < qlo.x) || (qhi.y < blo[c].y) || (bhi[c].y < qlo.y) ||
+                 (qhi.z < blo[c].z) || (bhi[c].z < qlo.z) || (qhi.w < blo[c].w) || (bhi[c].w < qlo.w);
+      sep |= __shfl_xor_sync(qmask, sep, 1, 4);
+      sep |= __shfl_xor_sync(qmask, sep, 2, 4);
+      if (sep) continue;
+      if (!leaf) {
+        if (q == 0) {
+          if (sp < kStack)
+            stack[sp] = make_int2(lk[c].x, lk[c].y);
+          else
+            atomicOr(&counters[3], 1ull);  // stack overflow: reported as an error
+        }
+        if (sp < kStack) sp++;
+        continue;
+      }
+      // Mesh::neighboringFaces (src/Mesh.cpp:13-20), then the reference's
+      // exact FP64 test (KDOPBroadPhase.cpp:132-137), its slabs split over
+      // the quad as above.
+      const int4 b = lk[c];
+      if (me.y == b.y || me.y == b.z || me.y == b.w || me.z == b.y || me.z == b.z || me.z == b.w || me.w == b.y ||
+          me.w == b.z || me.w == b.w)
+        continue;
+      bool xsep = false;
+      for (int k = 4 * q; k < 4 * q + 4 && k < 13; k++)
+        xsep |= (hi64[(int64_t)k * topo.nf + me.x] < lo64[(int64_t)k * topo.nf + b.x]) ||
+                (hi64[(int64_t)k * topo.nf + b.x] < lo64[(int64_t)k * topo.nf + me.x]);
+      xsep |= __shfl_xor_sync(qmask, xsep, 1, 4);
+      xsep |= __shfl_xor_sync(qmask, xsep, 2, 4);
+      if (xsep || q != 0) continue;
+      const unsigned long long idx = atomicAdd(&counters[0], 1ull);
+      if (idx < cap) {
+        pairs[2 * (int64_t)idx] = (uint32_t)me.x;
+        pairs[2 * (int64_t)idx + 1] = (uint32_t)b.x;
+      }
+    }
+  }
+  if (COUNT && tests) atomicAdd(&counters[4], tests);
+}
+
 // Warp-cooperative (packet) traversal.  A warp takes 32 consecutive leaves in
 // Morton order -- spatially close queries -- and walks the tree once for all
 // of them: each stack entry holds a node's two child references and the mask
@@ -1082,6 +1184,18 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[1], s));
   auto traverse = [&]() {
     const int32_t *lend = topo.ninst > 1 ? b.leaf_end : nullptr;
+    if (p.traversal == kTraversalQuad && kdop) {
+      const unsigned grid = (unsigned)((4 * (int64_t)nf + kThreads - 1) / kThreads);
+      if (p.count_tests)
+        find_pairs_quad<true><<<grid, kThreads, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend, b.leaf_box,
+                                                        b.node_box, b.lo64, b.hi64, b.pairs, (uint64_t)b.cap_pairs,
+                                                        b.counters);
+      else
+        find_pairs_quad<false><<<grid, kThreads, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend, b.leaf_box,
+                                                         b.node_box, b.lo64, b.hi64, b.pairs, (uint64_t)b.cap_pairs,
+                                                         b.counters);
+      return;
+    }
     if (p.traversal == kTraversalPacket) {
       const unsigned grid = (unsigned)((nf + 32 * kPacketWarps - 1) / (32 * kPacketWarps));
 #define BP_FIND(KK, CC)                                                                                         \

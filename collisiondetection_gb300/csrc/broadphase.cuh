@@ -76,9 +76,16 @@ struct BroadphaseBuffers {
 };
 
 // Traversal kernels: one thread per query leaf with a private stack (two
-// register budgets: up to 112 registers, or 80 with three blocks per SM), or
-// one warp per 32 consecutive query leaves with a shared stack.
-enum TraversalKind : int { kTraversalThread = 0, kTraversalPacket = 1, kTraversalThreadDense = 2 };
+// register budgets: up to 112 registers, or 80 with three blocks per SM),
+// one warp per 32 consecutive query leaves with a shared stack, or four lanes
+// per query leaf, each testing a quarter of the slabs (13-DOP trees; AABB
+// trees take the thread kernel).
+enum TraversalKind : int {
+  kTraversalThread = 0,
+  kTraversalPacket = 1,
+  kTraversalThreadDense = 2,
+  kTraversalQuad = 3
+};
 
 struct BroadphaseParams {
   int kind;

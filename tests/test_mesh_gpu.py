@@ -180,13 +180,14 @@ def test_refitted_tree_gives_the_built_trees_results(ctx, cloth):
 
 @pytest.mark.parametrize("label", ["kdop", "aabb"])
 def test_traversal_kernels_agree(ctx, cloth, label):
-    # The warp-per-32-faces traversal performs exactly the slab tests of the
-    # thread-per-face ones (each lane tests only the nodes its own query
-    # reaches), and all find the same candidates.
+    # The warp-per-32-faces and four-lanes-per-face traversals perform
+    # exactly the slab tests of the thread-per-face ones (each query is
+    # tested only against the nodes its own traversal reaches), and all find
+    # the same candidates.
     faces, frames = cloth
     k = 40
     out = {}
-    for trav in (0, 1, 2):
+    for trav in (0, 1, 2, 3):
         ctx.set_option("traversal", trav)
         ctx.set_option("count_slab_tests", 1)
         try:
@@ -197,7 +198,7 @@ def test_traversal_kernels_agree(ctx, cloth, label):
         finally:
             ctx.set_option("count_slab_tests", 0)
             ctx.set_option("traversal", 0)
-    for trav in (1, 2):
+    for trav in (1, 2, 3):
         np.testing.assert_array_equal(out[0][0], out[trav][0])
         np.testing.assert_array_equal(out[0][1], out[trav][1])
         assert out[0][2] == out[trav][2] > 0 and out[0][3] == out[trav][3]
