@@ -245,7 +245,9 @@ def mesh_summary(mesh, uneven):
                                   "identical": _identical(c3.get("parity")),
                                   "checked_steps": (c3.get("parity") or {}).get("steps"),
                                   "traversal": {"frac": tr.get("frac"), "achieved_gbs": tr.get("achieved_gbs"),
-                                                "ms": tr.get("traversal_ms")}}
+                                                "ms": tr.get("traversal_ms"),
+                                                "frac_built_tree": (tr.get("built") or {}).get("frac"),
+                                                "ms_built_tree": (tr.get("built") or {}).get("traversal_ms")}}
     if uneven:
         out["uneven_batch"] = {"instances": uneven.get("instances"), "faces": uneven.get("faces"),
                                "ms": uneven["one_call"]["ms"], "value": uneven["one_call"]["value"],
@@ -391,29 +393,41 @@ def mesh_section(ctx, stream, rank, args):
             "ms_per_step_max": 1e3 * max(dts), "stencil_tests": tests, "collisions": hits,
             "value": tests / total, "unit": "stencil tests/s"}
         # Traversal roofline of one step (k = steps / 2): slab tests from a
-        # counting run, device time from a timed run without the counter.
+        # counting run, device time from timed runs without the counter; on
+        # the tree the stepping kept and refitted since the first step, and
+        # on a tree built for this step.
         k = len(frames) // 2
         m.set_positions(frames[k], frames[k + 1])
-        ctx.set_option("count_slab_tests", 1)
-        m.broadphase(C.BROADPHASE_KDOP13, 1e-6)
-        tests = m.stats()["slab_tests"]
-        pairs = m.stats()["face_pairs"]
-        ctx.set_option("count_slab_tests", 0)
-        ctx.set_profiling(True)
-        trav, bpms = [], []
-        for _ in range(5):
-            m.broadphase(C.BROADPHASE_KDOP13, 1e-6)
-            trav.append(m.stats()["traversal_ms"])
-            bpms.append(m.stats()["broadphase_ms"])
-        ctx.set_profiling(False)
         peak, src = measured_peaks()
-        tms = statistics.median(trav)
-        algo = tests * 13 * 2 * 4 + pairs * 8  # 13-DOP FP32 slab per test, a pair written per hit
-        out["cloth_on_sphere_kdop"]["traversal"] = {
-            "kernel": "find_pairs<13>", "slab_tests": tests, "face_pairs": pairs, "traversal_ms": tms,
-            "broadphase_ms": statistics.median(bpms), "algorithmic_bytes": algo,
-            "achieved_gbs": algo / (tms / 1e3) / 1e9, "peak_gbs": peak, "frac": algo / (tms / 1e3) / 1e9 / peak,
-            "note": "the tree (about 300 B per face: two 128 B slab records and the links) fits in L2, so DRAM is not what bounds this traversal"}
+
+        def traversal(label):
+            ctx.set_option("count_slab_tests", 1)
+            m.broadphase(C.BROADPHASE_KDOP13, 1e-6)
+            tests = m.stats()["slab_tests"]
+            pairs = m.stats()["face_pairs"]
+            ctx.set_option("count_slab_tests", 0)
+            ctx.set_profiling(True)
+            trav, bpms = [], []
+            for _ in range(9):
+                m.broadphase(C.BROADPHASE_KDOP13, 1e-6)
+                trav.append(m.stats()["traversal_ms"])
+                bpms.append(m.stats()["broadphase_ms"])
+            ctx.set_profiling(False)
+            tms = statistics.median(trav)
+            algo = tests * 13 * 2 * 4 + pairs * 8  # 13-DOP FP32 slab per test, a pair written per hit
+            return {"tree": label, "kernel": "find_pairs_quad (four lanes per query face)", "slab_tests": tests,
+                    "face_pairs": pairs, "traversal_ms": tms, "broadphase_ms": statistics.median(bpms),
+                    "algorithmic_bytes": algo, "achieved_gbs": algo / (tms / 1e3) / 1e9, "peak_gbs": peak,
+                    "frac": algo / (tms / 1e3) / 1e9 / peak}
+
+        refitted = traversal("kept since the first step, refitted")
+        ctx.set_option("tree_refit", 0)
+        built = traversal("built for this step")
+        ctx.set_option("tree_refit", 1)
+        out["cloth_on_sphere_kdop"]["traversal"] = dict(
+            refitted, built=built,
+            note="the tree (about 300 B per face: two 128 B slab records and the links) fits in L2, so DRAM is not "
+                 "what bounds this traversal")
         if rank == 0:
             idx = [len(frames) - 2, len(frames) // 2, (4 * len(frames)) // 5]
             bp, nph, par = oracle_steps(m, frames, faces, 1e-6, idx)

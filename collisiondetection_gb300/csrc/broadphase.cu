@@ -344,19 +344,26 @@ __global__ void __launch_bounds__(kThreads) refit(int n, const int32_t *child, c
 
 // ------------------------------------------------------------------ traversal
 // The links a traversal needs, in 16-byte records beside the slab records so
-// that visiting a node costs one memory round trip: a stack entry holds the
-// two child references of a node whose slab the query overlapped, and a pop
-// loads both children's slab records and link records at once.
-//   node_links[i] = (child 0, child 1, first leaf, last leaf)   (child < 0: leaf ~child)
+// that visiting a node costs one memory round trip:
+//   node_links[i] = (child 0, child 1, split, last leaf)   (child < 0: leaf ~child)
 //   leaf_links[j] = (face, its three vertices)
 //   leaf_end[j]   = first sorted leaf of a later instance (instance meshes)
+// Child 0 of node i covers the sorted leaves [first, split] and child 1
+// [split + 1, last], so a stack entry that carries a node's links tells,
+// before any load, which children can hold a partner of the query (a later
+// leaf of the same instance); only those children's slab and link records
+// are then loaded, together.
 __global__ void __launch_bounds__(kThreads) link_tree(int n, const uint64_t *keys, uint64_t fmask, int ishift,
                                                       bool multi, const int32_t *faces, const int32_t *child,
                                                       const int32_t *range, int4 *node_links, int4 *leaf_links,
                                                       int32_t *leaf_end) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  if (i < n - 1) node_links[i] = make_int4(child[2 * i], child[2 * i + 1], range[2 * i], range[2 * i + 1]);
+  if (i < n - 1) {
+    const int c0 = child[2 * i];
+    const int split = c0 < 0 ? ~c0 : range[2 * c0 + 1];
+    node_links[i] = make_int4(c0, child[2 * i + 1], split, range[2 * i + 1]);
+  }
   const int f = (int)(keys[i] & fmask);
   leaf_links[i] = make_int4(f, faces[3 * f], faces[3 * f + 1], faces[3 * f + 2]);
   if (multi) {
@@ -375,18 +382,37 @@ __global__ void __launch_bounds__(kThreads) link_tree(int n, const uint64_t *key
   }
 }
 
+// A node on a traversal stack: its links (child 0, child 1, split, last).
+// Every node pushed has its first leaf before the query's instance end (the
+// root starts at leaf 0; child 1 is checked below; child 0 starts where its
+// parent does), so the stack need not carry it.
+struct StackEntry {
+  int4 lk;
+};
+
+// Which of an entry's children can hold a partner of query leaf s: a later
+// leaf (each pair once) of the same instance (before my_end).
+__device__ __forceinline__ bool child_wanted(const StackEntry &e, int c, int s, int my_end) {
+  return c ? (e.lk.w > s && e.lk.z + 1 < my_end) : (e.lk.z > s);
+}
+
+__device__ __forceinline__ StackEntry child_entry(const StackEntry &, int, const int4 &lk) { return StackEntry{lk}; }
+
 // The part of a face-pair test after the conservative FP32 slab test:
 // Mesh::neighboringFaces (src/Mesh.cpp:13-20) first -- most overlapping leaf
 // pairs are adjacent faces, and this integer test spares them the FP64 one
 // (FP64 compares run at 1/64 of the FP32 rate) -- then the reference's exact
 // FP64 slab test (KDOPBroadPhase.cpp:132-137, strict '<').
+__device__ __forceinline__ bool adjacent(const int4 &a, const int4 &b) {
+  return a.y == b.y || a.y == b.z || a.y == b.w || a.z == b.y || a.z == b.z || a.z == b.w || a.w == b.y ||
+         a.w == b.z || a.w == b.w;
+}
+
 template <int K>
-__device__ __forceinline__ bool exact_pair(const MeshTopology &topo, int fa, int a0, int a1, int a2, const int4 &b,
-                                           const double *lo64, const double *hi64) {
-  if (a0 == b.y || a0 == b.z || a0 == b.w || a1 == b.y || a1 == b.z || a1 == b.w || a2 == b.y || a2 == b.z ||
-      a2 == b.w)
-    return false;
-  const int fb = b.x;
+__device__ __forceinline__ bool exact_pair(const MeshTopology &topo, const int4 &a, const int4 &b, const double *lo64,
+                                           const double *hi64) {
+  if (adjacent(a, b)) return false;
+  const int fa = a.x, fb = b.x;
   for (int k = 0; k < K; k++)
     if ((hi64[(int64_t)k * topo.nf + fa] < lo64[(int64_t)k * topo.nf + fb]) ||
         (hi64[(int64_t)k * topo.nf + fb] < lo64[(int64_t)k * topo.nf + fa]))
@@ -403,16 +429,18 @@ __device__ __forceinline__ bool slabs_overlap(const float (&qlo)[K], const float
   return !sep;
 }
 
+__device__ __forceinline__ StackEntry root_entry(const int4 *node_links) { return StackEntry{__ldg(node_links)}; }
+
 // One thread per query leaf s, over the leaves after s in sorted order (each
 // pair once) and of the same instance.  COUNT: also count the slab tests
 // (leaf and node), for the traversal's algorithmic bytes; a separate variant
 // so that timed runs carry no counter.
 template <int K, bool COUNT, int MINB>
 __global__ void __launch_bounds__(kThreads, MINB) find_pairs(MeshTopology topo, int n, const int4 *node_links,
-                                                       const int4 *leaf_links, const int32_t *leaf_end,
-                                                       const float *leaf_box, const float *node_box,
-                                                       const double *lo64, const double *hi64, uint32_t *pairs,
-                                                       uint64_t cap, unsigned long long *counters) {
+                                                             const int4 *leaf_links, const int32_t *leaf_end,
+                                                             const float *leaf_box, const float *node_box,
+                                                             const double *lo64, const double *hi64, uint32_t *pairs,
+                                                             uint64_t cap, unsigned long long *counters) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n || n < 2) return;
   typedef BoxLayout<K> L;
@@ -420,12 +448,9 @@ __global__ void __launch_bounds__(kThreads, MINB) find_pairs(MeshTopology topo, 
   load_box<K>(leaf_box + (int64_t)s * L::S, qlo, qhi);
   const int4 me = __ldg(leaf_links + s);
   const int my_end = leaf_end ? leaf_end[s] : n;
-  int2 stack[kStack];
+  StackEntry stack[kStack];
   int sp = 0;
-  {
-    const int4 root = __ldg(node_links);
-    stack[sp++] = make_int2(root.x, root.y);
-  }
+  stack[sp++] = root_entry(node_links);
   unsigned long long tests = 0;
   // A valid tree is visited at most once per node (n - 1 internal nodes).
   for (int visits = 0; sp > 0; visits++) {
@@ -433,13 +458,15 @@ __global__ void __launch_bounds__(kThreads, MINB) find_pairs(MeshTopology topo, 
       atomicOr(&counters[3], 2ull);
       return;
     }
-    const int2 e = stack[--sp];
-    // both children's records at once
+    const StackEntry e = stack[--sp];
+    bool want[2];
     int4 lk[2];
     float blo[2][K], bhi[2][K];
 #pragma unroll
-    for (int c = 0; c < 2; c++) {
-      const int ch = c ? e.y : e.x;
+    for (int c = 0; c < 2; c++) {  // the wanted children's records at once
+      want[c] = child_wanted(e, c, s, my_end);
+      const int ch = c ? e.lk.y : e.lk.x;
+      if (!want[c]) continue;
       if (ch < 0) {
         lk[c] = __ldg(leaf_links + ~ch);
         load_box<K>(leaf_box + (int64_t)(~ch) * L::S, blo[c], bhi[c]);
@@ -450,27 +477,21 @@ __global__ void __launch_bounds__(kThreads, MINB) find_pairs(MeshTopology topo, 
     }
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      const int ch = c ? e.y : e.x;
+      if (!want[c]) continue;
+      if (COUNT) tests++;
+      if (!slabs_overlap<K>(qlo, qhi, blo[c], bhi[c])) continue;
+      const int ch = c ? e.lk.y : e.lk.x;
       if (ch < 0) {
-        const int j = ~ch;
-        if (j <= s || j >= my_end) continue;
-        if (COUNT) tests++;
-        if (!slabs_overlap<K>(qlo, qhi, blo[c], bhi[c])) continue;
-        if (!exact_pair<K>(topo, me.x, me.y, me.z, me.w, lk[c], lo64, hi64)) continue;
+        if (!exact_pair<K>(topo, me, lk[c], lo64, hi64)) continue;
         const unsigned long long idx = atomicAdd(&counters[0], 1ull);
         if (idx < cap) {
           pairs[2 * (int64_t)idx] = (uint32_t)me.x;
           pairs[2 * (int64_t)idx + 1] = (uint32_t)lk[c].x;
         }
+      } else if (sp < kStack) {
+        stack[sp++] = child_entry(e, c, lk[c]);
       } else {
-        // later leaves only, and no subtree that starts in a later instance
-        if (lk[c].w <= s || lk[c].z >= my_end) continue;
-        if (COUNT) tests++;
-        if (!slabs_overlap<K>(qlo, qhi, blo[c], bhi[c])) continue;
-        if (sp < kStack)
-          stack[sp++] = make_int2(lk[c].x, lk[c].y);
-        else
-          atomicOr(&counters[3], 1ull);  // stack overflow: reported as an error
+        atomicOr(&counters[3], 1ull);  // stack overflow: reported as an error
       }
     }
   }
@@ -488,12 +509,15 @@ __global__ void __launch_bounds__(kThreads, MINB) find_pairs(MeshTopology topo, 
 // resident.  The quad follows one traversal, so it never diverges; lane 0 of
 // the quad keeps the stack and hands each popped entry to the others.  Each
 // quad performs exactly the per-face traversal's slab tests.
-template <bool COUNT>
-__global__ void __launch_bounds__(kThreads) find_pairs_quad(MeshTopology topo, int n, const int4 *node_links,
-                                                            const int4 *leaf_links, const int32_t *leaf_end,
-                                                            const float *leaf_box, const float *node_box,
-                                                            const double *lo64, const double *hi64, uint32_t *pairs,
-                                                            uint64_t cap, unsigned long long *counters) {
+__device__ __forceinline__ int quad_bcast(unsigned qmask, int x) { return __shfl_sync(qmask, x, 0, 4); }
+
+template <bool COUNT, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) find_pairs_quad(MeshTopology topo, int n, const int4 *node_links,
+                                                                  const int4 *leaf_links, const int32_t *leaf_end,
+                                                                  const float *leaf_box, const float *node_box,
+                                                                  const double *lo64, const double *hi64,
+                                                                  uint32_t *pairs, uint64_t cap,
+                                                                  unsigned long long *counters) {
   typedef BoxLayout<13> L;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int s = (int)(t >> 2), q = (int)(t & 3);
@@ -504,29 +528,30 @@ __global__ void __launch_bounds__(kThreads) find_pairs_quad(MeshTopology topo, i
   const float4 qlo = __ldg(qrec + q), qhi = __ldg(qrec + L::V + q);
   const int4 me = __ldg(leaf_links + s);
   const int my_end = leaf_end ? leaf_end[s] : n;
-  int2 stack[kStack];
-  int sp = 0;
-  if (q == 0) {
-    const int4 root = __ldg(node_links);
-    stack[sp++] = make_int2(root.x, root.y);
-  }
-  sp = __shfl_sync(qmask, sp, 0, 4);
+  StackEntry stack[kStack];  // kept by lane 0 of the quad
+  int sp = 1;
+  if (q == 0) stack[0] = root_entry(node_links);
   unsigned long long tests = 0;
   for (int visits = 0; sp > 0; visits++) {
     if (visits >= n) {
       if (q == 0) atomicOr(&counters[3], 2ull);
       return;
     }
-    int2 e = make_int2(0, 0);
+    StackEntry e{make_int4(0, 0, 0, 0)};
     if (q == 0) e = stack[sp - 1];
     sp--;
-    e.x = __shfl_sync(qmask, e.x, 0, 4);
-    e.y = __shfl_sync(qmask, e.y, 0, 4);
+    e.lk.x = quad_bcast(qmask, e.lk.x);
+    e.lk.y = quad_bcast(qmask, e.lk.y);
+    e.lk.z = quad_bcast(qmask, e.lk.z);
+    e.lk.w = quad_bcast(qmask, e.lk.w);
+    bool want[2];
     int4 lk[2];
     float4 blo[2], bhi[2];
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      const int ch = c ? e.y : e.x;
+      want[c] = child_wanted(e, c, s, my_end);
+      if (!want[c]) continue;
+      const int ch = c ? e.lk.y : e.lk.x;
       const float4 *rec = reinterpret_cast<const float4 *>(ch < 0 ? leaf_box + (int64_t)(~ch) * L::S
                                                                    : node_box + (int64_t)ch * L::S);
       lk[c] = __ldg(ch < 0 ? leaf_links + ~ch : node_links + ch);
@@ -535,33 +560,27 @@ __global__ void __launch_bounds__(kThreads) find_pairs_quad(MeshTopology topo, i
     }
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      const int ch = c ? e.y : e.x;
-      const bool leaf = ch < 0;
-      const bool want = leaf ? ((~ch) > s && (~ch) < my_end) : (lk[c].w > s && lk[c].z < my_end);
-      if (!want) continue;  // uniform within the quad
+      if (!want[c]) continue;  // uniform within the quad
       if (COUNT && q == 0) tests++;
       bool sep = (qhi.x < blo[c].x) || (bhi[c].x < qlo.x) || (qhi.y < blo[c].y) || (bhi[c].y < qlo.y) ||
                  (qhi.z < blo[c].z) || (bhi[c].z < qlo.z) || (qhi.w < blo[c].w) || (bhi[c].w < qlo.w);
       sep |= __shfl_xor_sync(qmask, sep, 1, 4);
       sep |= __shfl_xor_sync(qmask, sep, 2, 4);
       if (sep) continue;
-      if (!leaf) {
-        if (q == 0) {
-          if (sp < kStack)
-            stack[sp] = make_int2(lk[c].x, lk[c].y);
-          else
-            atomicOr(&counters[3], 1ull);  // stack overflow: reported as an error
+      const int ch = c ? e.lk.y : e.lk.x;
+      if (ch >= 0) {
+        if (sp < kStack) {
+          if (q == 0) stack[sp] = child_entry(e, c, lk[c]);
+          sp++;
+        } else if (q == 0) {
+          atomicOr(&counters[3], 1ull);  // stack overflow: reported as an error
         }
-        if (sp < kStack) sp++;
         continue;
       }
-      // Mesh::neighboringFaces (src/Mesh.cpp:13-20), then the reference's
-      // exact FP64 test (KDOPBroadPhase.cpp:132-137), its slabs split over
-      // the quad as above.
+      // Mesh::neighboringFaces, then the exact FP64 test with its slabs
+      // split over the quad as above.
       const int4 b = lk[c];
-      if (me.y == b.y || me.y == b.z || me.y == b.w || me.z == b.y || me.z == b.z || me.z == b.w || me.w == b.y ||
-          me.w == b.z || me.w == b.w)
-        continue;
+      if (adjacent(me, b)) continue;
       bool xsep = false;
       for (int k = 4 * q; k < 4 * q + 4 && k < 13; k++)
         xsep |= (hi64[(int64_t)k * topo.nf + me.x] < lo64[(int64_t)k * topo.nf + b.x]) ||
@@ -581,17 +600,17 @@ __global__ void __launch_bounds__(kThreads) find_pairs_quad(MeshTopology topo, i
 
 // Warp-cooperative (packet) traversal.  A warp takes 32 consecutive leaves in
 // Morton order -- spatially close queries -- and walks the tree once for all
-// of them: each stack entry holds a node's two child references and the mask
-// of lanes whose query overlapped the node (a lane whose query misses a node
-// misses its whole subtree, since a parent's slab contains its children's).
-// At each pop every lane in the mask tests its own query against the two
-// child records, which all lanes load from the same addresses (one memory
-// request per 16-byte piece for the warp instead of one per lane); the lanes
-// that pass make up the child's mask.  Each lane therefore performs exactly
-// the slab tests of its own per-leaf traversal; the stack and the loads are
-// shared, and the chain of visits is the union of the lanes' traversals.
-// Pairs that pass the exact test are appended with one atomic per warp
-// (ballot + prefix of the lanes that emit).
+// of them: each stack entry holds a node and the mask of lanes whose query
+// overlapped it (a lane whose query misses a node misses its whole subtree,
+// since a parent's slab contains its children's).  At each pop every lane in
+// the mask tests its own query against the child records, which all lanes
+// load from the same addresses (one memory request per 16-byte piece for the
+// warp instead of one per lane); the lanes that pass make up the child's
+// mask.  Each lane therefore performs exactly the slab tests of its own
+// per-leaf traversal; the stack and the loads are shared, and the chain of
+// visits is the union of the lanes' traversals.  Pairs that pass the exact
+// test are appended with one atomic per warp (ballot + prefix of the lanes
+// that emit).
 constexpr int kPacketWarps = 4;
 constexpr int kPacketStack = 128;
 
@@ -619,7 +638,7 @@ __global__ void __launch_bounds__(kPacketWarps * 32, 4)
                       const int32_t *leaf_end, const float *leaf_box, const float *node_box, const double *lo64,
                       const double *hi64, uint32_t *pairs, uint64_t cap, unsigned long long *counters) {
   typedef BoxLayout<K> L;
-  __shared__ int2 st_node[kPacketWarps][kPacketStack];
+  __shared__ StackEntry st_node[kPacketWarps][kPacketStack];
   __shared__ unsigned st_mask[kPacketWarps][kPacketStack];
   const unsigned lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
@@ -642,8 +661,7 @@ __global__ void __launch_bounds__(kPacketWarps * 32, 4)
   }
   const unsigned all = __ballot_sync(0xffffffffu, valid);
   if (lane == 0) {
-    const int4 root = __ldg(node_links);
-    st_node[w][0] = make_int2(root.x, root.y);
+    st_node[w][0] = root_entry(node_links);
     st_mask[w][0] = all;
   }
   int sp = 1;
@@ -655,15 +673,18 @@ __global__ void __launch_bounds__(kPacketWarps * 32, 4)
       return;
     }
     sp--;
-    const int2 e = st_node[w][sp];
+    const StackEntry e = st_node[w][sp];
     const unsigned mask = st_mask[w][sp];
     __syncwarp();
     const bool mine = (mask >> lane) & 1u;
+    bool want[2];
     int4 lk[2];
     float blo[2][K], bhi[2][K];
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      const int ch = c ? e.y : e.x;
+      want[c] = mine && child_wanted(e, c, s, my_end);
+      const int ch = c ? e.lk.y : e.lk.x;
+      if (!__any_sync(0xffffffffu, want[c])) continue;
       if (ch < 0) {
         lk[c] = __ldg(leaf_links + ~ch);
         load_box<K>(leaf_box + (int64_t)(~ch) * L::S, blo[c], bhi[c]);
@@ -674,25 +695,21 @@ __global__ void __launch_bounds__(kPacketWarps * 32, 4)
     }
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      const int ch = c ? e.y : e.x;
+      if (!__any_sync(0xffffffffu, want[c])) continue;
+      if (COUNT && want[c]) tests++;
+      const bool hit = want[c] && slabs_overlap<K>(qlo, qhi, blo[c], bhi[c]);
+      const int ch = c ? e.lk.y : e.lk.x;
       if (ch < 0) {
-        const int j = ~ch;
-        const bool test = mine && j > s && j < my_end;
-        if (COUNT && test) tests++;
-        const bool emit = test && slabs_overlap<K>(qlo, qhi, blo[c], bhi[c]) &&
-                          exact_pair<K>(topo, me.x, me.y, me.z, me.w, lk[c], lo64, hi64);
-        emit_pairs(emit, me.x, lk[c].x, pairs, cap, counters);
+        emit_pairs(hit && exact_pair<K>(topo, me, lk[c], lo64, hi64), me.x, lk[c].x, pairs, cap, counters);
       } else {
-        const bool test = mine && lk[c].w > s && lk[c].z < my_end;
-        if (COUNT && test) tests++;
-        const unsigned m = __ballot_sync(0xffffffffu, test && slabs_overlap<K>(qlo, qhi, blo[c], bhi[c]));
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
         if (m) {
           if (sp >= kPacketStack) {  // deeper than any valid tree: reported as an error
             if (lane == 0) atomicOr(&counters[3], 1ull);
             return;
           }
           if (lane == 0) {
-            st_node[w][sp] = make_int2(lk[c].x, lk[c].y);
+            st_node[w][sp] = child_entry(e, c, lk[c]);
             st_mask[w][sp] = m;
           }
           sp++;
@@ -1184,16 +1201,20 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[1], s));
   auto traverse = [&]() {
     const int32_t *lend = topo.ninst > 1 ? b.leaf_end : nullptr;
-    if (p.traversal == kTraversalQuad && kdop) {
+    if ((p.traversal == kTraversalQuad || p.traversal == kTraversalQuadDense) && kdop) {
       const unsigned grid = (unsigned)((4 * (int64_t)nf + kThreads - 1) / kThreads);
-      if (p.count_tests)
-        find_pairs_quad<true><<<grid, kThreads, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend, b.leaf_box,
-                                                        b.node_box, b.lo64, b.hi64, b.pairs, (uint64_t)b.cap_pairs,
-                                                        b.counters);
-      else
-        find_pairs_quad<false><<<grid, kThreads, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend, b.leaf_box,
-                                                         b.node_box, b.lo64, b.hi64, b.pairs, (uint64_t)b.cap_pairs,
-                                                         b.counters);
+#define BP_QUAD(CC, MB)                                                                                  \
+  find_pairs_quad<CC, MB><<<grid, kThreads, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend, b.leaf_box, \
+                                                    b.node_box, b.lo64, b.hi64, b.pairs,                   \
+                                                    (uint64_t)b.cap_pairs, b.counters)
+      if (p.traversal == kTraversalQuadDense) {
+        if (p.count_tests) BP_QUAD(true, 5);
+        else BP_QUAD(false, 5);
+      } else {
+        if (p.count_tests) BP_QUAD(true, 1);
+        else BP_QUAD(false, 1);
+      }
+#undef BP_QUAD
       return;
     }
     if (p.traversal == kTraversalPacket) {

@@ -79,12 +79,13 @@ struct BroadphaseBuffers {
 // register budgets: up to 112 registers, or 80 with three blocks per SM),
 // one warp per 32 consecutive query leaves with a shared stack, or four lanes
 // per query leaf, each testing a quarter of the slabs (13-DOP trees; AABB
-// trees take the thread kernel).
+// trees take the thread kernel), with two register budgets.
 enum TraversalKind : int {
   kTraversalThread = 0,
   kTraversalPacket = 1,
   kTraversalThreadDense = 2,
-  kTraversalQuad = 3
+  kTraversalQuad = 3,
+  kTraversalQuadDense = 4
 };
 
 struct BroadphaseParams {

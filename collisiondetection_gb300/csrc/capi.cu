@@ -327,7 +327,7 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
     if (value < 0 || value > (1 << 20)) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "tree_max_refits must be in [0, 2^20]");
     ctx->opt_tree_max_refits = (int)value;
   } else if (key == "traversal") {
-    if (value < 0 || value > 3) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "traversal must be in [0, 3]");
+    if (value < 0 || value > 4) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "traversal must be in [0, 4]");
     ctx->opt_traversal = (int)value;
   } else if (key == "wave_min_rows") {
     if (value < 0) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "wave_min_rows must be >= 0");

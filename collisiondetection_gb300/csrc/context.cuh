@@ -91,7 +91,7 @@ struct ccd_context {
   int opt_pool_budget = ccd::kPoolBudget;
   int opt_warp_finish = 1;  // the slowest root solves run on whole warps
   int opt_count_tests = 0;
-  int opt_traversal = 0;  // broad-phase traversal (ccd_context_set_option "traversal")
+  int opt_traversal = 3;  // broad-phase traversal (ccd_context_set_option "traversal")
   int opt_tree_refit = 1;         // keep a mesh's tree and refit it while its quality holds
   int opt_tree_rebuild_pct = 130;  // rebuild once the node surface exceeds this percentage of its built value
   int opt_tree_max_refits = 64;    // ... or after this many refits in a row

@@ -114,7 +114,8 @@ int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
  *                    node's loads, 2 as 0 with a smaller register budget
  *                    (more threads resident per SM), 3 four lanes per query
  *                    face, each loading and testing a quarter of every
- *                    13-DOP record (AABB trees take 0); default 0
+ *                    13-DOP record (AABB trees take 0), 4 as 3 with a
+ *                    smaller register budget; default 3
  *   "pool_budget"    further steps the unfinished polynomials get, many per
  *                    warp, before the last ones are finished one per warp
  *                    (0: no limit); default 0

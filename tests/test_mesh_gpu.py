@@ -187,7 +187,7 @@ def test_traversal_kernels_agree(ctx, cloth, label):
     faces, frames = cloth
     k = 40
     out = {}
-    for trav in (0, 1, 2, 3):
+    for trav in (0, 1, 2, 3, 4):
         ctx.set_option("traversal", trav)
         ctx.set_option("count_slab_tests", 1)
         try:
@@ -197,8 +197,8 @@ def test_traversal_kernels_agree(ctx, cloth, label):
                 out[trav] = (vf, ee, m.stats()["slab_tests"], m.stats()["face_pairs"])
         finally:
             ctx.set_option("count_slab_tests", 0)
-            ctx.set_option("traversal", 0)
-    for trav in (1, 2, 3):
+            ctx.set_option("traversal", 3)
+    for trav in (1, 2, 3, 4):
         np.testing.assert_array_equal(out[0][0], out[trav][0])
         np.testing.assert_array_equal(out[0][1], out[trav][1])
         assert out[0][2] == out[trav][2] > 0 and out[0][3] == out[trav][3]
