@@ -68,8 +68,9 @@ def parse():
     ap.add_argument("--graph-iters", type=int, default=50)
     ap.add_argument("--autotune", type=int, default=1,
                     help="choose each context's refinement work split with ccd_autotune_prim_batch first (1) or not (0)")
-    ap.add_argument("--only", default="all", choices=["all", "device"],
-                    help="device: only the resident cull + refine steps (a short run for profilers)")
+    ap.add_argument("--only", default="all", choices=["all", "device", "mesh"],
+                    help="device: only the resident cull + refine steps; mesh: only the mesh configurations "
+                         "(two spheres, cloth on sphere), printing their summary (short runs for profilers)")
     ap.add_argument("--cloth-grid", type=int, default=256)
     ap.add_argument("--cloth-level", type=int, default=6)
     ap.add_argument("--cloth-steps", type=int, default=50)
@@ -909,12 +910,33 @@ def run_reference(args, rank, world, pg):
     print(json.dumps(line), flush=True)
 
 
+def run_mesh_only(args, rank, local):
+    """The mesh configurations alone (a short run for profilers)."""
+    import torch
+
+    import collisiondetection_gb300 as C
+    from collisiondetection_gb300 import build as B
+
+    B.build_library()
+    torch.cuda.set_device(local)
+    ctx = C.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    mesh = mesh_section(ctx, stream, rank, args)
+    if rank == 0:
+        print(json.dumps(round_floats({"mode": "mesh only", "mesh": mesh_summary(mesh, None)})), flush=True)
+    ctx.close()
+
+
 def run_ours(args, rank, world, local, pg):
     import torch
 
     import collisiondetection_gb300 as C
     from collisiondetection_gb300 import build as B
 
+    if args.only == "mesh":
+        run_mesh_only(args, rank, local)
+        return
     B.build_library()
     torch.cuda.set_device(local)
     vf, ee = workload(args.n_vf, args.n_ee)
