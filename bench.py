@@ -245,6 +245,7 @@ def mesh_summary(mesh, uneven):
         c3 = mesh.get("cloth_on_sphere_kdop", {})
         tr = c3.get("traversal", {})
         out["cloth_on_sphere"] = {"faces": c3.get("faces"), "ms_per_step": c3.get("ms_per_step"),
+                                  "direct_ms_per_step": (c3.get("direct") or {}).get("ms_per_step"),
                                   "identical": _identical(c3.get("parity")),
                                   "checked_steps": (c3.get("parity") or {}).get("steps"),
                                   "traversal": {"frac": tr.get("frac"), "achieved_gbs": tr.get("achieved_gbs"),
@@ -254,6 +255,7 @@ def mesh_summary(mesh, uneven):
     if uneven:
         out["uneven_batch"] = {"instances": uneven.get("instances"), "faces": uneven.get("faces"),
                                "ms": uneven["one_call"]["ms"], "value": uneven["one_call"]["value"],
+                               "graph_ms": uneven.get("one_call_graph", {}).get("ms"),
                                "per_instance_ms": uneven.get("per_instance_calls", {}).get("ms"),
                                "identical": _identical(uneven.get("parity"))}
     return out
@@ -329,7 +331,7 @@ def mesh_section(ctx, stream, rank, args):
     threads = os.cpu_count() or 1
     out = {}
 
-    def run_steps(m, frames, kind, eta, reps):
+    def run_steps(m, frames, kind, eta, reps, graph=False):
         ctx.synchronize()
         tests, hits, dts = 0, 0, []
         for _ in range(reps):
@@ -337,7 +339,7 @@ def mesh_section(ctx, stream, rank, args):
                 torch_sync()
                 t0 = time.perf_counter()
                 m.set_positions(frames[k], frames[k + 1])
-                vf, vft, ee, eet = m.detect(kind, eta, eta, path=C.PATH_CULL_REFINE)
+                vf, vft, ee, eet = m.detect(kind, eta, eta, path=C.PATH_CULL_REFINE, graph=graph)
                 dts.append(time.perf_counter() - t0)
                 st = m.stats()
                 tests += st["n_vf"] + st["n_ee"]
@@ -351,12 +353,13 @@ def mesh_section(ctx, stream, rank, args):
 
     def oracle_steps(m, frames, faces, eta, idx):
         """The oracle's broad and narrow phase on steps idx, timed, and each
-        step's candidate and colliding sets checked against the GPU's."""
+        step's candidate and colliding sets checked against the GPU's (the
+        graph-step entry point, as the timed steps use)."""
         t_bp = t_np = 0.0
         checks = []
         for k in idx:
             m.set_positions(frames[k], frames[k + 1])
-            col = m.detect(C.BROADPHASE_KDOP13, eta, eta, path=C.PATH_CULL_REFINE)
+            col = m.detect(C.BROADPHASE_KDOP13, eta, eta, path=C.PATH_CULL_REFINE, graph=True)
             cand = m.candidates()
             t0 = time.perf_counter()
             vf, ee = orc.broadphase(0, frames[k], frames[k + 1], faces, eta)
@@ -389,12 +392,24 @@ def mesh_section(ctx, stream, rank, args):
     with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3) as m:
         run_steps(m, frames[:4], C.BROADPHASE_KDOP13, 1e-6, 1)  # warm-up
         tests, hits, dts = run_steps(m, frames, C.BROADPHASE_KDOP13, 1e-6, 1)
-        total = sum(dts)
+    with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3) as m:
+        # the same steps through ccd_mesh_detect_graph (captured step replayed)
+        run_steps(m, frames[:4], C.BROADPHASE_KDOP13, 1e-6, 1, graph=True)  # warm-up
+        gtests, ghits, gdts = run_steps(m, frames, C.BROADPHASE_KDOP13, 1e-6, 1, graph=True)
+        total = sum(gdts)
         out["cloth_on_sphere_kdop"] = {
-            "faces": int(faces.shape[0]), "vertices": int(frames.shape[1] // 3), "steps": len(dts),
-            "ms_per_step": 1e3 * total / len(dts), "ms_per_step_p50": 1e3 * statistics.median(dts),
-            "ms_per_step_max": 1e3 * max(dts), "stencil_tests": tests, "collisions": hits,
-            "value": tests / total, "unit": "stencil tests/s"}
+            "faces": int(faces.shape[0]), "vertices": int(frames.shape[1] // 3), "steps": len(gdts),
+            "entry_point": "ccd_mesh_detect_graph", "ms_per_step": 1e3 * total / len(gdts),
+            "ms_per_step_p50": 1e3 * statistics.median(gdts), "ms_per_step_max": 1e3 * max(gdts),
+            "stencil_tests": gtests, "collisions": ghits, "value": gtests / total, "unit": "stencil tests/s",
+            "same_as_direct": bool(gtests == tests and ghits == hits),
+            "direct": {"entry_point": "ccd_mesh_detect", "ms_per_step": 1e3 * sum(dts) / len(dts),
+                       "ms_per_step_p50": 1e3 * statistics.median(dts)}}
+    with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3) as m:
+        run_steps(m, frames[:4], C.BROADPHASE_KDOP13, 1e-6, 1)
+        for k in range(len(frames) // 2):  # the kept tree as the stepping leaves it
+            m.set_positions(frames[k], frames[k + 1])
+            m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6, fetch=False)
         # Traversal roofline of one step (k = steps / 2): slab tests from a
         # counting run, device time from timed runs without the counter; on
         # the tree the stepping kept and refitted since the first step, and
@@ -746,9 +761,20 @@ def uneven_section(args, rank):
         dt = time.perf_counter() - t0
         st = m.stats()
         cand = m.candidates()
+        # The same step from a captured graph (ccd_mesh_detect_graph: the
+        # first call runs it directly and captures, the second replays).
+        m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6, fetch=False, graph=True)
+        t0 = time.perf_counter()
+        m.set_positions(frames[0], frames[1])
+        gcol = m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6, graph=True)
+        gdt = time.perf_counter() - t0
+        greplay = m.stats()["graph_replay"]
     tests = st["n_vf"] + st["n_ee"]
     out["one_call"] = {"ms": 1e3 * dt, "stencil_tests": tests, "collisions": st["vf_hits"] + st["ee_hits"],
-                       "value": tests / dt, "unit": "stencil tests/s"}
+                       "value": tests / dt, "unit": "stencil tests/s", "entry_point": "ccd_mesh_detect"}
+    out["one_call_graph"] = {"ms": 1e3 * gdt, "value": tests / gdt, "unit": "stencil tests/s",
+                             "entry_point": "ccd_mesh_detect_graph", "replayed": bool(greplay),
+                             "same_as_direct": all(np.array_equal(a, b) for a, b in zip(gcol, col))}
     if rank == 0:
         # The first `uneven_parity` instances through the oracle, each alone
         # (instances are never paired), against the one call's results for

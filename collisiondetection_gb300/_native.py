@@ -41,7 +41,7 @@ class MeshStats(ctypes.Structure):
                 ("vf_hits", ctypes.c_int64), ("ee_hits", ctypes.c_int64), ("slab_tests", ctypes.c_int64),
                 ("broadphase_ms", ctypes.c_float), ("traversal_ms", ctypes.c_float),
                 ("self_distance_eta", ctypes.c_double), ("tree_built", ctypes.c_int32),
-                ("tree_refits", ctypes.c_int32)]
+                ("tree_refits", ctypes.c_int32), ("graph_replay", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class VelocityFilterStats(ctypes.Structure):
@@ -119,6 +119,7 @@ def load(path: str = LIB):
     L.ccd_mesh_detect.argtypes = [_P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.POINTER(_I64), ctypes.POINTER(_I64)]
     L.ccd_mesh_get_collisions.argtypes = [_P, _P, _P, _P, _P]
+    L.ccd_mesh_detect_graph.argtypes = L.ccd_mesh_detect.argtypes
     L.ccd_mesh_last_stats.argtypes = [_P, ctypes.POINTER(MeshStats)]
     L.ccd_distance_batch.argtypes = [_P, ctypes.c_int, _I64, _P, _P, _P]
     L.ccd_distance_batch_device.argtypes = [_P, ctypes.c_int, _I64, _P, _P, _P]
@@ -481,12 +482,15 @@ class Mesh:
         return out
 
     def detect(self, kind: int = BROADPHASE_KDOP13, outer_eta: float = 1e-6, eta: float = 1e-6,
-               path: int = PATH_CULL_REFINE, fetch: bool = True):
-        """Broad phase + narrow phase on the device.  Returns the colliding
+               path: int = PATH_CULL_REFINE, fetch: bool = True, graph: bool = False):
+        """Broad phase + narrow phase on the device (ccd_mesh_detect, or with
+        graph=True ccd_mesh_detect_graph: the same results, later steps
+        replayed from a captured CUDA graph).  Returns the colliding
         (vf, vf_t, ee, ee_t) in set order, or the two counts if fetch is False."""
         nvf, nee = _I64(), _I64()
-        self.ctx._check(self.lib.ccd_mesh_detect(self.handle, kind, outer_eta, eta, path, ctypes.byref(nvf),
-                                                 ctypes.byref(nee)), "ccd_mesh_detect")
+        fn = self.lib.ccd_mesh_detect_graph if graph else self.lib.ccd_mesh_detect
+        self.ctx._check(fn(self.handle, kind, outer_eta, eta, path, ctypes.byref(nvf), ctypes.byref(nee)),
+                        "ccd_mesh_detect_graph" if graph else "ccd_mesh_detect")
         if not fetch:
             return nvf.value, nee.value
         vf = np.zeros((nvf.value, 4), np.int32)

@@ -728,10 +728,18 @@ __global__ void __launch_bounds__(kPacketWarps * 32, 4)
 // KDOPBroadPhase.cpp:150-183: 6 vertex-face and 9 edge-edge stencils per
 // pair, skipping those whose four vertices are all fixed.
 __global__ void __launch_bounds__(kThreads) stencil_keys(MeshTopology topo, KeyBits kb, const uint8_t *fixed,
-                                                         const uint32_t *pairs, int64_t npairs, uint64_t *vf_keys,
+                                                         const uint32_t *pairs, int64_t npairs,
+                                                         const unsigned long long *count, uint64_t *vf_keys,
                                                          uint64_t *ee_keys) {
   const int64_t pi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (pi >= npairs) return;
+  // With a device count (the graph step), slots past it hold no pair: their
+  // keys are kNoKey, which sort last and are never decoded.
+  if (count && (unsigned long long)pi >= *count) {
+    for (int k = 0; k < 6; k++) vf_keys[6 * pi + k] = kNoKey;
+    for (int k = 0; k < 9; k++) ee_keys[9 * pi + k] = kNoKey;
+    return;
+  }
   const int fa = (int)pairs[2 * pi], fb = (int)pairs[2 * pi + 1];
   int A[3], B[3];
   bool FA[3], FB[3];
@@ -755,6 +763,13 @@ __global__ void __launch_bounds__(kThreads) stencil_keys(MeshTopology topo, KeyB
   }
 }
 
+// Every stencil slot of [0, cap) := the same stencil (the graph step's
+// padding: slots past the real candidates).
+__global__ void __launch_bounds__(kThreads) fill_stencils(int32_t *out, int64_t cap, int4 st) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cap) reinterpret_cast<int4 *>(out)[i] = st;
+}
+
 __global__ void __launch_bounds__(kThreads) first_of_run(const uint64_t *keys, int64_t n, uint32_t *flags) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -765,11 +780,12 @@ __global__ void __launch_bounds__(kThreads) first_of_run(const uint64_t *keys, i
 // Unique keys -> stencils (reference order: keys are sorted).
 __global__ void __launch_bounds__(kThreads) decode_vf(MeshTopology topo, KeyBits kb, const uint64_t *keys,
                                                       const uint32_t *flags,
-                                                      const uint32_t *pos, int64_t n, int32_t *out) {
+                                                      const uint32_t *pos, int64_t n, int32_t *out, int64_t cap) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || !flags[i]) return;
   const uint64_t k = keys[i];
   const int64_t o = pos[i];
+  if (o >= cap) return;
   const int r = (int)(k & kb.rmask);
   out[4 * o] = (int32_t)(k >> kb.rbits);
   out[4 * o + 1] = topo.rank_triple[3 * r];
@@ -779,11 +795,12 @@ __global__ void __launch_bounds__(kThreads) decode_vf(MeshTopology topo, KeyBits
 
 __global__ void __launch_bounds__(kThreads) decode_ee(MeshTopology topo, KeyBits kb, const uint64_t *keys,
                                                       const uint32_t *flags,
-                                                      const uint32_t *pos, int64_t n, int32_t *out) {
+                                                      const uint32_t *pos, int64_t n, int32_t *out, int64_t cap) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || !flags[i]) return;
   const uint64_t k = keys[i];
   const int64_t o = pos[i];
+  if (o >= cap) return;
   const int r1 = (int)(k >> kb.ebits), r2 = (int)(k & kb.emask);
   out[4 * o] = topo.rank_edge[2 * r1];
   out[4 * o + 1] = topo.rank_edge[2 * r1 + 1];
@@ -1063,6 +1080,60 @@ __global__ void __launch_bounds__(kThreads) pair_search(int n, const uint64_t *k
   }
 }
 
+// Enqueues the traversal kernel the parameters choose; pairs past cap are
+// counted but not written.
+void enqueue_traversal(const MeshTopology &topo, const BroadphaseParams &p, BroadphaseBuffers &b, const KeyBits &kb,
+                       uint64_t cap, cudaStream_t s) {
+  const int nf = topo.nf;
+  const bool kdop = p.kind == kBvhKdop13;
+  const int32_t *lend = topo.ninst > 1 ? b.leaf_end : nullptr;
+  if ((p.traversal == kTraversalQuad || p.traversal == kTraversalQuadDense) && kdop) {
+    const unsigned grid = (unsigned)((4 * (int64_t)nf + kThreads - 1) / kThreads);
+#define BP_QUAD(CC, MB)                                                                                  \
+  find_pairs_quad<CC, MB><<<grid, kThreads, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend, b.leaf_box, \
+                                                  b.node_box, b.lo64, b.hi64, b.pairs,                   \
+                                                  cap, b.counters)
+    if (p.traversal == kTraversalQuadDense) {
+      if (p.count_tests) BP_QUAD(true, 5);
+      else BP_QUAD(false, 5);
+    } else {
+      if (p.count_tests) BP_QUAD(true, 1);
+      else BP_QUAD(false, 1);
+    }
+#undef BP_QUAD
+    return;
+  }
+  if (p.traversal == kTraversalPacket) {
+    const unsigned grid = (unsigned)((nf + 32 * kPacketWarps - 1) / (32 * kPacketWarps));
+#define BP_FIND(KK, CC)                                                                                         \
+  find_pairs_packet<KK, CC><<<grid, kPacketWarps * 32, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend,     \
+                                                             b.leaf_box, b.node_box, b.lo64, b.hi64,         \
+                                                             b.pairs, cap, b.counters)
+    if (kdop && p.count_tests) BP_FIND(13, true);
+    else if (kdop) BP_FIND(13, false);
+    else if (p.count_tests) BP_FIND(3, true);
+    else BP_FIND(3, false);
+#undef BP_FIND
+    return;
+  }
+#define BP_FIND(KK, CC, MB)                                                                                       \
+  find_pairs<KK, CC, MB><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend, b.leaf_box, \
+                                                        b.node_box, b.lo64, b.hi64, b.pairs,                  \
+                                                        cap, b.counters)
+  if (p.traversal == kTraversalThreadDense) {
+    if (kdop && p.count_tests) BP_FIND(13, true, 3);
+    else if (kdop) BP_FIND(13, false, 3);
+    else if (p.count_tests) BP_FIND(3, true, 3);
+    else BP_FIND(3, false, 3);
+  } else {
+    if (kdop && p.count_tests) BP_FIND(13, true, 2);
+    else if (kdop) BP_FIND(13, false, 2);
+    else if (p.count_tests) BP_FIND(3, true, 2);
+    else BP_FIND(3, false, 2);
+  }
+#undef BP_FIND
+}
+
 }  // namespace
 
 void broadphase_free(BroadphaseBuffers &b) {
@@ -1199,54 +1270,7 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   BP_CUDA(cudaGetLastError());
 
   if (p.ev[0]) BP_CUDA(cudaEventRecord(p.ev[1], s));
-  auto traverse = [&]() {
-    const int32_t *lend = topo.ninst > 1 ? b.leaf_end : nullptr;
-    if ((p.traversal == kTraversalQuad || p.traversal == kTraversalQuadDense) && kdop) {
-      const unsigned grid = (unsigned)((4 * (int64_t)nf + kThreads - 1) / kThreads);
-#define BP_QUAD(CC, MB)                                                                                  \
-  find_pairs_quad<CC, MB><<<grid, kThreads, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend, b.leaf_box, \
-                                                    b.node_box, b.lo64, b.hi64, b.pairs,                   \
-                                                    (uint64_t)b.cap_pairs, b.counters)
-      if (p.traversal == kTraversalQuadDense) {
-        if (p.count_tests) BP_QUAD(true, 5);
-        else BP_QUAD(false, 5);
-      } else {
-        if (p.count_tests) BP_QUAD(true, 1);
-        else BP_QUAD(false, 1);
-      }
-#undef BP_QUAD
-      return;
-    }
-    if (p.traversal == kTraversalPacket) {
-      const unsigned grid = (unsigned)((nf + 32 * kPacketWarps - 1) / (32 * kPacketWarps));
-#define BP_FIND(KK, CC)                                                                                         \
-  find_pairs_packet<KK, CC><<<grid, kPacketWarps * 32, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend,     \
-                                                               b.leaf_box, b.node_box, b.lo64, b.hi64,         \
-                                                               b.pairs, (uint64_t)b.cap_pairs, b.counters)
-      if (kdop && p.count_tests) BP_FIND(13, true);
-      else if (kdop) BP_FIND(13, false);
-      else if (p.count_tests) BP_FIND(3, true);
-      else BP_FIND(3, false);
-#undef BP_FIND
-      return;
-    }
-#define BP_FIND(KK, CC, MB)                                                                                       \
-  find_pairs<KK, CC, MB><<<grid_of(nf), kThreads, 0, s>>>(topo, nf, b.node_links, b.leaf_links, lend, b.leaf_box, \
-                                                          b.node_box, b.lo64, b.hi64, b.pairs,                  \
-                                                          (uint64_t)b.cap_pairs, b.counters)
-    if (p.traversal == kTraversalThreadDense) {
-      if (kdop && p.count_tests) BP_FIND(13, true, 3);
-      else if (kdop) BP_FIND(13, false, 3);
-      else if (p.count_tests) BP_FIND(3, true, 3);
-      else BP_FIND(3, false, 3);
-    } else {
-      if (kdop && p.count_tests) BP_FIND(13, true, 2);
-      else if (kdop) BP_FIND(13, false, 2);
-      else if (p.count_tests) BP_FIND(3, true, 2);
-      else BP_FIND(3, false, 2);
-    }
-#undef BP_FIND
-  };
+  auto traverse = [&]() { enqueue_traversal(topo, p, b, kb, (uint64_t)b.cap_pairs, s); };
   for (;;) {
     // pairs, vf, ee and the slab-test count; keeps the error word
     BP_CUDA(cudaMemsetAsync(b.counters, 0, 3 * sizeof(unsigned long long), s));
@@ -1285,7 +1309,7 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
     BP_CUDA(cudaStreamSynchronize(s));
     return 0;
   }
-  stencil_keys<<<grid_of(np), kThreads, 0, s>>>(topo, kb, p.fixed, b.pairs, np, b.vf_keys, b.ee_keys);
+  stencil_keys<<<grid_of(np), kThreads, 0, s>>>(topo, kb, p.fixed, b.pairs, np, nullptr, b.vf_keys, b.ee_keys);
   BP_CUDA(cudaGetLastError());
   // Sort, mark the first of each run of equal keys, scan, decode.
   for (int which = 0; which < 2; which++) {
@@ -1303,11 +1327,11 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
     BP_CUDA(cudaStreamSynchronize(s));
     if (which == 0) {
       BP_CUDA(grow(vf_out, vf_cap, 4 * (int64_t)count));
-      decode_vf<<<grid_of(n), kThreads, 0, s>>>(topo, kb, keys, b.flags, b.scan, n, *vf_out);
+      decode_vf<<<grid_of(n), kThreads, 0, s>>>(topo, kb, keys, b.flags, b.scan, n, *vf_out, INT64_MAX);
       *n_vf = count;
     } else {
       BP_CUDA(grow(ee_out, ee_cap, 4 * (int64_t)count));
-      decode_ee<<<grid_of(n), kThreads, 0, s>>>(topo, kb, keys, b.flags, b.scan, n, *ee_out);
+      decode_ee<<<grid_of(n), kThreads, 0, s>>>(topo, kb, keys, b.flags, b.scan, n, *ee_out, INT64_MAX);
       *n_ee = count;
     }
     BP_CUDA(cudaGetLastError());
@@ -1317,6 +1341,55 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
   return 0;
 }
 
+
+int broadphase_enqueue_refit(const MeshTopology &topo, const BroadphaseParams &p, BroadphaseBuffers &b,
+                             int64_t cap_pairs, int32_t *vf_out, int64_t cap_vf, int32_t *ee_out, int64_t cap_ee,
+                             int4 dummy, cudaStream_t s, cudaError_t *err) {
+  const int nf = topo.nf;
+  if (nf < 2 || b.tree_kind != p.kind || b.tree_nf != nf || b.tree_ninst != topo.ninst || cap_pairs > b.cap_pairs)
+    return 5;
+  const bool kdop = p.kind == kBvhKdop13;
+  const Axes ax = make_axes();
+  if (kdop)
+    leaf_slabs<13><<<grid_of(nf), kThreads, 0, s>>>(topo, p, ax, b.lo64, b.hi64, b.face_lo, b.face_hi, b.bounds);
+  else
+    leaf_slabs<3><<<grid_of(nf), kThreads, 0, s>>>(topo, p, ax, b.lo64, b.hi64, b.face_lo, b.face_hi, b.bounds);
+  const KeyBits kb = key_bits(topo);
+  if (kdop)
+    gather_leaves<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, b.face_lo, b.face_hi, b.leaf_box);
+  else
+    gather_leaves<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.keys, kb.fmask, b.face_lo, b.face_hi, b.leaf_box);
+  BP_CUDA(cudaMemsetAsync(b.arrive, 0, (size_t)nf * sizeof(uint32_t), s));
+  BP_CUDA(cudaMemsetAsync(b.counters, 0, 8 * sizeof(unsigned long long), s));
+  if (kdop)
+    refit<13><<<grid_of(nf), kThreads, 0, s>>>(nf, b.node_child, b.parent, b.arrive, b.leaf_box, b.node_box,
+                                               b.counters);
+  else
+    refit<3><<<grid_of(nf), kThreads, 0, s>>>(nf, b.node_child, b.parent, b.arrive, b.leaf_box, b.node_box,
+                                              b.counters);
+  enqueue_traversal(topo, p, b, kb, (uint64_t)cap_pairs, s);
+  stencil_keys<<<grid_of(cap_pairs), kThreads, 0, s>>>(topo, kb, p.fixed, b.pairs, cap_pairs, b.counters, b.vf_keys,
+                                                       b.ee_keys);
+  BP_CUDA(cudaGetLastError());
+  for (int which = 0; which < 2; which++) {
+    uint64_t *keys = which == 0 ? b.vf_keys : b.ee_keys;
+    const int64_t n = (which == 0 ? 6 : 9) * cap_pairs;
+    const int key_bits_used = which == 0 ? bits_for(std::max(topo.nv - 1, 1)) + kb.rbits : 2 * kb.ebits;
+    BP_CUDA(radix_sort_u64(keys, b.keys_alt, nullptr, nullptr, n, 0, key_bits_used + 1, b.temp, b.temp_bytes, s));
+    first_of_run<<<grid_of(n), kThreads, 0, s>>>(keys, n, b.flags);
+    uint32_t *total = (uint32_t *)(b.counters + 1 + which);
+    BP_CUDA(exclusive_scan_u32(b.flags, b.scan, n, total, b.temp, b.temp_bytes, s));
+    int32_t *out = which == 0 ? vf_out : ee_out;
+    const int64_t cap = which == 0 ? cap_vf : cap_ee;
+    fill_stencils<<<grid_of(cap), kThreads, 0, s>>>(out, cap, dummy);
+    if (which == 0)
+      decode_vf<<<grid_of(n), kThreads, 0, s>>>(topo, kb, keys, b.flags, b.scan, n, out, cap);
+    else
+      decode_ee<<<grid_of(n), kThreads, 0, s>>>(topo, kb, keys, b.flags, b.scan, n, out, cap);
+    BP_CUDA(cudaGetLastError());
+  }
+  return 0;
+}
 
 void point_tree_free(PointTreeBuffers &b) {
   void *ptrs[] = {b.pt_lo, b.pt_hi, b.leaf_box, b.node_box, b.node_child, b.node_range, b.parent, b.arrive, b.keys,

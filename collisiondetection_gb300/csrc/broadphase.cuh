@@ -118,6 +118,19 @@ int broadphase_run(const MeshTopology &topo, const BroadphaseParams &p, Broadpha
                    int64_t *n_pairs, int64_t *slab_tests, int num_sms, cudaStream_t s, cudaError_t *err,
                    bool *rebuilt = nullptr);
 
+// The step of a captured graph: the same candidate search on the kept tree
+// (refit only) with no host synchronisation, so that it can be captured.
+// Pairs beyond cap_pairs are counted (counters[0]) but not written; the
+// unique vertex-face / edge-edge counts go to counters[1] / counters[2] (as
+// uint32), and vf_out / ee_out (capacities cap_vf / cap_ee stencils) hold the
+// candidates in set order followed by copies of `dummy` up to the capacity.
+// The caller compares the counts with the capacities afterwards.  Returns 0,
+// 2 on a CUDA error (*err), 5 when no tree of this mesh and kind is kept or
+// cap_pairs exceeds the pair buffers.
+int broadphase_enqueue_refit(const MeshTopology &topo, const BroadphaseParams &p, BroadphaseBuffers &buf,
+                             int64_t cap_pairs, int32_t *vf_out, int64_t cap_vf, int32_t *ee_out, int64_t cap_ee,
+                             int4 dummy, cudaStream_t s, cudaError_t *err);
+
 void broadphase_free(BroadphaseBuffers &buf);
 
 // TrivialBroadPhase::findCollisionCandidates (src/TrivialBroadPhase.cpp:4-53):

@@ -132,9 +132,25 @@ struct ccd_mesh {
   int64_t n_col[2] = {0, 0};
   bool have_col = false;
   ccd_mesh_stats stats{};
+  // A captured refit-only detect step (ccd_mesh_detect_graph): its key, the
+  // buffers it was captured with, its capacities and the pinned words its
+  // counts come back in.
+  cudaGraphExec_t graph = nullptr;
+  std::vector<uintptr_t> graph_sig;
+  int graph_kind = -1, graph_path = -1;
+  double graph_outer = 0.0, graph_eta = 0.0;
+  int64_t gcap_pairs = 0, gcap[2] = {0, 0};
+  unsigned long long *h_graph = nullptr;  // [8] broad-phase counters, [8 + k] collisions of kind k
 };
 
 namespace {
+
+// Padding vertices after a mesh's own (indices nv .. nv + 3): pairwise at
+// least 1,000 apart and not moving, so that a vertex-face or edge-edge
+// stencil of them, and each sub-test of its chain, is rejected by the FP32
+// stage (or misses in FP64) for any eta below about 100.
+constexpr int kPadVerts = 4;
+const double kPadPositions[3 * kPadVerts] = {1e3, 0.0, 0.0, 0.0, 1e3, 0.0, 0.0, 0.0, 1e3, -1e3, -1e3, -1e3};
 
 int mesh_fail(ccd_mesh *m, int code, const std::string &msg) { return fail(m ? m->ctx : nullptr, code, msg); }
 
@@ -265,27 +281,36 @@ int narrow_device(ccd_mesh *m, Lane &L, int kind, int path, int64_t n, const int
 
 // whole: one mesh even when it is made of instances (faces of different
 // instances are paired too).
+ccd::MeshTopology mesh_topology(const ccd_mesh *m, bool whole) {
+  return ccd::MeshTopology{m->nv,        m->nf,        m->nranks,      m->nedges,
+                           m->faces,     m->face_rank, m->rank_triple, m->face_edges,
+                           m->rank_edge, whole ? nullptr : m->face_inst, whole ? 1 : m->ninst};
+}
+
+ccd::BroadphaseParams mesh_params(const ccd_mesh *m, int kind, double outer_eta) {
+  const ccd_context *ctx = m->ctx;
+  return ccd::BroadphaseParams{kind,
+                               outer_eta,
+                               m->qs,
+                               m->qe,
+                               m->has_history ? m->hist_off : nullptr,
+                               m->has_history ? m->hist_pos : nullptr,
+                               m->has_fixed ? m->fixed : nullptr,
+                               ctx->opt_count_tests != 0,
+                               (int)ctx->opt_traversal,
+                               ctx->opt_tree_refit != 0,
+                               (float)ctx->opt_tree_rebuild_pct / 100.0f,
+                               ctx->opt_tree_max_refits,
+                               {nullptr, nullptr, nullptr, nullptr}};
+}
+
 int run_broadphase(ccd_mesh *m, int kind, double outer_eta, bool whole = false) {
   ccd_context *ctx = m->ctx;
   m->have_cand = false;
   m->have_col = false;
   m->stats = ccd_mesh_stats{};
-  const ccd::MeshTopology topo{m->nv,         m->nf,         m->nranks,   m->nedges,
-                               m->faces,      m->face_rank,  m->rank_triple, m->face_edges,
-                               m->rank_edge,  whole ? nullptr : m->face_inst,  whole ? 1 : m->ninst};
-  ccd::BroadphaseParams p{kind,
-                          outer_eta,
-                          m->qs,
-                          m->qe,
-                          m->has_history ? m->hist_off : nullptr,
-                          m->has_history ? m->hist_pos : nullptr,
-                          m->has_fixed ? m->fixed : nullptr,
-                          ctx->opt_count_tests != 0,
-                          (int)ctx->opt_traversal,
-                          ctx->opt_tree_refit != 0,
-                          (float)ctx->opt_tree_rebuild_pct / 100.0f,
-                          ctx->opt_tree_max_refits,
-                          {nullptr, nullptr, nullptr, nullptr}};
+  const ccd::MeshTopology topo = mesh_topology(m, whole);
+  ccd::BroadphaseParams p = mesh_params(m, kind, outer_eta);
   const bool timed = ctx->profiling && m->nf >= 2;
   if (timed) {
     for (int k = 0; k < 4; k++) {
@@ -348,6 +373,8 @@ void free_mesh_buffers(ccd_mesh *m) {
                   n.eta_vv, n.h_prim, n.h_ve, n.h_vv, n.t_prim, n.t_ve, n.t_vv, n.surv, n.counters, n.stage.mem};
     for (void *p : lp) cudaFree(p);
   }
+  if (m->graph) cudaGraphExecDestroy(m->graph);
+  if (m->h_graph) cudaFreeHost(m->h_graph);
   ccd::broadphase_free(m->bp);
   ccd::point_tree_free(m->pt);
   for (cudaEvent_t e : m->bp_ev)
@@ -401,10 +428,17 @@ int create_mesh(ccd_context *ctx, int32_t nverts, int32_t nfaces, const int32_t 
     m->ninst = ninst;
   }
   auto alloc = [&]() -> int {
-    CCD_CUDA(cudaMalloc(&m->qs, 3 * (size_t)nverts * sizeof(double)));
-    CCD_CUDA(cudaMalloc(&m->qe, 3 * (size_t)nverts * sizeof(double)));
+    // Positions, then the four padding vertices of the graph step's
+    // candidate lists (far apart and still: a stencil of them never hits).
+    const size_t room = 3 * ((size_t)nverts + kPadVerts);
+    CCD_CUDA(cudaMalloc(&m->qs, room * sizeof(double)));
+    CCD_CUDA(cudaMalloc(&m->qe, room * sizeof(double)));
     CCD_CUDA(cudaMemsetAsync(m->qs, 0, 3 * (size_t)nverts * sizeof(double), ctx->stream));
     CCD_CUDA(cudaMemsetAsync(m->qe, 0, 3 * (size_t)nverts * sizeof(double), ctx->stream));
+    CCD_CUDA(cudaMemcpyAsync(m->qs + 3 * (size_t)nverts, kPadPositions, sizeof(kPadPositions), cudaMemcpyHostToDevice,
+                             ctx->stream));
+    CCD_CUDA(cudaMemcpyAsync(m->qe + 3 * (size_t)nverts, kPadPositions, sizeof(kPadPositions), cudaMemcpyHostToDevice,
+                             ctx->stream));
     CCD_CUDA(cudaMalloc(&m->fixed, (size_t)nverts));
     CCD_CUDA(cudaMalloc(&m->d_eta, sizeof(double)));
     CCD_CUDA(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
@@ -763,6 +797,229 @@ int ccd_mesh_detect(ccd_mesh *m, int broadphase_kind, double outer_eta, double e
   if (vf_hits) *vf_hits = m->n_col[0];
   if (ee_hits) *ee_hits = m->n_col[1];
   return CCD_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+void drop_graph(ccd_mesh *m) {
+  if (m->graph) cudaGraphExecDestroy(m->graph);
+  m->graph = nullptr;
+  m->graph_sig.clear();
+}
+
+// Every device buffer, capacity and option a captured step depends on: a
+// replay is valid only while all of them are unchanged.
+std::vector<uintptr_t> graph_signature(const ccd_mesh *m) {
+  const ccd_context *ctx = m->ctx;
+  const ccd::BroadphaseBuffers &b = m->bp;
+  std::vector<uintptr_t> v = {
+      (uintptr_t)m->qs, (uintptr_t)m->qe, (uintptr_t)m->fixed, (uintptr_t)m->has_fixed, (uintptr_t)m->d_eta,
+      (uintptr_t)m->cand[0], (uintptr_t)m->cand[1], (uintptr_t)m->col[0], (uintptr_t)m->col[1],
+      (uintptr_t)m->col_t[0], (uintptr_t)m->col_t[1], (uintptr_t)m->side,
+      (uintptr_t)b.lo64, (uintptr_t)b.hi64, (uintptr_t)b.face_lo, (uintptr_t)b.face_hi, (uintptr_t)b.leaf_box,
+      (uintptr_t)b.node_box, (uintptr_t)b.node_child, (uintptr_t)b.node_links, (uintptr_t)b.leaf_links,
+      (uintptr_t)b.leaf_end, (uintptr_t)b.parent, (uintptr_t)b.arrive, (uintptr_t)b.keys, (uintptr_t)b.counters,
+      (uintptr_t)b.pairs, (uintptr_t)b.vf_keys, (uintptr_t)b.ee_keys, (uintptr_t)b.keys_alt, (uintptr_t)b.flags,
+      (uintptr_t)b.scan, (uintptr_t)b.temp, (uintptr_t)b.temp_bytes, (uintptr_t)b.cap_pairs,
+      (uintptr_t)b.cap_faces, (uintptr_t)ctx->opt_wave_steps, (uintptr_t)ctx->opt_pool_budget,
+      (uintptr_t)ctx->opt_wave_min_rows, (uintptr_t)ctx->opt_warp_finish, (uintptr_t)ctx->opt_traversal,
+      (uintptr_t)ctx->opt_narrow_chunk};
+  for (const Lane &L : m->lane) {
+    const NarrowScratch &n = L.ns;
+    const uintptr_t lp[] = {(uintptr_t)L.hit,    (uintptr_t)L.t,         (uintptr_t)L.flags,   (uintptr_t)L.pos,
+                            (uintptr_t)L.scan_temp, (uintptr_t)L.scan_temp_cap, (uintptr_t)L.d_count,
+                            (uintptr_t)n.prim,   (uintptr_t)n.ve,        (uintptr_t)n.vv,      (uintptr_t)n.eta_prim,
+                            (uintptr_t)n.eta_ve, (uintptr_t)n.eta_vv,    (uintptr_t)n.h_prim,  (uintptr_t)n.h_ve,
+                            (uintptr_t)n.h_vv,   (uintptr_t)n.t_prim,    (uintptr_t)n.t_ve,    (uintptr_t)n.t_vv,
+                            (uintptr_t)n.surv,   (uintptr_t)n.counters,  (uintptr_t)n.cap,     (uintptr_t)n.stage.mem,
+                            (uintptr_t)n.stage.cap, (uintptr_t)n.stage.view.wd};
+    v.insert(v.end(), lp, lp + sizeof(lp) / sizeof(lp[0]));
+  }
+  return v;
+}
+
+// The kernels of one refit-only step, enqueued with no host
+// synchronisation: the broad phase on the kept tree into candidate lists
+// padded to their capacities, then both narrow-phase chains and the
+// compaction of their hits, and the counts copied to m->h_graph.
+int enqueue_graph_step(ccd_mesh *m, int kind, double outer_eta, int path) {
+  ccd_context *ctx = m->ctx;
+  const ccd::MeshTopology topo = mesh_topology(m, false);
+  ccd::BroadphaseParams p = mesh_params(m, kind, outer_eta);
+  p.count_tests = false;
+  cudaError_t err = cudaSuccess;
+  const int4 pad = make_int4(m->nv, m->nv + 1, m->nv + 2, m->nv + 3);
+  const int brc = ccd::broadphase_enqueue_refit(topo, p, m->bp, m->gcap_pairs, m->cand[0], m->gcap[0], m->cand[1],
+                                                m->gcap[1], pad, ctx->stream, &err);
+  if (brc == 2) return cuda_fail(ctx, err, "broadphase (graph step)");
+  if (brc) return mesh_fail(m, CCD_ERR_INVALID_ARGUMENT, "graph step without a kept tree");
+  CCD_CUDA(cudaEventRecord(m->fork, ctx->stream));
+  CCD_CUDA(cudaStreamWaitEvent(m->side, m->fork, 0));
+  for (int k = 0; k < 2; k++) {
+    Lane &L = m->lane[k];
+    const int64_t n = m->gcap[k];
+    int rc = narrow_device(m, L, k ? CCD_EDGE_EDGE : CCD_VERTEX_FACE, path, n, m->cand[k], m->d_eta, false, L.hit,
+                           L.t, nullptr);
+    if (rc) return rc;
+    CCD_CUDA(ccd::compact_hits(m->cand[k], L.hit, L.t, n, L.flags, L.pos, L.d_count, L.scan_temp,
+                               (size_t)L.scan_temp_cap, m->col[k], m->col_t[k], L.stream));
+  }
+  CCD_CUDA(cudaEventRecord(m->join, m->side));
+  CCD_CUDA(cudaStreamWaitEvent(ctx->stream, m->join, 0));
+  CCD_CUDA(cudaMemcpyAsync(m->h_graph, m->bp.counters, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  for (int k = 0; k < 2; k++)
+    CCD_CUDA(cudaMemcpyAsync(m->h_graph + 8 + k, m->lane[k].d_count, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+  return CCD_OK;
+}
+
+// Captures the step after a direct detect of the same kind (which built or
+// refitted the tree and sized every buffer for its counts): capacities are
+// the direct step's counts plus a quarter, and every buffer is grown to
+// them before the capture, so that the capture allocates nothing.
+int capture_graph_step(ccd_mesh *m, int kind, double outer_eta, double eta, int path) {
+  ccd_context *ctx = m->ctx;
+  drop_graph(m);
+  const int64_t pairs = m->stats.face_pairs;
+  m->gcap_pairs = std::min<int64_t>(m->bp.cap_pairs, std::max<int64_t>(pairs + pairs / 4, 4096));
+  for (int k = 0; k < 2; k++) {
+    const int64_t n = m->n_cand[k];
+    m->gcap[k] = std::min<int64_t>((k ? 9 : 6) * m->gcap_pairs, std::max<int64_t>(n + n / 4, 4096));
+  }
+  if (!m->h_graph) CCD_CUDA(cudaMallocHost(&m->h_graph, 10 * sizeof(unsigned long long)));
+  m->lane[0].stream = ctx->stream;
+  m->lane[1].stream = m->side;
+  for (int k = 0; k < 2; k++) {
+    Lane &L = m->lane[k];
+    const int64_t n = m->gcap[k];
+    int rc = grow(ctx, &m->cand[k], &m->cand_cap[k], 4 * n);
+    if (!rc) rc = grow(ctx, &L.hit, &L.hit_cap, n);
+    if (!rc) rc = grow(ctx, &L.t, &L.t_cap, n);
+    if (!rc) rc = grow(ctx, &L.flags, &L.flags_cap, n);
+    if (!rc) rc = grow(ctx, &L.pos, &L.pos_cap, n);
+    if (!rc) rc = grow(ctx, &L.scan_temp, &L.scan_temp_cap, (int64_t)ccd::scan_temp_bytes(n));
+    if (!rc) rc = grow(ctx, &m->col[k], &m->col_cap[k], 4 * n);
+    if (!rc) rc = grow(ctx, &m->col_t[k], &m->col_t_cap[k], n);
+    const int64_t chunk = std::min<int64_t>(n, ctx->opt_narrow_chunk);
+    if (!rc) rc = ensure_narrow(m, L, chunk);
+    if (!rc) rc = ensure_stage(ctx, L.ns.stage, chunk, L.stream);
+    if (rc) return rc;
+  }
+  CCD_CUDA(cudaMemcpyAsync(m->d_eta, &eta, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+  CCD_CUDA(cudaStreamSynchronize(m->side));
+  CCD_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  const int rc = enqueue_graph_step(m, kind, outer_eta, path);
+  cudaGraph_t g = nullptr;
+  const cudaError_t end = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (end != cudaSuccess) return cuda_fail(ctx, end, "cudaStreamEndCapture");
+  const cudaError_t inst = cudaGraphInstantiate(&m->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (inst != cudaSuccess) {
+    m->graph = nullptr;
+    return cuda_fail(ctx, inst, "cudaGraphInstantiate");
+  }
+  m->graph_sig = graph_signature(m);
+  m->graph_kind = kind;
+  m->graph_path = path;
+  m->graph_outer = outer_eta;
+  m->graph_eta = eta;
+  return CCD_OK;
+}
+
+// Replays the captured step.  Returns 1 (results not usable: a capacity was
+// exceeded or the traversal reported an error; the caller runs the direct
+// step) or 0 with the mesh's counts, stats and tree bookkeeping updated.
+int replay_graph_step(ccd_mesh *m, int *usable) {
+  ccd_context *ctx = m->ctx;
+  *usable = 0;
+  memset(m->h_graph, 0, 10 * sizeof(unsigned long long));
+  CCD_CUDA(cudaGraphLaunch(m->graph, ctx->stream));
+  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+  const unsigned long long *h = m->h_graph;
+  const int64_t pairs = (int64_t)h[0];
+  const int64_t nvf = (int64_t)(uint32_t)h[1], nee = (int64_t)(uint32_t)h[2];
+  if (h[3] || pairs > m->gcap_pairs || nvf > m->gcap[0] || nee > m->gcap[1]) return CCD_OK;
+  // tree quality, as a direct refit step judges it
+  ccd::BroadphaseBuffers &b = m->bp;
+  float area;
+  const uint32_t bits = (uint32_t)h[5];
+  memcpy(&area, &bits, sizeof(area));
+  if (b.build_area < 0.0f)
+    b.build_area = area;
+  else if (!(area <= (float)ctx->opt_tree_rebuild_pct / 100.0f * b.build_area))
+    b.rebuild_next = true;
+  b.refits++;
+  m->n_cand[0] = nvf;
+  m->n_cand[1] = nee;
+  m->n_col[0] = (int64_t)(uint32_t)h[8];
+  m->n_col[1] = (int64_t)(uint32_t)h[9];
+  m->stats = ccd_mesh_stats{};
+  m->stats.face_pairs = pairs;
+  m->stats.n_vf = nvf;
+  m->stats.n_ee = nee;
+  m->stats.vf_hits = m->n_col[0];
+  m->stats.ee_hits = m->n_col[1];
+  m->stats.slab_tests = -1;
+  m->stats.tree_built = 0;
+  m->stats.tree_refits = b.refits;
+  m->stats.graph_replay = 1;
+  m->have_cand = m->have_col = true;
+  *usable = 1;
+  return CCD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ccd_mesh_detect_graph(ccd_mesh *m, int broadphase_kind, double outer_eta, double eta, int path,
+                          int64_t *vf_hits, int64_t *ee_hits) {
+  if (!m) return CCD_ERR_INVALID_ARGUMENT;
+  ccd_context *ctx = m->ctx;
+  const bool eligible = broadphase_kind != CCD_BROADPHASE_TRIVIAL && !m->has_history && ctx->opt_tree_refit &&
+                        !ctx->profiling && !ctx->opt_count_tests && m->nf >= 2 && m->ninst >= 1;
+  if (eligible && m->graph && m->graph_kind == broadphase_kind && m->graph_path == path &&
+      m->graph_outer == outer_eta && m->graph_eta == eta && !m->bp.rebuild_next &&
+      m->bp.refits < ctx->opt_tree_max_refits && m->bp.tree_kind == broadphase_kind &&
+      graph_signature(m) == m->graph_sig) {
+    CCD_CUDA(cudaSetDevice(ctx->device));
+    int usable = 0;
+    const int rc = replay_graph_step(m, &usable);
+    if (rc) return rc;
+    if (usable) {
+      if (vf_hits) *vf_hits = m->n_col[0];
+      if (ee_hits) *ee_hits = m->n_col[1];
+      return CCD_OK;
+    }
+    drop_graph(m);  // counts outgrew the capture: the direct step below sizes a new one
+  }
+  int rc = ccd_mesh_detect(m, broadphase_kind, outer_eta, eta, path, vf_hits, ee_hits);
+  if (rc || !eligible || m->bp.tree_kind != broadphase_kind) return rc;
+  if (m->graph && graph_signature(m) == m->graph_sig && m->graph_kind == broadphase_kind &&
+      m->graph_path == path && m->graph_outer == outer_eta && m->graph_eta == eta)
+    return CCD_OK;
+  // Capture the step, then replay it once for this step's results: growing
+  // the buffers to the capture's capacities may have replaced the direct
+  // step's output arrays.  The step's results do not depend on the tree, so
+  // the replay's equal the direct step's.
+  rc = capture_graph_step(m, broadphase_kind, outer_eta, eta, path);
+  int usable = 0;
+  if (!rc) rc = replay_graph_step(m, &usable);
+  if (!rc && usable) {
+    if (vf_hits) *vf_hits = m->n_col[0];
+    if (ee_hits) *ee_hits = m->n_col[1];
+    return CCD_OK;
+  }
+  drop_graph(m);
+  return ccd_mesh_detect(m, broadphase_kind, outer_eta, eta, path, vf_hits, ee_hits);
 }
 
 int ccd_mesh_get_collisions(ccd_mesh *m, int32_t *vf, double *vf_t, int32_t *ee, double *ee_t) {

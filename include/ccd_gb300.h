@@ -289,6 +289,8 @@ typedef struct {
                                qualifying vertex distance (+inf if none); 0 otherwise */
   int32_t tree_built;       /* 1: the broad phase built its tree; 0: it refitted the kept one */
   int32_t tree_refits;      /* refit-only broad phases since the tree was last built */
+  int32_t graph_replay;     /* 1: ccd_mesh_detect_graph replayed its captured step */
+  int32_t reserved;
 } ccd_mesh_stats;
 
 /* faces: nfaces x 3 vertex indices in [0, nverts).  Topology is fixed for the
@@ -374,7 +376,25 @@ int ccd_narrowphase_separating_plane(ccd_mesh *mesh, int64_t n_vf, const int32_t
  * ccd_mesh_get_collisions, the candidates for ccd_broadphase_get. */
 int ccd_mesh_detect(ccd_mesh *mesh, int broadphase_kind, double outer_eta, double eta, int path, int64_t *vf_hits,
                     int64_t *ee_hits);
-/* Colliding stencils of the last ccd_mesh_detect in the reference's set
+/* No counterpart in the reference (it has no device work to capture).  The
+ * same step and results as ccd_mesh_detect, for a mesh stepped repeatedly
+ * with the same kind, paddings and path: the first call runs the step
+ * directly, then captures its refit-only form -- the broad phase on the
+ * kept tree, the narrow-phase chains and the compaction, with no host
+ * synchronisation in between -- into a CUDA graph on the context's stream,
+ * with room for a quarter more candidates than that step found; later calls
+ * replay the graph (one launch and one synchronisation).  The candidate
+ * lists of a replay are padded to their capacity with stencils of four
+ * padding vertices kept after the mesh's own, which never hit.  When a
+ * replay finds more pairs or stencils than the capture has room for, when
+ * the kept tree needs a rebuild, or when the context's options or the
+ * mesh's buffers changed, the call runs the step directly (and captures a
+ * new graph).  Needs the context's "tree_refit" on, profiling and
+ * "count_slab_tests" off, a two-entry step (no ccd_mesh_set_history) and a
+ * k-DOP or AABB broad phase; otherwise it is ccd_mesh_detect. */
+int ccd_mesh_detect_graph(ccd_mesh *mesh, int broadphase_kind, double outer_eta, double eta, int path,
+                          int64_t *vf_hits, int64_t *ee_hits);
+/* Colliding stencils of the last ccd_mesh_detect(_graph) in the reference's set
  * order with the t of their first hitting sub-test; any pointer may be NULL. */
 int ccd_mesh_get_collisions(ccd_mesh *mesh, int32_t *vf, double *vf_t, int32_t *ee, double *ee_t);
 int ccd_mesh_last_stats(const ccd_mesh *mesh, ccd_mesh_stats *out);

@@ -204,6 +204,83 @@ def test_traversal_kernels_agree(ctx, cloth, label):
         assert out[0][2] == out[trav][2] > 0 and out[0][3] == out[trav][3]
 
 
+@pytest.mark.parametrize("label", ["kdop", "aabb"])
+def test_graph_step_equals_direct_step(ctx, cloth, label):
+    # Consecutive cloth steps through ccd_mesh_detect_graph: the first one
+    # (and every step whose candidates outgrow the capture, as contact
+    # spreads from step 25 on) runs directly and captures; the others replay
+    # the captured graph.  Every step's candidates and collisions equal a
+    # direct step's on a mesh of its own.
+    faces, frames = cloth
+    eta = 1e-6
+    kind = KINDS[label]
+    got, replays = [], 0
+    with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3) as m:
+        for k in range(20, 45):
+            m.set_positions(frames[k], frames[k + 1])
+            col = m.detect(kind, eta, eta, graph=True)
+            got.append((col, m.candidates(), m.stats()))
+            replays += m.stats()["graph_replay"]
+    assert replays >= 10
+    with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3) as m:
+        for k, (col, cand, st) in zip(range(20, 45), got):
+            m.set_positions(frames[k], frames[k + 1])
+            ref = m.detect(kind, eta, eta)
+            rcand = m.candidates()
+            for a, b in zip(cand + col, rcand + ref):
+                np.testing.assert_array_equal(a, b)
+            assert st["n_vf"] == m.stats()["n_vf"] and st["face_pairs"] == m.stats()["face_pairs"]
+
+
+def test_graph_step_on_instances_matches_oracle(ctx, oracle):
+    # An instance mesh (32 instances of the uneven batch) replayed from its
+    # graph on a second step, against the oracle on each instance alone.
+    import oracle as O
+
+    sizes = W.uneven_sizes(512, seed=0)
+    pick = [int(i) for i in np.nonzero(sizes <= 30_000)[0][:32]]
+    faces, frames, vo, fo = W.uneven_batch(512, seed=0, select=pick, steps=2)
+    eta = 1e-6
+    with C.Mesh(ctx, faces, nverts=frames.shape[1] // 3, instances=(vo, fo)) as m:
+        m.set_positions(frames[0], frames[1])
+        m.detect(C.BROADPHASE_KDOP13, eta, eta, graph=True)
+        m.set_positions(frames[1], frames[2])
+        col = m.detect(C.BROADPHASE_KDOP13, eta, eta, graph=True)
+        assert m.stats()["graph_replay"] == 1
+        cand = m.candidates()
+    parts = {k: [] for k in ("vf_c", "ee_c", "vf_hit", "ee_hit", "vf_t", "ee_t")}
+    for i in range(32):
+        a, b = 3 * vo[i], 3 * vo[i + 1]
+        fi = faces[fo[i]:fo[i + 1]] - vo[i]
+        vf_c, ee_c = oracle.broadphase(0, frames[1][a:b], frames[2][a:b], fi, eta)
+        r = oracle.narrowphase(frames[1][a:b], frames[2][a:b], vf_c, eta, ee_c, eta, nthreads=os.cpu_count() or 4)
+        parts["vf_c"].append(vf_c + vo[i])
+        parts["ee_c"].append(ee_c + vo[i])
+        for k in ("vf_hit", "ee_hit", "vf_t", "ee_t"):
+            parts[k].append(r[k])
+    cat = {k: np.concatenate(v) for k, v in parts.items()}
+    r = O.compare_step_results(cat["vf_c"], cat["ee_c"], cat, cand, col)
+    assert r["identical_candidates"] and r["identical_collisions"], r
+    assert r["max_rel_t_err"] <= TOL
+
+
+def test_graph_step_falls_back_when_not_eligible(ctx, golden):
+    # With the context's tree refit off, or profiling on, the call is the
+    # direct step (and says so).
+    qs, qe, f, _, meta = _scene(golden, "spheres")
+    with C.Mesh(ctx, f, qs, qe) as m:
+        ref = m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6)
+        ctx.set_option("tree_refit", 0)
+        try:
+            for _ in range(3):
+                got = m.detect(C.BROADPHASE_KDOP13, 1e-6, 1e-6, graph=True)
+                assert m.stats()["graph_replay"] == 0
+        finally:
+            ctx.set_option("tree_refit", 1)
+        for a, b in zip(got, ref):
+            np.testing.assert_array_equal(a, b)
+
+
 def test_uneven_instances_match_oracle(ctx, oracle):
     # 32 instances of the 512-instance uneven batch (icospheres and sheet
     # pairs; the first 32 with at most 30,000 requested triangles, so that
