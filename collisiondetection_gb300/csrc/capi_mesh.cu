@@ -878,16 +878,19 @@ int enqueue_graph_step(ccd_mesh *m, int kind, double outer_eta, int path) {
 
 // Captures the step after a direct detect of the same kind (which built or
 // refitted the tree and sized every buffer for its counts): capacities are
-// the direct step's counts plus a quarter, and every buffer is grown to
-// them before the capture, so that the capture allocates nothing.
+// twice the direct step's counts, and every buffer is grown to them before
+// the capture, so that the capture allocates nothing.
 int capture_graph_step(ccd_mesh *m, int kind, double outer_eta, double eta, int path) {
   ccd_context *ctx = m->ctx;
   drop_graph(m);
+  // Twice the direct step's counts: a growing contact then outgrows a
+  // capture only every doubling, and each recapture (a direct step, the
+  // capture and its instantiation) costs several steps' host time.
   const int64_t pairs = m->stats.face_pairs;
-  m->gcap_pairs = std::min<int64_t>(m->bp.cap_pairs, std::max<int64_t>(pairs + pairs / 4, 4096));
+  m->gcap_pairs = std::min<int64_t>(m->bp.cap_pairs, std::max<int64_t>(2 * pairs, 4096));
   for (int k = 0; k < 2; k++) {
     const int64_t n = m->n_cand[k];
-    m->gcap[k] = std::min<int64_t>((k ? 9 : 6) * m->gcap_pairs, std::max<int64_t>(n + n / 4, 4096));
+    m->gcap[k] = std::min<int64_t>((k ? 9 : 6) * m->gcap_pairs, std::max<int64_t>(2 * n, 4096));
   }
   if (!m->h_graph) CCD_CUDA(cudaMallocHost(&m->h_graph, 10 * sizeof(unsigned long long)));
   m->lane[0].stream = ctx->stream;

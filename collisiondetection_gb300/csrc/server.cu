@@ -90,9 +90,10 @@ int run_job(ccd_context *ctx, Job &j) {
     const Clock::time_point t0 = Clock::now();
     rc = ccd_mesh_set_positions(m, j.frames + k * frame, j.frames + (k + 1) * frame);
     int64_t nvf = 0, nee = 0;
-    // The request's mesh (tree, buffers) stays resident across its steps,
-    // and steps after the first replay a captured graph of the step.
-    if (!rc) rc = ccd_mesh_detect_graph(m, r.broadphase_kind, r.outer_eta, r.eta, r.path, &nvf, &nee);
+    // The request's mesh (tree, buffers) stays resident across its steps.
+    // (A request's ten steps are too few for a captured step to repay its
+    // capture.)
+    if (!rc) rc = ccd_mesh_detect(m, r.broadphase_kind, r.outer_eta, r.eta, r.path, &nvf, &nee);
     if (!rc) {
       const size_t ovf = j.vf_t.size(), oee = j.ee_t.size();
       j.vf.resize(4 * (ovf + (size_t)nvf));

@@ -382,7 +382,7 @@ int ccd_mesh_detect(ccd_mesh *mesh, int broadphase_kind, double outer_eta, doubl
  * directly, then captures its refit-only form -- the broad phase on the
  * kept tree, the narrow-phase chains and the compaction, with no host
  * synchronisation in between -- into a CUDA graph on the context's stream,
- * with room for a quarter more candidates than that step found; later calls
+ * with room for twice the candidates that step found; later calls
  * replay the graph (one launch and one synchronisation).  The candidate
  * lists of a replay are padded to their capacity with stencils of four
  * padding vertices kept after the mesh's own, which never hit.  When a
