@@ -1184,6 +1184,18 @@ def run_ours(args, rank, world, local, pg):
                                            for k in ("vf", "ee")},
                     "refine_ms_per_launch": refine_ms_launch, "cull_ms_per_launch": cull_ms_launch,
                     "share_refine": (tm["refine_ms"] / (tm["cull_ms"] + tm["refine_ms"]))}
+        # The same work priced at the measured rates of each operation: adds,
+        # multiplies and square roots at the add / multiply rate, divisions at
+        # the division rate (several FP64 instructions each).  The survivors'
+        # share of each kind's operation mix is taken as their share of its
+        # flops.
+        t_peak = 0.0
+        for k in ("vf", "ee"):
+            ops, share = flops[k]["ops"], flops[k]["flops_survivors"] / max(1, flops[k]["flops_all_rows"])
+            t_peak += share * ((ops["add"] + ops["mul"] + ops["sqrt"]) / peak64["ops_per_s"]
+                               + ops["div"] / peak64["div_per_s"])
+        roofline["frac_division_priced"] = t_peak * 1e3 / ms_launches
+        roofline["fp64_latency_cycles"] = {op: round(peak64[op + "_latency_cycles"], 1) for op in ("add", "mul", "div")}
     # the FP32 cull's false negatives and the contact-time error of the
     # headline path, against the oracle (all rows) and the all-FP64 GPU paths
     parity = None
@@ -1218,7 +1230,8 @@ def run_ours(args, rank, world, local, pg):
             "gpu_launches": int(tm["launches"]),
             "e2e": compact(e2e, ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step", "matches_device_path")),
             "roofline": compact(roofline, ("kernel", "bound", "achieved", "peak", "unit", "frac", "peak_source",
-                                           "traffic", "flops_per_survivor")),
+                                           "traffic", "flops_per_survivor", "frac_division_priced",
+                                           "fp64_latency_cycles")),
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "fp64_path": ({"plain": fp64_tps, "staged": staged_tps, "speedup_vs_plain": value / (world * fp64_tps),

@@ -62,7 +62,8 @@ class TuneResult(ctypes.Structure):
 
 class Fp64Peak(ctypes.Structure):
     _fields_ = [("ops_per_s", ctypes.c_double), ("fma_flops_per_s", ctypes.c_double), ("ms", ctypes.c_double),
-                ("ops", ctypes.c_int64)]
+                ("ops", ctypes.c_int64), ("div_per_s", ctypes.c_double), ("add_latency_cycles", ctypes.c_double),
+                ("mul_latency_cycles", ctypes.c_double), ("div_latency_cycles", ctypes.c_double)]
 
 
 _lib = None

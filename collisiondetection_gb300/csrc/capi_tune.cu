@@ -85,6 +85,43 @@ __global__ void __launch_bounds__(kPeakThreads) fp64_chains(int iters, double a,
   if (sum == -1.0) sink[0] = sum;
 }
 
+// Division throughput: kChains independent chains x = c / x per thread
+// (c near 1.3, so every x stays near 1).
+__global__ void __launch_bounds__(kPeakThreads) fp64_div_chains(int iters, double c, double *sink) {
+  double x[kChains];
+#pragma unroll
+  for (int k = 0; k < kChains; k++) x[k] = 1.0 + 1e-3 * (double)(threadIdx.x + k);
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < kChains; k++) x[k] = c / x[k];
+  }
+  double sum = 0.0;
+#pragma unroll
+  for (int k = 0; k < kChains; k++) sum += x[k];
+  if (sum == -1.0) sink[0] = sum;
+}
+
+// Latency: one warp runs one dependent chain of each operation, timed with
+// the SM clock.  cycles[0..2] = add, multiply, division chain lengths in
+// cycles; the host divides by the chain length.
+__global__ void fp64_latency(int iters, double a, double b, double c, double *sink, long long *cycles) {
+  double x = 1.0 + 1e-3 * (double)threadIdx.x;
+  __syncwarp();
+  const long long t0 = clock64();
+  for (int i = 0; i < iters; i++) x = x + b;
+  const long long t1 = clock64();
+  for (int i = 0; i < iters; i++) x = x * a;
+  const long long t2 = clock64();
+  for (int i = 0; i < iters; i++) x = c / x;
+  const long long t3 = clock64();
+  if (x == -1.0) sink[0] = x;
+  if (threadIdx.x == 0) {
+    cycles[0] = t1 - t0;
+    cycles[1] = t2 - t1;
+    cycles[2] = t3 - t2;
+  }
+}
+
 }  // namespace
 
 using namespace ccd_capi;
@@ -260,33 +297,40 @@ int ccd_fp64_peak(ccd_context *ctx, int reps, ccd_fp64_peak_result *out) {
   const int grid = ctx->num_sms * std::max(1, per_sm);
   const int iters = 4096;
   double *sink = nullptr;
+  long long *cycles = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   struct Cleanup {
     double *&sink;
+    long long *&cycles;
     cudaEvent_t *ev;
     ~Cleanup() {
       cudaFree(sink);
+      cudaFree(cycles);
       for (int k = 0; k < 2; k++)
         if (ev[k]) cudaEventDestroy(ev[k]);
     }
-  } cleanup{sink, ev};
+  } cleanup{sink, cycles, ev};
   CCD_CUDA(cudaMalloc(&sink, sizeof(double)));
+  CCD_CUDA(cudaMalloc(&cycles, 3 * sizeof(long long)));
   for (int k = 0; k < 2; k++) CCD_CUDA(cudaEventCreate(&ev[k]));
-  const double a = 0.9999999, b = 1e-7;
-  float best[2] = {0.f, 0.f};
-  for (int fma = 0; fma < 2; fma++) {
-    for (int r = 0; r <= reps; r++) {  // the first run warms up
+  const double a = 0.9999999, b = 1e-7, c = 1.3;
+  const int div_iters = iters / 8;
+  float best[3] = {0.f, 0.f, 0.f};
+  for (int kind = 0; kind < 3; kind++) {  // add + multiply, fused multiply-add, division
+    for (int r = 0; r <= reps; r++) {     // the first run warms up
       CCD_CUDA(cudaEventRecord(ev[0], ctx->stream));
-      if (fma)
+      if (kind == 1)
         fp64_chains<true><<<grid, kPeakThreads, 0, ctx->stream>>>(iters, a, b, sink);
-      else
+      else if (kind == 0)
         fp64_chains<false><<<grid, kPeakThreads, 0, ctx->stream>>>(iters, a, b, sink);
+      else
+        fp64_div_chains<<<grid, kPeakThreads, 0, ctx->stream>>>(div_iters, c, sink);
       CCD_CUDA(cudaGetLastError());
       CCD_CUDA(cudaEventRecord(ev[1], ctx->stream));
       CCD_CUDA(cudaEventSynchronize(ev[1]));
       float ms = 0.f;
       CCD_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
-      if (r > 0 && (best[fma] == 0.f || ms < best[fma])) best[fma] = ms;
+      if (r > 0 && (best[kind] == 0.f || ms < best[kind])) best[kind] = ms;
     }
   }
   const double lanes = (double)grid * kPeakThreads * kChains * iters;
@@ -294,6 +338,18 @@ int ccd_fp64_peak(ccd_context *ctx, int reps, ccd_fp64_peak_result *out) {
   out->ms = best[0];
   out->ops_per_s = 2.0 * lanes / (best[0] * 1e-3);
   out->fma_flops_per_s = 2.0 * lanes / (best[1] * 1e-3);
+  out->div_per_s = (double)grid * kPeakThreads * kChains * div_iters / (best[2] * 1e-3);
+  const int lat_iters = 2048;
+  for (int r = 0; r < 2; r++) {  // the first run warms up
+    fp64_latency<<<1, 32, 0, ctx->stream>>>(lat_iters, a, b, c, sink, cycles);
+    CCD_CUDA(cudaGetLastError());
+  }
+  long long host_cycles[3] = {0, 0, 0};
+  CCD_CUDA(cudaMemcpyAsync(host_cycles, cycles, sizeof host_cycles, cudaMemcpyDeviceToHost, ctx->stream));
+  CCD_CUDA(cudaStreamSynchronize(ctx->stream));
+  out->add_latency_cycles = (double)host_cycles[0] / lat_iters;
+  out->mul_latency_cycles = (double)host_cycles[1] / lat_iters;
+  out->div_latency_cycles = (double)host_cycles[2] / lat_iters;
   return CCD_OK;
 }
 

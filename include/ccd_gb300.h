@@ -191,12 +191,19 @@ int ccd_prim_cull_device(ccd_context *ctx, int kind, int64_t n, const double *ro
  * the context's stream (best of `reps`).  ops_per_s counts one operation per
  * DADD or DMUL (the library is built without FMA contraction, so each of its
  * FP64 additions and multiplications is one such instruction); fma_flops_per_s
- * counts two per DFMA.  Blocks until done. */
+ * counts two per DFMA.  div_per_s is the same measure for correctly rounded
+ * FP64 divisions.  The latencies come from one warp running one dependent
+ * chain of each operation, timed with the SM clock (cycles per operation).
+ * Blocks until done. */
 typedef struct {
-  double ops_per_s;        /* FP64 add + multiply instructions per second (lanes) */
-  double fma_flops_per_s;  /* 2 x FP64 fused multiply-adds per second (lanes) */
-  double ms;               /* duration of the best add / multiply run */
-  int64_t ops;             /* operations of one add / multiply run */
+  double ops_per_s;           /* FP64 add + multiply instructions per second (lanes) */
+  double fma_flops_per_s;     /* 2 x FP64 fused multiply-adds per second (lanes) */
+  double ms;                  /* duration of the best add / multiply run */
+  int64_t ops;                /* operations of one add / multiply run */
+  double div_per_s;           /* FP64 divisions per second (lanes) */
+  double add_latency_cycles;  /* dependent FP64 addition */
+  double mul_latency_cycles;  /* dependent FP64 multiplication */
+  double div_latency_cycles;  /* dependent FP64 division */
 } ccd_fp64_peak_result;
 int ccd_fp64_peak(ccd_context *ctx, int reps, ccd_fp64_peak_result *out);
 

@@ -162,6 +162,11 @@ def test_fp64_peak_is_plausible(ctx):
     # GB300: about 1.2 TFLOP/s of FP64 FMA; DADD / DMUL issue at the same rate
     assert 1e11 < p["ops_per_s"] < 1e13 and 1e11 < p["fma_flops_per_s"] < 1e13
     assert p["ms"] > 0 and p["ops"] > 0
+    # a correctly rounded division is several dependent FP64 operations
+    assert 1e9 < p["div_per_s"] < p["ops_per_s"]
+    for op in ("add", "mul"):
+        assert 1.0 < p[op + "_latency_cycles"] < 1000.0
+    assert p["add_latency_cycles"] < p["div_latency_cycles"] < 10000.0
 
 
 def test_t_untouched_on_miss_and_eta_per_row(ctx):
