@@ -99,8 +99,11 @@ struct ccd_context {
   int64_t opt_chunk_rows = ccd_capi::kChunkRows;  // host-memory batches: rows per chunk
   // Mesh narrow phase: stencils per chunk.  Each chunk's refinement ends in
   // the latency-bound tail of its slowest root solves, so chunks are large
-  // (about 1.3 KB of rows and results per stencil).
-  int64_t opt_narrow_chunk = (int64_t)1 << 22;
+  // (about 1.3 KB of rows and results per stencil: 22 GB per kind for a step
+  // of 2^24 stencils or more, allocated for min(stencils, chunk)).  On the
+  // 512-instance batch (167 M stencils) 2^24 takes 12.3 s against 13.7 s
+  // at 2^22.
+  int64_t opt_narrow_chunk = (int64_t)1 << 24;
   int64_t opt_layer_events = (int64_t)1 << 20;      // velocity filter: firings per event-loop launch
   std::string err;
 };

@@ -124,8 +124,9 @@ int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
  *                    chunks; in [1024, 2^26], default 2^23
  *   "narrow_chunk"   mesh narrow phase (two-entry steps): stencils per chunk
  *                    of rows gathered and refined together (each chunk pays
- *                    the tail of its slowest root solves once); in
- *                    [1024, 2^24], default 2^22
+ *                    the tail of its slowest root solves once; the row
+ *                    scratch is about 200 B per stencil); in [1024, 2^24],
+ *                    default 2^24
  *   "layer_events_per_launch" ccd_velocity_filter: firings per launch of the
  *                    event loop (it pauses and continues); default 2^20
  *   "layer_grid_min" ccd_velocity_filter: when a penalty group holds this
