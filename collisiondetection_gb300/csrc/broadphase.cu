@@ -448,17 +448,23 @@ __global__ void __launch_bounds__(kThreads, MINB) find_pairs(MeshTopology topo, 
   load_box<K>(leaf_box + (int64_t)s * L::S, qlo, qhi);
   const int4 me = __ldg(leaf_links + s);
   const int my_end = leaf_end ? leaf_end[s] : n;
+  // The visited node stays in registers: a visit with one overlapping
+  // internal child goes on with it, and only the second of two goes through
+  // the stack (the same visits as pushing every child, in another order).
   StackEntry stack[kStack];
   int sp = 0;
-  stack[sp++] = root_entry(node_links);
+  StackEntry e = root_entry(node_links);
+  bool have = true;
   unsigned long long tests = 0;
   // A valid tree is visited at most once per node (n - 1 internal nodes).
-  for (int visits = 0; sp > 0; visits++) {
+  for (int visits = 0; have || sp > 0; visits++) {
     if (visits >= n) {
       atomicOr(&counters[3], 2ull);
       return;
     }
-    const StackEntry e = stack[--sp];
+    if (!have) e = stack[--sp];
+    have = false;
+    StackEntry next{make_int4(0, 0, 0, 0)};
     bool want[2];
     int4 lk[2];
     float blo[2][K], bhi[2][K];
@@ -488,12 +494,16 @@ __global__ void __launch_bounds__(kThreads, MINB) find_pairs(MeshTopology topo, 
           pairs[2 * (int64_t)idx] = (uint32_t)me.x;
           pairs[2 * (int64_t)idx + 1] = (uint32_t)lk[c].x;
         }
+      } else if (!have) {
+        next = child_entry(e, c, lk[c]);
+        have = true;
       } else if (sp < kStack) {
         stack[sp++] = child_entry(e, c, lk[c]);
       } else {
         atomicOr(&counters[3], 1ull);  // stack overflow: reported as an error
       }
     }
+    if (have) e = next;
   }
   if (COUNT && tests) atomicAdd(&counters[4], tests);
 }
@@ -528,22 +538,32 @@ __global__ void __launch_bounds__(kThreads, MINB) find_pairs_quad(MeshTopology t
   const float4 qlo = __ldg(qrec + q), qhi = __ldg(qrec + L::V + q);
   const int4 me = __ldg(leaf_links + s);
   const int my_end = leaf_end ? leaf_end[s] : n;
+  // The node being visited sits in registers of all four lanes: a visit that
+  // finds one overlapping internal child goes on with it directly, and only
+  // when both overlap does one go through the stack (lane 0's, broadcast to
+  // the quad when popped).  The set of visits, and so of slab tests, is the
+  // same as with every child pushed; only their order differs.
   StackEntry stack[kStack];  // kept by lane 0 of the quad
-  int sp = 1;
-  if (q == 0) stack[0] = root_entry(node_links);
+  int sp = 0;
+  StackEntry e = root_entry(node_links);
+  bool have = true;
   unsigned long long tests = 0;
-  for (int visits = 0; sp > 0; visits++) {
+  for (int visits = 0; have || sp > 0; visits++) {
     if (visits >= n) {
       if (q == 0) atomicOr(&counters[3], 2ull);
       return;
     }
-    StackEntry e{make_int4(0, 0, 0, 0)};
-    if (q == 0) e = stack[sp - 1];
-    sp--;
-    e.lk.x = quad_bcast(qmask, e.lk.x);
-    e.lk.y = quad_bcast(qmask, e.lk.y);
-    e.lk.z = quad_bcast(qmask, e.lk.z);
-    e.lk.w = quad_bcast(qmask, e.lk.w);
+    if (!have) {
+      StackEntry p{make_int4(0, 0, 0, 0)};
+      if (q == 0) p = stack[sp - 1];
+      sp--;
+      e.lk.x = quad_bcast(qmask, p.lk.x);
+      e.lk.y = quad_bcast(qmask, p.lk.y);
+      e.lk.z = quad_bcast(qmask, p.lk.z);
+      e.lk.w = quad_bcast(qmask, p.lk.w);
+    }
+    have = false;
+    StackEntry next{make_int4(0, 0, 0, 0)};
     bool want[2];
     int4 lk[2];
     float4 blo[2], bhi[2];
@@ -569,7 +589,10 @@ __global__ void __launch_bounds__(kThreads, MINB) find_pairs_quad(MeshTopology t
       if (sep) continue;
       const int ch = c ? e.lk.y : e.lk.x;
       if (ch >= 0) {
-        if (sp < kStack) {
+        if (!have) {  // every lane loaded lk[c]: no broadcast needed
+          next = child_entry(e, c, lk[c]);
+          have = true;
+        } else if (sp < kStack) {
           if (q == 0) stack[sp] = child_entry(e, c, lk[c]);
           sp++;
         } else if (q == 0) {
@@ -594,6 +617,7 @@ __global__ void __launch_bounds__(kThreads, MINB) find_pairs_quad(MeshTopology t
         pairs[2 * (int64_t)idx + 1] = (uint32_t)b.x;
       }
     }
+    if (have) e = next;
   }
   if (COUNT && tests) atomicAdd(&counters[4], tests);
 }
@@ -1097,8 +1121,8 @@ void enqueue_traversal(const MeshTopology &topo, const BroadphaseParams &p, Broa
       if (p.count_tests) BP_QUAD(true, 5);
       else BP_QUAD(false, 5);
     } else {
-      if (p.count_tests) BP_QUAD(true, 1);
-      else BP_QUAD(false, 1);
+      if (p.count_tests) BP_QUAD(true, 3);
+      else BP_QUAD(false, 3);
     }
 #undef BP_QUAD
     return;
