@@ -20,7 +20,7 @@ LIB = os.path.join(BUILD, "libccd_gb300.so")
 CU_SOURCES = ["narrow_vf.cu", "narrow_ee.cu", "narrow_vevv.cu", "narrow.cu", "stages.cu", "radix_sort.cu",
               "broadphase.cu", "mesh.cu", "capi.cu", "capi_mesh.cu",
               "capi_noalloc.cu", "capi_tune.cu", "server.cu", "distance.cu", "penalty.cu", "separating.cu", "velocity.cu"]
-HEADERS = ["ccd_common.h", "ccd_math.h", "ccd_math_tables.h", "ccd_jt.h", "ccd_jt_warp.h", "ccd_ctcd64.h", "ccd_cull32.h", "narrow.cuh", "narrow_kernels.cuh", "stages.cuh",
+HEADERS = ["ccd_common.h", "ccd_math.h", "ccd_math_tables.h", "ccd_jt.h", "ccd_jt_warp.h", "ccd_jt_shifts.h", "ccd_ctcd64.h", "ccd_cull32.h", "narrow.cuh", "narrow_kernels.cuh", "stages.cuh",
            "radix_sort.cuh", "broadphase.cuh", "mesh.cuh", "context.cuh", "ccd_distance.h", "distance.cuh", "separating.cuh", "penalty.cuh", "velocity.cuh", "ccd_heap.h"]
 
 NVCC_FLAGS = [

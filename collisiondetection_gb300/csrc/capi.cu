@@ -141,6 +141,9 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     view.wave_min_rows = ctx->opt_wave_min_rows;
     view.pool_budget = ctx->opt_pool_budget;
     view.warp_finish = ctx->opt_warp_finish;
+    view.shift_after = ctx->opt_shift_after;
+    view.pool_slots_min = ctx->opt_pool_slots_min;
+    view.pool_all = ctx->opt_pool_all;
     CCD_CUDA(ccd::launch_stages(b, surv, view, ctx->num_sms, s, &launches));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[2], s));
     if (pe) pe->stage_launches = launches;
@@ -161,6 +164,9 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     view.wave_min_rows = ctx->opt_wave_min_rows;
     view.pool_budget = ctx->opt_pool_budget;
     view.warp_finish = ctx->opt_warp_finish;
+    view.shift_after = ctx->opt_shift_after;
+    view.pool_slots_min = ctx->opt_pool_slots_min;
+    view.pool_all = ctx->opt_pool_all;
     CCD_CUDA(ccd::launch_stages(b, surv, view, ctx->num_sms, s, &launches));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[2], s));
     if (pe) pe->stage_launches = launches;
@@ -314,8 +320,17 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
   } else if (key == "count_slab_tests") {
     if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "count_slab_tests must be 0 or 1");
     ctx->opt_count_tests = (int)value;
+  } else if (key == "pool_slots_min") {
+    if (value < 1 || value > 64) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "pool_slots_min must be in [1, 64]");
+    ctx->opt_pool_slots_min = (int)value;
+  } else if (key == "pool_all") {
+    if (value < 0 || value > 32) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "pool_all must be in [0, 32]");
+    ctx->opt_pool_all = (int)value;
+  } else if (key == "shift_after") {
+    if (value < 0 || value > 19) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "shift_after must be in [0, 19]");
+    ctx->opt_shift_after = (int)value;
   } else if (key == "warp_finish") {
-    if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "warp_finish must be 0 or 1");
+    if (value < 0 || value > 2) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "warp_finish must be 0, 1 or 2");
     ctx->opt_warp_finish = (int)value;
   } else if (key == "tree_refit") {
     if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "tree_refit must be 0 or 1");

@@ -253,18 +253,25 @@ CCD_NOINLINE void estimate(S s, int type, double &uu, double &vv) {
 }
 
 // ---------------------------------------------------------------- transitions
-// Shift number CNT: rotate the shift point by 94 degrees and start the
-// fixed-shift stage (rpoly.h:217-224 and 284-291).
+// The shift point rotated by 94 degrees (rpoly.h:217-220).
 template <class S>
-CCD_NOINLINE void begin_shift(S s) {
+CCD_HD void rotate_shift(S s) {
   const double cosr = -0x1.1db902ec147e0p-4;  // cos(94.0 * 0.017453293)
   const double sinr = 0x1.fec0b6fc05f20p-1;   // sin(94.0 * 0.017453293)
-  const double xx = s.D(XX), yy = s.D(YY), bnd = s.D(BND);
+  const double xx = s.D(XX), yy = s.D(YY);
   const double xxx = cosr * xx - sinr * yy;
   const double ny = sinr * xx + cosr * yy;
   s.D(XX) = xxx;
   s.D(YY) = ny;
-  const double sr = bnd * xxx;
+}
+
+// Shift number CNT: rotate the shift point and start the fixed-shift stage
+// (rpoly.h:217-224 and 284-291).
+template <class S>
+CCD_NOINLINE void begin_shift(S s) {
+  rotate_shift(s);
+  const double bnd = s.D(BND);
+  const double sr = bnd * s.D(XX);
   s.D(U) = -2.0 * sr;
   s.D(V) = bnd;
   s.D(BETAV) = 0.25;

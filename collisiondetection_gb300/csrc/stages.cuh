@@ -34,6 +34,7 @@
 #pragma once
 
 #include "ccd_ctcd64.h"
+#include "ccd_jt_shifts.h"
 #include "ccd_jt_warp.h"
 #include "narrow.cuh"
 
@@ -82,7 +83,12 @@ struct StageScratch {
   int wave_steps;       // wavefront steps (0: pool kernel only)
   int64_t wave_min_rows;
   int pool_budget;      // steps the pool kernel gives a resumed job before handing it on
-  int warp_finish;      // 1: the last solves run on all 32 lanes of their warp (ccd_jt_warp.h); 0: on one lane
+  int warp_finish;      // how the last solves run: 0 on one lane; 1 on all 32 lanes of their warp
+                        // (ccd_jt_warp.h); 2 with a stage's remaining shifts tried at once, one per
+                        // lane (ccd_jt_shifts.h), once shift_after of its shifts have failed
+  int shift_after;
+  int pool_slots_min;   // pool kernel: fewest slots a warp may fill (its share of a small batch is spread)
+  int pool_all;         // pool kernel: once the queue is drained, at most this many solves left step together
 };
 
 // Bytes of the scratch for a tile of `cap` rows: three [slot][7][cap]
@@ -233,6 +239,19 @@ __device__ __forceinline__ int job_queue(const int *qbase, int nslots, int64_t g
   return q;
 }
 
+// The solve of state st run to its end by the whole warp, each lane trying
+// one of the stage's remaining shifts (ccd_jt_shifts.h); lane 0 writes its
+// spans.
+template <class Polys, class S>
+__device__ __forceinline__ void shift_solve(const StageScratch &sc, const S &st, int slot, int64_t j) {
+  jt::LocalStorage ls;
+  for (int f = 0; f < jt::kDoubles; f++) ls.d[f] = st.D(f);
+  for (int f = 0; f < jt::kInts; f++) ls.i[f] = st.I(f);
+  for (int k = 0; k < 6; k++) ls.zr[k] = st.Z(k);
+  jt::shifts::run(ls, sc.shift_after);
+  if ((threadIdx.x & 31) == 0) finish_job<Polys>(sc, jt::LocalState{&ls}, slot, j);
+}
+
 // Which jobs the pool kernel solves.  Default (list null): every queued job,
 // from the start.  After the wavefront steps: the jobs in list, resumed from
 // their field-major states; a job that takes `budget` more steps is handed on
@@ -267,6 +286,14 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
   __syncwarp();
   const uint32_t *tail = pj.list;
   const int njobs = tail ? (int)*pj.count : qbase[Polys::kSlots];
+  // Slots this warp fills at most: its fair share of the jobs, but no fewer
+  // than sc.pool_slots_min.  A small batch then spreads over more warps
+  // instead of filling the first warps' 64 slots while the rest of the grid
+  // idles: each warp advances fewer solves per iteration, with fewer
+  // divergent paths, and so each of them more often.
+  const int share = (int)(((int64_t)njobs + gridDim.x - 1) / gridDim.x);
+  const int lo = sc.pool_slots_min < 1 ? 1 : sc.pool_slots_min;
+  const int lim = share < lo ? lo : (share < kWarpPool ? share : kWarpPool);
   auto state = [&](int k) {
     const int64_t g = job_of[k];
     const int q = job_queue(qbase, Polys::kSlots, g);
@@ -289,8 +316,8 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
     __syncwarp();
     // Refill empty slots: one atomic per warp reserves consecutive jobs.
     if (!exhausted) {
-      const unsigned e0 = __ballot_sync(0xffffffffu, mode[lane] == jt::kEmpty);
-      const unsigned e1 = __ballot_sync(0xffffffffu, mode[lane + 32] == jt::kEmpty);
+      const unsigned e0 = __ballot_sync(0xffffffffu, lane < lim && mode[lane] == jt::kEmpty);
+      const unsigned e1 = __ballot_sync(0xffffffffu, lane + 32 < lim && mode[lane + 32] == jt::kEmpty);
       const int nempty = __popc(e0) + __popc(e1);
       if (nempty) {
         unsigned base = 0;
@@ -352,15 +379,26 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
       const int k = w0 ? __ffs(w0) - 1 : 32 + __ffs(w1) - 1;
       const int64_t g = job_of[k];
       const int q = job_queue(qbase, Polys::kSlots, g);
-      warp_solve<Polys>(sc, state(k), q, g - qbase[q]);
+      if (sc.warp_finish == 2)
+        shift_solve<Polys>(sc, state(k), q, g - qbase[q]);
+      else
+        warp_solve<Polys>(sc, state(k), q, g - qbase[q]);
       __syncwarp();
       if (lane == 0) mode[k] = jt::kEmpty;
       __syncwarp();
       continue;
     }
-    // Up to 32 slots of that phase, one per lane.
-    const unsigned b0 = __ballot_sync(0xffffffffu, mode[lane] == best);
-    const unsigned b1 = __ballot_sync(0xffffffffu, mode[lane + 32] == best);
+    // Up to 32 slots, one per lane: of the most populated phase (lanes on
+    // equal work), or -- once nothing is left to take and at most
+    // sc.pool_all solves remain -- all of them, whatever their phases: their
+    // lanes diverge, but every remaining solve advances at every iteration
+    // instead of waiting for its phase to be the most populated one.
+    const bool all = exhausted && working <= sc.pool_all;
+    const unsigned b0 = __ballot_sync(0xffffffffu, all ? (mode[lane] >= jt::kInit && mode[lane] < jt::kDone)
+                                                       : mode[lane] == best);
+    const unsigned b1 = __ballot_sync(0xffffffffu, all ? (mode[lane + 32] >= jt::kInit && mode[lane + 32] < jt::kDone)
+                                                       : mode[lane + 32] == best);
+    if (all) bestc = working;
     if ((b0 >> lane) & 1u) {
       const int r = __popc(b0 & lt);
       sel[r] = lane;
@@ -562,7 +600,9 @@ __global__ void __launch_bounds__(32) wave_finish(StageScratch sc, const uint32_
     int q;
     int64_t j;
     const jt::FieldState fs = wave_state<Polys>(sc, qbase, g, q, j);
-    if (whole) {
+    if (sc.warp_finish == 2) {
+      shift_solve<Polys>(sc, fs, q, j);
+    } else if (whole) {
       warp_solve<Polys>(sc, fs, q, j);
     } else {
       jt::LocalStorage st;

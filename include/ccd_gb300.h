@@ -119,6 +119,24 @@ int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
  *   "pool_budget"    further steps the unfinished polynomials get, many per
  *                    warp, before the last ones are finished one per warp
  *                    (0: no limit); default 0
+ *   "pool_slots_min" pool solver: a warp fills its share of the queued
+ *                    polynomials (the queue over the grid's warps), but at
+ *                    least this many of its 64 slots; a small share spreads
+ *                    a small batch over more warps; in [1, 64], default 4
+ *                    (64: the first warps fill all their slots)
+ *   "pool_all"       pool solver: once the queue is drained, a warp with at
+ *                    most this many solves left advances all of them at
+ *                    every iteration, whatever their phases, instead of the
+ *                    most populated phase's; in [0, 32], default 0
+ *   "warp_finish"    how a warp finishes a solve it holds alone (the last of
+ *                    its pool, or the one-per-warp finish): 0 on one lane,
+ *                    1 on all 32 lanes with independent operations spread
+ *                    over them, 2 each lane trying one of the stage's
+ *                    remaining shifts, the first that converges kept (the
+ *                    same results as the sequential order); default 1
+ *   "shift_after"    warp_finish 2: shifts of a stage tried one at a time
+ *                    before the remaining ones run at once; in [0, 19],
+ *                    default 2
  *   "chunk_rows"     ccd_prim_batch: largest chunk (rows) streamed through
  *                    the device, two in flight; a batch is cut into equal
  *                    chunks; in [1024, 2^26], default 2^23

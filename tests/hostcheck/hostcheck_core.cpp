@@ -76,3 +76,65 @@ extern "C" void hc_heap_replay(int n, const int *op, const int *op_key, const do
     }
   }
 }
+
+#include <cstring>
+
+#include "../../collisiondetection_gb300/csrc/ccd_jt_shifts.h"
+
+// The Jenkins-Traub solve with each stage's shifts resolved the way the
+// warp-parallel finish (csrc/ccd_jt_shifts.h) resolves them: every remaining
+// shift of the stage started from the stage's state (start_later_shift), run
+// to its end on its own copy, and the first one in order that finds a zero
+// taken (or the last one, when all of them fail).  Against the sequential
+// driver on the same polynomials: zeros, root count and status, bit for bit.
+// shifts_run[i] counts the shifts started ahead of time in solve i.
+extern "C" void hc_shift_check(int64_t n, const double *coef, const int *deg, double *zr_seq, int *roots_seq,
+                               double *zr_par, int *roots_par, int *status, int *shifts_run) {
+  using namespace ccd::jt;
+  for (int64_t p = 0; p < n; p++) {
+    const double *op = coef + 7 * p;
+    const int d = deg[p];
+    {
+      LocalStorage st;
+      std::memset(&st, 0, sizeof(st));
+      const LocalState s{&st};
+      start(s, op, d);
+      while (s.I(MODE) != kDone) step(s);
+      for (int k = 0; k < 6; k++) zr_seq[6 * p + k] = st.zr[k];
+      roots_seq[p] = s.I(ROOTS);
+      status[2 * p] = s.I(STATUS);
+    }
+    LocalStorage st;
+    std::memset(&st, 0, sizeof(st));
+    const LocalState s{&st};
+    start(s, op, d);
+    int ahead = 0;
+    while (s.I(MODE) != kDone) {
+      if (s.I(MODE) == kInit) {
+        step_init(s);
+        continue;
+      }
+      const int c0 = s.I(CNT), n0 = s.I(N);
+      LocalStorage win = st;
+      for (int lane = 0; c0 + lane < shifts::kShifts; lane++) {
+        LocalStorage ls = st;
+        const LocalState t{&ls};
+        if (lane > 0) {
+          shifts::start_later_shift(t, lane);
+          ahead++;
+        }
+        int o;
+        while ((o = shifts::shift_outcome(t, c0 + lane, n0)) == 0) step(t);
+        if (o == 2 || c0 + lane == shifts::kShifts - 1) {
+          win = ls;
+          break;
+        }
+      }
+      st = win;
+    }
+    for (int k = 0; k < 6; k++) zr_par[6 * p + k] = st.zr[k];
+    roots_par[p] = s.I(ROOTS);
+    status[2 * p + 1] = s.I(STATUS);
+    shifts_run[p] = ahead;
+  }
+}

@@ -111,23 +111,76 @@ def test_refine_all_equals_fp64_at_wavefront_size(ctx, kind):
 @pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE])
 @pytest.mark.parametrize("n", [4096, 600_000])
 def test_warp_finish_is_bit_identical(ctx, kind, n):
-    # The slowest solves advanced by all 32 lanes of a warp (independent
-    # divisions and K terms spread over lanes) against one lane alone: the
-    # same operations on the same operands, so the same bits.  4,096 rows
-    # take the pool kernel alone (its last solve per warp), 600,000 the
-    # wavefront and the one-solve-per-warp finish.
+    # The slowest solves advanced by all 32 lanes of a warp (1: independent
+    # divisions and K terms spread over lanes; 2: each lane trying one of the
+    # stage's remaining shifts, from the first shift on or after two failed
+    # ones) against one lane alone (0): the same operations on the same
+    # operands, so the same bits.  4,096 rows take the pool kernel alone (its
+    # last solve per warp), 600,000 the wavefront and the one-solve-per-warp
+    # finish.
     rows = C.workloads.primitive_batch(kind, n, seed=505)
     out = {}
-    for mode in (0, 1):
+    for mode, after in ((0, 2), (1, 2), (2, 0), (2, 2)):
         ctx.set_option("warp_finish", mode)
+        ctx.set_option("shift_after", after)
         try:
-            out[mode] = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_CULL_REFINE)
+            out[mode, after] = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_CULL_REFINE)
         finally:
             ctx.set_option("warp_finish", 1)
-    np.testing.assert_array_equal(out[0][0], out[1][0])
-    m = out[0][0] == 1
-    np.testing.assert_array_equal(out[0][1][m].view(np.uint64), out[1][1][m].view(np.uint64))
+            ctx.set_option("shift_after", 2)
+    ref = out[0, 2]
+    m = ref[0] == 1
     assert m.any()
+    for key, got in out.items():
+        np.testing.assert_array_equal(ref[0], got[0])
+        np.testing.assert_array_equal(ref[1][m].view(np.uint64), got[1][m].view(np.uint64))
+
+
+@pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE])
+def test_pool_spreading_is_bit_identical(ctx, kind):
+    # How many slots a pool warp fills and whether a drained warp steps all
+    # its remaining solves at once change only which warp and lane advance a
+    # solve, never its operations.
+    rows = C.workloads.primitive_batch(kind, 4096, seed=507)
+    out = {}
+    try:
+        for slots, every in ((64, 0), (4, 0), (1, 0), (4, 32), (64, 32)):
+            ctx.set_option("pool_slots_min", slots)
+            ctx.set_option("pool_all", every)
+            out[slots, every] = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_CULL_REFINE)
+    finally:
+        ctx.set_option("pool_slots_min", 4)
+        ctx.set_option("pool_all", 0)
+    ref = out[64, 0]
+    m = ref[0] == 1
+    assert m.any()
+    for got in out.values():
+        np.testing.assert_array_equal(ref[0], got[0])
+        np.testing.assert_array_equal(ref[1][m].view(np.uint64), got[1][m].view(np.uint64))
+
+
+@pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE])
+def test_one_per_warp_finish_is_bit_identical(ctx, kind):
+    # A pool budget hands the solves still running after it to the
+    # one-solve-per-warp finish kernel (wave_finish), which then runs with
+    # each of its three modes; every mode gives the same bits.
+    rows = C.workloads.primitive_batch(kind, 600_000, seed=506)
+    out = {}
+    ctx.set_option("pool_budget", 16)
+    try:
+        ctx.set_option("shift_after", 0)
+        for mode in (0, 1, 2):
+            ctx.set_option("warp_finish", mode)
+            out[mode] = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_CULL_REFINE)
+    finally:
+        ctx.set_option("warp_finish", 1)
+        ctx.set_option("shift_after", 2)
+        ctx.set_option("pool_budget", 0)
+    m = out[0][0] == 1
+    assert m.any()
+    for mode in (1, 2):
+        np.testing.assert_array_equal(out[0][0], out[mode][0])
+        np.testing.assert_array_equal(out[0][1][m].view(np.uint64), out[mode][1][m].view(np.uint64))
 
 
 @pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE, C.VERTEX_EDGE])
