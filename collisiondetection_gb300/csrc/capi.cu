@@ -142,6 +142,7 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     view.pool_budget = ctx->opt_pool_budget;
     view.warp_finish = ctx->opt_warp_finish;
     view.shift_after = ctx->opt_shift_after;
+    view.pool_slots = ctx->opt_pool_slots;
     view.pool_slots_min = ctx->opt_pool_slots_min;
     view.pool_all = ctx->opt_pool_all;
     CCD_CUDA(ccd::launch_stages(b, surv, view, ctx->num_sms, s, &launches));
@@ -165,6 +166,7 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     view.pool_budget = ctx->opt_pool_budget;
     view.warp_finish = ctx->opt_warp_finish;
     view.shift_after = ctx->opt_shift_after;
+    view.pool_slots = ctx->opt_pool_slots;
     view.pool_slots_min = ctx->opt_pool_slots_min;
     view.pool_all = ctx->opt_pool_all;
     CCD_CUDA(ccd::launch_stages(b, surv, view, ctx->num_sms, s, &launches));
@@ -320,6 +322,9 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
   } else if (key == "count_slab_tests") {
     if (value < 0 || value > 1) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "count_slab_tests must be 0 or 1");
     ctx->opt_count_tests = (int)value;
+  } else if (key == "pool_slots") {
+    if (value != 32 && value != 64) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "pool_slots must be 32 or 64");
+    ctx->opt_pool_slots = (int)value;
   } else if (key == "pool_slots_min") {
     if (value < 1 || value > 64) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "pool_slots_min must be in [1, 64]");
     ctx->opt_pool_slots_min = (int)value;

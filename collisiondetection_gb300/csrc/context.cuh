@@ -90,6 +90,7 @@ struct ccd_context {
   int64_t opt_wave_min_rows = ccd::kWaveMinRows;
   int opt_pool_budget = ccd::kPoolBudget;
   int opt_warp_finish = 1;  // the slowest root solves run on whole warps
+  int opt_pool_slots = 64;     // pool kernel (batches the wavefront does not take): slots per warp, 32 or 64
   int opt_pool_slots_min = 4;  // pool kernel: slots per warp at least (a small batch's jobs spread over warps)
   int opt_pool_all = 0;        // pool kernel: solves left that step together once its queue is drained
   int opt_shift_after = 2;  // warp_finish 2: failed shifts of a stage before the rest run at once

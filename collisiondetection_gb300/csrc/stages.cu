@@ -41,6 +41,7 @@ StageScratch stage_scratch_view(void *base, int64_t cap) {
   sc.pool_budget = 0;
   sc.warp_finish = 1;
   sc.shift_after = 2;
+  sc.pool_slots = stages::kWarpPool;
   sc.pool_slots_min = stages::kWarpPool;
   sc.pool_all = 0;
   return sc;

@@ -87,6 +87,7 @@ struct StageScratch {
                         // (ccd_jt_warp.h); 2 with a stage's remaining shifts tried at once, one per
                         // lane (ccd_jt_shifts.h), once shift_after of its shifts have failed
   int shift_after;
+  int pool_slots;       // pool kernel of a batch the wavefront does not take: 32 or 64 slots per warp
   int pool_slots_min;   // pool kernel: fewest slots a warp may fill (its share of a small batch is spread)
   int pool_all;         // pool kernel: once the queue is drained, at most this many solves left step together
 };
@@ -194,9 +195,11 @@ __global__ void __launch_bounds__(kStageThreads) stage_build(PrimBatch b, const 
   }
 }
 
-// Solver slots per warp (one warp per block), and the block's shared memory.
+// Solver slots per warp (one warp per block) at most, and the shared memory
+// of a block with `pool` slots.
 constexpr int kWarpPool = 64;
-constexpr size_t kPoolSmem = (size_t)kWarpPool * (jt::kDoubles * sizeof(double) + jt::kInts * sizeof(int));
+constexpr size_t pool_smem(int pool) { return (size_t)pool * (jt::kDoubles * sizeof(double) + jt::kInts * sizeof(int)); }
+constexpr size_t kPoolSmem = pool_smem(kWarpPool);
 
 // Spans of a finished solve, written to the polynomial's row slot.
 // Spans of a solve that found `roots` zeros tr[0 .. deg-1] (sorted in place).
@@ -264,14 +267,20 @@ struct PoolJobs {
   unsigned *spill_count;
 };
 
-template <class Polys>
+// POOL solver slots per warp (a multiple of 32; H = POOL / 32 slots per
+// lane): 64 packs more solves of one phase into each iteration, 32 halves the
+// shared memory a warp holds, so twice as many warps fit on an SM and hide
+// each other's FP64 latency.
+template <class Polys, int POOL>
 __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) {
+  constexpr int H = POOL / 32;
+  static_assert(POOL % 32 == 0 && H >= 1 && H <= 2, "pool of 32 or 64 slots");
   extern __shared__ double pool_d[];
-  int *pool_i = (int *)(pool_d + (size_t)kWarpPool * jt::kDoubles);
-  __shared__ int64_t job_of[kWarpPool];
+  int *pool_i = (int *)(pool_d + (size_t)POOL * jt::kDoubles);
+  __shared__ int64_t job_of[POOL];
   __shared__ int sel[32];
   __shared__ int qbase[kMaxSlots + 1];
-  __shared__ int steps[kWarpPool];
+  __shared__ int steps[POOL];
   const int lane = threadIdx.x;
   const unsigned lt = (1u << lane) - 1u;
   if (lane == 0) {
@@ -282,31 +291,33 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
     }
     qbase[Polys::kSlots] = acc;
   }
-  for (int k = lane; k < kWarpPool; k += 32) pool_i[jt::MODE * kWarpPool + k] = jt::kEmpty;
+  for (int k = lane; k < POOL; k += 32) pool_i[jt::MODE * POOL + k] = jt::kEmpty;
   __syncwarp();
   const uint32_t *tail = pj.list;
   const int njobs = tail ? (int)*pj.count : qbase[Polys::kSlots];
   // Slots this warp fills at most: its fair share of the jobs, but no fewer
   // than sc.pool_slots_min.  A small batch then spreads over more warps
-  // instead of filling the first warps' 64 slots while the rest of the grid
+  // instead of filling the first warps' slots while the rest of the grid
   // idles: each warp advances fewer solves per iteration, with fewer
-  // divergent paths, and so each of them more often.
+  // divergent paths, and so each of them more often.  The wavefront's
+  // leftovers (long solves, where packing lanes of one phase pays) fill
+  // every slot.
   const int share = (int)(((int64_t)njobs + gridDim.x - 1) / gridDim.x);
-  const int lo = sc.pool_slots_min < 1 ? 1 : sc.pool_slots_min;
-  const int lim = share < lo ? lo : (share < kWarpPool ? share : kWarpPool);
+  const int lo = tail ? POOL : (sc.pool_slots_min < 1 ? 1 : sc.pool_slots_min);
+  const int lim = share < lo ? lo : (share < POOL ? share : POOL);
   auto state = [&](int k) {
     const int64_t g = job_of[k];
     const int q = job_queue(qbase, Polys::kSlots, g);
     const int64_t j = g - qbase[q];
-    return jt::PoolState<kWarpPool>{pool_d, pool_i, k, sc.roots + (int64_t)q * 6 * sc.cap + j, sc.cap};
+    return jt::PoolState<POOL>{pool_d, pool_i, k, sc.roots + (int64_t)q * 6 * sc.cap + j, sc.cap};
   };
-  int *mode = pool_i + jt::MODE * kWarpPool;
+  int *mode = pool_i + jt::MODE * POOL;
   bool exhausted = njobs == 0;
   for (;;) {
     // Write out finished solves.
-    for (int k = lane; k < kWarpPool; k += 32) {
+    for (int k = lane; k < POOL; k += 32) {
       if (mode[k] == jt::kDone) {
-        const jt::PoolState<kWarpPool> st = state(k);
+        const jt::PoolState<POOL> st = state(k);
         const int64_t g = job_of[k];
         const int q = job_queue(qbase, Polys::kSlots, g);
         finish_job<Polys>(sc, st, q, g - qbase[q]);
@@ -316,26 +327,35 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
     __syncwarp();
     // Refill empty slots: one atomic per warp reserves consecutive jobs.
     if (!exhausted) {
-      const unsigned e0 = __ballot_sync(0xffffffffu, lane < lim && mode[lane] == jt::kEmpty);
-      const unsigned e1 = __ballot_sync(0xffffffffu, lane + 32 < lim && mode[lane + 32] == jt::kEmpty);
-      const int nempty = __popc(e0) + __popc(e1);
+      unsigned e[H];
+#pragma unroll
+      for (int h = 0; h < H; h++) {
+        const int k = lane + 32 * h;
+        e[h] = __ballot_sync(0xffffffffu, k < lim && mode[k] == jt::kEmpty);
+      }
+      int nempty = 0;
+#pragma unroll
+      for (int h = 0; h < H; h++) nempty += __popc(e[h]);
       if (nempty) {
         unsigned base = 0;
         if (lane == 0) base = atomicAdd(&sc.queue[kMaxSlots], (unsigned)nempty);
         base = __shfl_sync(0xffffffffu, base, 0);
         if ((int64_t)base + nempty >= njobs) exhausted = true;
-        for (int h = 0; h < 2; h++) {
-          const unsigned e = h ? e1 : e0;
-          if (!((e >> lane) & 1u)) continue;
+        int before = 0;
+#pragma unroll
+        for (int h = 0; h < H; h++) {
+          const int ahead = before;
+          before += __popc(e[h]);
+          if (!((e[h] >> lane) & 1u)) continue;
           const int k = lane + 32 * h;
-          const int64_t g0 = (int64_t)base + (h ? __popc(e0) : 0) + __popc(e & lt);
+          const int64_t g0 = (int64_t)base + ahead + __popc(e[h] & lt);
           if (g0 >= njobs) continue;
           const int64_t g = tail ? (int64_t)tail[g0] : g0;
           job_of[k] = g;
           steps[k] = 0;
           const int q = job_queue(qbase, Polys::kSlots, g);
           const int64_t j = g - qbase[q];
-          const jt::PoolState<kWarpPool> st{pool_d, pool_i, k, sc.roots + (int64_t)q * 6 * sc.cap + j, sc.cap};
+          const jt::PoolState<POOL> st{pool_d, pool_i, k, sc.roots + (int64_t)q * 6 * sc.cap + j, sc.cap};
           if (tail) {
             const jt::FieldState fs{sc.wd, sc.wi, g, sc.jcap, st.zr, sc.cap};
             for (int f = 0; f < jt::kDoubles; f++) st.D(f) = fs.D(f);
@@ -354,8 +374,9 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
     int best = 0, bestc = 0, working = 0;
     bool pending = false;
     for (int m = jt::kInit; m <= jt::kDone; m++) {
-      const int c = __popc(__ballot_sync(0xffffffffu, mode[lane] == m)) +
-                    __popc(__ballot_sync(0xffffffffu, mode[lane + 32] == m));
+      int c = 0;
+#pragma unroll
+      for (int h = 0; h < H; h++) c += __popc(__ballot_sync(0xffffffffu, mode[lane + 32 * h] == m));
       if (m == jt::kDone) {
         pending = c > 0;
       } else {
@@ -373,10 +394,13 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
     if (exhausted && working == 1 && sc.warp_finish) {
       // The warp's last unfinished solve, with no job left to take: all 32
       // lanes copy its state and advance it together to the end
-      // (jt::warp::step), then lane 0 writes it out.
-      const unsigned w0 = __ballot_sync(0xffffffffu, mode[lane] == best);
-      const unsigned w1 = __ballot_sync(0xffffffffu, mode[lane + 32] == best);
-      const int k = w0 ? __ffs(w0) - 1 : 32 + __ffs(w1) - 1;
+      // (jt::warp::step, or one shift per lane), then lane 0 writes it out.
+      int k = 0;
+#pragma unroll
+      for (int h = H - 1; h >= 0; h--) {
+        const unsigned w = __ballot_sync(0xffffffffu, mode[lane + 32 * h] == best);
+        if (w) k = 32 * h + __ffs(w) - 1;
+      }
       const int64_t g = job_of[k];
       const int q = job_queue(qbase, Polys::kSlots, g);
       if (sc.warp_finish == 2)
@@ -394,23 +418,26 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
     // lanes diverge, but every remaining solve advances at every iteration
     // instead of waiting for its phase to be the most populated one.
     const bool all = exhausted && working <= sc.pool_all;
-    const unsigned b0 = __ballot_sync(0xffffffffu, all ? (mode[lane] >= jt::kInit && mode[lane] < jt::kDone)
-                                                       : mode[lane] == best);
-    const unsigned b1 = __ballot_sync(0xffffffffu, all ? (mode[lane + 32] >= jt::kInit && mode[lane + 32] < jt::kDone)
-                                                       : mode[lane + 32] == best);
-    if (all) bestc = working;
-    if ((b0 >> lane) & 1u) {
-      const int r = __popc(b0 & lt);
-      sel[r] = lane;
+    unsigned b[H];
+#pragma unroll
+    for (int h = 0; h < H; h++) {
+      const int m = mode[lane + 32 * h];
+      b[h] = __ballot_sync(0xffffffffu, all ? (m >= jt::kInit && m < jt::kDone) : m == best);
     }
-    if ((b1 >> lane) & 1u) {
-      const int r = __popc(b0) + __popc(b1 & lt);
-      if (r < 32) sel[r] = lane + 32;
+    if (all) bestc = working;
+    int before = 0;
+#pragma unroll
+    for (int h = 0; h < H; h++) {
+      if ((b[h] >> lane) & 1u) {
+        const int r = before + __popc(b[h] & lt);
+        if (r < 32) sel[r] = lane + 32 * h;
+      }
+      before += __popc(b[h]);
     }
     __syncwarp();
     if (lane < bestc) {
       const int k = sel[lane];
-      const jt::PoolState<kWarpPool> st = state(k);
+      const jt::PoolState<POOL> st = state(k);
       jt::step(st);
       if (pj.budget > 0 && mode[k] != jt::kDone && ++steps[k] >= pj.budget) {
         // Hand the job on: its state back home, its index to the spill list.
@@ -675,7 +702,9 @@ cudaError_t run(const PrimBatch &b, const int32_t *list, const StageScratch &sc,
   cudaError_t e;
   const int64_t tiles = (b.n + sc.cap - 1) / sc.cap;
   const int grid = stage_grid(sc.cap, num_sms);
-  const int pool_grid = num_sms * 5;  // five 40 KB warp pools fit one SM's shared memory
+  // Five 64-slot warp pools (about 41 KB each) fit one SM's shared memory,
+  // ten 32-slot ones (about 21 KB; 168 registers a lane allow 12 warps).
+  const int pool_grid = num_sms * 5, pool32_grid = num_sms * 10;
   const int wave_grid = num_sms * 8;
   for (int64_t tile = 0; tile < tiles; tile++) {
     e = cudaMemsetAsync(sc.queue, 0, (kMaxSlots + 1) * sizeof(unsigned), s);
@@ -700,11 +729,15 @@ cudaError_t run(const PrimBatch &b, const int32_t *list, const StageScratch &sc,
       // few that exceed its step budget finish one per warp, as many warps as
       // can be resident at once.  The wavefront lists are free again and hold
       // the spilled jobs.
-      stage_roots<Polys><<<pool_grid, 32, kPoolSmem, s>>>(sc, PoolJobs{sc.tail, tcount, sc.pool_budget, sc.wlist, scount});
+      stage_roots<Polys, kWarpPool><<<pool_grid, 32, kPoolSmem, s>>>(
+          sc, PoolJobs{sc.tail, tcount, sc.pool_budget, sc.wlist, scount});
       wave_finish<Polys><<<num_sms * 32, 32, 0, s>>>(sc, sc.wlist, scount);
       *launches += steps + 4;
     } else {
-      stage_roots<Polys><<<pool_grid, 32, kPoolSmem, s>>>(sc, PoolJobs{nullptr, nullptr, 0, nullptr, nullptr});
+      if (sc.pool_slots == 32)
+        stage_roots<Polys, 32><<<pool32_grid, 32, pool_smem(32), s>>>(sc, PoolJobs{nullptr, nullptr, 0, nullptr, nullptr});
+      else
+        stage_roots<Polys, kWarpPool><<<pool_grid, 32, kPoolSmem, s>>>(sc, PoolJobs{nullptr, nullptr, 0, nullptr, nullptr});
       *launches += 1;
     }
     stage_combine<Polys><<<grid, kStageThreads, 0, s>>>(b, list, tile * sc.cap, sc);

@@ -119,6 +119,9 @@ int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
  *   "pool_budget"    further steps the unfinished polynomials get, many per
  *                    warp, before the last ones are finished one per warp
  *                    (0: no limit); default 0
+ *   "pool_slots"     pool solver of a batch the wavefront does not take:
+ *                    solver slots per warp, 64 (five warps per SM) or 32
+ *                    (ten warps per SM); default 64
  *   "pool_slots_min" pool solver: a warp fills its share of the queued
  *                    polynomials (the queue over the grid's warps), but at
  *                    least this many of its 64 slots; a small share spreads
