@@ -57,7 +57,8 @@ class BatchTimings(ctypes.Structure):
 class TuneResult(ctypes.Structure):
     _fields_ = [("wave_steps", ctypes.c_int32), ("pool_budget", ctypes.c_int32), ("wave_min_rows", ctypes.c_int64),
                 ("candidates", ctypes.c_int32), ("mismatches", ctypes.c_int32), ("chosen", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("default_ms", ctypes.c_double), ("best_ms", ctypes.c_double)]
+                ("warp_finish", ctypes.c_int32), ("default_ms", ctypes.c_double), ("best_ms", ctypes.c_double),
+                ("shift_after", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Fp64Peak(ctypes.Structure):

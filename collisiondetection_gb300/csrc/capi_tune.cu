@@ -3,8 +3,9 @@
 // The refinement of a large vertex-face or edge-edge batch splits its root
 // solves between a lock-step wavefront (wave_steps launches over every queued
 // polynomial), a pool kernel that packs the unfinished solves many per warp
-// (pool_budget steps each), and a one-per-warp finish of the last ones; batches
-// below wave_min_rows skip the wavefront.  Which split is fastest depends on
+// (pool_budget steps each), and a one-per-warp finish of the last ones (on
+// all lanes of the warp, or with a stage's remaining shifts tried at once,
+// warp_finish / shift_after); batches below wave_min_rows skip the wavefront.  Which split is fastest depends on
 // the batch (how many rows survive the cull, how many solves run long) and on
 // the GPU, so the tuner times each candidate split on the caller's own rows
 // and keeps the fastest.  A split changes only the schedule of the solves,
@@ -38,6 +39,8 @@ __global__ void count_mismatches(const uint8_t *h0, const double *t0, const uint
 struct Split {
   int wave_steps;
   int pool_budget;
+  int warp_finish;
+  int shift_after;
 };
 
 struct TuneBuffers {
@@ -154,7 +157,7 @@ int ccd_autotune_prim_batch(ccd_context *ctx, int kind, int64_t n, const double 
   // is committed at the end.
   struct Saved {
     ccd_context *ctx;
-    int steps, budget;
+    int steps, budget, finish, after;
     int64_t min_rows;
     bool profiling, committed = false;
     ~Saved() {
@@ -162,21 +165,29 @@ int ccd_autotune_prim_batch(ccd_context *ctx, int kind, int64_t n, const double 
       if (committed) return;
       ctx->opt_wave_steps = steps;
       ctx->opt_pool_budget = budget;
+      ctx->opt_warp_finish = finish;
+      ctx->opt_shift_after = after;
       ctx->opt_wave_min_rows = min_rows;
     }
-  } saved{ctx, ctx->opt_wave_steps, ctx->opt_pool_budget, ctx->opt_wave_min_rows, ctx->profiling};
+  } saved{ctx,          ctx->opt_wave_steps,     ctx->opt_pool_budget, ctx->opt_warp_finish,
+          ctx->opt_shift_after, ctx->opt_wave_min_rows, ctx->profiling};
   const int saved_steps = saved.steps, saved_budget = saved.budget;
+  const int saved_finish = saved.finish, saved_after = saved.after;
   const int64_t saved_min_rows = saved.min_rows;
   ctx->profiling = false;
 
   // The context's own settings come first: their output is the one every
   // other candidate must reproduce.  Then the pool kernel alone, then the
-  // wavefront at each step count with each pool budget.
+  // wavefront at each step count with each pool budget, then short pool
+  // budgets whose leftovers finish one per warp with their stages' remaining
+  // shifts tried at once.
   std::vector<Split> cands;
-  cands.push_back({n >= saved_min_rows ? saved_steps : 0, saved_budget});
-  cands.push_back({0, 0});
+  cands.push_back({n >= saved_min_rows ? saved_steps : 0, saved_budget, saved_finish, saved_after});
+  cands.push_back({0, 0, saved_finish, saved_after});
   for (int steps : {16, 32, 48, 64, 96, 128})
-    for (int budget : {0, 256, 4096}) cands.push_back({steps, budget});
+    for (int budget : {0, 256, 4096}) cands.push_back({steps, budget, saved_finish, saved_after});
+  for (int steps : {32, 48, 64})
+    for (int budget : {64, 256}) cands.push_back({steps, budget, 2, 1});
 
   // One run of the batch under the current options into output set k, with
   // the contact times starting as NaN (t is written only where hit).
@@ -199,6 +210,8 @@ int ccd_autotune_prim_batch(ccd_context *ctx, int kind, int64_t n, const double 
     // The wavefront runs only for batches of at least wave_min_rows rows.
     ctx->opt_wave_steps = c.wave_steps;
     ctx->opt_pool_budget = c.pool_budget;
+    ctx->opt_warp_finish = c.warp_finish;
+    ctx->opt_shift_after = c.shift_after;
     ctx->opt_wave_min_rows = std::min<int64_t>(saved_min_rows, n);
     int rc = run(k, nullptr);
     std::vector<float> times;
@@ -271,16 +284,22 @@ int ccd_autotune_prim_batch(ccd_context *ctx, int kind, int64_t n, const double 
     // Batches as large as this one take the wavefront with the chosen split.
     ctx->opt_wave_steps = best.wave_steps;
     ctx->opt_pool_budget = best.pool_budget;
+    ctx->opt_warp_finish = best.warp_finish;
+    ctx->opt_shift_after = best.shift_after;
     ctx->opt_wave_min_rows = std::min<int64_t>(saved_min_rows, n);
   } else {
     // The pool kernel alone won: batches up to this size skip the wavefront;
     // larger ones keep the context's split.
     ctx->opt_wave_steps = saved_steps;
     ctx->opt_pool_budget = saved_budget;
+    ctx->opt_warp_finish = saved_finish;
+    ctx->opt_shift_after = saved_after;
     ctx->opt_wave_min_rows = std::max<int64_t>(saved_min_rows, n + 1);
   }
   out->wave_steps = ctx->opt_wave_steps;
   out->pool_budget = ctx->opt_pool_budget;
+  out->warp_finish = ctx->opt_warp_finish;
+  out->shift_after = ctx->opt_shift_after;
   out->wave_min_rows = ctx->opt_wave_min_rows;
   out->chosen = best_i;
   return CCD_OK;

@@ -234,11 +234,14 @@ int ccd_fp64_peak(ccd_context *ctx, int reps, ccd_fp64_peak_result *out);
  * stencil).  Chooses the work split of the FP64 refinement for batches like
  * the given one: how many lock-step wavefront steps every queued root solve
  * takes ("wave_steps"), how many further steps the pool kernel gives each
- * unfinished solve ("pool_budget"), and the batch size from which the
+ * unfinished solve ("pool_budget"), how the solves left after that finish
+ * ("warp_finish", "shift_after"), and the batch size from which the
  * wavefront runs at all ("wave_min_rows").  It runs `rows` (device memory, a
  * vertex-face or edge-edge batch of n rows, CCD_PATH_CULL_REFINE) once to
  * warm up and `reps` timed times under the context's own split, the pool
- * kernel alone, each of 18 wavefront splits and the context's own split once
+ * kernel alone, each of 18 wavefront splits, 6 wavefront splits whose
+ * leftovers after a short pool budget finish one per warp with their stages'
+ * remaining shifts tried at once, and the context's own split once
  * more, checks that every split's hits and contact times equal the first
  * split's bit for bit, and sets the fastest matching split as the context's
  * options.  Blocks until done;
@@ -251,9 +254,11 @@ typedef struct {
   int32_t candidates;    /* splits timed */
   int32_t mismatches;    /* splits whose output differed (never chosen; 0 expected) */
   int32_t chosen;        /* index of the chosen split in the order timed (0: the context's own) */
-  int32_t reserved;
+  int32_t warp_finish;   /* the context's options after the call */
   double default_ms;     /* median time of the context's own split */
   double best_ms;        /* median time of the chosen split */
+  int32_t shift_after;
+  int32_t reserved;
 } ccd_tune_result;
 int ccd_autotune_prim_batch(ccd_context *ctx, int kind, int64_t n, const double *rows, const double *eta,
                             int64_t eta_count, int reps, ccd_tune_result *out);

@@ -54,11 +54,12 @@ def test_autotune_keeps_results_and_sets_a_split(setup, oracle, kind):
     h0, t0 = _run(torch, ctx, stream, kind, d_rows, d_eta, n)
 
     res = ctx.autotune_prim_batch(kind, n, d_rows.data_ptr(), d_eta.data_ptr(), 1, reps=2)
-    assert res["candidates"] == 20
+    assert res["candidates"] == 26
     assert res["mismatches"] == 0
     assert 0 <= res["chosen"] < res["candidates"]
     assert 0 < res["best_ms"] <= res["default_ms"]
     assert 0 <= res["wave_steps"] <= 4096 and res["pool_budget"] >= 0 and res["wave_min_rows"] >= 0
+    assert res["warp_finish"] in (0, 1, 2) and 0 <= res["shift_after"] < 20
 
     h1, t1 = _run(torch, ctx, stream, kind, d_rows, d_eta, n)
     assert np.array_equal(h0, h1)
