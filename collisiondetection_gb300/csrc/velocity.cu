@@ -31,15 +31,25 @@ namespace {
 // critical path.
 constexpr int kSharedGroups = 4096;
 
+// PenaltyGroupComparator (src/ActiveLayers.cpp:18-21): a ranks below b when
+// b fires first; PenaltyGroup::nextFireTime is nextstep * dt.  With the queue
+// in shared memory, each group's firing time is kept there too (key,
+// recomputed by the same product whenever its step changes), so that a
+// comparison on the loop's critical path is two loads and one FP64 compare
+// instead of two conversions and two products.
 struct FireLater {
   const int *nextstep;
   const double *dt;
-  // PenaltyGroupComparator (src/ActiveLayers.cpp:18-21): a ranks below b when
-  // b fires first; PenaltyGroup::nextFireTime is nextstep * dt.
+  const double *key;  // null: computed from nextstep and dt
   __device__ bool operator()(int a, int b) const {
+    if (key) return key[b] < key[a];
     return (double)nextstep[b] * dt[b] < (double)nextstep[a] * dt[a];
   }
 };
+
+__device__ __forceinline__ double fire_time(const int *nextstep, const double *dt, int grp) {
+  return (double)nextstep[grp] * dt[grp];
+}
 
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) layer_events(LayerGroups g, LayerState s, int64_t max_events) {
@@ -52,12 +62,14 @@ __global__ void __launch_bounds__(THREADS) layer_events(LayerGroups g, LayerStat
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const bool in_shared = g.ngroups <= kSharedGroups;
   double *dt_q = in_shared ? smem : nullptr;
-  int *next_q = in_shared ? reinterpret_cast<int *>(smem + g.ngroups) : g.nextstep;
+  double *key_q = in_shared ? smem + g.ngroups : nullptr;
+  int *next_q = in_shared ? reinterpret_cast<int *>(smem + 2 * g.ngroups) : g.nextstep;
   int *heap = in_shared ? next_q + g.ngroups : g.heap;
   if (in_shared) {
     for (int i = tid; i < g.ngroups; i += THREADS) {
       dt_q[i] = g.dt[i];
       next_q[i] = g.nextstep[i];
+      key_q[i] = fire_time(g.nextstep, g.dt, i);
     }
     for (int i = tid; i < *g.heap_size; i += THREADS) heap[i] = g.heap[i];
   } else {
@@ -68,7 +80,7 @@ __global__ void __launch_bounds__(THREADS) layer_events(LayerGroups g, LayerStat
     sh_base = *s.log_n;
   }
   __syncthreads();
-  const FireLater later{next_q, dt_q};
+  const FireLater later{next_q, dt_q, key_q};
   int action = 0;
   int64_t done = 0;
   for (int64_t ev = 0;; ev++) {
@@ -79,7 +91,7 @@ __global__ void __launch_bounds__(THREADS) layer_events(LayerGroups g, LayerStat
         a = 1;
       } else {
         grp = heap[0];
-        t = (double)next_q[grp] * dt_q[grp];
+        t = key_q ? key_q[grp] : fire_time(next_q, dt_q, grp);
         if (!(t < s.term)) {
           a = 1;
         } else if (ev >= max_events || sh_base + (g.gv_off[grp + 1] - g.gv_off[grp]) > s.log_cap) {
@@ -188,6 +200,7 @@ __global__ void __launch_bounds__(THREADS) layer_events(LayerGroups g, LayerStat
     }
     if (tid == 0) {
       next_q[grp] += 1;  // PenaltyGroup::incrementTimeStep
+      if (key_q) key_q[grp] = fire_time(next_q, dt_q, grp);
       heap_push(heap, &sh_heap_size, grp, later);
     }
     done++;
@@ -286,20 +299,22 @@ __global__ void __launch_bounds__(kGridThreads) layer_events_grid(LayerGroups g,
   const int lane = threadIdx.x & 31;
   const bool in_shared = g.ngroups <= kSharedGroups;
   double *dt_q = in_shared ? smem : const_cast<double *>(g.dt);
-  int *next_q = in_shared ? reinterpret_cast<int *>(smem + g.ngroups) : g.nextstep;
+  double *key_q = in_shared ? smem + g.ngroups : nullptr;
+  int *next_q = in_shared ? reinterpret_cast<int *>(smem + 2 * g.ngroups) : g.nextstep;
   int *heap = in_shared ? next_q + g.ngroups : g.heap;
   if (blockIdx.x == 0) {
     if (in_shared) {
       for (int i = threadIdx.x; i < g.ngroups; i += blockDim.x) {
         dt_q[i] = g.dt[i];
         next_q[i] = g.nextstep[i];
+        key_q[i] = fire_time(g.nextstep, g.dt, i);
       }
       for (int i = threadIdx.x; i < *g.heap_size; i += blockDim.x) heap[i] = g.heap[i];
     }
     if (threadIdx.x == 0) sh_heap_size = *g.heap_size;
     __syncthreads();
   }
-  const FireLater later{next_q, dt_q};
+  const FireLater later{next_q, dt_q, key_q};
   // The leader decides the next firing: pops it from the queue, or stops
   // (1: the next firing time reaches the end; 2: the event budget or the
   // log's room, counting `pending` entries not yet appended, is used up).
@@ -310,7 +325,7 @@ __global__ void __launch_bounds__(kGridThreads) layer_events_grid(LayerGroups g,
       a = 1;
     } else {
       grp = heap[0];
-      t = (double)next_q[grp] * dt_q[grp];
+      t = key_q ? key_q[grp] : fire_time(next_q, dt_q, grp);
       if (!(t < s.term)) {
         a = 1;
       } else if (ev >= max_events || (int64_t)__ldcg((const long long *)s.log_n) + pending +
@@ -363,6 +378,7 @@ __global__ void __launch_bounds__(kGridThreads) layer_events_grid(LayerGroups g,
     // firing times, which phase (3) does not touch)
     if (leader) {
       next_q[grp] += 1;  // PenaltyGroup::incrementTimeStep
+      if (key_q) key_q[grp] = fire_time(next_q, dt_q, grp);
       heap_push(heap, &sh_heap_size, grp, later);
       decide(ev + 1, v1 - v0);
     }
@@ -491,7 +507,8 @@ unsigned grid_of(int64_t n, int threads) { return (unsigned)std::max<int64_t>(1,
 
 cudaError_t launch_layer_events(const LayerGroups &g, const LayerState &s, int64_t max_events, int64_t max_group,
                                 int64_t grid_min, cudaStream_t st) {
-  const size_t shared = g.ngroups <= kSharedGroups ? (size_t)g.ngroups * (sizeof(double) + 2 * sizeof(int)) + 16 : 0;
+  const size_t shared =
+      g.ngroups <= kSharedGroups ? (size_t)g.ngroups * (2 * sizeof(double) + 2 * sizeof(int)) + 16 : 0;
   if (max_group >= grid_min) {
     // every block must be resident at once: size the grid by occupancy
     if (shared > 48 * 1024)
