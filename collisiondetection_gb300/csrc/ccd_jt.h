@@ -101,6 +101,14 @@ struct FieldState {
   CCD_HD int &I(int f) const { return i[f * stride + g]; }
 };
 
+// Every division of the solver's phases calls one out-of-line copy of the
+// division sequence: the pool kernel runs every phase's code in the warps of
+// one SM at once, and stalls most on instruction fetch; one shared copy in
+// place of 30-odd inline ones measured 10% off the two-sphere step and 3-4%
+// off the headline batch.  The quotient is the IEEE one, as inline.
+CCD_NOINLINE double jt_div(double a, double b) { return a / b; }
+#define JT_DIV(a, b) jt_div((a), (b))
+
 // ---------------------------------------------------------------- primitives
 // Quotient and remainder of p by x^2 + u x + v  (rpoly.h:680-695).
 template <class S>
@@ -122,7 +130,7 @@ CCD_NOINLINE void divide(S s, int nn, int src, int dst, double u, double v, int 
 // Zeros of a z^2 + b1 z + c  (rpoly.h:702-754).
 CCD_NOINLINE void quadratic(double a, double b1, double c, double &sr, double &si, double &lr, double &li) {
   if (a == 0.0) {
-    sr = (b1 != 0.0) ? -c / b1 : 0.0;
+    sr = (b1 != 0.0) ? JT_DIV(-c, b1) : 0.0;
     lr = 0.0;
     si = 0.0;
     li = 0.0;
@@ -130,7 +138,7 @@ CCD_NOINLINE void quadratic(double a, double b1, double c, double &sr, double &s
   }
   if (c == 0.0) {
     sr = 0.0;
-    lr = -b1 / a;
+    lr = JT_DIV(-b1, a);
     si = 0.0;
     li = 0.0;
     return;
@@ -138,22 +146,22 @@ CCD_NOINLINE void quadratic(double a, double b1, double c, double &sr, double &s
   double b = b1 / 2.0, d, e;
   if (fabs(b) < fabs(c)) {
     e = (c < 0.0) ? -a : a;
-    e = b * (b / fabs(c)) - e;
+    e = b * JT_DIV(b, fabs(c)) - e;
     d = sqrt(fabs(e)) * sqrt(fabs(c));
   } else {
-    e = 1.0 - (a / b) * (c / b);
+    e = 1.0 - JT_DIV(a, b) * JT_DIV(c, b);
     d = sqrt(fabs(e)) * fabs(b);
   }
   if (e < 0.0) {
-    sr = -b / a;
+    sr = JT_DIV(-b, a);
     lr = sr;
-    si = fabs(d / a);
+    si = fabs(JT_DIV(d, a));
     li = -si;
   } else {
     if (b >= 0.0) d = -d;
-    lr = (-b + d) / a;
+    lr = JT_DIV(-b + d, a);
     sr = 0.0;
-    if (lr != 0.0) sr = (c / lr) / a;
+    if (lr != 0.0) sr = JT_DIV(JT_DIV(c, lr), a);
     si = 0.0;
     li = 0.0;
   }
@@ -168,22 +176,22 @@ CCD_NOINLINE int scalars(S s) {
   const double a = s.D(A), b = s.D(B), c = s.D(C), d = s.D(DD);
   if (!(fabs(c) > fabs(s.D(K + n - 1) * 100.0 * kEps)) && !(fabs(d) > fabs(s.D(K + n - 2) * 100.0 * kEps))) return 3;
   if (fabs(d) < fabs(c)) {
-    const double e = a / c, f = d / c, g = u * e, h = v * b;
+    const double e = JT_DIV(a, c), f = JT_DIV(d, c), g = u * e, h = v * b;
     s.D(E) = e;
     s.D(F) = f;
     s.D(G) = g;
     s.D(H) = h;
-    s.D(A3) = a * e + (h / c + g) * b;
-    s.D(A1) = b - a * (d / c);
+    s.D(A3) = a * e + (JT_DIV(h, c) + g) * b;
+    s.D(A1) = b - a * JT_DIV(d, c);
     s.D(A7) = a + g * d + h * f;
     return 1;
   }
-  const double e = a / d, f = c / d, g = u * b, h = v * b;
+  const double e = JT_DIV(a, d), f = JT_DIV(c, d), g = u * b, h = v * b;
   s.D(E) = e;
   s.D(F) = f;
   s.D(G) = g;
   s.D(H) = h;
-  s.D(A3) = (a + g) * e + h * (b / d);
+  s.D(A3) = (a + g) * e + h * JT_DIV(b, d);
   s.D(A1) = b * f - a;
   s.D(A7) = (f + u) * a + h;
   return 2;
@@ -207,8 +215,8 @@ CCD_NOINLINE void next_k(S s, int type) {
     for (int i = 2; i < n; i++) s.D(K + i) = a3 * s.D(QK + i - 2) - a7 * s.D(QP + i - 1);
     return;
   }
-  a7 /= a1;
-  a3 /= a1;
+  a7 = JT_DIV(a7, a1);
+  a3 = JT_DIV(a3, a1);
   s.D(A7) = a7;
   s.D(A3) = a3;
   s.D(K) = s.D(QP);
@@ -236,8 +244,8 @@ CCD_NOINLINE void estimate(S s, int type, double &uu, double &vv) {
     a5 = c + (u + v * f) * d;
   }
   const double pn = s.D(P + n);
-  const double b1 = -s.D(K + n - 1) / pn;
-  const double b2 = -(s.D(K + n - 2) + b1 * s.D(P + n - 1)) / pn;
+  const double b1 = JT_DIV(-s.D(K + n - 1), pn);
+  const double b2 = JT_DIV(-(s.D(K + n - 2) + b1 * s.D(P + n - 1)), pn);
   const double c1 = v * b2 * a1;
   const double c2 = b1 * a7;
   const double c3 = b1 * b1 * a3;
@@ -248,8 +256,8 @@ CCD_NOINLINE void estimate(S s, int type, double &uu, double &vv) {
     vv = 0.0;
     return;
   }
-  uu = u - (u * (c3 + c2) + v * (b1 * a1 + b2 * a7)) / den;
-  vv = v * (1.0 + c4 / den);
+  uu = u - JT_DIV(u * (c3 + c2) + v * (b1 * a1 + b2 * a7), den);
+  vv = v * (1.0 + JT_DIV(c4, den));
 }
 
 // ---------------------------------------------------------------- transitions
@@ -312,7 +320,7 @@ template <class S>
 CCD_HD void finish_low(S s) {
   const int n = s.I(N), deg = s.I(DEG);
   if (n == 1) {
-    s.Z(deg - 1) = -s.D(P + 1) / s.D(P);
+    s.Z(deg - 1) = JT_DIV(-s.D(P + 1), s.D(P));
   } else {
     double si, li, sr, lr;
     quadratic(s.D(P), s.D(P + 1), s.D(P + 2), sr, si, lr, li);
@@ -447,8 +455,8 @@ CCD_NOINLINE void step_init(S s) {
     if (x > maxc) maxc = x;
     if (x != 0.0 && x < minc) minc = x;
   }
-  double sc = lo / minc;
-  const bool keep = (sc > 1.0 && kInfin / sc < maxc) || (sc <= 1.0 && maxc < 10.0);
+  double sc = JT_DIV(lo, minc);
+  const bool keep = (sc > 1.0 && JT_DIV(kInfin, sc) < maxc) || (sc <= 1.0 && maxc < 10.0);
   if (!keep) {
     if (sc == 0.0) sc = kSmalno;
     const int l = (int)(cr_log(sc) / 0x1.62e42fefa39efp-1 + 0.5);  // log(sc) / log(2.0)
@@ -461,7 +469,7 @@ CCD_NOINLINE void step_init(S s) {
   pt[n] = -pt[n];
   x = cr_exp((cr_log(-pt[n]) - cr_log(pt[0])) / (double)n);
   if (pt[n - 1] != 0.0) {
-    xm = -pt[n] / pt[n - 1];
+    xm = JT_DIV(-pt[n], pt[n - 1]);
     if (xm < x) x = xm;
   }
   for (int it = 0;; it++) {
@@ -478,7 +486,7 @@ CCD_NOINLINE void step_init(S s) {
     x = xm;
   }
   dx = x;
-  for (int it = 0; fabs(dx / x) > 0.005; it++) {
+  for (int it = 0; fabs(JT_DIV(dx, x)) > 0.005; it++) {
     if (it >= kBoundLimit) {
       s.I(STATUS) |= kStatusRootLimit;
       s.I(ROOTS) = -1;
@@ -492,20 +500,20 @@ CCD_NOINLINE void step_init(S s) {
       df = df * x + ff;
     }
     ff = ff * x + pt[n];
-    dx = ff / df;
+    dx = JT_DIV(ff, df);
     x -= dx;
   }
   s.D(BND) = x;
   // Derivative as the first K polynomial, then five unshifted steps.
   const int nm1 = n - 1;
-  for (int i = 1; i < n; i++) s.D(K + i) = (double)(n - i) * s.D(P + i) / (double)n;
+  for (int i = 1; i < n; i++) s.D(K + i) = JT_DIV((double)(n - i) * s.D(P + i), (double)n);
   s.D(K) = s.D(P);
   const double aa = s.D(P + n), bb = s.D(P + n - 1);
   bool zerok = (s.D(K + n - 1) == 0);
   for (int jj = 0; jj < 5; jj++) {
     const double cc = s.D(K + n - 1);
     if (!zerok) {
-      const double t = -aa / cc;
+      const double t = JT_DIV(-aa, cc);
       for (int i = 0; i < nm1; i++) {
         const int j = n - i - 1;
         s.D(K + j) = t * s.D(K + j - 1) + s.D(P + j);
@@ -542,13 +550,13 @@ CCD_NOINLINE void step_fixed(S s) {
   const double vv = vi;
   double ss = 0.0;
   const double kn1 = s.D(K + n - 1);
-  if (kn1 != 0.0) ss = -s.D(P + n) / kn1;
+  if (kn1 != 0.0) ss = JT_DIV(-s.D(P + n), kn1);
   double tv = 1.0, ts = 1.0;
   s.D(VV) = vv;
   s.D(SS) = ss;
   if (s.I(J) != 0 && type != 3) {
-    if (vv != 0.0) tv = fabs((vv - s.D(OVV)) / vv);
-    if (ss != 0.0) ts = fabs((ss - s.D(OSS)) / ss);
+    if (vv != 0.0) tv = fabs(JT_DIV(vv - s.D(OVV), vv));
+    if (ss != 0.0) ts = fabs(JT_DIV(ss - s.D(OSS), ss));
     const double otv = s.D(OTV), ots = s.D(OTS);
     const double tvv = (tv < otv) ? tv * otv : 1.0;
     const double tss = (ts < ots) ? ts * ots : 1.0;
@@ -626,7 +634,7 @@ CCD_NOINLINE void step_quad(S s) {
     quad_failed(s);
     return;
   }
-  s.D(RELSTP) = fabs((vi - v) / vi);
+  s.D(RELSTP) = fabs(JT_DIV(vi - v, vi));
   s.D(U) = ui;
   s.D(V) = vi;
 }
@@ -672,14 +680,14 @@ CCD_NOINLINE void step_real(S s) {
     s.D(K) = 0.0;
     for (int i = 1; i < n; i++) s.D(K + i) = s.D(QK + i - 1);
   } else {
-    t = -pv / kv;
+    t = JT_DIV(-pv, kv);
     s.D(K) = s.D(QP);
     for (int i = 1; i < n; i++) s.D(K + i) = t * s.D(QK + i - 1) + s.D(QP + i);
   }
   kv = s.D(K);
   for (int i = 1; i < n; i++) kv = kv * x + s.D(K + i);
   t = 0.0;
-  if (fabs(kv) > fabs(s.D(K + n - 1) * 10.0 * kEps)) t = -pv / kv;
+  if (fabs(kv) > fabs(s.D(K + n - 1) * 10.0 * kEps)) t = JT_DIV(-pv, kv);
   s.D(RT) = t;
   s.D(RX) = x + t;
 }
