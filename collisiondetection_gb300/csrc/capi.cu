@@ -145,6 +145,7 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     view.pool_slots = ctx->opt_pool_slots;
     view.pool_slots_min = ctx->opt_pool_slots_min;
     view.pool_all = ctx->opt_pool_all;
+    view.pool_phase_sync = ctx->opt_pool_phase_sync;
     CCD_CUDA(ccd::launch_stages(b, surv, view, ctx->num_sms, s, &launches));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[2], s));
     if (pe) pe->stage_launches = launches;
@@ -169,6 +170,7 @@ int enqueue_batch(ccd_context *ctx, const ccd::PrimBatch &b, int path, int32_t *
     view.pool_slots = ctx->opt_pool_slots;
     view.pool_slots_min = ctx->opt_pool_slots_min;
     view.pool_all = ctx->opt_pool_all;
+    view.pool_phase_sync = ctx->opt_pool_phase_sync;
     CCD_CUDA(ccd::launch_stages(b, surv, view, ctx->num_sms, s, &launches));
     if (pe) CCD_CUDA(cudaEventRecord(pe->ev[2], s));
     if (pe) pe->stage_launches = launches;
@@ -328,6 +330,9 @@ int ccd_context_set_option(ccd_context *ctx, const char *name, int64_t value) {
   } else if (key == "pool_slots_min") {
     if (value < 1 || value > 64) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "pool_slots_min must be in [1, 64]");
     ctx->opt_pool_slots_min = (int)value;
+  } else if (key == "pool_phase_sync") {
+    if (value < 0 || value > 30) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "pool_phase_sync must be in [0, 30]");
+    ctx->opt_pool_phase_sync = (int)value;
   } else if (key == "pool_all") {
     if (value < 0 || value > 32) return fail(ctx, CCD_ERR_INVALID_ARGUMENT, "pool_all must be in [0, 32]");
     ctx->opt_pool_all = (int)value;

@@ -825,7 +825,7 @@ std::vector<uintptr_t> graph_signature(const ccd_mesh *m) {
       (uintptr_t)b.scan, (uintptr_t)b.temp, (uintptr_t)b.temp_bytes, (uintptr_t)b.cap_pairs,
       (uintptr_t)b.cap_faces, (uintptr_t)ctx->opt_wave_steps, (uintptr_t)ctx->opt_pool_budget,
       (uintptr_t)ctx->opt_wave_min_rows, (uintptr_t)ctx->opt_warp_finish, (uintptr_t)ctx->opt_traversal,
-      (uintptr_t)ctx->opt_shift_after, (uintptr_t)ctx->opt_pool_slots_min, (uintptr_t)ctx->opt_pool_slots, (uintptr_t)ctx->opt_pool_all,
+      (uintptr_t)ctx->opt_shift_after, (uintptr_t)ctx->opt_pool_slots_min, (uintptr_t)ctx->opt_pool_slots, (uintptr_t)ctx->opt_pool_all, (uintptr_t)ctx->opt_pool_phase_sync,
       (uintptr_t)ctx->opt_narrow_chunk};
   for (const Lane &L : m->lane) {
     const NarrowScratch &n = L.ns;

@@ -92,7 +92,8 @@ struct ccd_context {
   int opt_warp_finish = 1;  // the slowest root solves run on whole warps
   int opt_pool_slots = 64;     // pool kernel (batches the wavefront does not take): slots per warp, 32 or 64
   int opt_pool_slots_min = 4;  // pool kernel: slots per warp at least (a small batch's jobs spread over warps)
-  int opt_pool_all = 0;        // pool kernel: solves left that step together once its queue is drained
+  int opt_pool_all = 0;
+  int opt_pool_phase_sync = 16;  // pool kernel: prefer the phase of the SM clock's 2^k-cycle window (0: off)        // pool kernel: solves left that step together once its queue is drained
   int opt_shift_after = 2;  // warp_finish 2: failed shifts of a stage before the rest run at once
   int opt_count_tests = 0;
   int opt_traversal = 3;  // broad-phase traversal (ccd_context_set_option "traversal")

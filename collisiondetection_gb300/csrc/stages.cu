@@ -44,6 +44,7 @@ StageScratch stage_scratch_view(void *base, int64_t cap) {
   sc.pool_slots = stages::kWarpPool;
   sc.pool_slots_min = stages::kWarpPool;
   sc.pool_all = 0;
+  sc.pool_phase_sync = 0;
   return sc;
 }
 

@@ -90,6 +90,7 @@ struct StageScratch {
   int pool_slots;       // pool kernel of a batch the wavefront does not take: 32 or 64 slots per warp
   int pool_slots_min;   // pool kernel: fewest slots a warp may fill (its share of a small batch is spread)
   int pool_all;         // pool kernel: once the queue is drained, at most this many solves left step together
+  int pool_phase_sync;  // pool kernel: 0, or k: prefer the phase of the SM clock's current 2^k-cycle window
 };
 
 // Bytes of the scratch for a tile of `cap` rows: three [slot][7][cap]
@@ -390,6 +391,20 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
     if (bestc == 0) {
       if (exhausted && !pending) break;
       continue;
+    }
+    if (sc.pool_phase_sync) {
+      // The phase of this moment (rotating every 2^k cycles of the SM's
+      // clock, alike for the warps of one SM) when it holds at least half
+      // as many solves as the most populated one: the SM's warps then run
+      // the same phase's code at once.
+      const int pref = jt::kInit + (int)((clock64() >> sc.pool_phase_sync) & 3);
+      int c = 0;
+#pragma unroll
+      for (int h = 0; h < H; h++) c += __popc(__ballot_sync(0xffffffffu, mode[lane + 32 * h] == pref));
+      if (2 * c >= bestc && c > 0) {
+        best = pref;
+        bestc = c;
+      }
     }
     if (exhausted && working == 1 && sc.warp_finish) {
       // The warp's last unfinished solve, with no job left to take: all 32

@@ -131,6 +131,12 @@ int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
  *                    most this many solves left advances all of them at
  *                    every iteration, whatever their phases, instead of the
  *                    most populated phase's; in [0, 32], default 0
+ *   "pool_phase_sync" pool solver: 0, or k: a warp advances the solver
+ *                    phase of the current 2^k-cycle window of its SM's clock
+ *                    (the same for the SM's warps, so they run one phase's
+ *                    code at once) when it holds at least half as many
+ *                    solves as the most populated phase; in [0, 30],
+ *                    default 16
  *   "warp_finish"    how a warp finishes a solve it holds alone (the last of
  *                    its pool, or the one-per-warp finish): 0 on one lane,
  *                    1 on all 32 lanes with independent operations spread

@@ -138,20 +138,22 @@ def test_warp_finish_is_bit_identical(ctx, kind, n):
 
 @pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE])
 def test_pool_spreading_is_bit_identical(ctx, kind):
-    # How many slots a pool warp fills and whether a drained warp steps all
-    # its remaining solves at once change only which warp and lane advance a
-    # solve, never its operations.
+    # How many slots a pool warp fills, whether a drained warp steps all its
+    # remaining solves at once and which phase a warp prefers change only
+    # which warp and lane advance a solve, never its operations.
     rows = C.workloads.primitive_batch(kind, 4096, seed=507)
     out = {}
     try:
-        for slots, every in ((64, 0), (4, 0), (1, 0), (4, 32), (64, 32)):
+        for slots, every, sync in ((64, 0, 0), (4, 0, 16), (1, 0, 0), (4, 32, 16), (64, 32, 12)):
             ctx.set_option("pool_slots_min", slots)
             ctx.set_option("pool_all", every)
-            out[slots, every] = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_CULL_REFINE)
+            ctx.set_option("pool_phase_sync", sync)
+            out[slots, every, sync] = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_CULL_REFINE)
     finally:
         ctx.set_option("pool_slots_min", 4)
         ctx.set_option("pool_all", 0)
-    ref = out[64, 0]
+        ctx.set_option("pool_phase_sync", 16)
+    ref = out[64, 0, 0]
     m = ref[0] == 1
     assert m.any()
     for got in out.values():
