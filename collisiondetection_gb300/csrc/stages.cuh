@@ -392,11 +392,12 @@ __global__ void __launch_bounds__(32) stage_roots(StageScratch sc, PoolJobs pj) 
       if (exhausted && !pending) break;
       continue;
     }
-    if (sc.pool_phase_sync) {
+    if (sc.pool_phase_sync && !tail) {
       // The phase of this moment (rotating every 2^k cycles of the SM's
       // clock, alike for the warps of one SM) when it holds at least half
       // as many solves as the most populated one: the SM's warps then run
-      // the same phase's code at once.
+      // the same phase's code at once.  Not for the wavefront's leftovers,
+      // long solves whose lanes the most populated phase packs best.
       const int pref = jt::kInit + (int)((clock64() >> sc.pool_phase_sync) & 3);
       int c = 0;
 #pragma unroll

@@ -131,7 +131,8 @@ int ccd_last_batch_timings(ccd_context *ctx, ccd_batch_timings *out);
  *                    most this many solves left advances all of them at
  *                    every iteration, whatever their phases, instead of the
  *                    most populated phase's; in [0, 32], default 0
- *   "pool_phase_sync" pool solver: 0, or k: a warp advances the solver
+ *   "pool_phase_sync" pool solver of a batch the wavefront does not take:
+ *                    0, or k: a warp advances the solver
  *                    phase of the current 2^k-cycle window of its SM's clock
  *                    (the same for the SM's warps, so they run one phase's
  *                    code at once) when it holds at least half as many
