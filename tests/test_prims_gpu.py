@@ -138,22 +138,25 @@ def test_warp_finish_is_bit_identical(ctx, kind, n):
 
 @pytest.mark.parametrize("kind", [C.VERTEX_FACE, C.EDGE_EDGE])
 def test_pool_spreading_is_bit_identical(ctx, kind):
-    # How many slots a pool warp fills, whether a drained warp steps all its
-    # remaining solves at once and which phase a warp prefers change only
-    # which warp and lane advance a solve, never its operations.
+    # How many slots a pool warp has and fills, whether a drained warp steps
+    # all its remaining solves at once and which phase a warp prefers change
+    # only which warp and lane advance a solve, never its operations.
     rows = C.workloads.primitive_batch(kind, 4096, seed=507)
     out = {}
     try:
-        for slots, every, sync in ((64, 0, 0), (4, 0, 16), (1, 0, 0), (4, 32, 16), (64, 32, 12)):
+        for pool, slots, every, sync in ((64, 64, 0, 0), (64, 4, 0, 16), (64, 1, 0, 0), (64, 4, 32, 16),
+                                         (64, 64, 32, 12), (32, 4, 0, 16), (32, 32, 8, 0)):
+            ctx.set_option("pool_slots", pool)
             ctx.set_option("pool_slots_min", slots)
             ctx.set_option("pool_all", every)
             ctx.set_option("pool_phase_sync", sync)
-            out[slots, every, sync] = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_CULL_REFINE)
+            out[pool, slots, every, sync] = ctx.prim_batch(kind, rows, 1e-6, path=C.PATH_CULL_REFINE)
     finally:
+        ctx.set_option("pool_slots", 64)
         ctx.set_option("pool_slots_min", 4)
         ctx.set_option("pool_all", 0)
         ctx.set_option("pool_phase_sync", 16)
-    ref = out[64, 0, 0]
+    ref = out[64, 64, 0, 0]
     m = ref[0] == 1
     assert m.any()
     for got in out.values():
