@@ -273,6 +273,19 @@ def serving_summary(serving):
             "fp64_one_at_a_time_req_s": serving.get("fp64_one_at_a_time", {}).get("throughput_req_s")}
 
 
+def small_batch_summary(graph):
+    """The small-batch step (4,096 + 4,096 rows by default) issued directly
+    and replayed from a CUDA graph: ms per step on the device."""
+    if not graph:
+        return None
+    if "error" in graph:
+        return {"error": graph["error"]}
+    return {"rows_per_kind": graph.get("rows_per_kind"),
+            "ms_direct": graph["direct"]["device_us_per_step"] / 1e3,
+            "ms_graph": graph["graph"]["device_us_per_step"] / 1e3,
+            "replays_match": graph.get("replays_match_direct_call")}
+
+
 def _identical(par):
     if not par:
         return None
@@ -1238,6 +1251,7 @@ def run_ours(args, rank, world, local, pg):
                            "speedup_vs_staged": value / (world * staged_tps)} if fp64_tps else None),
             "parity": parity_summary(parity),
             "mesh": mesh_summary(mesh, uneven),
+            "small_batch": small_batch_summary(graph),
             "serving": serving_summary(serving),
             "detail": detail_path,
         }

@@ -68,3 +68,13 @@ def test_round_floats_keeps_the_line_short():
     r = bench.round_floats(x)
     assert r["a"] == 0.33333 and r["b"] == [0.66667, 5] and r["c"]["d"] == 123460000.0
     assert r["e"] == "x" and r["f"] is None and r["g"] is True
+
+
+def test_small_batch_summary():
+    g = {"rows_per_kind": 4096, "iters": 50, "direct": {"device_us_per_step": 3081.8, "wall_us_per_step": 3082.0},
+         "graph": {"device_us_per_step": 2983.9, "wall_us_per_step": 2984.2}, "replays_match_direct_call": True}
+    r = bench.small_batch_summary(g)
+    assert r["rows_per_kind"] == 4096 and r["replays_match"] is True
+    assert abs(r["ms_direct"] - 3.0818) < 1e-12 and abs(r["ms_graph"] - 2.9839) < 1e-12
+    assert bench.small_batch_summary(None) is None
+    assert bench.small_batch_summary({"error": "CcdError: x"}) == {"error": "CcdError: x"}
